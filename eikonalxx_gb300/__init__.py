@@ -1,0 +1,318 @@
+"""eikonalxx_gb300 -- GB300-native level-set fast-sweeping eikonal solver.
+
+Python binding of the C ABI in include/eikx/eikx_c.h (libeikx.so, built in-tree by
+eikonalxx_gb300/build.py).  The solve runs on the GPU through the native library;
+there is no CPU fallback: importing the binding without the built library raises.
+
+The objects mirror the reference's (uofuseismo/eikonalxx) solver workflow:
+Solver3D.initialize(options, geometry) -> setVelocityModel -> setSource -> solve ->
+getTravelTimeField, with many sources solved in one batched launch (``solve_batch``).
+"""
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libeikx.so")
+
+EIKX_OK = 0
+EIKX_ERR_INVALID = -1
+EIKX_ERR_STATE = -2
+EIKX_ERR_CUDA = -3
+EIKX_ERR_TIMEOUT = -4
+EIKX_ERR_ALLOC = -5
+EIKX_ERR_UNSUPPORTED = -6
+F32, F64 = 0, 1
+HOST, DEVICE = 0, 1
+NATURAL, TRANSPOSED = 0, 1
+
+# every symbol include/eikx/eikx_c.h declares
+EXPORTED = [
+    "eikx_options_default", "eikx_create", "eikx_destroy", "eikx_last_error", "eikx_get_stats",
+    "eikx_set_grid3d", "eikx_set_slowness3d", "eikx_set_nodal_velocity3d", "eikx_get_slowness3d",
+    "eikx_solve3d", "eikx_set_grid2d", "eikx_set_slowness2d", "eikx_set_nodal_velocity2d",
+    "eikx_solve2d", "eikx_graph3d_tables", "eikx_levels2d", "eikx_analytic3d", "eikx_analytic2d",
+]
+
+
+class EikxError(RuntimeError):
+    """A failed C-ABI call; ``code`` is the eikx_status."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"eikx error {code}: {msg}")
+        self.code = code
+
+
+class InvalidArgument(EikxError, ValueError):
+    pass
+
+
+class StateError(EikxError):
+    pass
+
+
+class TimeoutError_(EikxError):
+    pass
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("n_sweeps", ctypes.c_int), ("tolerance", ctypes.c_double),
+                ("factored_radius", ctypes.c_int), ("init_sweeps", ctypes.c_int),
+                ("init_fp64", ctypes.c_int), ("spin_limit_log2", ctypes.c_int),
+                ("test_drop_blocks", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("n_fields", ctypes.c_int), ("iterations_max", ctypes.c_int),
+                ("iterations_min", ctypes.c_int), ("sweeps_launched", ctypes.c_int),
+                ("kernel_launches", ctypes.c_int), ("residual_last", ctypes.c_double),
+                ("device_ms", ctypes.c_double)]
+
+
+class _Src3(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_double), ("y", ctypes.c_double), ("z", ctypes.c_double)]
+
+
+class _Src2(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_double), ("z", ctypes.c_double)]
+
+
+_lib = None
+
+
+def load(path=None):
+    """Load libeikx.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"{p} is missing: build it with `python eikonalxx_gb300/build.py` "
+                          "(the solver has no CPU fallback)")
+    lib = ctypes.CDLL(p)
+    c_int, c_double, vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+    ip = ctypes.POINTER(ctypes.c_int)
+    lib.eikx_options_default.argtypes = [ctypes.POINTER(_Options)]
+    lib.eikx_options_default.restype = None
+    lib.eikx_create.argtypes = [ctypes.POINTER(vp), c_int]
+    lib.eikx_destroy.argtypes = [vp]
+    lib.eikx_last_error.restype = ctypes.c_char_p
+    lib.eikx_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
+    lib.eikx_set_grid3d.argtypes = [vp, c_int, c_int, c_int] + [c_double] * 6
+    lib.eikx_set_slowness3d.argtypes = [vp, vp, c_int, c_int, c_int]
+    lib.eikx_set_nodal_velocity3d.argtypes = [vp, vp, c_int, c_int, c_int]
+    lib.eikx_get_slowness3d.argtypes = [vp, vp, c_int]
+    lib.eikx_solve3d.argtypes = [vp, ctypes.POINTER(_Src3), c_int, ctypes.POINTER(_Options), c_int, vp, c_int]
+    lib.eikx_set_grid2d.argtypes = [vp, c_int, c_int] + [c_double] * 4
+    lib.eikx_set_slowness2d.argtypes = [vp, vp, c_int, c_int, c_int]
+    lib.eikx_set_nodal_velocity2d.argtypes = [vp, vp, c_int, c_int, c_int]
+    lib.eikx_solve2d.argtypes = [vp, ctypes.POINTER(_Src2), c_int, ctypes.POINTER(_Options), c_int, vp, c_int]
+    lib.eikx_graph3d_tables.argtypes = [c_int, c_int, c_int, c_int, ip, ip, ip, ip, ip, ip, ip]
+    lib.eikx_levels2d.argtypes = [c_int, c_int, c_int, ip, ip, ip]
+    lib.eikx_analytic3d.argtypes = [vp, ctypes.POINTER(_Src3), c_double, c_double, vp, c_int]
+    lib.eikx_analytic2d.argtypes = [vp, ctypes.POINTER(_Src2), c_double, c_double, vp, c_int]
+    for name in EXPORTED:
+        if name not in ("eikx_options_default", "eikx_last_error", "eikx_levels2d", "eikx_graph3d_tables"):
+            getattr(lib, name).restype = c_int
+    lib.eikx_graph3d_tables.restype = c_int
+    lib.eikx_levels2d.restype = c_int
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc == EIKX_OK:
+        return
+    msg = load().eikx_last_error().decode()
+    if rc == EIKX_ERR_INVALID:
+        raise InvalidArgument(rc, msg)
+    if rc == EIKX_ERR_STATE:
+        raise StateError(rc, msg)
+    if rc == EIKX_ERR_TIMEOUT:
+        raise TimeoutError_(rc, msg)
+    raise EikxError(rc, msg)
+
+
+@dataclass
+class Options:
+    """SolverOptions (include/eikonalxx/solverOptions.hpp) plus the GPU knobs."""
+    n_sweeps: int = 5
+    tolerance: float = 1e-5
+    factored_radius: int = 3
+    init_sweeps: bool = True
+    init_fp64: bool = True
+    spin_limit_log2: int = 22
+    test_drop_blocks: int = 0   # test hook only (see eikx_options.test_drop_blocks)
+
+    def _c(self):
+        o = _Options()
+        o.n_sweeps = int(self.n_sweeps)
+        o.tolerance = float(self.tolerance)
+        o.factored_radius = int(self.factored_radius)
+        o.init_sweeps = int(bool(self.init_sweeps))
+        o.init_fp64 = int(bool(self.init_fp64))
+        o.spin_limit_log2 = int(self.spin_limit_log2)
+        o.test_drop_blocks = int(self.test_drop_blocks)
+        return o
+
+
+def _ptr(a):
+    """(pointer, where) of a numpy array or a CUDA torch tensor."""
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("arrays must be C-contiguous")
+        return ctypes.c_void_p(a.ctypes.data), HOST
+    if hasattr(a, "data_ptr") and hasattr(a, "is_cuda"):
+        if not a.is_contiguous():
+            raise ValueError("tensors must be contiguous")
+        return ctypes.c_void_p(a.data_ptr()), (DEVICE if a.is_cuda else HOST)
+    raise TypeError("expected a numpy array or a torch tensor")
+
+
+def _dtype_code(a):
+    dt = str(a.dtype)
+    if dt in ("float32", "torch.float32"):
+        return F32
+    if dt in ("float64", "torch.float64"):
+        return F64
+    raise TypeError(f"unsupported dtype {dt}")
+
+
+class Context:
+    """One GPU, its stream, buffers and cached sweep-schedule graphs (eikx_ctx)."""
+
+    def __init__(self, device=0):
+        lib = load()
+        h = ctypes.c_void_p()
+        _check(lib.eikx_create(ctypes.byref(h), int(device)))
+        self._h = h
+        self._lib = lib
+        self.grid3 = None
+        self.grid2 = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.eikx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- 3D ---------------------------------------------------------------
+    def set_grid3d(self, nx, ny, nz, dx, dy, dz, x0=0.0, y0=0.0, z0=0.0):
+        _check(self._lib.eikx_set_grid3d(self._h, nx, ny, nz, dx, dy, dz, x0, y0, z0))
+        self.grid3 = (nx, ny, nz, dx, dy, dz, x0, y0, z0)
+
+    def set_slowness3d(self, s, ordering=NATURAL):
+        p, where = _ptr(s)
+        _check(self._lib.eikx_set_slowness3d(self._h, p, _dtype_code(s), ordering, where))
+
+    def set_nodal_velocity3d(self, v, ordering=NATURAL):
+        p, where = _ptr(v)
+        _check(self._lib.eikx_set_nodal_velocity3d(self._h, p, _dtype_code(v), ordering, where))
+
+    def get_slowness3d(self, dtype=np.float64):
+        nx, ny, nz = self.grid3[:3]
+        out = np.empty((nx - 1) * (ny - 1) * (nz - 1), dtype=dtype)
+        _check(self._lib.eikx_get_slowness3d(self._h, ctypes.c_void_p(out.ctypes.data), _dtype_code(out)))
+        return out
+
+    def solve3d(self, sources, options=None, precision=F32, out=None):
+        """Solve one field per source; returns (n_src, nz, ny, nx) (numpy, or `out`)."""
+        src = np.atleast_2d(np.asarray(sources, dtype=np.float64))
+        n = src.shape[0]
+        arr = (_Src3 * n)(*[_Src3(*map(float, s)) for s in src])
+        nx, ny, nz = self.grid3[:3]
+        if out is None:
+            out = np.empty((n, nz, ny, nx), dtype=np.float32 if precision == F32 else np.float64)
+        p, where = _ptr(out)
+        o = (options or Options())._c()
+        _check(self._lib.eikx_solve3d(self._h, arr, n, ctypes.byref(o), precision, p, where))
+        return out
+
+    # ---- 2D ---------------------------------------------------------------
+    def set_grid2d(self, nx, nz, dx, dz, x0=0.0, z0=0.0):
+        _check(self._lib.eikx_set_grid2d(self._h, nx, nz, dx, dz, x0, z0))
+        self.grid2 = (nx, nz, dx, dz, x0, z0)
+
+    def set_slowness2d(self, s, ordering=NATURAL):
+        p, where = _ptr(s)
+        _check(self._lib.eikx_set_slowness2d(self._h, p, _dtype_code(s), ordering, where))
+
+    def set_nodal_velocity2d(self, v, ordering=NATURAL):
+        p, where = _ptr(v)
+        _check(self._lib.eikx_set_nodal_velocity2d(self._h, p, _dtype_code(v), ordering, where))
+
+    def solve2d(self, sources, options=None, precision=F64, out=None):
+        """Solve one field per (x, z) source; returns (n_src, nz, nx)."""
+        src = np.atleast_2d(np.asarray(sources, dtype=np.float64))
+        n = src.shape[0]
+        arr = (_Src2 * n)(*[_Src2(float(s[0]), float(s[1])) for s in src])
+        nx, nz = self.grid2[:2]
+        if out is None:
+            out = np.empty((n, nz, nx), dtype=np.float32 if precision == F32 else np.float64)
+        p, where = _ptr(out)
+        o = (options or Options())._c()
+        _check(self._lib.eikx_solve2d(self._h, arr, n, ctypes.byref(o), precision, p, where))
+        return out
+
+    # ---- analytic (FP64, GPU) -----------------------------------------------
+    def analytic3d(self, source, v_top, v_bottom):
+        nx, ny, nz = self.grid3[:3]
+        out = np.empty((nz, ny, nx), dtype=np.float64)
+        s = _Src3(*map(float, source))
+        _check(self._lib.eikx_analytic3d(self._h, ctypes.byref(s), v_top, v_bottom,
+                                         ctypes.c_void_p(out.ctypes.data), HOST))
+        return out
+
+    def analytic2d(self, source, v_top, v_bottom):
+        nx, nz = self.grid2[:2]
+        out = np.empty((nz, nx), dtype=np.float64)
+        s = _Src2(float(source[0]), float(source[1]))
+        _check(self._lib.eikx_analytic2d(self._h, ctypes.byref(s), v_top, v_bottom,
+                                         ctypes.c_void_p(out.ctypes.data), HOST))
+        return out
+
+    def stats(self):
+        s = _Stats()
+        _check(self._lib.eikx_get_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+
+def graph3d_tables(sweep, nx, ny, nz):
+    """Graph3D<Sweep(sweep+1)> tables (host): dict of numpy int32 arrays."""
+    lib = load()
+    n = nx * ny * nz
+    ls = np.zeros(nx + ny + nz - 1, np.int32)
+    arrs = [np.zeros(n, np.int32) for _ in range(5)]
+    mx = ctypes.c_int(0)
+    P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    nl = lib.eikx_graph3d_tables(sweep, nx, ny, nz, P(ls), *[P(a) for a in arrs], ctypes.byref(mx))
+    if nl < 0:
+        _check(nl)
+    return {"n_levels": nl, "level_start": ls, "node_to_index": arrs[0], "to_x": arrs[1],
+            "to_y": arrs[2], "to_z": arrs[3], "index_to_level": arrs[4], "max_level_size": mx.value}
+
+
+def levels2d(sweep, nx, nz):
+    """2D level-set visiting order (host): (level_start, ix, iz)."""
+    lib = load()
+    ls = np.zeros(nx + nz, np.int32)
+    ix = np.zeros(nx * nz, np.int32)
+    iz = np.zeros(nx * nz, np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    nl = lib.eikx_levels2d(sweep, nx, nz, P(ls), P(ix), P(iz))
+    if nl < 0:
+        _check(nl)
+    return ls, ix, iz

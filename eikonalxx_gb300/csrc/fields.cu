@@ -1,0 +1,370 @@
+// Per-field kernels around the sweeps: source initialisation, model preparation,
+// solve-state reset, the per-iteration convergence check and the analytic fields.
+// All are single-pass and HBM-bound; grids are sized in multiples of the SM count by
+// the caller's grid-stride loops.
+#include "sweep.h"
+#include <cmath>
+
+namespace eikx {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int gridFor(long long n, int threads = kThreads) {
+    long long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 152LL * 32) b = 152LL * 32;
+    return static_cast<int>(b);
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return max(lo, min(hi, v)); }
+
+// Travel-time initialisation (Solver3D::initializeTravelTimes, src/solver3d.cpp:21-84):
+// every node := HUGE, the 8 corners of the source cell := s_src * |x - x_s|, the
+// distance and product evaluated in FP64 (fp64 = 1) or in the field type.
+template <class T>
+__global__ void init3Kernel(T *tt, int nFields, long long fieldStride, int pitch, int nx, int ny,
+                            int nz, double dx, double dy, double dz, const Corner3 *corners, int fp64) {
+    const long long perField = static_cast<long long>(pitch) * ny * nz;
+    const long long n = perField * nFields;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int f = static_cast<int>(i / perField);
+        long long r = i - f * perField;
+        const int ix = static_cast<int>(r % pitch);
+        r /= pitch;
+        const int iy = static_cast<int>(r % ny);
+        const int iz = static_cast<int>(r / ny);
+        const Corner3 cn = corners[f];
+        T v = static_cast<T>(1.e10);
+        if (ix - cn.isx >= 0 && ix - cn.isx <= 1 && iy - cn.isy >= 0 && iy - cn.isy <= 1 &&
+            iz - cn.isz >= 0 && iz - cn.isz <= 1 && ix < nx) {
+            if (fp64) {
+                v = static_cast<T>(analyticT3<double>(ix, iy, iz, dx, dy, dz, cn.xo, cn.yo, cn.zo, cn.s));
+            } else {
+                v = analyticT3<T>(ix, iy, iz, static_cast<T>(dx), static_cast<T>(dy), static_cast<T>(dz),
+                                  static_cast<T>(cn.xo), static_cast<T>(cn.yo), static_cast<T>(cn.zo),
+                                  static_cast<T>(cn.s));
+            }
+        }
+        tt[static_cast<long long>(f) * fieldStride + r * pitch + ix] = v;
+    }
+}
+
+// 2D (Solver2D::initializeTravelTimes, src/solver2d.cpp:61-105).
+template <class T>
+__global__ void init2Kernel(T *tt, int nFields, long long fieldStride, int pitch, int nx, int nz,
+                            double dx, double dz, const Corner3 *corners, int fp64) {
+    const long long perField = static_cast<long long>(pitch) * nz;
+    const long long n = perField * nFields;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int f = static_cast<int>(i / perField);
+        const long long r = i - f * perField;
+        const int ix = static_cast<int>(r % pitch);
+        const int iz = static_cast<int>(r / pitch);
+        const Corner3 cn = corners[f];
+        T v = static_cast<T>(1.e10);
+        if (ix - cn.isx >= 0 && ix - cn.isx <= 1 && iz - cn.isz >= 0 && iz - cn.isz <= 1 && ix < nx) {
+            if (fp64) {
+                v = static_cast<T>(analyticT2<double>(ix, iz, dx, dz, cn.xo, cn.zo, cn.s));
+            } else {
+                v = analyticT2<T>(ix, iz, static_cast<T>(dx), static_cast<T>(dz), static_cast<T>(cn.xo),
+                                  static_cast<T>(cn.zo), static_cast<T>(cn.s));
+            }
+        }
+        tt[static_cast<long long>(f) * fieldStride + static_cast<long long>(iz) * pitch + ix] = v;
+    }
+}
+
+// Edge-replicated slowness: padded cell p holds cell clamp(p - 1) on every axis, so a
+// node i reads padded cells i and i + 1 without the clamps of
+// gridToSurroundingSlownessIndices (solverUtilities3d.hpp:1300-1442).
+template <class T, class U>
+__global__ void pad3Kernel(T *sp, int spPitch, const U *s, int nx, int ny, int nz) {
+    const int ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
+    const long long n = static_cast<long long>(spPitch) * (ny + 1) * (nz + 1);
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int px = static_cast<int>(i % spPitch);
+        const long long r = i / spPitch;
+        const int py = static_cast<int>(r % (ny + 1));
+        const int pz = static_cast<int>(r / (ny + 1));
+        const int cx = clampi(px - 1, 0, ncx - 1), cy = clampi(py - 1, 0, ncy - 1),
+                  cz = clampi(pz - 1, 0, ncz - 1);
+        sp[i] = static_cast<T>(s[(static_cast<long long>(cz) * ncy + cy) * ncx + cx]);
+    }
+}
+
+template <class T, class U>
+__global__ void pad2Kernel(T *sp, int spPitch, const U *s, int nx, int nz) {
+    const int ncx = nx - 1, ncz = nz - 1;
+    const long long n = static_cast<long long>(spPitch) * (nz + 1);
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int px = static_cast<int>(i % spPitch);
+        const int pz = static_cast<int>(i / spPitch);
+        const int cx = clampi(px - 1, 0, ncx - 1), cz = clampi(pz - 1, 0, ncz - 1);
+        sp[i] = static_cast<T>(s[static_cast<long long>(cz) * ncx + cx]);
+    }
+}
+
+// Nodal velocity -> cell slowness = 8 / (sum of the 8 corner velocities), summed in pairs
+// as interpolate3d (src/model3d.cpp:79-137); ordering 1 reads the transposed (XYZ) input.
+template <class U>
+__global__ void nodal3Kernel(double *slow, const U *v, int nx, int ny, int nz, int ordering) {
+    const long long ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
+    const long long n = ncx * ncy * ncz;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long ix = i % ncx, iy = (i / ncx) % ncy, iz = i / (ncx * ncy);
+        long long i1, i3, i5;
+        long long d1, d3, d5;  // strides of +x, +y, +z in the input
+        if (ordering == 0) {
+            d1 = 1; d3 = ncx + 1; d5 = (ncx + 1) * (ncy + 1);
+            i1 = iz * d5 + iy * d3 + ix;
+        } else {
+            d1 = static_cast<long long>(ncz + 1) * (ncy + 1); d3 = ncz + 1; d5 = 1;
+            // the reference's transposed indices: idx1 = ix*(ncz+1)*(ncy+1) + iy*(ncz+1) + iz,
+            // idx2 = idx1 + 1, idx3 = idx1 + (ncz+1), idx5 = idx1 + (ncz+1)*(ncy+1)
+            i1 = ix * d1 + iy * d3 + iz;
+            d1 = 1; d5 = static_cast<long long>(ncz + 1) * (ncy + 1);
+        }
+        i3 = i1 + d3;
+        i5 = i1 + d5;
+        const U sum1 = v[i1] + v[i1 + d1];
+        const U sum2 = v[i3] + v[i3 + d1];
+        const U sum3 = v[i5] + v[i5 + d1];
+        const U sum4 = v[i5 + d3] + v[i5 + d3 + d1];
+        const U eight = 8;
+        slow[i] = static_cast<double>(eight / (sum1 + sum2 + sum3 + sum4));
+    }
+}
+
+template <class U>
+__global__ void nodal2Kernel(double *slow, const U *v, int nx, int nz, int ordering) {
+    const long long ncx = nx - 1, ncz = nz - 1;
+    const long long n = ncx * ncz;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long ix = i % ncx, iz = i / ncx;
+        long long i1, d1, d3;
+        if (ordering == 0) { i1 = iz * (ncx + 1) + ix; d1 = 1; d3 = ncx + 1; }
+        else { i1 = ix * (ncz + 1) + iz; d1 = 1; d3 = ncz + 1; }
+        const U sum1 = v[i1] + v[i1 + d1];
+        const U sum2 = v[i1 + d3] + v[i1 + d3 + d1];
+        const U four = 4;
+        slow[i] = static_cast<double>(four / (sum1 + sum2));
+    }
+}
+
+// Cell values in natural or transposed order -> natural-order slowness (double master).
+// `U` values are slowness already (the caller converts velocities on the host side).
+template <class U>
+__global__ void cells3Kernel(double *slow, const U *c, int nx, int ny, int nz, int ordering) {
+    const long long ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
+    const long long n = ncx * ncy * ncz;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long ix = i % ncx, iy = (i / ncx) % ncy, iz = i / (ncx * ncy);
+        const long long src = ordering == 0 ? i : (ix * ncy + iy) * ncz + iz;
+        slow[i] = static_cast<double>(c[src]);
+    }
+}
+
+template <class U>
+__global__ void cells2Kernel(double *slow, const U *c, int nx, int nz, int ordering) {
+    const long long ncx = nx - 1, ncz = nz - 1;
+    const long long n = ncx * ncz;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long ix = i % ncx, iz = i / ncx;
+        const long long src = ordering == 0 ? i : ix * ncz + iz;
+        slow[i] = static_cast<double>(c[src]);
+    }
+}
+
+__global__ void resetKernel(SolveState st, int nFields, int buf) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gthreads = gridDim.x * blockDim.x;
+    for (int i = gtid; i < st.nProgress; i += gthreads) st.progress[buf][i] = 0u;
+    const long long nres = static_cast<long long>(nFields) * st.residualStride;
+    for (long long i = gtid; i < nres; i += gthreads) st.residual[i] = 0ull;
+    for (int i = gtid; i < nFields; i += gthreads) {
+        st.converged[i] = 0;
+        st.iterations[i] = 0;
+    }
+    if (gtid == 0) {
+        *st.queue[buf] = 0u;
+        *st.abortFlag = 0;
+    }
+}
+
+// After refinement iteration `iteration`: a field whose largest decrease over the
+// iteration's sweeps fell below tol is frozen (later sweeps skip it).
+__global__ void checkKernel(SolveState st, int nFields, int firstSlot, int nSlots, int iteration,
+                            double tol) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nFields; f += gridDim.x * blockDim.x) {
+        if (st.converged[f]) continue;
+        double m = 0;
+        for (int k = 0; k < nSlots; ++k)
+            m = fmax(m, __longlong_as_double(static_cast<long long>(
+                            st.residual[static_cast<long long>(f) * st.residualStride + firstSlot + k])));
+        st.iterations[f] = iteration + 1;
+        if (m < tol) st.converged[f] = 1;
+    }
+}
+
+// Analytic linear-gradient / homogeneous travel times in FP64
+// (src/analytic/linearGradient3d.cpp:12-116, linearGradient2d.cpp:12-124).
+__global__ void analytic3Kernel(double *t, int nx, int ny, int nz, double dx, double dy, double dz,
+                                double xs, double ys, double zs, double vTop, double vBottom) {
+    const double gz = (vBottom - vTop) / ((nz - 1) * dz);
+    const double absG2 = gz * gz;
+    const double absG = sqrt(absG2);
+    const double v0 = vTop + gz * zs;
+    const double s0 = 1 / v0;
+    const bool gradient = fabs(vTop - vBottom) > 1.e-14;
+    const long long n = static_cast<long long>(nx) * ny * nz;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int ix = static_cast<int>(i % nx);
+        const int iy = static_cast<int>((i / nx) % ny);
+        const int iz = static_cast<int>(i / (static_cast<long long>(nx) * ny));
+        if (gradient) {
+            const double ddx = ix * dx - xs, ddy = iy * dy - ys, ddz = iz * dz - zs;
+            const double dist2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            const double vel = v0 + 0 * ddx + 0 * ddy + gz * ddz;
+            const double arg = 1 + (s0 * absG2 * dist2) / (2 * vel);
+            t[i] = acosh(arg) / absG;
+        } else {
+            const double ddx = xs - ix * dx, ddy = ys - iy * dy, ddz = zs - iz * dz;
+            t[i] = sqrt(ddx * ddx + ddy * ddy + ddz * ddz) * s0;
+        }
+    }
+}
+
+__global__ void analytic2Kernel(double *t, int nx, int nz, double dx, double dz, double xs, double zs,
+                                double vTop, double vBottom) {
+    const double gz = (vBottom - vTop) / ((nz - 1) * dz);
+    const double absG2 = gz * gz;
+    const double absG = sqrt(absG2);
+    const double v0 = vTop + gz * zs;
+    const double s0 = 1 / v0;
+    const bool gradient = fabs(vTop - vBottom) > 1.e-14;
+    const long long n = static_cast<long long>(nx) * nz;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int ix = static_cast<int>(i % nx);
+        const int iz = static_cast<int>(i / nx);
+        if (gradient) {
+            const double ddx = ix * dx - xs, ddz = iz * dz - zs;
+            const double dist2 = ddx * ddx + ddz * ddz;
+            const double vel = v0 + 0 * ddx + gz * ddz;
+            const double arg = 1 + (s0 * absG2 * dist2) / (2 * vel);
+            t[i] = acosh(arg) / absG;
+        } else {
+            t[i] = hypot(xs - ix * dx, zs - iz * dz) * s0;
+        }
+    }
+}
+
+}  // namespace
+
+template <class T>
+cudaError_t launchInit3(T *tt, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
+                        double dx, double dy, double dz, const Corner3 *corners, int fp64, cudaStream_t s) {
+    const long long n = static_cast<long long>(pitch) * ny * nz * nFields;
+    init3Kernel<T><<<gridFor(n), kThreads, 0, s>>>(tt, nFields, fieldStride, pitch, nx, ny, nz, dx, dy, dz,
+                                                    corners, fp64);
+    return cudaGetLastError();
+}
+template <class T>
+cudaError_t launchInit2(T *tt, int nFields, long long fieldStride, int pitch, int nx, int nz, double dx,
+                        double dz, const Corner3 *corners, int fp64, cudaStream_t s) {
+    const long long n = static_cast<long long>(pitch) * nz * nFields;
+    init2Kernel<T><<<gridFor(n), kThreads, 0, s>>>(tt, nFields, fieldStride, pitch, nx, nz, dx, dz, corners, fp64);
+    return cudaGetLastError();
+}
+template <class T, class U>
+cudaError_t launchPadSlowness3(T *sp, int spPitch, const U *s, int nx, int ny, int nz, cudaStream_t st) {
+    const long long n = static_cast<long long>(spPitch) * (ny + 1) * (nz + 1);
+    pad3Kernel<T, U><<<gridFor(n), kThreads, 0, st>>>(sp, spPitch, s, nx, ny, nz);
+    return cudaGetLastError();
+}
+template <class T, class U>
+cudaError_t launchPadSlowness2(T *sp, int spPitch, const U *s, int nx, int nz, cudaStream_t st) {
+    const long long n = static_cast<long long>(spPitch) * (nz + 1);
+    pad2Kernel<T, U><<<gridFor(n), kThreads, 0, st>>>(sp, spPitch, s, nx, nz);
+    return cudaGetLastError();
+}
+template <class U>
+cudaError_t launchNodalToCell3(double *slow, const U *v, int nx, int ny, int nz, int ordering, cudaStream_t s) {
+    const long long n = static_cast<long long>(nx - 1) * (ny - 1) * (nz - 1);
+    nodal3Kernel<U><<<gridFor(n), kThreads, 0, s>>>(slow, v, nx, ny, nz, ordering);
+    return cudaGetLastError();
+}
+template <class U>
+cudaError_t launchNodalToCell2(double *slow, const U *v, int nx, int nz, int ordering, cudaStream_t s) {
+    const long long n = static_cast<long long>(nx - 1) * (nz - 1);
+    nodal2Kernel<U><<<gridFor(n), kThreads, 0, s>>>(slow, v, nx, nz, ordering);
+    return cudaGetLastError();
+}
+template <class U>
+cudaError_t launchCellsToNatural3(double *slow, const U *c, int nx, int ny, int nz, int ordering, cudaStream_t s) {
+    const long long n = static_cast<long long>(nx - 1) * (ny - 1) * (nz - 1);
+    cells3Kernel<U><<<gridFor(n), kThreads, 0, s>>>(slow, c, nx, ny, nz, ordering);
+    return cudaGetLastError();
+}
+template <class U>
+cudaError_t launchCellsToNatural2(double *slow, const U *c, int nx, int nz, int ordering, cudaStream_t s) {
+    const long long n = static_cast<long long>(nx - 1) * (nz - 1);
+    cells2Kernel<U><<<gridFor(n), kThreads, 0, s>>>(slow, c, nx, nz, ordering);
+    return cudaGetLastError();
+}
+cudaError_t launchResetState(const SolveState &st, int nFields, int progressBuf, cudaStream_t s) {
+    resetKernel<<<gridFor(st.nProgress + static_cast<long long>(nFields) * st.residualStride), kThreads, 0, s>>>(
+        st, nFields, progressBuf);
+    return cudaGetLastError();
+}
+cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots, int iteration,
+                                   double tol, cudaStream_t s) {
+    checkKernel<<<gridFor(nFields, 128), 128, 0, s>>>(st, nFields, firstSlot, nSlots, iteration, tol);
+    return cudaGetLastError();
+}
+cudaError_t launchAnalytic3(double *t, int nx, int ny, int nz, double dx, double dy, double dz, double xs,
+                            double ys, double zs, double vTop, double vBottom, cudaStream_t s) {
+    const long long n = static_cast<long long>(nx) * ny * nz;
+    analytic3Kernel<<<gridFor(n), kThreads, 0, s>>>(t, nx, ny, nz, dx, dy, dz, xs, ys, zs, vTop, vBottom);
+    return cudaGetLastError();
+}
+cudaError_t launchAnalytic2(double *t, int nx, int nz, double dx, double dz, double xs, double zs, double vTop,
+                            double vBottom, cudaStream_t s) {
+    const long long n = static_cast<long long>(nx) * nz;
+    analytic2Kernel<<<gridFor(n), kThreads, 0, s>>>(t, nx, nz, dx, dz, xs, zs, vTop, vBottom);
+    return cudaGetLastError();
+}
+
+template cudaError_t launchInit3<float>(float *, int, long long, int, int, int, int, double, double, double,
+                                        const Corner3 *, int, cudaStream_t);
+template cudaError_t launchInit3<double>(double *, int, long long, int, int, int, int, double, double, double,
+                                         const Corner3 *, int, cudaStream_t);
+template cudaError_t launchInit2<float>(float *, int, long long, int, int, int, double, double, const Corner3 *,
+                                        int, cudaStream_t);
+template cudaError_t launchInit2<double>(double *, int, long long, int, int, int, double, double,
+                                         const Corner3 *, int, cudaStream_t);
+template cudaError_t launchPadSlowness3<float, double>(float *, int, const double *, int, int, int, cudaStream_t);
+template cudaError_t launchPadSlowness3<double, double>(double *, int, const double *, int, int, int, cudaStream_t);
+template cudaError_t launchPadSlowness2<float, double>(float *, int, const double *, int, int, cudaStream_t);
+template cudaError_t launchPadSlowness2<double, double>(double *, int, const double *, int, int, cudaStream_t);
+template cudaError_t launchNodalToCell3<float>(double *, const float *, int, int, int, int, cudaStream_t);
+template cudaError_t launchNodalToCell3<double>(double *, const double *, int, int, int, int, cudaStream_t);
+template cudaError_t launchNodalToCell2<float>(double *, const float *, int, int, int, cudaStream_t);
+template cudaError_t launchNodalToCell2<double>(double *, const double *, int, int, int, cudaStream_t);
+template cudaError_t launchCellsToNatural3<float>(double *, const float *, int, int, int, int, cudaStream_t);
+template cudaError_t launchCellsToNatural3<double>(double *, const double *, int, int, int, int, cudaStream_t);
+template cudaError_t launchCellsToNatural2<float>(double *, const float *, int, int, int, cudaStream_t);
+template cudaError_t launchCellsToNatural2<double>(double *, const double *, int, int, int, cudaStream_t);
+
+}  // namespace eikx

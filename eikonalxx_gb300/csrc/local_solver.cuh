@@ -1,0 +1,525 @@
+// Upwind local solvers of the eikonal equation, device side.
+//
+// These evaluate the same operators, in the same floating-point operation order, as
+// the reference's finiteDifference functions:
+//   3D uniform      include/private/solverUtilities3d.hpp:258-558
+//   3D non-uniform  include/private/solverUtilities3d.hpp:562-824
+//   2D uniform      include/private/solverUtilities2d.hpp:347-472
+//   2D non-uniform  include/private/solverUtilities2d.hpp:474-614
+// The translation unit is compiled with --fmad=false, -prec-sqrt=true and
+// -prec-div=true, so each operation rounds exactly as the CPU code (IEEE binary32 /
+// binary64, correctly rounded sqrt and division, no contraction) and a sweep
+// reproduces the reference's travel times bit for bit.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace eikx {
+
+template <class T> __device__ __forceinline__ T dmin(T a, T b);
+template <> __device__ __forceinline__ float dmin(float a, float b) { return fminf(a, b); }
+template <> __device__ __forceinline__ double dmin(double a, double b) { return fmin(a, b); }
+template <class T> __device__ __forceinline__ T dmax(T a, T b);
+template <> __device__ __forceinline__ float dmax(float a, float b) { return fmaxf(a, b); }
+template <> __device__ __forceinline__ double dmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float dsqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
+
+// Per-sweep constants (getSweepFiniteDifferenceSigns, solverUtilities3d.hpp:843-925
+// and solverUtilities2d.hpp:888-926): a flipped axis is swept in decreasing order,
+// its analytic-time shift is +1 and its derivative sign -1.
+struct SweepSigns {
+    int ixShift, iyShift, izShift;
+    int signX, signY, signZ;
+};
+
+// Source description as the sweep objects hold it (Solver3DSweep::setSourceInformation,
+// include/private/solver3d.hpp:131-144): source cell, offsets from the origin and the
+// source-cell slowness, all in the sweep's type.
+template <class T> struct SourceT {
+    int isx, isy, isz;
+    T xs, ys, zs;
+    T sSrc;
+};
+
+// Analytic homogeneous time and gradient (computeAnalyticalTravelTime,
+// solverUtilities3d.hpp:138-208).
+template <class T>
+__device__ __forceinline__ T analyticT3(int ix, int iy, int iz, T dx, T dy, T dz, T xs, T ys,
+                                        T zs, T s) {
+    T x = ix * dx, y = iy * dy, z = iz * dz;
+    T ddx = x - xs, ddy = y - ys, ddz = z - zs;
+    T dist = dsqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+    return s * dist;
+}
+template <class T>
+__device__ __forceinline__ void analyticTG3(int ix, int iy, int iz, T dx, T dy, T dz, T xs,
+                                            T ys, T zs, T s, T &t, T &gx, T &gy, T &gz) {
+    T x = ix * dx, y = iy * dy, z = iz * dz;
+    T ddx = x - xs, ddy = y - ys, ddz = z - zs;
+    T dist = dsqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+    t = s * dist;
+    gx = 0; gy = 0; gz = 0;
+    if (dist > 0) {
+        gx = (s * ddx) / dist;
+        gy = (s * ddy) / dist;
+        gz = (s * ddz) / dist;
+    }
+}
+
+// The neighbour naming of the reference's 3D stencil (gridToSurroundingTravelTimeIndices,
+// solverUtilities3d.hpp:1460-1586; gridToSurroundingSlownessIndices, :1300-1442), with
+// "up" = one step against the sweep direction along an axis:
+//   t1 = x-up, t2 = x-up,y-up, t3 = y-up, t4 = z-up, t5 = x-up,z-up, t6 = all up,
+//   t7 = y-up,z-up;  s0 = home cell, s1 = x-neighbour cell, s2 = x,y, s3 = y, s4 = z,
+//   s5 = x,z, s7 = y,z.
+template <class T> struct Stencil3 {
+    T s0, s1, s2, s3, s4, s5, s7;
+    T t1, t2, t3, t4, t5, t6, t7;
+};
+
+// 3D uniform-grid update (solverUtilities3d.hpp:258-558).  The factored branch is the
+// reference's as shipped: T0 built from the home-cell slowness s0.
+template <class T>
+__device__ __forceinline__ T fd3Uniform(int radius, T h, const SourceT<T> &src,
+                                        const SweepSigns &sg, int ix, int iy, int iz,
+                                        const Stencil3<T> &n) {
+    const T huge = static_cast<T>(1.e10);
+    const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7;
+    const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7;
+    T tUpd;
+    T minS0S3 = dmin(s0, s3);
+    T minS0S1 = dmin(s0, s1);
+    T minS0S4 = dmin(s0, s4);
+    T t1d1 = t1 + h * dmin(minS0S3, dmin(s4, s7));
+    T t1d2 = t3 + h * dmin(minS0S4, dmin(s1, s5));
+    T t1d3 = t4 + h * dmin(minS0S1, dmin(s2, s3));
+    T t1d = dmin(dmin(t1d1, t1d2), t1d3);
+    T hs03 = h * minS0S3;
+    T hs01 = h * minS0S1;
+    T hs04 = h * minS0S4;
+    if (abs(src.isx - ix) > radius || abs(src.isy - iy) > radius || abs(src.isz - iz) > radius) {
+        // 2D critically refracted (diagonal) operators in the XZ, YZ and XY planes
+        T dXZ = t1 - t4;
+        T detXZ = 2 * (hs03 * hs03) - dXZ * dXZ;
+        T t2d = huge;
+        if (detXZ > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03) t2d = t5 + dsqrt(detXZ);
+        T dYZ = t3 - t4;
+        T detYZ = 2 * (hs01 * hs01) - dYZ * dYZ;
+        T t2d2 = huge;
+        if (detYZ > 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01) t2d2 = t7 + dsqrt(detYZ);
+        t2d = dmin(t2d, t2d2);
+        T dXY = t1 - t3;
+        T detXY = 2 * (hs04 * hs04) - dXY * dXY;
+        T t2d3 = huge;
+        if (detXY > 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04) t2d3 = t2 + dsqrt(detXY);
+        t2d = dmin(t2d, t2d3);
+        // 8-point operator, taken only when the wave travels the sweep's way
+        T t3d = huge;
+        if (dmin(t1d, t2d) > dmax(dmax(t1, t4), t3)) {
+            const T third = static_cast<T>(0.33333333333333333333333);
+            const T half = static_cast<T>(0.5);
+            T Tx = t1 + half * (-t4 + t5 - t3 + t2) - t7 + t6;
+            T Ty = t3 + half * (-t4 + t7 - t1 + t2) - t5 + t6;
+            T Tz = t4 + half * (-t1 + t5 - t3 + t7) - t2 + t6;
+            T det = 27 * (h * s0) * (h * s0) - (Tx - Ty) * (Tx - Ty) - (Tx - Tz) * (Tx - Tz) -
+                    (Ty - Tz) * (Ty - Tz);
+            if (det >= 0) t3d = third * ((Tx + Ty + Tz) + dsqrt(det));
+        }
+        tUpd = dmin(t1d, dmin(t2d, t3d));
+    } else {
+        const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
+        T t0, dt0dx, dt0dy, dt0dz;
+        analyticTG3(ix, iy, iz, h, h, h, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
+        const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
+        T tau1 = t1 - analyticT3(xu, iy, iz, h, h, h, xs, ys, zs, s0);
+        T tau2 = t2 - analyticT3(xu, yu, iz, h, h, h, xs, ys, zs, s0);
+        T tau3 = t3 - analyticT3(ix, yu, iz, h, h, h, xs, ys, zs, s0);
+        T tau4 = t4 - analyticT3(ix, iy, zu, h, h, h, xs, ys, zs, s0);
+        T tau5 = t5 - analyticT3(xu, iy, zu, h, h, h, xs, ys, zs, s0);
+        T tau6 = t6 - analyticT3(xu, yu, zu, h, h, h, xs, ys, zs, s0);
+        T tau7 = t7 - analyticT3(ix, yu, zu, h, h, h, xs, ys, zs, s0);
+        dt0dx = sg.signX * dt0dx;
+        dt0dy = sg.signY * dt0dy;
+        dt0dz = sg.signZ * dt0dz;
+        const T half = static_cast<T>(0.5);
+        T hi = 1 / h;
+        T h2inv = 1 / (h * h);
+        T a = h2inv;
+        T pXZ = tau1 - tau4 + tau5;
+        T qXZ = tau4 - tau1 + tau5;
+        T b = (2 * hi) * (dt0dx + dt0dz) - (2 * h2inv) * tau5;
+        T c = (half * h2inv) * (pXZ * pXZ + qXZ * qXZ) - (2 * hi) * (dt0dx * pXZ + dt0dz * qXZ) +
+              2 * (sSrc * sSrc - s0 * s0 + dt0dy * dt0dy);
+        T det = b * b - 4 * a * c;
+        T t2d = huge;
+        if (det > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03) {
+            t2d = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (t2d < t1 || t2d < t4) t2d = huge;
+        }
+        T pYZ = tau3 - tau4 + tau7;
+        T qYZ = tau4 - tau3 + tau7;
+        b = (2 * hi) * (dt0dy + dt0dz) - (2 * h2inv) * tau7;
+        c = (half * h2inv) * (pYZ * pYZ + qYZ * qYZ) - (2 * hi) * (dt0dy * pYZ + dt0dz * qYZ) +
+            2 * (sSrc * sSrc - s0 * s0 + dt0dx * dt0dx);
+        det = b * b - 4 * a * c;
+        T t2d2 = huge;
+        if (det >= 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01) {
+            t2d2 = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (t2d2 < t3 || t2d2 < t4) t2d2 = huge;
+        }
+        t2d = dmin(t2d, t2d2);
+        T pXY = tau1 - tau3 + tau2;
+        T qXY = tau3 - tau1 + tau2;
+        b = (2 * hi) * (dt0dx + dt0dy) - (2 * h2inv) * tau2;
+        c = (half * h2inv) * (pXY * pXY + qXY * qXY) - (2 * hi) * (dt0dx * pXY + dt0dy * qXY) +
+            2 * (sSrc * sSrc - s0 * s0 + dt0dz * dt0dz);
+        det = b * b - 4 * a * c;
+        T t2d3 = huge;
+        if (det >= 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04) {
+            t2d3 = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (t2d3 < t1 || t2d3 < t3) t2d3 = huge;
+        }
+        t2d = dmin(t2d, t2d3);
+        T t3d = huge;
+        if (dmin(t1d, t2d) > dmax(dmax(t1, t4), t3)) {
+            T taux = tau1 + half * (-tau4 + tau5 - tau3 + tau2) - tau7 + tau6;
+            T tauy = tau3 + half * (-tau4 + tau7 - tau1 + tau2) - tau5 + tau6;
+            T tauz = tau4 + half * (-tau1 + tau5 - tau3 + tau7) - tau2 + tau6;
+            a = 3 * h2inv;
+            b = -2 * h2inv * (taux + tauy + tauz) + (6 * hi) * (dt0dx + dt0dy + dt0dz);
+            c = h2inv * (taux * taux + tauy * tauy + tauz * tauz) -
+                (6 * hi) * (dt0dx * taux + dt0dy * tauy + dt0dz * tauz) + 9 * (sSrc * sSrc - s0 * s0);
+            det = b * b - 4 * a * c;
+            if (det >= 0) t3d = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (t3d < t1 || t3d < t3 || t3d < t4) t3d = huge;
+        }
+        tUpd = dmin(t1d, dmin(t2d, t3d));
+    }
+    return tUpd;
+}
+
+// Grid constants of the non-uniform 3D solver (include/private/solver3d.hpp:247-261),
+// computed on the host in the field type and passed by value.
+template <class T> struct Spacing3 {
+    T dx, dy, dz, dxInv, dyInv, dzInv, dx2Inv, dy2Inv, dz2Inv;
+    T dx_dz, dz_dx, dy_dz, dz_dy, dx_dy, dy_dx;
+    T dx2_p_dz2_inv, dy2_p_dz2_inv, dx2_p_dy2_inv;
+};
+
+// 3D non-uniform update (solverUtilities3d.hpp:562-824).
+template <class T>
+__device__ __forceinline__ T fd3NonUniform(int radius, const Spacing3<T> &g, const SourceT<T> &src,
+                                           const SweepSigns &sg, int ix, int iy, int iz,
+                                           const Stencil3<T> &n) {
+    const T huge = static_cast<T>(1.e10);
+    const T dx = g.dx, dy = g.dy, dz = g.dz;
+    const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7;
+    const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7;
+    T tUpd;
+    T minS0S3 = dmin(s0, s3);
+    T minS0S1 = dmin(s0, s1);
+    T minS0S4 = dmin(s0, s4);
+    T t1d1 = t1 + dx * dmin(minS0S3, dmin(s4, s7));
+    T t1d2 = t3 + dy * dmin(minS0S4, dmin(s1, s5));
+    T t1d3 = t4 + dz * dmin(minS0S1, dmin(s2, s3));
+    T t1d = dmin(dmin(t1d1, t1d2), t1d3);
+    if (abs(src.isx - ix) > radius || abs(src.isy - iy) > radius || abs(src.isz - iz) > radius) {
+        T dXZ = t1 - t4;
+        T detXZ = (dx * dx + dz * dz) * (minS0S3 * minS0S3) - dXZ * dXZ;
+        T t2d = huge;
+        if (detXZ > 0 && t1 < t4 + dz * minS0S3 && t4 < t1 + dx * minS0S3) {
+            T TxXZ = t1 - t4 + t5;
+            T TzXZ = t4 - t1 + t5;
+            t2d = (TxXZ * g.dz_dx + TzXZ * g.dx_dz) + 2 * dsqrt(detXZ);
+            t2d = ((dx * dz) * g.dx2_p_dz2_inv) * t2d;
+        }
+        T dYZ = t3 - t4;
+        T detYZ = (dy * dy + dz * dz) * (minS0S1 * minS0S1) - dYZ * dYZ;
+        T t2d2 = huge;
+        if (detYZ > 0 && t3 < t4 + dz * minS0S1 && t4 < t3 + dy * minS0S1) {
+            T TyYZ = t3 - t4 + t7;
+            T TzYZ = t4 - t3 + t7;
+            t2d2 = (TyYZ * g.dz_dy + TzYZ * g.dy_dz) + 2 * dsqrt(detYZ);
+            t2d2 = ((dy * dz) * g.dy2_p_dz2_inv) * t2d2;
+        }
+        t2d = dmin(t2d, t2d2);
+        T dXY = t1 - t3;
+        T detXY = (dx * dx + dy * dy) * (minS0S4 * minS0S4) - dXY * dXY;
+        T t2d3 = huge;
+        if (detXY > 0 && t3 < t1 + dx * minS0S4 && t1 < t3 + dy * minS0S4) {
+            T TxXY = t1 - t3 + t2;
+            T TyXY = t3 - t1 + t2;
+            t2d3 = (TxXY * g.dy_dx + TyXY * g.dx_dy) + 2 * dsqrt(detXY);
+            t2d3 = ((dx * dy) * g.dx2_p_dy2_inv) * t2d3;
+        }
+        t2d = dmin(t2d, t2d3);
+        T t3d = huge;
+        if (dmin(t1d, t2d) > dmax(dmax(t1, t4), t3)) {
+            const T half = static_cast<T>(0.5);
+            T Tx = t1 + half * (-t4 + t5 - t3 + t2) - t7 + t6;
+            T Ty = t3 + half * (-t4 + t7 - t1 + t2) - t5 + t6;
+            T Tz = t4 + half * (-t1 + t5 - t3 + t7) - t2 + t6;
+            T det = 9 * (s0 * s0) * (g.dx2Inv + g.dy2Inv + g.dz2Inv) -
+                    ((Tx - Tz) * (Tx - Tz)) * (g.dx2Inv * g.dz2Inv) -
+                    ((Ty - Tz) * (Ty - Tz)) * (g.dy2Inv * g.dz2Inv) -
+                    ((Tx - Ty) * (Tx - Ty)) * (g.dx2Inv * g.dy2Inv);
+            if (det >= 0)
+                t3d = (Tx * g.dx2Inv + Ty * g.dy2Inv + Tz * g.dz2Inv + dsqrt(det)) /
+                      (g.dx2Inv + g.dy2Inv + g.dz2Inv);
+        }
+        tUpd = dmin(t1d, dmin(t2d, t3d));
+    } else {
+        const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
+        T t0, dt0dx, dt0dy, dt0dz;
+        analyticTG3(ix, iy, iz, dx, dy, dz, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
+        const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
+        T tau1 = t1 - analyticT3(xu, iy, iz, dx, dy, dz, xs, ys, zs, s0);
+        T tau2 = t2 - analyticT3(xu, yu, iz, dx, dy, dz, xs, ys, zs, s0);
+        T tau3 = t3 - analyticT3(ix, yu, iz, dx, dy, dz, xs, ys, zs, s0);
+        T tau4 = t4 - analyticT3(ix, iy, zu, dx, dy, dz, xs, ys, zs, s0);
+        T tau5 = t5 - analyticT3(xu, iy, zu, dx, dy, dz, xs, ys, zs, s0);
+        T tau6 = t6 - analyticT3(xu, yu, zu, dx, dy, dz, xs, ys, zs, s0);
+        T tau7 = t7 - analyticT3(ix, yu, zu, dx, dy, dz, xs, ys, zs, s0);
+        dt0dx = sg.signX * dt0dx;
+        dt0dy = sg.signY * dt0dy;
+        dt0dz = sg.signZ * dt0dz;
+        const T dxInv = g.dxInv, dyInv = g.dyInv, dzInv = g.dzInv;
+        const T dx2Inv = g.dx2Inv, dy2Inv = g.dy2Inv, dz2Inv = g.dz2Inv;
+        T p = tau1 - tau4 + tau5;
+        T q = tau4 - tau1 + tau5;
+        T a = dx2Inv + dz2Inv;
+        T b = 4 * (dxInv * dt0dx + dzInv * dt0dz) - 2 * (p * dx2Inv + q * dz2Inv);
+        T c = (p * p) * dx2Inv + (q * q) * dz2Inv - 4 * ((dt0dx * p) * dxInv + (dt0dz * q) * dzInv) +
+              4 * (sSrc * sSrc - s0 * s0 + dt0dy * dt0dy);
+        T det = b * b - 4 * a * c;
+        T t2d = huge;
+        if (det > 0 && t1 < t4 + dz * minS0S3 && t4 < t1 + dx * minS0S3) {
+            t2d = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (t2d < t1 || t2d < t4) t2d = huge;
+        }
+        p = tau3 - tau4 + tau7;
+        q = tau4 - tau3 + tau7;
+        a = dy2Inv + dz2Inv;
+        b = 4 * (dyInv * dt0dy + dzInv * dt0dz) - 2 * (p * dy2Inv + q * dz2Inv);
+        c = (p * p) * dy2Inv + (q * q) * dz2Inv - 4 * ((dt0dy * p) * dyInv + (dt0dz * q) * dzInv) +
+            4 * (sSrc * sSrc - s0 * s0 + dt0dx * dt0dx);
+        det = b * b - 4 * a * c;
+        T t2d2 = huge;
+        if (det > 0 && t3 < t4 + dz * minS0S1 && t4 < t3 + dy * minS0S1) {
+            t2d2 = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (t2d2 < t3 || t2d2 < t4) t2d2 = huge;
+        }
+        t2d = dmin(t2d, t2d2);
+        p = tau1 - tau3 + tau2;
+        q = tau3 - tau1 + tau2;
+        a = dx2Inv + dy2Inv;
+        b = 4 * (dxInv * dt0dx + dyInv * dt0dy) - 2 * (p * dx2Inv + q * dy2Inv);
+        c = (p * p) * dx2Inv + (q * q) * dy2Inv - 4 * ((dt0dx * p) * dxInv + (dt0dy * q) * dyInv) +
+            4 * (sSrc * sSrc - s0 * s0 + dt0dz * dt0dz);
+        det = b * b - 4 * a * c;
+        T t2d3 = huge;
+        if (det > 0 && t3 < t1 + dx * minS0S4 && t1 < t3 + dy * minS0S4) {
+            t2d3 = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (t2d3 < t1 || t2d3 < t3) t2d3 = huge;
+        }
+        t2d = dmin(t2d, t2d3);
+        T t3d = huge;
+        if (dmin(t1d, t2d) > dmax(dmax(t1, t4), t3)) {
+            const T half = static_cast<T>(0.5);
+            T taux = tau1 + half * (-tau4 + tau5 - tau3 + tau2) - tau7 + tau6;
+            T tauy = tau3 + half * (-tau4 + tau7 - tau1 + tau2) - tau5 + tau6;
+            T tauz = tau4 + half * (-tau1 + tau5 - tau3 + tau7) - tau2 + tau6;
+            a = dx2Inv + dy2Inv + dz2Inv;
+            b = -2 * (taux * dx2Inv + tauy * dy2Inv + tauz * dz2Inv) +
+                6 * (dxInv * dt0dx + dyInv * dt0dy + dzInv * dt0dz);
+            c = (taux * taux) * dx2Inv + (tauy * tauy) * dy2Inv + (tauz * tauz) * dz2Inv -
+                6 * (dt0dx * taux * dxInv + dt0dy * tauy * dyInv + dt0dz * tauz * dzInv) +
+                9 * (sSrc * sSrc - s0 * s0);
+            det = b * b - 4 * a * c;
+            if (det >= 0) t3d = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (t3d < t1 || t3d < t3 || t3d < t4) t3d = huge;
+        }
+        tUpd = dmin(t1d, dmin(t2d, t3d));
+    }
+    return tUpd;
+}
+
+// ---------------------------------------------------------------------------- 2D
+
+// hypot by Borges, "An Improved Algorithm for hypot(a,b)", arXiv:1904.09481 (2019),
+// fused correction step; the oracle uses the same steps so both sides round alike.
+__device__ __forceinline__ double eikxHypot(double a, double b) {
+    a = fabs(a); b = fabs(b);
+    if (a < b) { double t = a; a = b; b = t; }
+    if (b == 0) return a;
+    double h = sqrt(fma(a, a, b * b));
+    double h2 = h * h;
+    double a2 = a * a;
+    double x = fma(-b, b, h2 - a2) + fma(h, h, -h2) - fma(a, a, -a2);
+    return h - x / (2 * h);
+}
+__device__ __forceinline__ float eikxHypot(float a, float b) {
+    double da = a, db = b;
+    return static_cast<float>(sqrt(da * da + db * db));
+}
+
+template <class T>
+__device__ __forceinline__ T analyticT2(int ix, int iz, T dx, T dz, T xs, T zs, T s) {
+    T x = ix * dx, z = iz * dz;
+    T ddx = x - xs, ddz = z - zs;
+    return s * eikxHypot(ddx, ddz);
+}
+template <class T>
+__device__ __forceinline__ void analyticTG2(int ix, int iz, T dx, T dz, T xs, T zs, T s, T &t,
+                                            T &gx, T &gz) {
+    T x = ix * dx, z = iz * dz;
+    T ddx = x - xs, ddz = z - zs;
+    T dist = eikxHypot(ddx, ddz);
+    t = s * dist;
+    gx = 0; gz = 0;
+    if (dist > 0) {
+        gx = (s * ddx) / dist;
+        gz = (s * ddz) / dist;
+    }
+}
+
+// 2D grid constants (include/private/solver2d.hpp:41-46), host-computed.
+template <class T> struct Spacing2 {
+    T dx, dz, dx_dz, dz_dx, cosTheta, sinTheta;
+};
+
+// 2D uniform update (solverUtilities2d.hpp:347-472).  t1 = x-up, t2 = diagonal,
+// t3 = z-up; s0 home cell, s1 x-neighbour cell, s3 z-neighbour cell.
+template <class T>
+__device__ __forceinline__ T fd2Uniform(int radius, T h, const SourceT<T> &src,
+                                        const SweepSigns &sg, int ix, int iz, T s0, T s1, T s3,
+                                        T t1, T t2, T t3) {
+    const T huge = static_cast<T>(1.e10);
+    const T sqrt1_2 = static_cast<T>(0.70710678118654752440);
+    T tUpd;
+    T t0x = t1 + h * dmin(s0, s3);
+    T t0z = t3 + h * dmin(s0, s1);
+    T t0Update1 = dmin(t0x, t0z);
+    T hs0 = h * s0;
+    T dTx = t3 - t2;
+    T dTz = t1 - t2;
+    T sx = sqrt1_2 * s0;
+    T sz = sqrt1_2 * s0;
+    if (abs(src.isx - ix) > radius || abs(src.isz - iz) > radius) {
+        T t0a = huge;
+        T deta = hs0 * hs0 - dTz * dTz;
+        if (dTz >= 0 && deta >= 0 && dTz <= h * sz) t0a = t1 + h * dsqrt(deta);
+        T t0b = huge;
+        T detb = hs0 * hs0 - dTx * dTx;
+        if (dTx >= 0 && detb >= 0 && dTx <= h * sx) t0b = t3 + h * dsqrt(detb);
+        T t0Update2 = dmin(t0a, t0b);
+        T dtCross = t1 - t3;
+        T detc = 2 * (hs0 * hs0) - dtCross * dtCross;
+        T t0Update3 = huge;
+        if (dTx >= 0 && dTz >= 0 && detc > 0 && t3 <= t1 + hs0 && t1 <= t3 + hs0)
+            t0Update3 = t2 + dsqrt(detc);
+        tUpd = dmin(dmin(t0Update1, t0Update2), t0Update3);
+    } else {
+        T t0Update3 = huge;
+        if (dTx >= 0 && dTz >= 0 && t1 < t3 + hs0 && t3 < t1 + hs0) {
+            const T sSrc = src.sSrc;
+            T dt0dx, dt0dz, t0;
+            analyticTG2(ix, iz, h, h, src.xs, src.zs, sSrc, t0, dt0dx, dt0dz);
+            T tau1 = t1 - analyticT2(ix + sg.ixShift, iz, h, h, src.xs, src.zs, sSrc);
+            T tau2 = t2 - analyticT2(ix + sg.ixShift, iz + sg.izShift, h, h, src.xs, src.zs, sSrc);
+            T tau3 = t3 - analyticT2(ix, iz + sg.izShift, h, h, src.xs, src.zs, sSrc);
+            dt0dx = sg.signX * dt0dx;
+            dt0dz = sg.signZ * dt0dz;
+            T tauX = tau1 - tau3 + tau2;
+            T tauZ = tau3 - tau1 + tau2;
+            const T one = 1, two = 2, four = 4;
+            T h2 = h * h;
+            T a = one / h2;
+            T b = two / h * (dt0dx + dt0dz) - two / h2 * tau2;
+            T c = one / (two * h2) * (tauX * tauX + tauZ * tauZ) -
+                  two / h * (dt0dx * tauX + dt0dz * tauZ) + two * (sSrc * sSrc - s0 * s0);
+            T det = b * b - four * a * c;
+            if (det >= 0) {
+                T tau = (-b + dsqrt(det)) / (two * a);
+                t0Update3 = t0 + tau;
+            }
+            if (t0Update3 < t1 || t0Update3 < t3) t0Update3 = huge;
+        }
+        tUpd = dmin(t0Update1, t0Update3);
+    }
+    return tUpd;
+}
+
+// 2D non-uniform update (solverUtilities2d.hpp:474-614).
+template <class T>
+__device__ __forceinline__ T fd2NonUniform(int radius, const Spacing2<T> &g, const SourceT<T> &src,
+                                           const SweepSigns &sg, int ix, int iz, T s0, T s1, T s3,
+                                           T t1, T t2, T t3) {
+    const T huge = static_cast<T>(1.e10);
+    const T dx = g.dx, dz = g.dz;
+    T tUpd;
+    T t0x = t1 + dx * dmin(s0, s3);
+    T t0z = t3 + dz * dmin(s0, s1);
+    T t0Update1 = dmin(t0x, t0z);
+    T dTx = t3 - t2;
+    T dTz = t1 - t2;
+    T sx = g.cosTheta * s0;
+    T sz = g.sinTheta * s0;
+    T hxs0 = dx * s0;
+    T hzs0 = dz * s0;
+    if (abs(src.isx - ix) > radius || abs(src.isz - iz) > radius) {
+        T t0a = huge;
+        T deta = hzs0 * hzs0 - dTz * dTz;
+        if (dTz >= 0 && deta >= 0 && dTz <= dz * sz) t0a = t1 + g.dx_dz * dsqrt(deta);
+        T t0b = huge;
+        T detb = hxs0 * hxs0 - dTx * dTx;
+        if (dTx >= 0 && detb >= 0 && dTx <= dx * sx) t0b = t3 + g.dz_dx * dsqrt(detb);
+        T t0Update2 = dmin(t0a, t0b);
+        T dxdz = g.cosTheta * g.sinTheta;
+        T tildeTx = t1 - t3 + t2;
+        T tildeTz = t3 - t1 + t2;
+        T dtCross = t1 - t3;
+        T detc = hxs0 * hxs0 + hzs0 * hzs0 - dtCross * dtCross;
+        T t0Update3 = huge;
+        if (dTx >= 0 && dTz >= 0 && detc > 0 && t1 < t3 + hzs0 && t3 < t1 + hxs0) {
+            t0Update3 = tildeTx * g.dz_dx + tildeTz * g.dx_dz + 2 * dsqrt(detc);
+            t0Update3 = dxdz * t0Update3;
+        }
+        if (t0Update3 < 0) t0Update3 = huge;
+        tUpd = dmin(dmin(t0Update1, t0Update2), t0Update3);
+    } else {
+        T t0Update3 = huge;
+        if (dTx >= 0 && dTz >= 0 && t1 < t3 + hzs0 && t3 < t1 + hxs0) {
+            const T sSrc = src.sSrc;
+            T dt0dx, dt0dz, t0;
+            analyticTG2(ix, iz, dx, dz, src.xs, src.zs, sSrc, t0, dt0dx, dt0dz);
+            T tau1 = t1 - analyticT2(ix + sg.ixShift, iz, dx, dz, src.xs, src.zs, sSrc);
+            T tau2 = t2 - analyticT2(ix + sg.ixShift, iz + sg.izShift, dx, dz, src.xs, src.zs, sSrc);
+            T tau3 = t3 - analyticT2(ix, iz + sg.izShift, dx, dz, src.xs, src.zs, sSrc);
+            dt0dx = sg.signX * dt0dx;
+            dt0dz = sg.signZ * dt0dz;
+            T tauX = tau1 - tau3 + tau2;
+            T tauZ = tau3 - tau1 + tau2;
+            const T one = 1, two = 2, four = 4;
+            T hx2inv = one / (dx * dx);
+            T hz2inv = one / (dz * dz);
+            T dxinv = one / dx;
+            T dzinv = one / dz;
+            T a = hx2inv + hz2inv;
+            T b = four * (dxinv * dt0dx + dzinv * dt0dz) - two * (tauX * hx2inv + tauZ * hz2inv);
+            T c = (tauX * tauX) * hx2inv + (tauZ * tauZ) * hz2inv -
+                  four * ((dt0dx * tauX) * dxinv + (dt0dz * tauZ) * dzinv) +
+                  four * (sSrc * sSrc - s0 * s0);
+            T det = b * b - four * a * c;
+            if (det >= 0) {
+                T tau = (-b + dsqrt(det)) / (two * a);
+                t0Update3 = t0 + tau;
+            }
+            if (t0Update3 < t1 || t0Update3 < t3) t0Update3 = huge;
+        }
+        tUpd = dmin(t0Update1, t0Update3);
+    }
+    return tUpd;
+}
+
+}  // namespace eikx

@@ -1,0 +1,115 @@
+// Kernel argument blocks and launchers of the sweep and field kernels.
+// Included by the CUDA translation units and by the host runtime (capi.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "local_solver.cuh"
+
+namespace eikx {
+
+// Warp-block shape of the 3D kernel: LY3 x LZ3 x-pencils per warp.
+constexpr int LY3 = 8, LZ3 = 4;
+// 2D kernel: 32 x-rows per warp.
+constexpr int LZ2 = 32;
+constexpr int kWarpsPerBlock = 4;
+
+// Device state shared by all sweeps of one solve (one entry per field unless noted).
+struct SolveState {
+    unsigned *progress[2];          // per (field, warp block) progress counters, double-buffered
+    unsigned *queue[2];             // work-queue heads, double-buffered
+    int nProgress;                  // entries in each progress buffer
+    unsigned long long *residual;   // [field][sweep slot] largest decrease (double bits)
+    int residualStride;             // slots per field
+    int *converged;                 // 1 once a field's iteration decrease fell below tol
+    int *iterations;                // refinement iterations each field ran
+    int *abortFlag;                 // raised when a bounded wait ran out
+    const int4 *order;              // work queue: (field, by, bz, 0) sorted by start step
+    int totalItems;                 // fields * warp blocks per field
+    unsigned long long spinLimit;   // polls before a wait gives up
+};
+
+template <class T> struct Sweep3Args {
+    T *tt;                    // travel-time fields, row pitch `pitch`, rows (y,z) natural
+    long long fieldStride;    // elements per field
+    int pitch;                // padded x extent Px (multiple of 4) = walk length
+    const T *sp;              // edge-replicated slowness: (nz+1) x (ny+1) x spPitch
+    int spPitch;              // >= Px + 1
+    long long spPlane;        // spPitch * (ny + 1)
+    int nx, ny, nz;
+    int tilesY, tilesZ;       // warp blocks per field along y', z'
+    const SourceT<T> *srcs;   // per field
+    SolveState st;
+    int buf;                  // which progress/queue buffer this sweep uses
+    int residualSlot;         // residual slot this sweep writes
+    int sweep;                // 0..7 = Sweep1..Sweep8
+    int init;                 // 1 = source-limited initialisation sweep
+    int radius;               // factored-eikonal radius
+    T h;                      // uniform spacing
+    Spacing3<T> sp3;          // non-uniform constants
+};
+
+template <class T> struct Sweep2Args {
+    T *tt;
+    long long fieldStride;
+    int pitch;                // Px
+    const T *sp;              // (nz+1) x spPitch
+    int spPitch;
+    int nx, nz;
+    int tilesZ;
+    const SourceT<T> *srcs;
+    SolveState st;
+    int buf;
+    int residualSlot;
+    int sweep;                // 0..3 = Sweep1..Sweep4
+    int init;
+    int radius;
+    T h;
+    Spacing2<T> sp2;
+};
+
+// Launchers (sweep.cu).  blocks = persistent grid size.
+template <class T>
+cudaError_t launchSweep3(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s);
+template <class T>
+cudaError_t launchSweep2(const Sweep2Args<T> &a, bool uniform, int blocks, cudaStream_t s);
+// Resident blocks per SM of the sweep kernels (for the persistent grid size).
+template <class T> int sweep3BlocksPerSM(bool uniform);
+template <class T> int sweep2BlocksPerSM(bool uniform);
+size_t sweep3SmemBytes(size_t elem);
+size_t sweep2SmemBytes(size_t elem);
+
+// Field kernels (fields.cu).
+struct Corner3 {
+    int isx, isy, isz;
+    double xo, yo, zo, s;     // source offsets and source-cell slowness (FP64)
+};
+template <class T>
+cudaError_t launchInit3(T *tt, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
+                        double dx, double dy, double dz, const Corner3 *corners, int fp64,
+                        cudaStream_t s);
+template <class T>
+cudaError_t launchInit2(T *tt, int nFields, long long fieldStride, int pitch, int nx, int nz,
+                        double dx, double dz, const Corner3 *corners, int fp64, cudaStream_t s);
+template <class T, class U>
+cudaError_t launchPadSlowness3(T *sp, int spPitch, const U *s, int nx, int ny, int nz, cudaStream_t st);
+template <class T, class U>
+cudaError_t launchPadSlowness2(T *sp, int spPitch, const U *s, int nx, int nz, cudaStream_t st);
+template <class U>
+cudaError_t launchNodalToCell3(double *slow, const U *v, int nx, int ny, int nz, int ordering,
+                               cudaStream_t s);
+template <class U>
+cudaError_t launchNodalToCell2(double *slow, const U *v, int nx, int nz, int ordering, cudaStream_t s);
+template <class U>
+cudaError_t launchCellsToNatural3(double *slow, const U *c, int nx, int ny, int nz, int ordering,
+                                  cudaStream_t s);
+template <class U>
+cudaError_t launchCellsToNatural2(double *slow, const U *c, int nx, int nz, int ordering, cudaStream_t s);
+cudaError_t launchResetState(const SolveState &st, int nFields, int progressBuf, cudaStream_t s);
+cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,
+                                   int iteration, double tol, cudaStream_t s);
+cudaError_t launchAnalytic3(double *t, int nx, int ny, int nz, double dx, double dy, double dz,
+                            double xs, double ys, double zs, double vTop, double vBottom, cudaStream_t s);
+cudaError_t launchAnalytic2(double *t, int nx, int nz, double dx, double dz, double xs, double zs,
+                            double vTop, double vBottom, cudaStream_t s);
+
+}  // namespace eikx

@@ -1,0 +1,168 @@
+/*
+ * eikx_c.h -- the C ABI of the GB300-native eikonal solver.
+ *
+ * This is the drop-in boundary for the level-set fast-sweeping path of
+ * uofuseismo/eikonalxx v0.2.0.  Every call takes plain pointers and sizes; no
+ * CUDA or C++ types cross it.  The C++ API in include/eikonalxx/ (Solver3D,
+ * Solver2D, Model3D, ... with the reference's names and exceptions) is a thin
+ * layer over these entry points, and a Python, Go (cgo), Java (JNI/Panama) or
+ * Node (N-API) binding can bind them directly.
+ *
+ * Conventions
+ *   - Grids are node-based: nx*ny*nz travel-time nodes, (nx-1)*(ny-1)*(nz-1)
+ *     slowness cells, natural order (x fastest, then y, then z), exactly as
+ *     include/private/grid.hpp:15-53 of the reference.
+ *   - Every entry point returns an eikx_status (0 = success).  On failure the
+ *     thread-local message from eikx_last_error() says why.
+ *   - A context owns one CUDA device, its stream, device buffers and the CUDA
+ *     graphs of the sweep schedules it has run.  Contexts are independent; one
+ *     context must not be used from two threads at once (as the reference's
+ *     solvers, which are not thread-safe).
+ *   - Solves are synchronous: when eikx_solve* returns, the output is written.
+ */
+#ifndef EIKX_C_H
+#define EIKX_C_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct eikx_ctx eikx_ctx;
+typedef int eikx_status;
+
+enum {
+    EIKX_OK = 0,
+    EIKX_ERR_INVALID = -1,     /* bad argument: maps to std::invalid_argument */
+    EIKX_ERR_STATE = -2,       /* call out of order: maps to std::runtime_error */
+    EIKX_ERR_CUDA = -3,        /* CUDA runtime error (device missing, launch failed) */
+    EIKX_ERR_TIMEOUT = -4,     /* a bounded inter-tile wait ran out; field not valid */
+    EIKX_ERR_ALLOC = -5,       /* device or host allocation failed */
+    EIKX_ERR_UNSUPPORTED = -6  /* option combination not supported */
+};
+
+enum { EIKX_F32 = 0, EIKX_F64 = 1 };                 /* arithmetic / storage type */
+enum { EIKX_ORDER_NATURAL = 0, EIKX_ORDER_TRANSPOSED = 1 }; /* Ordering3D::ZYX / XYZ */
+enum { EIKX_HOST = 0, EIKX_DEVICE = 1 };             /* where a pointer lives */
+
+/* Solver options.  The first four mirror SolverOptions
+ * (include/eikonalxx/solverOptions.hpp:11-111, defaults src/solverOptions.cpp:5-21). */
+typedef struct {
+    int n_sweeps;          /* refinement iterations, each = all 8 (3D) / 4 (2D) sweeps; default 5 */
+    double tolerance;      /* s; an iteration whose largest decrease is below this ends the
+                              solve (the reference stores but never applies it); <= 0 runs
+                              all n_sweeps iterations, as the reference does; default 1e-5 */
+    int factored_radius;   /* factored-eikonal radius in grid points; default 3 */
+    int init_sweeps;       /* 1 = run the source-limited initialisation pass first; default 1 */
+    int init_fp64;         /* 1 = source-corner times computed in FP64 then rounded to the
+                              field type (default); 0 = in the field type, as the reference */
+    int spin_limit_log2;   /* bound on each inter-tile wait: 2^n polls (0 = default 22) */
+    int test_drop_blocks;  /* test hook, 0 in production: the host leaves the first n warp
+                              blocks of the work queue out, so the blocks downstream of them
+                              wait on progress that never comes; their bounded waits run
+                              out and the solve returns EIKX_ERR_TIMEOUT (the context stays
+                              usable).  Exercises failure detection without a GPU fault. */
+    int reserved[5];
+} eikx_options;
+
+/* Fills *opt with the defaults above. */
+void eikx_options_default(eikx_options *opt);
+
+/* A source (or, by reciprocity, a station) at an absolute position in metres.
+ * Its cell is min(nCell-1, floor((x-x0)/dx)) per axis, as Source3D
+ * (src/source3d.cpp:161-297). */
+typedef struct { double x, y, z; } eikx_source3d;
+typedef struct { double x, z; } eikx_source2d;
+
+/* Per-solve statistics of the last eikx_solve3d/2d call on a context. */
+typedef struct {
+    int n_fields;            /* fields solved by the call */
+    int iterations_max;      /* largest number of refinement iterations any field ran */
+    int iterations_min;
+    int sweeps_launched;     /* sweep kernels launched (init pass included) */
+    int kernel_launches;     /* all kernels launched by the call (graph nodes included) */
+    double residual_last;    /* largest decrease of the last iteration over all fields (s) */
+    double device_ms;        /* device time of the solve (CUDA events) */
+} eikx_stats;
+
+/* ---- context ----------------------------------------------------------- */
+/* Replaces: the implicit per-solver state of Solver3D/Solver2D
+ * (src/solver3d.cpp:16-111 Solver3DImpl, src/solver2d.cpp:28-225 Solver2DImpl). */
+eikx_status eikx_create(eikx_ctx **ctx, int device);
+eikx_status eikx_destroy(eikx_ctx *ctx);
+const char *eikx_last_error(void);
+eikx_status eikx_get_stats(const eikx_ctx *ctx, eikx_stats *stats);
+
+/* ---- 3D ---------------------------------------------------------------- */
+/* Replaces Solver3D::initialize (src/solver3d.cpp:148-194): grid points (>= 3 per
+ * axis, include/eikonalxx/geometry3d.hpp / src/geometry3d.cpp:73-80), spacing (> 0)
+ * and origin. */
+eikx_status eikx_set_grid3d(eikx_ctx *ctx, int nx, int ny, int nz, double dx, double dy,
+                            double dz, double x0, double y0, double z0);
+
+/* Replaces Solver3D::setVelocityModel (src/solver3d.cpp:197-249) with a model given
+ * as cell slowness (s/m, as Model3D::getSlownessPointer, src/model3d.cpp:407-415).
+ * dtype: EIKX_F32/F64; ordering: natural or transposed; where: host or device. */
+eikx_status eikx_set_slowness3d(eikx_ctx *ctx, const void *slowness, int dtype, int ordering,
+                                int where);
+
+/* Replaces Model3D::setNodalVelocities (src/model3d.cpp:286-314) + setVelocityModel:
+ * nodal velocities (m/s) -> cell slowness 8/sum(8 corners) computed on the GPU. */
+eikx_status eikx_set_nodal_velocity3d(eikx_ctx *ctx, const void *velocity, int dtype,
+                                      int ordering, int where);
+
+/* Copies the cell slowness the context holds (natural order) to host memory. */
+eikx_status eikx_get_slowness3d(const eikx_ctx *ctx, void *slowness, int dtype);
+
+/* Replaces Solver3D::setSource + Solver3D::solve + getTravelTimeField
+ * (src/solver3d.cpp:351-500, :503-525).  Solves n_src independent fields (one per
+ * source) on the context's model in one batched launch schedule.
+ * precision: EIKX_F32 (FP32 sweeps, FP64 corner init) or EIKX_F64.
+ * t_out: n_src * nx*ny*nz values of the precision's type, natural order, host or
+ * device (where).  opt may be NULL for the defaults. */
+eikx_status eikx_solve3d(eikx_ctx *ctx, const eikx_source3d *src, int n_src,
+                         const eikx_options *opt, int precision, void *t_out, int where);
+
+/* ---- 2D ---------------------------------------------------------------- */
+/* Replaces Solver2D::initialize (src/solver2d.cpp:291-343). */
+eikx_status eikx_set_grid2d(eikx_ctx *ctx, int nx, int nz, double dx, double dz, double x0,
+                            double z0);
+/* Replaces Solver2D::setVelocityModel (src/solver2d.cpp:406-438). */
+eikx_status eikx_set_slowness2d(eikx_ctx *ctx, const void *slowness, int dtype, int ordering,
+                                int where);
+/* Replaces Model2D::setNodalVelocities (src/model2d.cpp:263-290). */
+eikx_status eikx_set_nodal_velocity2d(eikx_ctx *ctx, const void *velocity, int dtype,
+                                      int ordering, int where);
+/* Replaces Solver2D::setSource + Solver2D::solve + getTravelTimeField
+ * (src/solver2d.cpp:462-565, :883-905). */
+eikx_status eikx_solve2d(eikx_ctx *ctx, const eikx_source2d *src, int n_src,
+                         const eikx_options *opt, int precision, void *t_out, int where);
+
+/* ---- level-set tables (host) ------------------------------------------- */
+/* Replaces Graph3D<E>::initialize and its accessors (src/graph3d.cpp:120-317):
+ * sweep = 0..7 (Sweep1..Sweep8).  Arrays: level_start[nx+ny+nz-1],
+ * node_to_index/to_x/to_y/to_z/index_to_level[nx*ny*nz].  Returns the number of
+ * levels (> 0) or an eikx_status (< 0). */
+int eikx_graph3d_tables(int sweep, int nx, int ny, int nz, int *level_start,
+                        int *node_to_index, int *to_x, int *to_y, int *to_z,
+                        int *index_to_level, int *max_level_size);
+
+/* Replaces the 2D level helpers makeLevelOffset / sweepLevelIndexToGrid
+ * (solverUtilities2d.hpp:1063-1266): the (ix, iz) visiting order of sweep 0..3.
+ * Arrays: level_start[nx+nz], order_ix/order_iz[nx*nz].  Returns the number of
+ * levels or an eikx_status. */
+int eikx_levels2d(int sweep, int nx, int nz, int *level_start, int *order_ix, int *order_iz);
+
+/* ---- analytic fields on the GPU (FP64) ---------------------------------- */
+/* Replaces Analytic::LinearGradient3D::solve / Homogeneous3D::solve
+ * (src/analytic/linearGradient3d.cpp:28-116, homogeneous3d.cpp:22-70): travel times
+ * for v(z) = vTop + (vBottom-vTop)*z/((nz-1)dz) (vTop == vBottom: homogeneous) on the
+ * context's 3D grid.  t_out: nx*ny*nz doubles, host or device. */
+eikx_status eikx_analytic3d(eikx_ctx *ctx, const eikx_source3d *src, double v_top,
+                            double v_bottom, double *t_out, int where);
+eikx_status eikx_analytic2d(eikx_ctx *ctx, const eikx_source2d *src, double v_top,
+                            double v_bottom, double *t_out, int where);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EIKX_C_H */

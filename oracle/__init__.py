@@ -1,0 +1,141 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes front-ends of the CPU checkers: the project's restatement of the reference's
+algorithm (libeikx_oracle.so, eikx_oracle.cpp) and, where it was built, the
+reference's own code (libeikx_ref.so, ref_driver.cpp).  Imported only by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline legs; the solver never uses it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_d = ctypes.c_double
+_P = lambda a: ctypes.c_void_p(a.ctypes.data)
+
+
+def _load(path):
+    return ctypes.CDLL(path)
+
+
+class Oracle:
+    """The project's CPU restatement (bit-identical to the reference's sweep)."""
+
+    def __init__(self):
+        self.lib = _load(_build.build_oracle())
+        self.lib.oracle_sweep3d_f32.restype = ctypes.c_double
+        self.lib.oracle_sweep3d_f64.restype = ctypes.c_double
+        self.lib.oracle_hypot.restype = ctypes.c_double
+
+    def solve3d(self, slow, grid, src_cell, src_off, n_sweeps=2, radius=3, tol=-1.0, init_fp64=True,
+                init_sweeps=True, residuals=False):
+        nx, ny, nz, dx, dy, dz = grid
+        dt = slow.dtype
+        tt = np.zeros(nx * ny * nz, dt)
+        res = np.zeros(max(1, 8 * n_sweeps), np.float64)
+        it = ctypes.c_int(0)
+        f = self.lib.oracle_solve3d_f64 if dt == np.float64 else self.lib.oracle_solve3d_f32
+        f(nx, ny, nz, _d(dx), _d(dy), _d(dz), int(src_cell[0]), int(src_cell[1]), int(src_cell[2]),
+          _d(src_off[0]), _d(src_off[1]), _d(src_off[2]), _P(np.ascontiguousarray(slow)), n_sweeps, radius,
+          _d(tol), int(init_fp64), int(init_sweeps), _P(tt), _P(res), ctypes.byref(it))
+        tt = tt.reshape(nz, ny, nx)
+        return (tt, res[:8 * it.value].reshape(-1, 8), it.value) if residuals else tt
+
+    def solve2d(self, slow, grid, src_cell, src_off, n_sweeps=2, radius=3, tol=-1.0, init_fp64=True,
+                init_sweeps=True, hypot_mode=1, residuals=False):
+        nx, nz, dx, dz = grid
+        dt = slow.dtype
+        self.lib.oracle_set_hypot_mode(int(hypot_mode))
+        tt = np.zeros(nx * nz, dt)
+        res = np.zeros(max(1, 4 * n_sweeps), np.float64)
+        it = ctypes.c_int(0)
+        f = self.lib.oracle_solve2d_f64 if dt == np.float64 else self.lib.oracle_solve2d_f32
+        f(nx, nz, _d(dx), _d(dz), int(src_cell[0]), int(src_cell[1]), _d(src_off[0]), _d(src_off[1]),
+          _P(np.ascontiguousarray(slow)), n_sweeps, radius, _d(tol), int(init_fp64), int(init_sweeps),
+          _P(tt), _P(res), ctypes.byref(it))
+        tt = tt.reshape(nz, nx)
+        return (tt, res[:4 * it.value].reshape(-1, 4), it.value) if residuals else tt
+
+    def graph3d(self, sweep, nx, ny, nz):
+        n = nx * ny * nz
+        ls = np.zeros(nx + ny + nz - 1, np.int32)
+        a = [np.zeros(n, np.int32) for _ in range(5)]
+        mx = ctypes.c_int()
+        nl = self.lib.oracle_graph3d(sweep, nx, ny, nz, _P(ls), *[_P(x) for x in a], ctypes.byref(mx))
+        return {"n_levels": nl, "level_start": ls, "node_to_index": a[0], "to_x": a[1], "to_y": a[2],
+                "to_z": a[3], "index_to_level": a[4], "max_level_size": mx.value}
+
+    def linear_gradient3d(self, grid, src_off, v_top, v_bottom):
+        nx, ny, nz, dx, dy, dz = grid
+        t = np.zeros(nx * ny * nz)
+        self.lib.oracle_linear_gradient3d(nx, ny, nz, _d(dx), _d(dy), _d(dz), _d(src_off[0]), _d(src_off[1]),
+                                          _d(src_off[2]), _d(v_top), _d(v_bottom), _P(t))
+        return t.reshape(nz, ny, nx)
+
+    def linear_gradient2d(self, grid, src_off, v_top, v_bottom):
+        nx, nz, dx, dz = grid
+        t = np.zeros(nx * nz)
+        self.lib.oracle_linear_gradient2d(nx, nz, _d(dx), _d(dz), _d(src_off[0]), _d(src_off[1]), _d(v_top),
+                                          _d(v_bottom), _P(t))
+        return t.reshape(nz, nx)
+
+    def nodal_to_cell3d(self, v, nx, ny, nz, ordering=0):
+        v = np.ascontiguousarray(v)
+        s = np.zeros((nx - 1) * (ny - 1) * (nz - 1), v.dtype)
+        f = self.lib.oracle_nodal_to_cell3d_f64 if v.dtype == np.float64 else self.lib.oracle_nodal_to_cell3d_f32
+        f(nx, ny, nz, _P(v), ordering, _P(s))
+        return s
+
+    def nodal_to_cell2d(self, v, nx, nz, ordering=0):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        s = np.zeros((nx - 1) * (nz - 1))
+        self.lib.oracle_nodal_to_cell2d_f64(nx, nz, _P(v), ordering, _P(s))
+        return s
+
+
+class Reference:
+    """The reference's own sweep code (oracle/_ref); None-valued if not built."""
+
+    def __init__(self):
+        path = _build.build_ref()
+        if path is None:
+            raise FileNotFoundError("reference sources are not available here")
+        self.lib = _load(path)
+
+    def solve3d(self, slow, grid, src_cell, src_off, n_sweeps=2, radius=3, init_sweeps=True):
+        nx, ny, nz, dx, dy, dz = grid
+        tt = np.zeros(nx * ny * nz, slow.dtype)
+        f = self.lib.ref_solve3d_f64 if slow.dtype == np.float64 else self.lib.ref_solve3d_f32
+        rc = f(nx, ny, nz, _d(dx), _d(dy), _d(dz), int(src_cell[0]), int(src_cell[1]), int(src_cell[2]),
+               _d(src_off[0]), _d(src_off[1]), _d(src_off[2]), _P(np.ascontiguousarray(slow)), n_sweeps,
+               radius, int(init_sweeps), _P(tt))
+        if rc != 0:
+            raise RuntimeError("reference solve failed")
+        return tt.reshape(nz, ny, nx)
+
+    def solve2d(self, slow, grid, src_cell, src_off, n_sweeps=2, radius=3, init_sweeps=True):
+        nx, nz, dx, dz = grid
+        tt = np.zeros(nx * nz, slow.dtype)
+        f = self.lib.ref_solve2d_f64 if slow.dtype == np.float64 else self.lib.ref_solve2d_f32
+        rc = f(nx, nz, _d(dx), _d(dz), int(src_cell[0]), int(src_cell[1]), _d(src_off[0]), _d(src_off[1]),
+               _P(np.ascontiguousarray(slow)), n_sweeps, radius, int(init_sweeps), _P(tt))
+        if rc != 0:
+            raise RuntimeError("reference solve failed")
+        return tt.reshape(nz, nx)
+
+    def graph3d(self, sweep, nx, ny, nz):
+        n = nx * ny * nz
+        ls = np.zeros(nx + ny + nz - 1, np.int32)
+        a = [np.zeros(n, np.int32) for _ in range(5)]
+        mx = ctypes.c_int()
+        nl = self.lib.ref_graph3d(sweep, nx, ny, nz, _P(ls), *[_P(x) for x in a], ctypes.byref(mx))
+        return {"n_levels": nl, "level_start": ls, "node_to_index": a[0], "to_x": a[1], "to_y": a[2],
+                "to_z": a[3], "index_to_level": a[4], "max_level_size": mx.value}
+
+
+def source_cell(pos, origin, spacing, n):
+    """Cell and offset of a source coordinate, as the reference's Source3D."""
+    off = pos - origin
+    return min(n - 2, int(off / spacing)), off

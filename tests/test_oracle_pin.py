@@ -1,0 +1,126 @@
+"""The oracle pinned against the reference's own code and its golden vectors (CPU)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import random_slowness
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _case3(rng, nx, ny, nz, dx, dy, dz, dtype):
+    s = random_slowness(rng, (nz - 1) * (ny - 1) * (nx - 1), dtype=dtype)
+    cell = [int(rng.integers(0, n - 1)) for n in (nx, ny, nz)]
+    off = [(c + rng.uniform()) * d for c, d in zip(cell, (dx, dy, dz))]
+    return s, (nx, ny, nz, dx, dy, dz), cell, off
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("radius", [0, 3, 1000])
+@pytest.mark.parametrize("shape", [(9, 10, 11, 100., 100., 100.), (13, 7, 8, 100., 120., 90.),
+                                   (3, 3, 3, 50., 50., 50.), (6, 4, 12, 25., 25., 25.)])
+def test_oracle_3d_matches_reference_bitwise(oracle, reference, dtype, radius, shape):
+    rng = np.random.default_rng(hash((shape, radius)) % 2**32)
+    s, g, cell, off = _case3(rng, *shape, dtype)
+    t_ref = reference.solve3d(s, g, cell, off, n_sweeps=2, radius=radius)
+    t_or = oracle.solve3d(s, g, cell, off, n_sweeps=2, radius=radius, init_fp64=False)
+    assert np.array_equal(t_ref.view(np.uint8), t_or.view(np.uint8))
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("radius", [0, 3, 1000])
+@pytest.mark.parametrize("shape", [(31, 27, 10., 10.), (25, 33, 10., 12.5), (3, 3, 10., 10.)])
+def test_oracle_2d_matches_reference_bitwise(oracle, reference, dtype, radius, shape):
+    rng = np.random.default_rng(hash((shape, radius, 2)) % 2**32)
+    nx, nz, dx, dz = shape
+    s = random_slowness(rng, (nz - 1) * (nx - 1), dtype=dtype)
+    cell = [int(rng.integers(0, nx - 1)), int(rng.integers(0, nz - 1))]
+    off = [(cell[0] + rng.uniform()) * dx, (cell[1] + rng.uniform()) * dz]
+    t_ref = reference.solve2d(s, shape, cell, off, n_sweeps=2, radius=radius)
+    # hypot_mode 0: std::hypot, as the reference calls it
+    t_or = oracle.solve2d(s, shape, cell, off, n_sweeps=2, radius=radius, init_fp64=False, hypot_mode=0)
+    assert np.array_equal(t_ref.view(np.uint8), t_or.view(np.uint8))
+
+
+def test_oracle_2d_own_hypot_within_an_ulp(oracle, reference):
+    """The GPU's hypot (Borges 2019) differs from std::hypot by at most an ulp."""
+    rng = np.random.default_rng(7)
+    shape = (31, 27, 10., 10.)
+    s = random_slowness(rng, 30 * 26)
+    t_ref = reference.solve2d(s, shape, [11, 9], [115.0, 93.0], n_sweeps=2, radius=1000)
+    t_or = oracle.solve2d(s, shape, [11, 9], [115.0, 93.0], n_sweeps=2, radius=1000, init_fp64=False,
+                          hypot_mode=1)
+    assert np.max(np.abs(t_ref - t_or)) <= 1e-15
+
+
+def test_graph3d_golden(oracle):
+    g = json.load(open(os.path.join(GOLDEN, "graph3d_4x3x5.json")))
+    nx, ny, nz = g["nx"], g["ny"], g["nz"]
+    for e in range(8):
+        t = oracle.graph3d(e, nx, ny, nz)
+        assert t["n_levels"] == g["n_levels"]
+        assert t["max_level_size"] == g["max_level_size"]
+        assert t["level_start"].tolist() == g["level_start"]
+        assert t["node_to_index"].tolist() == g["node_in_level_to_index"][e]
+        idx = t["node_to_index"]
+        assert np.array_equal(t["to_x"], idx % nx)
+        assert np.array_equal(t["to_y"], (idx // nx) % ny)
+        assert np.array_equal(t["to_z"], idx // (nx * ny))
+
+
+@pytest.mark.parametrize("shape", [(4, 3, 5), (5, 3, 7), (7, 6, 3), (11, 4, 9)])
+def test_graph3d_oracle_matches_reference(oracle, reference, shape):
+    for e in range(8):
+        a, b = oracle.graph3d(e, *shape), reference.graph3d(e, *shape)
+        for k in a:
+            if isinstance(a[k], np.ndarray):
+                assert np.array_equal(a[k], b[k]), (e, k)
+            else:
+                assert a[k] == b[k], (e, k)
+
+
+def test_residual_and_convergence_rule(oracle):
+    """A solve stops after the first iteration whose largest decrease is below tol."""
+    rng = np.random.default_rng(3)
+    s, g, cell, off = _case3(rng, 17, 15, 13, 100., 100., 100., np.float64)
+    t, res, it = oracle.solve3d(s, g, cell, off, n_sweeps=10, radius=0, tol=1e-9, residuals=True)
+    assert 1 <= it <= 10
+    per_iter = res.max(axis=1)
+    assert per_iter[-1] < 1e-9 or it == 10
+    assert np.all(per_iter[:-1] >= 1e-9)
+    t_full = oracle.solve3d(s, g, cell, off, n_sweeps=it, radius=0, tol=-1)
+    assert np.array_equal(t, t_full)
+
+
+def test_analytic_homogeneous_matches_closed_form(oracle):
+    g = (21, 19, 17, 10., 11., 12.)
+    t = oracle.linear_gradient3d(g, (53.0, 41.0, 77.0), 3000.0, 3000.0)
+    z, y, x = np.meshgrid(np.arange(17) * 12., np.arange(19) * 11., np.arange(21) * 10., indexing="ij")
+    exact = np.sqrt((x - 53.) ** 2 + (y - 41.) ** 2 + (z - 77.) ** 2) / 3000.
+    assert np.max(np.abs(t - exact)) < 1e-15
+
+
+def test_analytic_linear_gradient_satisfies_eikonal(oracle):
+    """|grad T| = 1/v(z) for the linear-gradient solution (central differences)."""
+    nx, nz, dx, dz = 201, 101, 5., 5.
+    t = oracle.linear_gradient2d((nx, nz, dx, dz), (500., 250.), 3000., 4250.)
+    gz, gx = np.gradient(t, dz, dx)
+    zz = np.arange(nz)[:, None] * dz
+    v = 3000. + (4250. - 3000.) * zz / ((nz - 1) * dz)
+    err = np.abs(np.sqrt(gx ** 2 + gz ** 2) * v - 1.0)[5:-5, 5:-5]
+    dist = np.hypot(np.arange(nx)[None, :] * dx - 500., zz - 250.)[5:-5, 5:-5]
+    assert np.max(err[dist > 100]) < 1e-3
+
+
+def test_nodal_to_cell_orderings_agree(oracle):
+    rng = np.random.default_rng(5)
+    nx, ny, nz = 6, 5, 4
+    v = rng.uniform(2000, 5000, (nz, ny, nx))
+    s_nat = oracle.nodal_to_cell3d(v.ravel(), nx, ny, nz, 0)
+    s_tr = oracle.nodal_to_cell3d(np.ascontiguousarray(v.transpose(2, 1, 0)).ravel(), nx, ny, nz, 1)
+    assert np.allclose(s_nat, s_tr, rtol=1e-14)  # pairwise sums differ in order
+    mean = (v[:-1, :-1, :-1] + v[:-1, :-1, 1:] + v[:-1, 1:, :-1] + v[:-1, 1:, 1:] + v[1:, :-1, :-1] +
+            v[1:, :-1, 1:] + v[1:, 1:, :-1] + v[1:, 1:, 1:]) / 8
+    assert np.allclose(s_nat, (1 / mean).ravel(), rtol=1e-14)
