@@ -1,0 +1,346 @@
+"""Benchmark: 3D travel-time grids/s of the level-set fast-sweeping solver on GB300.
+
+Workload (the reference's plain 3D configuration): a 256 x 256 x 128 grid, h = 50 m,
+8 horizontal layers with velocities uniform in [3000, 7000] m/s increasing with depth,
+times (1 + p) for a Gaussian random field p (correlation length 1 km, +-5 %), nodal
+velocities -> cell slowness; FP32 sweeps with FP64 corner initialisation; factored radius
+3; refinement iterations until the largest decrease of an iteration is below 1e-5 s
+(at most 10).  A step solves FIELDS independent fields (one seeded source each) in one
+batched launch schedule.  The data are synthetic (seeded), generated by
+eikonalxx_gb300/synthetic.py.
+
+Prints one JSON line (rank 0).  ``value`` is device-timed throughput with the model
+resident in HBM; ``e2e`` times the public API call a user makes (nodal velocities from
+pinned host memory in, travel-time fields to pinned host memory out) every step.
+``--impl reference`` times the reference's CPU sweep code (oracle/_ref when it was built
+here, else the project's bit-identical CPU port) on the host cores instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "3D travel-time grids/s at max err <=1e-4 s vs FP64; batched+learned vs plain"
+NX, NY, NZ, H = 256, 256, 128, 50.0
+MODEL_SEED, SOURCE_SEED = 20240601, 7
+N_SWEEPS_MAX, TOL, RADIUS = 10, 1e-5, 3
+L2_BYTES = 129 * 2 ** 20
+BYTES_PER_NODE_SWEEP = 12          # FP32: read T, read slowness, write T
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return world, rank
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic():
+    """DRAM bytes per sweep launch from the committed ncu summary, or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "sweep3d_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+        self.device_index = device_index
+
+    def __enter__(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for s in self.samples for n, v in zip(names, s[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_workload(fields):
+    from eikonalxx_gb300 import synthetic
+    v = synthetic.layered_grf_model(NX, NY, NZ, H, MODEL_SEED)
+    src = synthetic.uniform_sources(fields, NX, NY, NZ, H, SOURCE_SEED)
+    return v, src
+
+
+def run_gpu(args):
+    import torch
+    import eikonalxx_gb300 as ex
+
+    world, rank = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.cuda.current_device()
+    fields = args.fields
+    v, src_all = make_workload(fields * world)
+    src = src_all[rank * fields:(rank + 1) * fields]   # weak scaling: each rank its own fields
+    n_nodes = NX * NY * NZ
+
+    ctx = ex.Context(dev)
+    ctx.set_grid3d(NX, NY, NZ, H, H, H)
+    v_host = torch.from_numpy(v.ravel()).pin_memory()
+    ctx.set_nodal_velocity3d(v_host)
+    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS)
+    out_dev = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device=f"cuda:{dev}")
+    out_host = torch.empty((fields, NZ, NY, NX), dtype=torch.float32).pin_memory()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    def step_device():
+        ctx.solve3d(src, opt, ex.F32, out=out_dev)
+        return ctx.stats()
+
+    # accuracy: one field against the FP64 solve of the same schedule (GPU FP64 is
+    # bit-identical to the FP64 oracle in the tests); not timed
+    acc = {}
+    if rank == 0 and not args.skip_accuracy:
+        t32 = ctx.solve3d(src[:1], opt, ex.F32)[0].astype(np.float64)
+        o64 = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=1e-9, factored_radius=RADIUS)
+        t64 = ctx.solve3d(src[:1], o64, ex.F64)[0]
+        d = np.abs(t32 - t64)
+        acc = {"max_err_vs_fp64_s": float(d.max()), "rms_err_vs_fp64_s": float(np.sqrt(np.mean(d ** 2))),
+               "fp64_iterations": ctx.stats()["iterations_max"]}
+
+    for _ in range(args.warmup):
+        step_device()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    per_step_ms, iters, launches, wall = [], [], 0, []
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)             # evict L2 between timed steps (outside the timing)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = step_device()
+            wall.append((time.perf_counter() - t0) * 1e3)
+            per_step_ms.append(st["device_ms"])
+            iters.append(st["iterations_max"])
+            launches += st["kernel_launches"]
+    torch.cuda.synchronize()
+    ms = float(np.mean(per_step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = fields * world / (ms / 1e3)
+
+    # roofline of the sweep kernel: per-launch durations from CUDA events around each sweep
+    prof = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True)
+    ctx.solve3d(src, prof, ex.F32, out=out_dev)
+    pst = ctx.stats()
+    sweep_launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
+    bytes_per_launch = BYTES_PER_NODE_SWEEP * n_nodes * fields
+    achieved = bytes_per_launch / (sweep_launch_ms / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    tr = _traffic()
+
+    # end to end through the public API with host buffers every step
+    e2e_ms = []
+    for i in range(max(1, args.warmup) + args.steps):
+        t0 = time.perf_counter()
+        ctx.set_nodal_velocity3d(v_host)
+        ctx.solve3d(src, opt, ex.F32, out=out_host)
+        if i >= max(1, args.warmup):
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e = fields * world / (float(np.mean(e2e_ms)) / 1e3)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered+GRF model, seeded sources)",
+        "config": {"workload": f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, "
+                               f"{fields} independent sources per step per GPU",
+                   "grid": [NX, NY, NZ], "h_m": H, "fields_per_step": fields, "precision": "fp32 sweeps, fp64 init",
+                   "factored_radius": RADIUS, "tolerance_s": TOL, "max_iterations": N_SWEEPS_MAX,
+                   "l2": "flushed (write of 2x L2) between timed steps; per-step fields exceed L2",
+                   "parallelism": f"replicas x{world} (sources sharded, no collective)"},
+        "roofline": {"bound": "hbm", "kernel": "sweep3Kernel<float,uniform>", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "bytes_per_launch": bytes_per_launch, "launch_ms": sweep_launch_ms,
+                     "traffic": (tr["dram_bytes_per_launch"] if tr else None)},
+        "e2e": {"value": e2e, "unit": "grids/s", "h2d_bytes_per_step": int(v.nbytes + 24 * fields),
+                "d2h_bytes_per_step": int(4 * n_nodes * fields), "ms_per_step": float(np.mean(e2e_ms))},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "iterations": {"max": int(max(iters)), "min": int(min(iters))},
+        "wall_ms_per_step": float(np.mean(wall)), "accuracy": acc,
+        "cpu_baseline": cpu_baseline(args.cpu_seconds) if not args.skip_cpu else None,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _cpu_solver():
+    """(kind, callable solving one sweep of one field) of the best CPU path present."""
+    from oracle import Oracle, Reference
+    try:
+        ref = Reference()
+        kind = "reference"
+    except Exception:
+        ref = None
+        kind = "port"
+    return kind, ref, Oracle()
+
+
+def _host_slowness(v):
+    from oracle import Oracle
+    return Oracle().nodal_to_cell3d(v.ravel(), NX, NY, NZ, 0)
+
+
+def cpu_sweep_rate(seconds, threads):
+    """Full-size FP32 sweeps of the CPU path (one field per thread) -> node-updates/s."""
+    import ctypes
+    kind, ref, orc = _cpu_solver()
+    v, src = make_workload(max(1, threads))
+    s = _host_slowness(v)
+    nn = NX * NY * NZ
+
+    def one(i, out):
+        pos = src[i]
+        cell = [min(n - 2, int(p / H)) for p, n in zip(pos, (NX, NY, NZ))]
+        tt = np.full(nn, 1e10, np.float32)
+        d = ctypes.c_double
+        n_done, t0 = 0, time.perf_counter()
+        P = lambda a: ctypes.c_void_p(a.ctypes.data)
+        while time.perf_counter() - t0 < seconds / 2 or n_done == 0:
+            e = n_done % 8
+            if kind == "reference":
+                ref.lib.ref_sweep3d_f32(e, 0, NX, NY, NZ, d(H), d(H), d(H), cell[0], cell[1], cell[2],
+                                        d(pos[0]), d(pos[1]), d(pos[2]), RADIUS, P(s), P(tt))
+            else:
+                orc.lib.oracle_sweep3d_f32(e, 0, NX, NY, NZ, d(H), d(H), d(H), cell[0], cell[1], cell[2],
+                                           d(pos[0]), d(pos[1]), d(pos[2]), RADIUS, P(s), P(tt))
+            n_done += 1
+        out[i] = (n_done, time.perf_counter() - t0)
+
+    res = {}
+    th = [threading.Thread(target=one, args=(i, res)) for i in range(threads)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    rate = sum(n * nn / dt for n, dt in res.values())
+    return kind, rate, sum(n for n, _ in res.values())
+
+
+def _sweeps_per_grid():
+    """Sweeps one config grid needs on the GPU path (init pass + iterations), for the
+    CPU extrapolation; measured by the GPU arm, else the schedule maximum."""
+    return 8 * (1 + 4)
+
+
+def cpu_baseline(seconds, threads=1, sweeps_per_grid=None):
+    kind, rate, n = cpu_sweep_rate(seconds, threads)
+    spg = sweeps_per_grid or _sweeps_per_grid()
+    grids_per_s = rate / (NX * NY * NZ * spg)
+    return {"value": grids_per_s, "unit": "grids/s", "cores": threads, "kind": kind,
+            "sample": f"{n} full-size {NX}x{NY}x{NZ} FP32 sweeps ({threads} field(s), one per thread) "
+                      f"in ~{seconds:g} s, extrapolated at {spg} sweeps per grid"}
+
+
+def run_reference(args):
+    world, rank = _dist()
+    if rank != 0:
+        return
+    threads = args.cpu_threads or (os.cpu_count() or 1)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        kind, rate, n = cpu_sweep_rate(args.cpu_seconds / max(1, args.steps), threads)
+        if i >= args.warmup:
+            vals.append(rate)
+    rate = float(np.mean(vals))
+    spg = _sweeps_per_grid()
+    value = rate / (NX * NY * NZ * spg)
+    line = {
+        "metric": METRIC, "value": value, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered+GRF model, seeded sources)",
+        "impl": "reference",
+        "config": {"workload": f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, one field per host thread",
+                   "grid": [NX, NY, NZ], "h_m": H, "precision": "fp32 sweeps"},
+        "cpu_baseline": {"value": value, "unit": "grids/s", "cores": threads, "kind": kind,
+                         "sample": f"per step ~{args.cpu_seconds / max(1, args.steps):.0f} s of full-size FP32 "
+                                   f"sweeps, one field per thread, extrapolated at {spg} sweeps per grid"},
+        "e2e": {"value": value, "unit": "grids/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--fields", type=int, default=8, help="independent sources per step per GPU")
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -61,14 +61,15 @@ class _Options(ctypes.Structure):
     _fields_ = [("n_sweeps", ctypes.c_int), ("tolerance", ctypes.c_double),
                 ("factored_radius", ctypes.c_int), ("init_sweeps", ctypes.c_int),
                 ("init_fp64", ctypes.c_int), ("spin_limit_log2", ctypes.c_int),
-                ("test_drop_blocks", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("test_drop_blocks", ctypes.c_int), ("profile_sweeps", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
 
 
 class _Stats(ctypes.Structure):
     _fields_ = [("n_fields", ctypes.c_int), ("iterations_max", ctypes.c_int),
                 ("iterations_min", ctypes.c_int), ("sweeps_launched", ctypes.c_int),
                 ("kernel_launches", ctypes.c_int), ("residual_last", ctypes.c_double),
-                ("device_ms", ctypes.c_double)]
+                ("device_ms", ctypes.c_double), ("sweep_ms", ctypes.c_double)]
 
 
 class _Src3(ctypes.Structure):
@@ -145,6 +146,7 @@ class Options:
     init_fp64: bool = True
     spin_limit_log2: int = 22
     test_drop_blocks: int = 0   # test hook only (see eikx_options.test_drop_blocks)
+    profile_sweeps: bool = False  # time each sweep kernel with CUDA events (no graph)
 
     def _c(self):
         o = _Options()
@@ -155,6 +157,7 @@ class Options:
         o.init_fp64 = int(bool(self.init_fp64))
         o.spin_limit_log2 = int(self.spin_limit_log2)
         o.test_drop_blocks = int(self.test_drop_blocks)
+        o.profile_sweeps = int(bool(self.profile_sweeps))
         return o
 
 

@@ -107,6 +107,7 @@ struct eikx_ctx {
     int numSMs = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<cudaEvent_t> sweepEv;   // per-sweep timing (profile_sweeps)
     // 3D model
     int nx = 0, ny = 0, nz = 0;
     double dx = 0, dy = 0, dz = 0, x0 = 0, y0 = 0, z0 = 0;
@@ -357,6 +358,15 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
 
     int launches = 0;
     int sweepsLaunched = 0;
+    const bool profile = o.profile_sweeps != 0;
+    const int nSweepLaunches = nSweepKinds * ((o.init_sweeps ? 1 : 0) + nSweeps);
+    if (profile) {
+        while (static_cast<int>(c->sweepEv.size()) < 2 * nSweepLaunches) {
+            cudaEvent_t e;
+            EIKX_CUDA(cudaEventCreate(&e));
+            c->sweepEv.push_back(e);
+        }
+    }
     auto enqueue = [&]() -> eikx_status {
         launches = 0;
         sweepsLaunched = 0;
@@ -371,6 +381,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
                                            w.corners.as<eikx::Corner3>(), o.init_fp64 ? 1 : 0, c->stream));
         ++launches;
         auto sweep = [&](int e, int init, int slot) -> eikx_status {
+            if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched], c->stream));
             if (DIM == 3) {
                 eikx::Sweep3Args<T> a{};
                 a.tt = w.tt.as<T>(); a.fieldStride = fieldStride; a.pitch = Px;
@@ -404,6 +415,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
                 a.sp2 = g;
                 EIKX_CUDA(eikx::launchSweep2<T>(a, uniform, blocks, c->stream));
             }
+            if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched + 1], c->stream));
             buf ^= 1;
             ++launches;
             ++sweepsLaunched;
@@ -423,7 +435,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     };
 
     EIKX_CUDA(cudaEventRecord(c->ev0, c->stream));
-    if (c->useGraphs) {
+    if (c->useGraphs && !profile) {
         if (!(c->graphExec && c->graphKey == sk)) {
             dropGraph(c);
             cudaGraph_t graph = nullptr;
@@ -447,13 +459,12 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     } else {
         if (eikx_status r = enqueue(); r != EIKX_OK) return r;
     }
-    EIKX_CUDA(cudaEventRecord(c->ev1, c->stream));
-
     // one pitched copy for all fields: rows of nx values out of rows of Px
     const cudaMemcpyKind kind = where == EIKX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     EIKX_CUDA(cudaMemcpy2DAsync(tOut, static_cast<size_t>(nx) * sizeof(T), w.tt.p, static_cast<size_t>(Px) * sizeof(T),
                                 static_cast<size_t>(nx) * sizeof(T), static_cast<size_t>(ny) * nz * nSrc, kind,
                                 c->stream));
+    EIKX_CUDA(cudaEventRecord(c->ev1, c->stream));
     std::vector<int> iters(nSrc);
     int aborted = 0;
     EIKX_CUDA(cudaMemcpyAsync(iters.data(), w.iterations.p, nSrc * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -485,6 +496,16 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     }
     s.residual_last = rl;
     s.sweeps_launched = sweepsLaunched;
+    s.sweep_ms = -1;
+    if (profile) {
+        double tot = 0;
+        for (int i = 0; i < sweepsLaunched; ++i) {
+            float m = 0;
+            cudaEventElapsedTime(&m, c->sweepEv[2 * i], c->sweepEv[2 * i + 1]);
+            tot += m;
+        }
+        s.sweep_ms = tot;
+    }
     s.kernel_launches = launches;
     s.device_ms = ms;
     c->stats = s;
@@ -541,6 +562,7 @@ eikx_status eikx_destroy(eikx_ctx *c) {
     dropGraph(c);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (cudaEvent_t e : c->sweepEv) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return EIKX_OK;

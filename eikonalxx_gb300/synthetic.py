@@ -1,0 +1,46 @@
+"""Seeded synthetic velocity models and source sets for the benchmark workloads.
+
+The reference ships no benchmark data; the workloads are defined by their recipe:
+  * layered + Gaussian-random-field models: ``n_layers`` horizontal layers of equal
+    thickness with velocities drawn uniformly from [vmin, vmax] and sorted to increase
+    with depth, multiplied by (1 + p) where p is white noise filtered with a Gaussian
+    kernel (correlation length ``corr_m``), scaled to +-``pert`` and clipped;
+  * sources drawn uniformly in the domain (or on its top surface, for station tables
+    computed by reciprocity).
+"""
+import numpy as np
+
+
+def grf(shape, spacing, corr_m, rng):
+    """Zero-mean, unit-max Gaussian random field with a Gaussian correlation kernel."""
+    noise = rng.standard_normal(shape)
+    freqs = [np.fft.fftfreq(n, d=spacing) for n in shape[:-1]] + [np.fft.rfftfreq(shape[-1], d=spacing)]
+    grids = np.meshgrid(*freqs, indexing="ij", sparse=True)
+    k2 = sum(g ** 2 for g in grids)
+    # Gaussian kernel exp(-r^2/corr^2) has spectrum ~ exp(-pi^2 corr^2 k^2)
+    filt = np.exp(-(np.pi ** 2) * corr_m ** 2 * k2)
+    field = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=shape)
+    field -= field.mean()
+    m = np.max(np.abs(field))
+    return field / m if m > 0 else field
+
+
+def layered_grf_model(nx, ny, nz, h, seed, n_layers=8, vmin=3000.0, vmax=7000.0, pert=0.05,
+                      corr_m=1000.0, dtype=np.float32):
+    """Nodal velocities (nz, ny, nx) of the layered + GRF recipe."""
+    rng = np.random.default_rng(seed)
+    layer_v = np.sort(rng.uniform(vmin, vmax, n_layers))
+    iz = np.arange(nz)
+    layer = np.minimum(iz * n_layers // nz, n_layers - 1)
+    v = np.broadcast_to(layer_v[layer][:, None, None], (nz, ny, nx)).astype(np.float64)
+    p = grf((nz, ny, nx), h, corr_m, rng) * pert
+    v = v * (1.0 + np.clip(p, -pert, pert))
+    return np.ascontiguousarray(v, dtype=dtype)
+
+
+def uniform_sources(n, nx, ny, nz, h, seed, surface=False):
+    """n source positions (x, y, z) in metres, uniform in the domain (or on z = 0)."""
+    rng = np.random.default_rng(seed)
+    xyz = np.column_stack([rng.uniform(0, (nx - 1) * h, n), rng.uniform(0, (ny - 1) * h, n),
+                           np.zeros(n) if surface else rng.uniform(0, (nz - 1) * h, n)])
+    return xyz

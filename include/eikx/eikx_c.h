@@ -61,7 +61,9 @@ typedef struct {
                               wait on progress that never comes; their bounded waits run
                               out and the solve returns EIKX_ERR_TIMEOUT (the context stays
                               usable).  Exercises failure detection without a GPU fault. */
-    int reserved[5];
+    int profile_sweeps;    /* 1 = run the schedule without the CUDA graph and time every sweep
+                              kernel with CUDA events (eikx_stats.sweep_ms); 0 = graph replay */
+    int reserved[4];
 } eikx_options;
 
 /* Fills *opt with the defaults above. */
@@ -81,7 +83,8 @@ typedef struct {
     int sweeps_launched;     /* sweep kernels launched (init pass included) */
     int kernel_launches;     /* all kernels launched by the call (graph nodes included) */
     double residual_last;    /* largest decrease of the last iteration over all fields (s) */
-    double device_ms;        /* device time of the solve (CUDA events) */
+    double device_ms;        /* device time of the solve incl. the copy-out (CUDA events) */
+    double sweep_ms;         /* summed device time of the sweep kernels (profile_sweeps), else -1 */
 } eikx_stats;
 
 /* ---- context ----------------------------------------------------------- */
