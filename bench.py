@@ -221,9 +221,27 @@ def run_gpu(args):
         "gpu_launches": int(launches), "clocks": clk.summary(),
         "iterations": {"max": int(max(iters)), "min": int(min(iters))},
         "wall_ms_per_step": float(np.mean(wall)), "accuracy": acc,
-        "cpu_baseline": cpu_baseline(args.cpu_seconds) if not args.skip_cpu else None,
+        "cpu_baseline": (cpu_baseline(args.cpu_seconds, 1, _sweeps_per_grid(max(iters)))
+                         if not args.skip_cpu else None),
     }
     print(json.dumps(line), flush=True)
+
+
+def profile_case(fields):
+    """The workload's grid and model, `fields` sources, one refinement iteration, without
+    the CUDA graph: 8 source-limited sweeps then 8 full sweeps (launches 9-16)."""
+    import torch
+    import eikonalxx_gb300 as ex
+    v, src = make_workload(fields)
+    ctx = ex.Context(torch.cuda.current_device())
+    ctx.set_grid3d(NX, NY, NZ, H, H, H)
+    ctx.set_nodal_velocity3d(v.ravel())
+    opt = ex.Options(n_sweeps=1, tolerance=-1, factored_radius=RADIUS, profile_sweeps=True)
+    out = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device="cuda")
+    ctx.solve3d(src, opt, ex.F32, out=out)
+    st = ctx.stats()
+    print(json.dumps({"profile_case": True, "fields": fields, "sweep_ms_mean": st["sweep_ms"] / st["sweeps_launched"],
+                      "device_ms": st["device_ms"]}))
 
 
 def _cpu_solver():
@@ -251,10 +269,17 @@ def cpu_sweep_rate(seconds, threads):
     s = _host_slowness(v)
     nn = NX * NY * NZ
 
+    # start from a realistic field (homogeneous-medium times at the mean slowness), so
+    # the operators take the branches they take in a real solve
+    zz, yy, xx = np.meshgrid(np.arange(NZ) * H, np.arange(NY) * H, np.arange(NX) * H, indexing="ij",
+                             sparse=True)
+    s_mean = float(np.mean(s))
+
     def one(i, out):
         pos = src[i]
         cell = [min(n - 2, int(p / H)) for p, n in zip(pos, (NX, NY, NZ))]
-        tt = np.full(nn, 1e10, np.float32)
+        tt = (np.sqrt((xx - pos[0]) ** 2 + (yy - pos[1]) ** 2 + (zz - pos[2]) ** 2) * s_mean * 1.05
+              ).astype(np.float32).ravel()
         d = ctypes.c_double
         n_done, t0 = 0, time.perf_counter()
         P = lambda a: ctypes.c_void_p(a.ctypes.data)
@@ -279,10 +304,11 @@ def cpu_sweep_rate(seconds, threads):
     return kind, rate, sum(n for n, _ in res.values())
 
 
-def _sweeps_per_grid():
-    """Sweeps one config grid needs on the GPU path (init pass + iterations), for the
-    CPU extrapolation; measured by the GPU arm, else the schedule maximum."""
-    return 8 * (1 + 4)
+def _sweeps_per_grid(iterations=None):
+    """Sweeps one grid of this workload takes (init pass + refinement iterations), for
+    the CPU extrapolation: the GPU arm passes the iterations it measured; otherwise the
+    count the workload converges in (4 iterations, measured on GB300)."""
+    return 8 * (1 + (iterations if iterations else 4))
 
 
 def cpu_baseline(seconds, threads=1, sweeps_per_grid=None):
@@ -333,7 +359,12 @@ def main():
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="one solve of the workload (1 refinement iteration) for ncu captures")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.fields)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

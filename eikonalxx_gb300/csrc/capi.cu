@@ -85,8 +85,7 @@ bool locate(double x, double x0, double d, int n, int *cell, double *offset) {
 }
 
 struct Workspace {
-    DevBuf tt, progress0, progress1, queue, residual, converged, iterations, abortFlag, order, srcs,
-        corners;
+    DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners;
     PinnedBuf stage;
     std::vector<int> orderKey;   // (tilesY, tilesZ, nFields, dim) of the uploaded order table
 };
@@ -114,7 +113,7 @@ struct eikx_ctx {
     bool haveGrid3 = false, haveSlow3 = false;
     DevBuf slow3;                  // natural-order cell slowness, FP64
     std::vector<double> hostSlow3; // host mirror (source-cell slowness lookups)
-    DevBuf spad3[2];
+    DevBuf spad3[2][2];            // [precision][0: shifted for +x sweeps, 1: unshifted]
     bool spadValid3[2] = {false, false};
     // 2D model
     int nx2 = 0, nz2 = 0;
@@ -122,7 +121,7 @@ struct eikx_ctx {
     bool haveGrid2 = false, haveSlow2 = false;
     DevBuf slow2;
     std::vector<double> hostSlow2;
-    DevBuf spad2[2];
+    DevBuf spad2[2][2];
     bool spadValid2[2] = {false, false};
     DevBuf scratch;                // staging for host inputs and analytic fields
     Workspace ws;
@@ -229,7 +228,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     const double dx = DIM == 3 ? c->dx : c->dx2, dy = DIM == 3 ? c->dy : 1.0, dz = DIM == 3 ? c->dz : c->dz2;
     const double x0 = DIM == 3 ? c->x0 : c->x02, y0 = DIM == 3 ? c->y0 : 0.0, z0 = DIM == 3 ? c->z0 : c->z02;
     const int Px = roundUp(nx, 4);
-    const int spPitch = roundUp(Px + 1, 4);
+    const int spPitch = Px + 8;
     const long long fieldStride = static_cast<long long>(Px) * ny * nz;
     const std::vector<double> &hs = DIM == 3 ? c->hostSlow3 : c->hostSlow2;
 
@@ -259,19 +258,23 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
         corners[i] = eikx::Corner3{cx, cy, cz, ox, oy, oz, static_cast<double>(static_cast<T>(s))};
     }
 
-    // padded slowness in the sweep precision
-    DevBuf &spad = DIM == 3 ? c->spad3[P] : c->spad2[P];
+    // edge-replicated slowness in the sweep precision: one copy shifted by V-1 columns
+    // (16-byte chunks of V elements) for +x sweeps, one unshifted for -x sweeps
+    DevBuf *spad = DIM == 3 ? c->spad3[P] : c->spad2[P];
     bool &spadValid = DIM == 3 ? c->spadValid3[P] : c->spadValid2[P];
-    const size_t spElems = static_cast<size_t>(spPitch) * (ny + 1) * (nz + 1);
-    if (!spadValid || spad.bytes < spElems * sizeof(T)) {
-        if (spad.bytes < spElems * sizeof(T)) dropGraph(c);
-        EIKX_CUDA(spad.ensure(spElems * sizeof(T)));
-        if (DIM == 3)
-            EIKX_CUDA((eikx::launchPadSlowness3<T, double>(spad.as<T>(), spPitch, c->slow3.as<double>(), nx, ny, nz,
-                                                           c->stream)));
-        else
-            EIKX_CUDA((eikx::launchPadSlowness2<T, double>(spad.as<T>(), spPitch, c->slow2.as<double>(), nx, nz,
-                                                           c->stream)));
+    const size_t spElems = static_cast<size_t>(spPitch) * (DIM == 3 ? ny + 1 : 1) * (nz + 1);
+    if (!spadValid || spad[0].bytes < spElems * sizeof(T)) {
+        if (spad[0].bytes < spElems * sizeof(T)) dropGraph(c);
+        for (int k = 0; k < 2; ++k) {
+            EIKX_CUDA(spad[k].ensure(spElems * sizeof(T)));
+            const int shift = k == 0 ? static_cast<int>(16 / sizeof(T)) - 1 : 0;
+            if (DIM == 3)
+                EIKX_CUDA((eikx::launchPadSlowness3<T, double>(spad[k].as<T>(), spPitch, shift, c->slow3.as<double>(),
+                                                               nx, ny, nz, c->stream)));
+            else
+                EIKX_CUDA((eikx::launchPadSlowness2<T, double>(spad[k].as<T>(), spPitch, shift, c->slow2.as<double>(),
+                                                               nx, nz, c->stream)));
+        }
         spadValid = true;
     }
 
@@ -285,11 +288,20 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     const int resStride = nSweepKinds * (1 + nSweeps);
     Workspace &w = c->ws;
     const size_t ttBytes = static_cast<size_t>(fieldStride) * nSrc * sizeof(T);
-    const void *before[] = {w.tt.p, w.progress0.p, w.progress1.p, w.residual.p, w.converged.p,
+    const int mailWords = static_cast<int>(sizeof(T) / 4);   // tagged 64-bit words per value
+    const size_t mboxBytes = static_cast<size_t>(nProgress) * (DIM == 3 ? ly + lz : 1) * Px * mailWords * 8;
+    const void *before[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
                             w.iterations.p, w.order.p, w.srcs.p, w.corners.p};
     EIKX_CUDA(w.tt.ensure(ttBytes));
-    EIKX_CUDA(w.progress0.ensure(static_cast<size_t>(nProgress) * 4));
-    EIKX_CUDA(w.progress1.ensure(static_cast<size_t>(nProgress) * 4));
+    if (w.mbox.bytes < mboxBytes || !w.mbox.p) {
+        // fresh words carry tag 0, which no sweep uses
+        EIKX_CUDA(w.mbox.ensure(mboxBytes));
+        EIKX_CUDA(cudaMemsetAsync(w.mbox.p, 0, w.mbox.bytes, c->stream));
+    }
+    if (!w.epoch.p) {
+        EIKX_CUDA(w.epoch.ensure(sizeof(unsigned)));
+        EIKX_CUDA(cudaMemsetAsync(w.epoch.p, 0, sizeof(unsigned), c->stream));
+    }
     EIKX_CUDA(w.queue.ensure(2 * sizeof(unsigned)));
     EIKX_CUDA(w.residual.ensure(static_cast<size_t>(nSrc) * resStride * 8));
     EIKX_CUDA(w.converged.ensure(static_cast<size_t>(nSrc) * 4));
@@ -298,7 +310,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     EIKX_CUDA(w.order.ensure(static_cast<size_t>(nProgress) * 16));
     EIKX_CUDA(w.srcs.ensure(static_cast<size_t>(nSrc) * sizeof(eikx::SourceT<T>)));
     EIKX_CUDA(w.corners.ensure(static_cast<size_t>(nSrc) * sizeof(eikx::Corner3)));
-    const void *after[] = {w.tt.p, w.progress0.p, w.progress1.p, w.residual.p, w.converged.p,
+    const void *after[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
                            w.iterations.p, w.order.p, w.srcs.p, w.corners.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) dropGraph(c);
 
@@ -324,12 +336,13 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
         w.orderKey = key;
     }
 
+    const int nSweepLaunches = nSweepKinds * ((o.init_sweeps ? 1 : 0) + nSweeps);
     eikx::SolveState st{};
-    st.progress[0] = w.progress0.as<unsigned>();
-    st.progress[1] = w.progress1.as<unsigned>();
     st.queue[0] = w.queue.as<unsigned>();
     st.queue[1] = w.queue.as<unsigned>() + 1;
-    st.nProgress = nProgress;
+    st.mbox = w.mbox.as<unsigned long long>();
+    st.epoch = w.epoch.as<unsigned>();
+    st.epochStride = nSweepLaunches + 1;
     st.residual = w.residual.as<unsigned long long>();
     st.residualStride = resStride;
     st.converged = w.converged.as<int>();
@@ -354,12 +367,11 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     sk.nSweeps = nSweeps; sk.radius = o.factored_radius; sk.initSweeps = o.init_sweeps ? 1 : 0;
     sk.initFp64 = o.init_fp64 ? 1 : 0; sk.uniform = uniform; sk.blocks = blocks; sk.tol = o.tolerance;
     sk.h = dx; sk.dx = dx; sk.dy = dy; sk.dz = dz; sk.spin = st.spinLimit; sk.dropBlocks = drop;
-    sk.tt = w.tt.p; sk.sp = spad.p; sk.srcs = w.srcs.p; sk.corners = w.corners.p;
+    sk.tt = w.tt.p; sk.sp = spad[0].p; sk.srcs = w.srcs.p; sk.corners = w.corners.p;
 
     int launches = 0;
     int sweepsLaunched = 0;
     const bool profile = o.profile_sweeps != 0;
-    const int nSweepLaunches = nSweepKinds * ((o.init_sweeps ? 1 : 0) + nSweeps);
     if (profile) {
         while (static_cast<int>(c->sweepEv.size()) < 2 * nSweepLaunches) {
             cudaEvent_t e;
@@ -385,9 +397,11 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
             if (DIM == 3) {
                 eikx::Sweep3Args<T> a{};
                 a.tt = w.tt.as<T>(); a.fieldStride = fieldStride; a.pitch = Px;
-                a.sp = spad.as<T>(); a.spPitch = spPitch; a.spPlane = static_cast<long long>(spPitch) * (ny + 1);
+                a.spPos = spad[0].as<T>(); a.spNeg = spad[1].as<T>(); a.spPitch = spPitch;
+                a.spPlane = static_cast<long long>(spPitch) * (ny + 1);
                 a.nx = nx; a.ny = ny; a.nz = nz; a.tilesY = tilesY; a.tilesZ = tilesZ;
                 a.srcs = w.srcs.as<eikx::SourceT<T>>(); a.st = st; a.buf = buf; a.residualSlot = slot;
+                a.sweepIndex = sweepsLaunched;
                 a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = static_cast<T>(dx);
                 const T tdx = static_cast<T>(dx), tdy = static_cast<T>(dy), tdz = static_cast<T>(dz);
                 eikx::Spacing3<T> g;
@@ -404,8 +418,10 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
             } else {
                 eikx::Sweep2Args<T> a{};
                 a.tt = w.tt.as<T>(); a.fieldStride = fieldStride; a.pitch = Px;
-                a.sp = spad.as<T>(); a.spPitch = spPitch; a.nx = nx; a.nz = nz; a.tilesZ = tilesZ;
+                a.spPos = spad[0].as<T>(); a.spNeg = spad[1].as<T>(); a.spPitch = spPitch;
+                a.nx = nx; a.nz = nz; a.tilesZ = tilesZ;
                 a.srcs = w.srcs.as<eikx::SourceT<T>>(); a.st = st; a.buf = buf; a.residualSlot = slot;
+                a.sweepIndex = sweepsLaunched;
                 a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = static_cast<T>(dx);
                 eikx::Spacing2<T> g;
                 g.dx = static_cast<T>(dx); g.dz = static_cast<T>(dz);

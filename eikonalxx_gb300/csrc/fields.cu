@@ -80,9 +80,11 @@ __global__ void init2Kernel(T *tt, int nFields, long long fieldStride, int pitch
 
 // Edge-replicated slowness: padded cell p holds cell clamp(p - 1) on every axis, so a
 // node i reads padded cells i and i + 1 without the clamps of
-// gridToSurroundingSlownessIndices (solverUtilities3d.hpp:1300-1442).
+// gridToSurroundingSlownessIndices (solverUtilities3d.hpp:1300-1442).  Along x the
+// copy is stored `shift` columns to the right, which aligns the cells a forward sweep
+// streams with the 16-byte chunks of its travel-time rows.
 template <class T, class U>
-__global__ void pad3Kernel(T *sp, int spPitch, const U *s, int nx, int ny, int nz) {
+__global__ void pad3Kernel(T *sp, int spPitch, int shift, const U *s, int nx, int ny, int nz) {
     const int ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
     const long long n = static_cast<long long>(spPitch) * (ny + 1) * (nz + 1);
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
@@ -91,21 +93,21 @@ __global__ void pad3Kernel(T *sp, int spPitch, const U *s, int nx, int ny, int n
         const long long r = i / spPitch;
         const int py = static_cast<int>(r % (ny + 1));
         const int pz = static_cast<int>(r / (ny + 1));
-        const int cx = clampi(px - 1, 0, ncx - 1), cy = clampi(py - 1, 0, ncy - 1),
+        const int cx = clampi(px - 1 - shift, 0, ncx - 1), cy = clampi(py - 1, 0, ncy - 1),
                   cz = clampi(pz - 1, 0, ncz - 1);
         sp[i] = static_cast<T>(s[(static_cast<long long>(cz) * ncy + cy) * ncx + cx]);
     }
 }
 
 template <class T, class U>
-__global__ void pad2Kernel(T *sp, int spPitch, const U *s, int nx, int nz) {
+__global__ void pad2Kernel(T *sp, int spPitch, int shift, const U *s, int nx, int nz) {
     const int ncx = nx - 1, ncz = nz - 1;
     const long long n = static_cast<long long>(spPitch) * (nz + 1);
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
         const int px = static_cast<int>(i % spPitch);
         const int pz = static_cast<int>(i / spPitch);
-        const int cx = clampi(px - 1, 0, ncx - 1), cz = clampi(pz - 1, 0, ncz - 1);
+        const int cx = clampi(px - 1 - shift, 0, ncx - 1), cz = clampi(pz - 1, 0, ncz - 1);
         sp[i] = static_cast<T>(s[static_cast<long long>(cz) * ncx + cx]);
     }
 }
@@ -185,10 +187,11 @@ __global__ void cells2Kernel(double *slow, const U *c, int nx, int nz, int order
     }
 }
 
+// Start of a solve: fresh residual slots and flags, and a new range of mailbox tags
+// (words written by earlier solves can never match a tag of this one).
 __global__ void resetKernel(SolveState st, int nFields, int buf) {
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gthreads = gridDim.x * blockDim.x;
-    for (int i = gtid; i < st.nProgress; i += gthreads) st.progress[buf][i] = 0u;
     const long long nres = static_cast<long long>(nFields) * st.residualStride;
     for (long long i = gtid; i < nres; i += gthreads) st.residual[i] = 0ull;
     for (int i = gtid; i < nFields; i += gthreads) {
@@ -198,6 +201,7 @@ __global__ void resetKernel(SolveState st, int nFields, int buf) {
     if (gtid == 0) {
         *st.queue[buf] = 0u;
         *st.abortFlag = 0;
+        *st.epoch += static_cast<unsigned>(st.epochStride);
     }
 }
 
@@ -288,15 +292,15 @@ cudaError_t launchInit2(T *tt, int nFields, long long fieldStride, int pitch, in
     return cudaGetLastError();
 }
 template <class T, class U>
-cudaError_t launchPadSlowness3(T *sp, int spPitch, const U *s, int nx, int ny, int nz, cudaStream_t st) {
+cudaError_t launchPadSlowness3(T *sp, int spPitch, int shift, const U *s, int nx, int ny, int nz, cudaStream_t st) {
     const long long n = static_cast<long long>(spPitch) * (ny + 1) * (nz + 1);
-    pad3Kernel<T, U><<<gridFor(n), kThreads, 0, st>>>(sp, spPitch, s, nx, ny, nz);
+    pad3Kernel<T, U><<<gridFor(n), kThreads, 0, st>>>(sp, spPitch, shift, s, nx, ny, nz);
     return cudaGetLastError();
 }
 template <class T, class U>
-cudaError_t launchPadSlowness2(T *sp, int spPitch, const U *s, int nx, int nz, cudaStream_t st) {
+cudaError_t launchPadSlowness2(T *sp, int spPitch, int shift, const U *s, int nx, int nz, cudaStream_t st) {
     const long long n = static_cast<long long>(spPitch) * (nz + 1);
-    pad2Kernel<T, U><<<gridFor(n), kThreads, 0, st>>>(sp, spPitch, s, nx, nz);
+    pad2Kernel<T, U><<<gridFor(n), kThreads, 0, st>>>(sp, spPitch, shift, s, nx, nz);
     return cudaGetLastError();
 }
 template <class U>
@@ -323,9 +327,8 @@ cudaError_t launchCellsToNatural2(double *slow, const U *c, int nx, int nz, int 
     cells2Kernel<U><<<gridFor(n), kThreads, 0, s>>>(slow, c, nx, nz, ordering);
     return cudaGetLastError();
 }
-cudaError_t launchResetState(const SolveState &st, int nFields, int progressBuf, cudaStream_t s) {
-    resetKernel<<<gridFor(st.nProgress + static_cast<long long>(nFields) * st.residualStride), kThreads, 0, s>>>(
-        st, nFields, progressBuf);
+cudaError_t launchResetState(const SolveState &st, int nFields, int buf, cudaStream_t s) {
+    resetKernel<<<gridFor(static_cast<long long>(nFields) * st.residualStride), kThreads, 0, s>>>(st, nFields, buf);
     return cudaGetLastError();
 }
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots, int iteration,
@@ -354,10 +357,11 @@ template cudaError_t launchInit2<float>(float *, int, long long, int, int, int, 
                                         int, cudaStream_t);
 template cudaError_t launchInit2<double>(double *, int, long long, int, int, int, double, double,
                                          const Corner3 *, int, cudaStream_t);
-template cudaError_t launchPadSlowness3<float, double>(float *, int, const double *, int, int, int, cudaStream_t);
-template cudaError_t launchPadSlowness3<double, double>(double *, int, const double *, int, int, int, cudaStream_t);
-template cudaError_t launchPadSlowness2<float, double>(float *, int, const double *, int, int, cudaStream_t);
-template cudaError_t launchPadSlowness2<double, double>(double *, int, const double *, int, int, cudaStream_t);
+template cudaError_t launchPadSlowness3<float, double>(float *, int, int, const double *, int, int, int, cudaStream_t);
+template cudaError_t launchPadSlowness3<double, double>(double *, int, int, const double *, int, int, int,
+                                                        cudaStream_t);
+template cudaError_t launchPadSlowness2<float, double>(float *, int, int, const double *, int, int, cudaStream_t);
+template cudaError_t launchPadSlowness2<double, double>(double *, int, int, const double *, int, int, cudaStream_t);
 template cudaError_t launchNodalToCell3<float>(double *, const float *, int, int, int, int, cudaStream_t);
 template cudaError_t launchNodalToCell3<double>(double *, const double *, int, int, int, int, cudaStream_t);
 template cudaError_t launchNodalToCell2<float>(double *, const float *, int, int, int, cudaStream_t);

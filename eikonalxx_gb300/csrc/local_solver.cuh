@@ -98,33 +98,36 @@ __device__ __forceinline__ T fd3Uniform(int radius, T h, const SourceT<T> &src,
     T hs01 = h * minS0S1;
     T hs04 = h * minS0S4;
     if (abs(src.isx - ix) > radius || abs(src.isy - iy) > radius || abs(src.isz - iz) > radius) {
-        // 2D critically refracted (diagonal) operators in the XZ, YZ and XY planes
+        // 2D critically refracted (diagonal) operators in the XZ, YZ and XY planes.
+        // Evaluated branch-free: every lane runs the same instructions and a failed
+        // condition selects `huge`; a taken operator rounds exactly as the reference's.
+        const T one = 1;
         T dXZ = t1 - t4;
         T detXZ = 2 * (hs03 * hs03) - dXZ * dXZ;
-        T t2d = huge;
-        if (detXZ > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03) t2d = t5 + dsqrt(detXZ);
+        const bool cXZ = detXZ > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03;
+        const T rXZ = dsqrt(cXZ ? detXZ : one);
+        T t2d = cXZ ? t5 + rXZ : huge;
         T dYZ = t3 - t4;
         T detYZ = 2 * (hs01 * hs01) - dYZ * dYZ;
-        T t2d2 = huge;
-        if (detYZ > 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01) t2d2 = t7 + dsqrt(detYZ);
-        t2d = dmin(t2d, t2d2);
+        const bool cYZ = detYZ > 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01;
+        const T rYZ = dsqrt(cYZ ? detYZ : one);
+        t2d = dmin(t2d, cYZ ? t7 + rYZ : huge);
         T dXY = t1 - t3;
         T detXY = 2 * (hs04 * hs04) - dXY * dXY;
-        T t2d3 = huge;
-        if (detXY > 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04) t2d3 = t2 + dsqrt(detXY);
-        t2d = dmin(t2d, t2d3);
+        const bool cXY = detXY > 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04;
+        const T rXY = dsqrt(cXY ? detXY : one);
+        t2d = dmin(t2d, cXY ? t2 + rXY : huge);
         // 8-point operator, taken only when the wave travels the sweep's way
-        T t3d = huge;
-        if (dmin(t1d, t2d) > dmax(dmax(t1, t4), t3)) {
-            const T third = static_cast<T>(0.33333333333333333333333);
-            const T half = static_cast<T>(0.5);
-            T Tx = t1 + half * (-t4 + t5 - t3 + t2) - t7 + t6;
-            T Ty = t3 + half * (-t4 + t7 - t1 + t2) - t5 + t6;
-            T Tz = t4 + half * (-t1 + t5 - t3 + t7) - t2 + t6;
-            T det = 27 * (h * s0) * (h * s0) - (Tx - Ty) * (Tx - Ty) - (Tx - Tz) * (Tx - Tz) -
-                    (Ty - Tz) * (Ty - Tz);
-            if (det >= 0) t3d = third * ((Tx + Ty + Tz) + dsqrt(det));
-        }
+        const T third = static_cast<T>(0.33333333333333333333333);
+        const T half = static_cast<T>(0.5);
+        T Tx = t1 + half * (-t4 + t5 - t3 + t2) - t7 + t6;
+        T Ty = t3 + half * (-t4 + t7 - t1 + t2) - t5 + t6;
+        T Tz = t4 + half * (-t1 + t5 - t3 + t7) - t2 + t6;
+        T det = 27 * (h * s0) * (h * s0) - (Tx - Ty) * (Tx - Ty) - (Tx - Tz) * (Tx - Tz) -
+                (Ty - Tz) * (Ty - Tz);
+        const bool c3 = dmin(t1d, t2d) > dmax(dmax(t1, t4), t3) && det >= 0;
+        const T r3 = dsqrt(c3 ? det : one);
+        T t3d = c3 ? third * ((Tx + Ty + Tz) + r3) : huge;
         tUpd = dmin(t1d, dmin(t2d, t3d));
     } else {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;

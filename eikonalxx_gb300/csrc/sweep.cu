@@ -21,15 +21,47 @@ constexpr int kThreads = 32 * kWarpsPerBlock;
 
 template <class T> __device__ __forceinline__ T hugeT() { return static_cast<T>(1.e10); }
 
-// Zero the other progress buffer and queue head for the next sweep.  The launch
-// boundary orders this before the next sweep reads them.
+// Zero the queue head the next sweep uses; the launch boundary orders it before use.
 __device__ __forceinline__ void clearNext(const SolveState &st, int buf) {
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int gthreads = gridDim.x * blockDim.x;
-    unsigned *nxt = st.progress[buf ^ 1];
-    for (int i = gtid; i < st.nProgress; i += gthreads) nxt[i] = 0u;
-    if (gtid == 0) *st.queue[buf ^ 1] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *st.queue[buf ^ 1] = 0u;
 }
+
+// Own-row stream: the travel times and slowness of one lane's x'-pencil, consumed one
+// element per step in walk order, fetched in 16-byte chunks one chunk ahead.
+//   T row     forward (+x sweep): chunk k at row + k*V;   reverse: row + Px - (k+1)*V
+//   slowness  forward: shifted copy, chunk k at srow + (k+1)*V; reverse: srow + Px - (k+1)*V
+template <class T> struct RowStream {
+    static constexpr int V = Chunk<T>::kN;
+    Chunk<T> tCur, tNxt, sCur, sNxt;
+    const T *row, *srow;
+    int Px, rev, nChunks;
+    __device__ __forceinline__ const T *tAddr(int k) const { return rev ? row + Px - (k + 1) * V : row + k * V; }
+    __device__ __forceinline__ const T *sAddr(int k) const { return rev ? srow + Px - (k + 1) * V : srow + (k + 1) * V; }
+    __device__ __forceinline__ void start() {
+        tCur.load(tAddr(0));
+        sCur.load(sAddr(0));
+        if (nChunks > 1) {
+            tNxt.load(tAddr(1));
+            sNxt.load(sAddr(1));
+        }
+    }
+    // values of walk position xp (called for xp = 0, 1, 2, ... in order)
+    __device__ __forceinline__ void take(int xp, T &t, T &s) {
+        const int e = xp & (V - 1);
+        if (e == 0 && xp > 0) {
+            tCur = tNxt;
+            sCur = sNxt;
+            const int k = (xp / V) + 1;
+            if (k < nChunks) {
+                tNxt.load(tAddr(k));
+                sNxt.load(sAddr(k));
+            }
+        }
+        const int i = rev ? V - 1 - e : e;
+        t = tCur.at(i);
+        s = sCur.at(i);
+    }
+};
 
 template <class T, bool UNIFORM>
 __global__ void __launch_bounds__(kThreads) sweep3Kernel(const Sweep3Args<T> a) {
@@ -41,6 +73,8 @@ __global__ void __launch_bounds__(kThreads) sweep3Kernel(const Sweep3Args<T> a) 
     const SolveState &st = a.st;
     clearNext(st, a.buf);
     if (ldVolatile(st.abortFlag)) return;
+    constexpr int W = Mail<T>::kWords;
+    const unsigned tag = *st.epoch + static_cast<unsigned>(a.sweepIndex);
 
     const int fx = a.sweep & 1, fy = (a.sweep >> 1) & 1, fz = (a.sweep >> 2) & 1;
     SweepSigns sg;
@@ -48,11 +82,9 @@ __global__ void __launch_bounds__(kThreads) sweep3Kernel(const Sweep3Args<T> a) 
     sg.signX = fx ? -1 : 1; sg.signY = fy ? -1 : 1; sg.signZ = fz ? -1 : 1;
     const int Px = a.pitch;
     const int nSteps = Px + LY3 + LZ3 - 2;
-    const int spMaxX = a.spPitch - 1;
-    const int sColOff = fx ? 0 : 1;   // own slowness column: the "offset" cell side
-    const int tilesPerField = a.tilesY * a.tilesZ;
-    unsigned *progress = st.progress[a.buf];
+    const T *sp = fx ? a.spNeg : a.spPos;
     const T huge = hugeT<T>();
+    const long long faceWords = static_cast<long long>(LY3 + LZ3) * Px * W;
 
     // helper lanes stand in for the virtual upwind lanes of the halo row/column
     const bool helper = lane < HZ3 + LY3;
@@ -82,96 +114,135 @@ __global__ void __launch_bounds__(kThreads) sweep3Kernel(const Sweep3Args<T> a) 
         const bool yzUpd = laneValid && ya >= ylo && ya <= yhi && za >= zlo && za <= zhi;
         T *field = a.tt + static_cast<long long>(f) * a.fieldStride;
         T *row = field + (static_cast<long long>(za) * a.ny + ya) * a.pitch;
-        const T *srow = a.sp + static_cast<long long>(za + (fz ? 0 : 1)) * a.spPlane +
-                        static_cast<long long>(ya + (fy ? 0 : 1)) * a.spPitch;
-        // virtual lane rows
+        RowStream<T> rs;
+        rs.row = row;
+        rs.srow = sp + static_cast<long long>(za + (fz ? 0 : 1)) * a.spPlane +
+                  static_cast<long long>(ya + (fy ? 0 : 1)) * a.spPitch;
+        rs.Px = Px;
+        rs.rev = fx;
+        rs.nChunks = Px / RowStream<T>::V;
+        if (laneValid) rs.start();
+
+        // mailbox: this block's faces, and the upstream face row a helper lane reads
+        const long long tileId = (static_cast<long long>(f) * a.tilesZ + c) * a.tilesY + b;
+        unsigned long long *box = st.mbox + tileId * faceWords;
+        unsigned long long *yFace = box + static_cast<long long>(lz) * Px * W;          // ly == LY-1
+        unsigned long long *zFace = box + static_cast<long long>(LZ3 + ly) * Px * W;    // lz == LZ-1
         const int vyp = y0 + vly, vzp = z0 + vlz;
         const bool vValid = helper && vyp >= 0 && vzp >= 0 && vyp < a.ny && vzp < a.nz;
-        const int vya = vValid ? reflect(vyp, a.ny, fy) : 0;
-        const int vza = vValid ? reflect(vzp, a.nz, fz) : 0;
-        const T *vrow = field + (static_cast<long long>(vza) * a.ny + vya) * a.pitch;
-        const T *vsrow = a.sp + static_cast<long long>(vza + (fz ? 0 : 1)) * a.spPlane +
-                         static_cast<long long>(vya + (fy ? 0 : 1)) * a.spPitch;
-        const unsigned *upY = b > 0 ? progress + f * tilesPerField + c * a.tilesY + (b - 1) : nullptr;
-        const unsigned *upZ = c > 0 ? progress + f * tilesPerField + (c - 1) * a.tilesY + b : nullptr;
-        unsigned *mine = progress + f * tilesPerField + c * a.tilesY + b;
-        unsigned knownY = 0, knownZ = 0;
-        bool ok = true;
+        const unsigned long long *vbox = st.mbox;
+        const T *vsrow = sp;
+        if (vValid) {
+            const int vya = reflect(vyp, a.ny, fy), vza = reflect(vzp, a.nz, fz);
+            if (vly < 0) {
+                const long long up = vlz >= 0 ? tileId - 1 : tileId - a.tilesY - 1;
+                vbox = st.mbox + up * faceWords + static_cast<long long>(vlz >= 0 ? vlz : LZ3 - 1) * Px * W;
+            } else {
+                vbox = st.mbox + (tileId - a.tilesY) * faceWords + static_cast<long long>(LZ3 + vly) * Px * W;
+            }
+            vsrow = sp + static_cast<long long>(vza + (fz ? 0 : 1)) * a.spPlane +
+                    static_cast<long long>(vya + (fy ? 0 : 1)) * a.spPitch;
+        }
 
-        // Fill the halo entries of ring slot `sv` (values the virtual lanes produce at step sv).
-        auto prefetch = [&](int sv) {
+        // Halo pipeline.  The values the virtual lanes produce at step sv go into ring slot
+        // sv; the reads for step sv are issued at step sv - kPref into register slot
+        // sv % kPref and checked (and stored into the ring) at step sv.
+        auto haloT = [&](int sv) { return sv - vly - vlz; };
+        auto haloValid = [&](int xv) { return vValid && xv >= 0 && xv < Px; };
+        auto haloStore = [&](int sv, T tv, T svv) {
+            const int slot = (sv & (kRing - 1)) * kPlane3 + vslot;
+            tring[slot] = tv;
+            sring[slot] = svv;
+        };
+        auto fillNow = [&](int sv) -> bool {
             bool good = true;
-            if (lane == 0) {
-                const int needY = max(0, min(sv + LY3 + 1, nSteps));
-                const int needZ = max(0, min(sv + LZ3 + 1, nSteps));
-                if (upY) good = waitAtLeast(upY, needY, knownY, st.abortFlag, st.spinLimit);
-                if (good && upZ) good = waitAtLeast(upZ, needZ, knownZ, st.abortFlag, st.spinLimit);
-            }
-            good = __shfl_sync(kFull, good ? 1 : 0, 0) != 0;
-            if (good && helper) {
-                const int xv = sv - vly - vlz;
+            if (helper) {
+                const int xv = haloT(sv);
                 T tv = huge, svv = huge;
-                if (vValid && xv >= 0 && xv < Px) {
-                    const int xa = reflect(xv, Px, fx);
-                    tv = ldL2(vrow + xa);
-                    svv = vsrow[min(xa + sColOff, spMaxX)];
+                if (haloValid(xv)) {
+                    good = Mail<T>::get(vbox + static_cast<long long>(xv) * W, tag, tv, st.abortFlag, st.spinLimit);
+                    svv = vsrow[fx ? Px - 1 - xv : xv + RowStream<T>::V];
                 }
-                const int slot = (sv & (kRing - 1)) * kPlane3 + vslot;
-                tring[slot] = tv;
-                sring[slot] = svv;
+                haloStore(sv, tv, svv);
             }
-            return good;
+            return __all_sync(kFull, good);
+        };
+        MailSlot<T> mslot[kPref];
+        T sslot[kPref];
+        auto issue = [&](int j, int sv) {
+            const int xv = haloT(sv);
+            if (helper && haloValid(xv)) {
+                mslot[j].issue(vbox + static_cast<long long>(xv) * W);
+                sslot[j] = vsrow[fx ? Px - 1 - xv : xv + RowStream<T>::V];
+            }
+        };
+        auto consume = [&](int j, int sv) -> bool {
+            bool good = true;
+            if (helper) {
+                const int xv = haloT(sv);
+                T tv = huge, svv = huge;
+                if (haloValid(xv)) {
+                    good = mslot[j].take(vbox + static_cast<long long>(xv) * W, tag, tv, st.abortFlag, st.spinLimit);
+                    svv = sslot[j];
+                }
+                haloStore(sv, tv, svv);
+            }
+            return __all_sync(kFull, good);
         };
 
-        for (int sv = -2; sv < kPref && ok; ++sv) ok = prefetch(sv);
+        bool ok = fillNow(-2) && fillNow(-1);
+#pragma unroll
+        for (int j = 0; j < kPref; ++j) issue(j, j);
         T res = 0;
-        for (int s = 0; s < nSteps && ok; ++s) {
-            ok = prefetch(s + kPref);
-            if (!ok) break;
-            const int xp = s - ly - lz;
-            const bool active = laneValid && xp >= 0 && xp < Px;
-            const int xa = reflect(xp, Px, fx);
-            T t0 = huge, sOwn = huge;
-            if (active) {
-                t0 = row[xa];
-                sOwn = srow[min(xa + sColOff, spMaxX)];
-            }
-            const int cur = (s & (kRing - 1)) * kPlane3;
-            const int p1 = ((s - 1) & (kRing - 1)) * kPlane3;
-            const int p2 = ((s - 2) & (kRing - 1)) * kPlane3;
-            const int p3 = ((s - 3) & (kRing - 1)) * kPlane3;
-            sring[cur + myslot] = sOwn;
-            __syncwarp();
-            Stencil3<T> n;
-            n.t1 = tring[p1 + myslot];
-            n.t3 = tring[p1 + myslot - 1];
-            n.t2 = tring[p2 + myslot - 1];
-            n.t4 = tring[p1 + myslot - HY3];
-            n.t5 = tring[p2 + myslot - HY3];
-            n.t7 = tring[p2 + myslot - HY3 - 1];
-            n.t6 = tring[p3 + myslot - HY3 - 1];
-            n.s0 = sring[p3 + myslot - HY3 - 1];
-            n.s1 = sring[p2 + myslot - HY3 - 1];
-            n.s2 = sring[p1 + myslot - HY3];
-            n.s3 = sring[p2 + myslot - HY3];
-            n.s4 = sring[p2 + myslot - 1];
-            n.s5 = sring[p1 + myslot - 1];
-            n.s7 = sring[p1 + myslot];
-            T v = t0;
-            if (active && yzUpd && xa >= xlo && xa <= xhi) {
-                const T tu = UNIFORM ? fd3Uniform<T>(a.radius, a.h, src, sg, xa, ya, za, n)
-                                     : fd3NonUniform<T>(a.radius, a.sp3, src, sg, xa, ya, za, n);
-                if (tu < t0) {
-                    v = tu;
-                    row[xa] = tu;
-                    res = dmax(res, t0 - tu);
-                }
-            }
-            tring[cur + myslot] = v;
-            if (((s + 1) % kPub) == 0 || s == nSteps - 1) {
-                fenceAcqRel();
+        for (int s0 = 0; s0 < nSteps && ok; s0 += kPref) {
+#pragma unroll
+            for (int j = 0; j < kPref; ++j) {
+                const int s = s0 + j;
+                if (!ok || s >= nSteps) continue;
+                ok = consume(j, s);
+                if (!ok) continue;
+                issue(j, s + kPref);
+                const int xp = s - ly - lz;
+                const bool active = laneValid && xp >= 0 && xp < Px;
+                const int xa = reflect(xp, Px, fx);
+                T t0 = huge, sOwn = huge;
+                if (active) rs.take(xp, t0, sOwn);
+                const int cur = (s & (kRing - 1)) * kPlane3;
+                const int p1 = ((s - 1) & (kRing - 1)) * kPlane3;
+                const int p2 = ((s - 2) & (kRing - 1)) * kPlane3;
+                const int p3 = ((s - 3) & (kRing - 1)) * kPlane3;
+                sring[cur + myslot] = sOwn;
                 __syncwarp();
-                if (lane == 0) stRelease(mine, static_cast<unsigned>(s + 1));
+                Stencil3<T> n;
+                n.t1 = tring[p1 + myslot];
+                n.t3 = tring[p1 + myslot - 1];
+                n.t2 = tring[p2 + myslot - 1];
+                n.t4 = tring[p1 + myslot - HY3];
+                n.t5 = tring[p2 + myslot - HY3];
+                n.t7 = tring[p2 + myslot - HY3 - 1];
+                n.t6 = tring[p3 + myslot - HY3 - 1];
+                n.s0 = sring[p3 + myslot - HY3 - 1];
+                n.s1 = sring[p2 + myslot - HY3 - 1];
+                n.s2 = sring[p1 + myslot - HY3];
+                n.s3 = sring[p2 + myslot - HY3];
+                n.s4 = sring[p2 + myslot - 1];
+                n.s5 = sring[p1 + myslot - 1];
+                n.s7 = sring[p1 + myslot];
+                T v = t0;
+                if (active && yzUpd && xa >= xlo && xa <= xhi) {
+                    const T tu = UNIFORM ? fd3Uniform<T>(a.radius, a.h, src, sg, xa, ya, za, n)
+                                         : fd3NonUniform<T>(a.radius, a.sp3, src, sg, xa, ya, za, n);
+                    if (tu < t0) {
+                        v = tu;
+                        row[xa] = tu;
+                        res = dmax(res, t0 - tu);
+                    }
+                }
+                tring[cur + myslot] = v;
+                if (active) {
+                    if (ly == LY3 - 1) Mail<T>::put(yFace + static_cast<long long>(xp) * W, tag, v);
+                    if (lz == LZ3 - 1) Mail<T>::put(zFace + static_cast<long long>(xp) * W, tag, v);
+                }
             }
         }
         if (!ok) break;
@@ -192,6 +263,8 @@ __global__ void __launch_bounds__(kThreads) sweep2Kernel(const Sweep2Args<T> a) 
     const SolveState &st = a.st;
     clearNext(st, a.buf);
     if (ldVolatile(st.abortFlag)) return;
+    constexpr int W = Mail<T>::kWords;
+    const unsigned tag = *st.epoch + static_cast<unsigned>(a.sweepIndex);
 
     const int fx = a.sweep & 1, fz = (a.sweep >> 1) & 1;
     SweepSigns sg;
@@ -199,11 +272,10 @@ __global__ void __launch_bounds__(kThreads) sweep2Kernel(const Sweep2Args<T> a) 
     sg.signX = fx ? -1 : 1; sg.signY = 1; sg.signZ = fz ? -1 : 1;
     const int Px = a.pitch;
     const int nSteps = Px + LZ2 - 1;
-    const int spMaxX = a.spPitch - 1;
-    const int sColOff = fx ? 0 : 1;
-    unsigned *progress = st.progress[a.buf];
+    const T *sp = fx ? a.spNeg : a.spPos;
     const T huge = hugeT<T>();
     const int myslot = lz + 1;
+    const long long faceWords = static_cast<long long>(Px) * W;
 
     while (true) {
         unsigned q = 0;
@@ -224,78 +296,105 @@ __global__ void __launch_bounds__(kThreads) sweep2Kernel(const Sweep2Args<T> a) 
         const bool zUpd = laneValid && za >= zlo && za <= zhi;
         T *field = a.tt + static_cast<long long>(f) * a.fieldStride;
         T *row = field + static_cast<long long>(za) * a.pitch;
-        const T *srow = a.sp + static_cast<long long>(za + (fz ? 0 : 1)) * a.spPitch;
-        // lane 0 also stands in for the virtual lane z' = z0 - 1
+        RowStream<T> rs;
+        rs.row = row;
+        rs.srow = sp + static_cast<long long>(za + (fz ? 0 : 1)) * a.spPitch;
+        rs.Px = Px;
+        rs.rev = fx;
+        rs.nChunks = Px / RowStream<T>::V;
+        if (laneValid) rs.start();
+        const long long tileId = static_cast<long long>(f) * a.tilesZ + c;
+        unsigned long long *face = st.mbox + tileId * faceWords;   // written by lane LZ2-1
+        // lane 0 also stands in for the virtual lane z' = z0 - 1 (row LZ2-1 of block c-1)
         const bool vValid = (lane == 0) && c > 0;
+        const unsigned long long *vbox = st.mbox + (tileId - (c > 0 ? 1 : 0)) * faceWords;
         const int vza = vValid ? reflect(z0 - 1, a.nz, fz) : 0;
-        const T *vrow = field + static_cast<long long>(vza) * a.pitch;
-        const T *vsrow = a.sp + static_cast<long long>(vza + (fz ? 0 : 1)) * a.spPitch;
-        const unsigned *up = c > 0 ? progress + f * a.tilesZ + (c - 1) : nullptr;
-        unsigned *mine = progress + f * a.tilesZ + c;
-        unsigned known = 0;
-        bool ok = true;
+        const T *vsrow = sp + static_cast<long long>(vza + (fz ? 0 : 1)) * a.spPitch;
 
-        auto prefetch = [&](int sv) {
+        // Halo pipeline as in the 3D kernel: lane 0 stands in for the virtual lane, whose
+        // value at step sv is node x' = sv + 1 of the upstream block's last row.
+        auto haloValid = [&](int xv) { return vValid && xv >= 0 && xv < Px; };
+        auto haloStore = [&](int sv, T tv, T svv) {
+            const int slot = (sv & (kRing - 1)) * kPlane2;
+            tring[slot] = tv;
+            sring[slot] = svv;
+        };
+        auto fillNow = [&](int sv) -> bool {
             bool good = true;
-            if (lane == 0 && up) {
-                const int need = max(0, min(sv + LZ2 + 1, nSteps));
-                good = waitAtLeast(up, need, known, st.abortFlag, st.spinLimit);
-            }
-            good = __shfl_sync(kFull, good ? 1 : 0, 0) != 0;
-            if (good && lane == 0) {
+            if (lane == 0) {
                 const int xv = sv + 1;
                 T tv = huge, svv = huge;
-                if (vValid && xv >= 0 && xv < Px) {
-                    const int xa = reflect(xv, Px, fx);
-                    tv = ldL2(vrow + xa);
-                    svv = vsrow[min(xa + sColOff, spMaxX)];
+                if (haloValid(xv)) {
+                    good = Mail<T>::get(vbox + static_cast<long long>(xv) * W, tag, tv, st.abortFlag, st.spinLimit);
+                    svv = vsrow[fx ? Px - 1 - xv : xv + RowStream<T>::V];
                 }
-                const int slot = (sv & (kRing - 1)) * kPlane2;
-                tring[slot] = tv;
-                sring[slot] = svv;
+                haloStore(sv, tv, svv);
             }
-            return good;
+            return __all_sync(kFull, good);
+        };
+        MailSlot<T> mslot[kPref];
+        T sslot[kPref];
+        auto issue = [&](int j, int sv) {
+            const int xv = sv + 1;
+            if (lane == 0 && haloValid(xv)) {
+                mslot[j].issue(vbox + static_cast<long long>(xv) * W);
+                sslot[j] = vsrow[fx ? Px - 1 - xv : xv + RowStream<T>::V];
+            }
+        };
+        auto consume = [&](int j, int sv) -> bool {
+            bool good = true;
+            if (lane == 0) {
+                const int xv = sv + 1;
+                T tv = huge, svv = huge;
+                if (haloValid(xv)) {
+                    good = mslot[j].take(vbox + static_cast<long long>(xv) * W, tag, tv, st.abortFlag, st.spinLimit);
+                    svv = sslot[j];
+                }
+                haloStore(sv, tv, svv);
+            }
+            return __all_sync(kFull, good);
         };
 
-        for (int sv = -1; sv < kPref && ok; ++sv) ok = prefetch(sv);
+        bool ok = fillNow(-1);
+#pragma unroll
+        for (int j = 0; j < kPref; ++j) issue(j, j);
         T res = 0;
-        for (int s = 0; s < nSteps && ok; ++s) {
-            ok = prefetch(s + kPref);
-            if (!ok) break;
-            const int xp = s - lz;
-            const bool active = laneValid && xp >= 0 && xp < Px;
-            const int xa = reflect(xp, Px, fx);
-            T t0 = huge, sOwn = huge;
-            if (active) {
-                t0 = row[xa];
-                sOwn = srow[min(xa + sColOff, spMaxX)];
-            }
-            const int cur = (s & (kRing - 1)) * kPlane2;
-            const int p1 = ((s - 1) & (kRing - 1)) * kPlane2;
-            const int p2 = ((s - 2) & (kRing - 1)) * kPlane2;
-            sring[cur + myslot] = sOwn;
-            __syncwarp();
-            const T t1 = tring[p1 + myslot];
-            const T t3 = tring[p1 + myslot - 1];
-            const T t2 = tring[p2 + myslot - 1];
-            const T s0 = sring[p2 + myslot - 1];
-            const T s1 = sring[p1 + myslot - 1];
-            const T s3 = sring[p1 + myslot];
-            T v = t0;
-            if (active && zUpd && xa >= xlo && xa <= xhi) {
-                const T tu = UNIFORM ? fd2Uniform<T>(a.radius, a.h, src, sg, xa, za, s0, s1, s3, t1, t2, t3)
-                                     : fd2NonUniform<T>(a.radius, a.sp2, src, sg, xa, za, s0, s1, s3, t1, t2, t3);
-                if (tu < t0) {
-                    v = tu;
-                    row[xa] = tu;
-                    res = dmax(res, t0 - tu);
-                }
-            }
-            tring[cur + myslot] = v;
-            if (((s + 1) % kPub) == 0 || s == nSteps - 1) {
-                fenceAcqRel();
+        for (int s0 = 0; s0 < nSteps && ok; s0 += kPref) {
+#pragma unroll
+            for (int j = 0; j < kPref; ++j) {
+                const int s = s0 + j;
+                if (!ok || s >= nSteps) continue;
+                ok = consume(j, s);
+                if (!ok) continue;
+                issue(j, s + kPref);
+                const int xp = s - lz;
+                const bool active = laneValid && xp >= 0 && xp < Px;
+                const int xa = reflect(xp, Px, fx);
+                T t0 = huge, sOwn = huge;
+                if (active) rs.take(xp, t0, sOwn);
+                const int cur = (s & (kRing - 1)) * kPlane2;
+                const int p1 = ((s - 1) & (kRing - 1)) * kPlane2;
+                const int p2 = ((s - 2) & (kRing - 1)) * kPlane2;
+                sring[cur + myslot] = sOwn;
                 __syncwarp();
-                if (lane == 0) stRelease(mine, static_cast<unsigned>(s + 1));
+                const T t1 = tring[p1 + myslot];
+                const T t3 = tring[p1 + myslot - 1];
+                const T t2 = tring[p2 + myslot - 1];
+                const T s0 = sring[p2 + myslot - 1];
+                const T s1 = sring[p1 + myslot - 1];
+                const T s3 = sring[p1 + myslot];
+                T v = t0;
+                if (active && zUpd && xa >= xlo && xa <= xhi) {
+                    const T tu = UNIFORM ? fd2Uniform<T>(a.radius, a.h, src, sg, xa, za, s0, s1, s3, t1, t2, t3)
+                                         : fd2NonUniform<T>(a.radius, a.sp2, src, sg, xa, za, s0, s1, s3, t1, t2, t3);
+                    if (tu < t0) {
+                        v = tu;
+                        row[xa] = tu;
+                        res = dmax(res, t0 - tu);
+                    }
+                }
+                tring[cur + myslot] = v;
+                if (active && lz == LZ2 - 1) Mail<T>::put(face + static_cast<long long>(xp) * W, tag, v);
             }
         }
         if (!ok) break;

@@ -15,9 +15,10 @@ constexpr int kWarpsPerBlock = 4;
 
 // Device state shared by all sweeps of one solve (one entry per field unless noted).
 struct SolveState {
-    unsigned *progress[2];          // per (field, warp block) progress counters, double-buffered
-    unsigned *queue[2];             // work-queue heads, double-buffered
-    int nProgress;                  // entries in each progress buffer
+    unsigned *queue[2];             // work-queue heads, double-buffered across sweeps
+    unsigned long long *mbox;       // per warp block: its downstream faces, tagged words
+    unsigned *epoch;                // sweep-tag base, advanced by the reset of each solve
+    int epochStride;                // tags a solve uses (sweep launches + 1)
     unsigned long long *residual;   // [field][sweep slot] largest decrease (double bits)
     int residualStride;             // slots per field
     int *converged;                 // 1 once a field's iteration decrease fell below tol
@@ -32,14 +33,16 @@ template <class T> struct Sweep3Args {
     T *tt;                    // travel-time fields, row pitch `pitch`, rows (y,z) natural
     long long fieldStride;    // elements per field
     int pitch;                // padded x extent Px (multiple of 4) = walk length
-    const T *sp;              // edge-replicated slowness: (nz+1) x (ny+1) x spPitch
-    int spPitch;              // >= Px + 1
+    const T *spPos;           // edge-replicated slowness, columns shifted by 3 (+x sweeps)
+    const T *spNeg;           // edge-replicated slowness, unshifted (-x sweeps)
+    int spPitch;              // row pitch of both (multiple of 4, >= Px + 8)
     long long spPlane;        // spPitch * (ny + 1)
     int nx, ny, nz;
     int tilesY, tilesZ;       // warp blocks per field along y', z'
     const SourceT<T> *srcs;   // per field
     SolveState st;
-    int buf;                  // which progress/queue buffer this sweep uses
+    int buf;                  // which queue head this sweep uses
+    int sweepIndex;           // position of this sweep in the solve (its mailbox tag offset)
     int residualSlot;         // residual slot this sweep writes
     int sweep;                // 0..7 = Sweep1..Sweep8
     int init;                 // 1 = source-limited initialisation sweep
@@ -52,13 +55,15 @@ template <class T> struct Sweep2Args {
     T *tt;
     long long fieldStride;
     int pitch;                // Px
-    const T *sp;              // (nz+1) x spPitch
+    const T *spPos;           // (nz+1) x spPitch, columns shifted by 3 (+x sweeps)
+    const T *spNeg;           // unshifted (-x sweeps)
     int spPitch;
     int nx, nz;
     int tilesZ;
     const SourceT<T> *srcs;
     SolveState st;
     int buf;
+    int sweepIndex;
     int residualSlot;
     int sweep;                // 0..3 = Sweep1..Sweep4
     int init;
@@ -90,10 +95,12 @@ cudaError_t launchInit3(T *tt, int nFields, long long fieldStride, int pitch, in
 template <class T>
 cudaError_t launchInit2(T *tt, int nFields, long long fieldStride, int pitch, int nx, int nz,
                         double dx, double dz, const Corner3 *corners, int fp64, cudaStream_t s);
+// Edge-replicated slowness: element (pz, py, i) = S[clamp(pz-1), clamp(py-1), clamp(i-1-shift)].
 template <class T, class U>
-cudaError_t launchPadSlowness3(T *sp, int spPitch, const U *s, int nx, int ny, int nz, cudaStream_t st);
+cudaError_t launchPadSlowness3(T *sp, int spPitch, int shift, const U *s, int nx, int ny, int nz,
+                               cudaStream_t st);
 template <class T, class U>
-cudaError_t launchPadSlowness2(T *sp, int spPitch, const U *s, int nx, int nz, cudaStream_t st);
+cudaError_t launchPadSlowness2(T *sp, int spPitch, int shift, const U *s, int nx, int nz, cudaStream_t st);
 template <class U>
 cudaError_t launchNodalToCell3(double *slow, const U *v, int nx, int ny, int nz, int ordering,
                                cudaStream_t s);
@@ -104,7 +111,7 @@ cudaError_t launchCellsToNatural3(double *slow, const U *c, int nx, int ny, int 
                                   cudaStream_t s);
 template <class U>
 cudaError_t launchCellsToNatural2(double *slow, const U *c, int nx, int nz, int ordering, cudaStream_t s);
-cudaError_t launchResetState(const SolveState &st, int nFields, int progressBuf, cudaStream_t s);
+cudaError_t launchResetState(const SolveState &st, int nFields, int buf, cudaStream_t s);
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,
                                    int iteration, double tol, cudaStream_t s);
 cudaError_t launchAnalytic3(double *t, int nx, int ny, int nz, double dx, double dy, double dz,
