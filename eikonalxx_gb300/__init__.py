@@ -34,6 +34,7 @@ EXPORTED = [
     "eikx_set_grid3d", "eikx_set_slowness3d", "eikx_set_nodal_velocity3d", "eikx_get_slowness3d",
     "eikx_solve3d", "eikx_set_grid2d", "eikx_set_slowness2d", "eikx_set_nodal_velocity2d",
     "eikx_solve2d", "eikx_graph3d_tables", "eikx_levels2d", "eikx_analytic3d", "eikx_analytic2d",
+    "eikx_solve3d_noalloc",
 ]
 
 

@@ -795,3 +795,6 @@ eikx_status eikx_analytic2d(eikx_ctx *c, const eikx_source2d *src, double vTop, 
 }
 
 }  // extern "C"
+
+// Lets other translation units of the library report through eikx_last_error().
+eikx_status eikxSetLastError(eikx_status code, const char *msg) { return fail(code, msg); }

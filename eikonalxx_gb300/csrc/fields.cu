@@ -360,6 +360,7 @@ template cudaError_t launchInit2<double>(double *, int, long long, int, int, int
 template cudaError_t launchPadSlowness3<float, double>(float *, int, int, const double *, int, int, int, cudaStream_t);
 template cudaError_t launchPadSlowness3<double, double>(double *, int, int, const double *, int, int, int,
                                                         cudaStream_t);
+template cudaError_t launchPadSlowness3<float, float>(float *, int, int, const float *, int, int, int, cudaStream_t);
 template cudaError_t launchPadSlowness2<float, double>(float *, int, int, const double *, int, int, cudaStream_t);
 template cudaError_t launchPadSlowness2<double, double>(double *, int, int, const double *, int, int, cudaStream_t);
 template cudaError_t launchNodalToCell3<float>(double *, const float *, int, int, int, int, cudaStream_t);

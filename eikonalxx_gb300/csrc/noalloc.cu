@@ -1,0 +1,259 @@
+// eikx_solve3d_noalloc: a 3D FP32 solve that allocates nothing.
+//
+// Who needs it: callers that must not allocate GPU memory while they run -- code that
+// runs between the steps of a host framework which owns every device allocation (a
+// memory pool that would be bypassed and fragmented by cudaMalloc), real-time or
+// embedded pipelines that forbid allocation after start-up, and hosts that call the
+// solver from a context where cudaMalloc/cudaFree would synchronise the device or
+// fail outright.  The regular entry points (eikx_solve3d) keep per-context buffers
+// that they grow with cudaMalloc; this one keeps every intermediate buffer of the
+// solve in one fixed array compiled into the library.
+//
+// The scratch: a file-scope `static __device__` array of kScratchBytes (64 MiB).  Every
+// GPU that loads the library holds it until the process exits, whether or not this
+// entry point is ever called.  A grid needs about 15 bytes per node of it (padded
+// travel times 4 B, two edge-replicated slowness copies 8 B, block-face mailbox 3 B,
+// plus a few kB); grids whose need exceeds the array are rejected with
+// EIKX_ERR_INVALID before anything runs -- about 4 million nodes (e.g. 160^3).
+//
+// Sharing: all calls on a device share the array and it keeps the previous call's
+// contents.  Whatever a solve requires to start at zero (queue heads, residual slots,
+// convergence flags, the abort flag) is cleared by the solve itself; mailbox words
+// carry a tag that only the current solve uses.  Two calls whose work overlaps on the
+// GPU (different streams, or different host threads) race on the array and corrupt
+// each other's fields: serialise them.
+//
+// Set-up: the first call on a device, with that device current, looks up the device
+// address of the array (cudaGetSymbolAddress; in host code the array's name is only a
+// host-side stand-in) and clears the array once.  That first call should therefore be
+// made before any stream capture.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "eikx/eikx_c.h"
+#include "sweep.h"
+
+eikx_status eikxSetLastError(eikx_status code, const char *msg);
+
+namespace {
+
+constexpr size_t kScratchBytes = 64ull << 20;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char gScratch[kScratchBytes];
+
+std::mutex gSetupMutex;
+void *gScratchAddr[kMaxDevices] = {};
+
+eikx_status err(eikx_status code, const std::string &msg) { return eikxSetLastError(code, msg.c_str()); }
+
+#define NOALLOC_CUDA(expr)                                                                        \
+    do {                                                                                          \
+        cudaError_t e_ = (expr);                                                                  \
+        if (e_ != cudaSuccess) return err(EIKX_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Device address of the scratch array on the current device; the first call per device
+// resolves it and clears the array.
+eikx_status scratchAddress(int device, cudaStream_t stream, unsigned char **out) {
+    std::lock_guard<std::mutex> lock(gSetupMutex);
+    if (device < 0 || device >= kMaxDevices) return err(EIKX_ERR_UNSUPPORTED, "device index above 63");
+    if (!gScratchAddr[device]) {
+        void *p = nullptr;
+        NOALLOC_CUDA(cudaGetSymbolAddress(&p, gScratch));
+        NOALLOC_CUDA(cudaMemsetAsync(p, 0, kScratchBytes, stream));
+        gScratchAddr[device] = p;
+    }
+    *out = static_cast<unsigned char *>(gScratchAddr[device]);
+    return EIKX_OK;
+}
+
+// Bump allocator over the scratch array (256-byte aligned regions).
+struct Carve {
+    unsigned char *base;
+    size_t used = 0;
+    template <class X> X *take(size_t count) {
+        used = (used + 255) & ~static_cast<size_t>(255);
+        X *p = reinterpret_cast<X *>(base ? base + used : nullptr);
+        used += count * sizeof(X);
+        return p;
+    }
+};
+
+// Work order of one field's warp blocks, sorted by start step (by*LY + bz*LZ, then by):
+// each thread ranks its block by counting the blocks that come before it.
+__global__ void orderKernel(int4 *order, int tilesY, int tilesZ) {
+    const int n = tilesY * tilesZ;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int b = t % tilesY, c = t / tilesY;
+        const int key = b * eikx::LY3 + c * eikx::LZ3;
+        int rank = 0;
+        for (int u = 0; u < n; ++u) {
+            const int b2 = u % tilesY, c2 = u / tilesY;
+            const int k2 = b2 * eikx::LY3 + c2 * eikx::LZ3;
+            rank += (k2 < key || (k2 == key && b2 < b)) ? 1 : 0;
+        }
+        order[rank] = make_int4(0, b, c, 0);
+    }
+}
+
+// Source table of the field: the source-cell slowness is read from the caller's model.
+__global__ void sourceKernel(eikx::SourceT<float> *src, eikx::Corner3 *corner, const float *slowness, int ncx,
+                             int ncy, int cx, int cy, int cz, double ox, double oy, double oz) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const float s = slowness[(static_cast<long long>(cz) * ncy + cy) * ncx + cx];
+    src->isx = cx; src->isy = cy; src->isz = cz;
+    src->xs = static_cast<float>(ox); src->ys = static_cast<float>(oy); src->zs = static_cast<float>(oz);
+    src->sSrc = s;
+    corner->isx = cx; corner->isy = cy; corner->isz = cz;
+    corner->xo = ox; corner->yo = oy; corner->zo = oz;
+    corner->s = static_cast<double>(s);
+}
+
+bool locate(double x, double x0, double d, int n, int *cell, double *offset) {
+    const double x1 = x0 + static_cast<double>(n - 1) * d;
+    if (!(x >= x0 && x <= x1)) return false;
+    *offset = x - x0;
+    *cell = std::min(n - 2, static_cast<int>(*offset / d));
+    return true;
+}
+
+}  // namespace
+
+extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, double dy, double dz, double x0,
+                                            double y0, double z0, const float *slowness,
+                                            const eikx_source3d *src, const eikx_options *opt, float *tOut,
+                                            void *streamHandle) {
+    if (nx < 3 || ny < 3 || nz < 3) return err(EIKX_ERR_INVALID, "grid needs at least 3 points per axis");
+    if (!(dx > 0) || !(dy > 0) || !(dz > 0)) return err(EIKX_ERR_INVALID, "grid spacing must be positive");
+    if (!slowness || !src || !tOut) return err(EIKX_ERR_INVALID, "slowness, source and output must not be NULL");
+    eikx_options o;
+    if (opt) o = *opt; else eikx_options_default(&o);
+    if (o.n_sweeps < 0) return err(EIKX_ERR_INVALID, "n_sweeps must be non-negative");
+    int cx, cy, cz;
+    double ox, oy, oz;
+    if (!locate(src->x, x0, dx, nx, &cx, &ox) || !locate(src->y, y0, dy, ny, &cy, &oy) ||
+        !locate(src->z, z0, dz, nz, &cz, &oz))
+        return err(EIKX_ERR_INVALID, "source position outside the grid");
+
+    // layout and scratch need (same shapes as eikx_solve3d)
+    const int Px = (nx + 3) / 4 * 4;
+    const int spPitch = Px + 8;
+    const int tilesY = (ny + eikx::LY3 - 1) / eikx::LY3, tilesZ = (nz + eikx::LZ3 - 1) / eikx::LZ3;
+    const int nTiles = tilesY * tilesZ;
+    const int nSweeps = o.n_sweeps;
+    const int nSweepLaunches = 8 * ((o.init_sweeps ? 1 : 0) + nSweeps);
+    const int resStride = 8 * (1 + nSweeps);
+    const size_t spElems = static_cast<size_t>(spPitch) * (ny + 1) * (nz + 1);
+    Carve plan{nullptr};
+    plan.take<float>(static_cast<size_t>(Px) * ny * nz);                       // travel times
+    plan.take<float>(spElems);                                                  // slowness, +x sweeps
+    plan.take<float>(spElems);                                                  // slowness, -x sweeps
+    plan.take<unsigned long long>(static_cast<size_t>(nTiles) * (eikx::LY3 + eikx::LZ3) * Px);  // mailbox
+    plan.take<unsigned long long>(static_cast<size_t>(resStride));             // residual slots
+    plan.take<unsigned>(8);                                                     // queue heads, epoch, flags
+    plan.take<int4>(static_cast<size_t>(nTiles));                               // work order
+    plan.take<eikx::SourceT<float>>(1);
+    plan.take<eikx::Corner3>(1);
+    if (plan.used > kScratchBytes)
+        return err(EIKX_ERR_INVALID, "grid " + std::to_string(nx) + "x" + std::to_string(ny) + "x" +
+                                         std::to_string(nz) + " needs " + std::to_string(plan.used) +
+                                         " bytes of scratch; the no-allocation solve has " +
+                                         std::to_string(kScratchBytes) + " (64 MiB)");
+
+    cudaStream_t stream = static_cast<cudaStream_t>(streamHandle);
+    int device = 0;
+    NOALLOC_CUDA(cudaGetDevice(&device));
+    unsigned char *base = nullptr;
+    if (eikx_status r = scratchAddress(device, stream, &base); r != EIKX_OK) return r;
+    Carve cv{base};
+    float *tt = cv.take<float>(static_cast<size_t>(Px) * ny * nz);
+    float *spPos = cv.take<float>(spElems);
+    float *spNeg = cv.take<float>(spElems);
+    unsigned long long *mbox = cv.take<unsigned long long>(static_cast<size_t>(nTiles) * (eikx::LY3 + eikx::LZ3) * Px);
+    unsigned long long *residual = cv.take<unsigned long long>(static_cast<size_t>(resStride));
+    unsigned *small = cv.take<unsigned>(8);   // [0..1] queue heads, [2] epoch, [3] abort, [4] converged, [5] iterations
+    int4 *order = cv.take<int4>(static_cast<size_t>(nTiles));
+    eikx::SourceT<float> *srcDev = cv.take<eikx::SourceT<float>>(1);
+    eikx::Corner3 *cornerDev = cv.take<eikx::Corner3>(1);
+
+    int numSMs = 0;
+    NOALLOC_CUDA(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device));
+    const double eps = std::numeric_limits<float>::epsilon() * 100;
+    const bool uniform = std::abs(dx - dy) < eps && std::abs(dx - dz) < eps;
+    const int perSM = eikx::sweep3BlocksPerSM<float>(uniform);
+    const int blocks = std::max(1, std::min(numSMs * perSM, (nTiles + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock));
+
+    eikx::SolveState st{};
+    st.queue[0] = small;
+    st.queue[1] = small + 1;
+    st.epoch = small + 2;
+    st.abortFlag = reinterpret_cast<int *>(small + 3);
+    st.converged = reinterpret_cast<int *>(small + 4);
+    st.iterations = reinterpret_cast<int *>(small + 5);
+    st.mbox = mbox;
+    st.epochStride = nSweepLaunches + 1;
+    st.residual = residual;
+    st.residualStride = resStride;
+    st.order = order;
+    const int drop = std::min(std::max(o.test_drop_blocks, 0), nTiles);
+    st.order = order + drop;
+    st.totalItems = nTiles - drop;
+    const int spinLog2 = o.spin_limit_log2 > 0 ? std::min(o.spin_limit_log2, 40) : 22;
+    st.spinLimit = 1ull << spinLog2;
+
+    orderKernel<<<(nTiles + 127) / 128, 128, 0, stream>>>(order, tilesY, tilesZ);
+    NOALLOC_CUDA(cudaGetLastError());
+    sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, slowness, nx - 1, ny - 1, cx, cy, cz, ox, oy, oz);
+    NOALLOC_CUDA(cudaGetLastError());
+    NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spPos, spPitch, 3, slowness, nx, ny, nz, stream)));
+    NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spNeg, spPitch, 0, slowness, nx, ny, nz, stream)));
+    NOALLOC_CUDA(eikx::launchResetState(st, 1, 0, stream));
+    NOALLOC_CUDA(eikx::launchInit3<float>(tt, 1, static_cast<long long>(Px) * ny * nz, Px, nx, ny, nz, dx, dy, dz,
+                                          cornerDev, o.init_fp64 ? 1 : 0, stream));
+    const float fdx = static_cast<float>(dx), fdy = static_cast<float>(dy), fdz = static_cast<float>(dz);
+    eikx::Spacing3<float> g;
+    g.dx = fdx; g.dy = fdy; g.dz = fdz;
+    g.dxInv = 1 / fdx; g.dyInv = 1 / fdy; g.dzInv = 1 / fdz;
+    g.dx2Inv = 1 / (fdx * fdx); g.dy2Inv = 1 / (fdy * fdy); g.dz2Inv = 1 / (fdz * fdz);
+    g.dx_dz = fdx / fdz; g.dz_dx = fdz / fdx; g.dy_dz = fdy / fdz; g.dz_dy = fdz / fdy;
+    g.dx_dy = fdx / fdy; g.dy_dx = fdy / fdx;
+    g.dx2_p_dz2_inv = 1 / (fdx * fdx + fdz * fdz);
+    g.dy2_p_dz2_inv = 1 / (fdy * fdy + fdz * fdz);
+    g.dx2_p_dy2_inv = 1 / (fdx * fdx + fdy * fdy);
+    int buf = 0, launched = 0;
+    auto sweep = [&](int e, int init, int slot) -> eikx_status {
+        eikx::Sweep3Args<float> a{};
+        a.tt = tt; a.fieldStride = static_cast<long long>(Px) * ny * nz; a.pitch = Px;
+        a.spPos = spPos; a.spNeg = spNeg; a.spPitch = spPitch; a.spPlane = static_cast<long long>(spPitch) * (ny + 1);
+        a.nx = nx; a.ny = ny; a.nz = nz; a.tilesY = tilesY; a.tilesZ = tilesZ;
+        a.srcs = srcDev; a.st = st; a.buf = buf; a.sweepIndex = launched; a.residualSlot = slot;
+        a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = fdx; a.sp3 = g;
+        NOALLOC_CUDA(eikx::launchSweep3<float>(a, uniform, blocks, stream));
+        buf ^= 1;
+        ++launched;
+        return EIKX_OK;
+    };
+    if (o.init_sweeps)
+        for (int e = 0; e < 8; ++e)
+            if (eikx_status r = sweep(e, 1, e); r != EIKX_OK) return r;
+    for (int k = 0; k < nSweeps; ++k) {
+        for (int e = 0; e < 8; ++e)
+            if (eikx_status r = sweep(e, 0, 8 * (1 + k) + e); r != EIKX_OK) return r;
+        NOALLOC_CUDA(eikx::launchCheckConvergence(st, 1, 8 * (1 + k), 8, k, o.tolerance, stream));
+    }
+    NOALLOC_CUDA(cudaMemcpy2DAsync(tOut, static_cast<size_t>(nx) * sizeof(float), tt, static_cast<size_t>(Px) * sizeof(float),
+                                   static_cast<size_t>(nx) * sizeof(float), static_cast<size_t>(ny) * nz,
+                                   cudaMemcpyDeviceToDevice, stream));
+    int aborted = 0;
+    NOALLOC_CUDA(cudaMemcpyAsync(&aborted, st.abortFlag, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NOALLOC_CUDA(cudaStreamSynchronize(stream));
+    if (aborted) return err(EIKX_ERR_TIMEOUT, "a bounded inter-tile wait ran out; the field is not valid");
+    return EIKX_OK;
+}

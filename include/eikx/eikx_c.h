@@ -165,6 +165,32 @@ eikx_status eikx_analytic3d(eikx_ctx *ctx, const eikx_source3d *src, double v_to
 eikx_status eikx_analytic2d(eikx_ctx *ctx, const eikx_source2d *src, double v_top,
                             double v_bottom, double *t_out, int where);
 
+/* ---- solve without allocating ------------------------------------------ */
+/* No counterpart in the reference: an addition of this library for callers that must
+ * not allocate GPU memory while they run -- hosts whose framework owns every device
+ * allocation through its own pool, real-time pipelines that forbid allocation after
+ * start-up, code running where cudaMalloc would synchronise or is not allowed.
+ * One FP32 3D field (FP64 corner initialisation) is solved with the schedule of
+ * eikx_solve3d; every intermediate buffer lives in a fixed 64 MiB array compiled into
+ * the library (each GPU that loads the library holds it until exit), so the call makes
+ * no cudaMalloc, cudaFree or other allocating call.
+ *   slowness: device pointer, (nx-1)(ny-1)(nz-1) cell slownesses (s/m), natural order.
+ *   src, opt: host pointers (opt may be NULL for the defaults).
+ *   t_out:    device pointer, nx*ny*nz travel times, natural order.
+ *   stream:   a cudaStream_t (NULL = the legacy default stream); the call returns when
+ *             the field is written.
+ * Limit: a grid needs about 15 bytes of the array per node (padded fields, two slowness
+ * copies, block-face mailbox); larger grids -- beyond about 4 million nodes -- return
+ * EIKX_ERR_INVALID without running.  All calls on a device share the array and it keeps
+ * the last call's contents (each solve clears what must start at zero); calls that
+ * overlap on the GPU race and must be serialised by the caller.  The first call on a
+ * device looks up the array's device address and clears it, so make that first call
+ * before any stream capture. */
+eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, double dy, double dz,
+                                 double x0, double y0, double z0, const float *slowness,
+                                 const eikx_source3d *src, const eikx_options *opt,
+                                 float *t_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
