@@ -1,0 +1,48 @@
+// A point source in a 3D grid (drop-in for include/eikonalxx/source3d.hpp of the
+// reference).  A location must lie inside the grid; its offset is location - origin and
+// its cell min(nCell - 1, int(offset / spacing)) on each axis.
+#ifndef EIKONALXX_SOURCE_3D_HPP
+#define EIKONALXX_SOURCE_3D_HPP
+#include <memory>
+#include <ostream>
+#include <string>
+namespace EikonalXX
+{
+class Geometry3D;
+class Source3D
+{
+public:
+    Source3D();
+    Source3D(const Source3D &other);
+    Source3D(Source3D &&other) noexcept;
+    Source3D& operator=(const Source3D &other);
+    Source3D& operator=(Source3D &&other) noexcept;
+    ~Source3D();
+    void setGeometry(const Geometry3D &geometry);
+    [[nodiscard]] Geometry3D getGeometry() const;
+    [[nodiscard]] bool haveGeometry() const noexcept;
+    void setLocationInX(double x);
+    [[nodiscard]] double getLocationInX() const;
+    [[nodiscard]] double getOffsetInX() const;
+    [[nodiscard]] int getCellInX() const;
+    [[nodiscard]] bool haveLocationInX() const noexcept;
+    void setLocationInY(double y);
+    [[nodiscard]] double getLocationInY() const;
+    [[nodiscard]] double getOffsetInY() const;
+    [[nodiscard]] int getCellInY() const;
+    [[nodiscard]] bool haveLocationInY() const noexcept;
+    void setLocationInZ(double z);
+    [[nodiscard]] double getLocationInZ() const;
+    [[nodiscard]] double getOffsetInZ() const;
+    [[nodiscard]] int getCellInZ() const;
+    [[nodiscard]] bool haveLocationInZ() const noexcept;
+    void setZToFreeSurface();
+    [[nodiscard]] int getCell() const;
+    void clear() noexcept;
+private:
+    class Source3DImpl;
+    std::unique_ptr<Source3DImpl> pImpl;
+};
+std::ostream& operator<<(std::ostream &os, const Source3D &source);
+}
+#endif
