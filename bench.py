@@ -33,6 +33,7 @@ METRIC = "3D travel-time grids/s at max err <=1e-4 s vs FP64; batched+learned vs
 NX, NY, NZ, H = 256, 256, 128, 50.0
 MODEL_SEED, SOURCE_SEED = 20240601, 7
 N_SWEEPS_MAX, TOL, RADIUS = 10, 1e-5, 3
+PAIR = [True]  # pair_fields option of the GPU arm (set from the command line)
 L2_BYTES = 129 * 2 ** 20
 BYTES_PER_NODE_SWEEP = 12          # FP32: read T, read slowness, write T
 
@@ -136,7 +137,7 @@ def run_gpu(args):
     ctx.set_grid3d(NX, NY, NZ, H, H, H)
     v_host = torch.from_numpy(v.ravel()).pin_memory()
     ctx.set_nodal_velocity3d(v_host)
-    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS)
+    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, pair_fields=PAIR[0])
     out_dev = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device=f"cuda:{dev}")
     out_host = torch.empty((fields, NZ, NY, NX), dtype=torch.float32).pin_memory()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -181,7 +182,8 @@ def run_gpu(args):
     value = fields * world / (ms / 1e3)
 
     # roofline of the sweep kernel: per-launch durations from CUDA events around each sweep
-    prof = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True)
+    prof = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True,
+                      pair_fields=PAIR[0])
     ctx.solve3d(src, prof, ex.F32, out=out_dev)
     pst = ctx.stats()
     sweep_launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
@@ -212,7 +214,8 @@ def run_gpu(args):
                    "factored_radius": RADIUS, "tolerance_s": TOL, "max_iterations": N_SWEEPS_MAX,
                    "l2": "flushed (write of 2x L2) between timed steps; per-step fields exceed L2",
                    "parallelism": f"replicas x{world} (sources sharded, no collective)"},
-        "roofline": {"bound": "hbm", "kernel": "sweep3Kernel<float,uniform>", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": ("sweep3PairKernel" if PAIR[0] and fields >= 2
+                                                else "sweep3Kernel<float,uniform>"), "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "bytes_per_launch": bytes_per_launch, "launch_ms": sweep_launch_ms,
                      "traffic": (tr["dram_bytes_per_launch"] if tr else None)},
@@ -236,7 +239,7 @@ def profile_case(fields):
     ctx = ex.Context(torch.cuda.current_device())
     ctx.set_grid3d(NX, NY, NZ, H, H, H)
     ctx.set_nodal_velocity3d(v.ravel())
-    opt = ex.Options(n_sweeps=1, tolerance=-1, factored_radius=RADIUS, profile_sweeps=True)
+    opt = ex.Options(n_sweeps=1, tolerance=-1, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0])
     out = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device="cuda")
     ctx.solve3d(src, opt, ex.F32, out=out)
     st = ctx.stats()
@@ -359,9 +362,12 @@ def main():
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--single-field-kernel", action="store_true",
+                    help="sweep one field per lane (the paired two-field kernel is the default for FP32)")
     ap.add_argument("--profile-case", action="store_true",
                     help="one solve of the workload (1 refinement iteration) for ncu captures")
     args = ap.parse_args()
+    PAIR[0] = not args.single_field_kernel
     if args.profile_case:
         profile_case(args.fields)
         return

@@ -63,7 +63,7 @@ class _Options(ctypes.Structure):
                 ("factored_radius", ctypes.c_int), ("init_sweeps", ctypes.c_int),
                 ("init_fp64", ctypes.c_int), ("spin_limit_log2", ctypes.c_int),
                 ("test_drop_blocks", ctypes.c_int), ("profile_sweeps", ctypes.c_int),
-                ("reserved", ctypes.c_int * 4)]
+                ("pair_fields", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class _Stats(ctypes.Structure):
@@ -148,6 +148,7 @@ class Options:
     spin_limit_log2: int = 22
     test_drop_blocks: int = 0   # test hook only (see eikx_options.test_drop_blocks)
     profile_sweeps: bool = False  # time each sweep kernel with CUDA events (no graph)
+    pair_fields: bool = True      # two fields per GPU lane for FP32 uniform batches
 
     def _c(self):
         o = _Options()
@@ -159,6 +160,7 @@ class Options:
         o.spin_limit_log2 = int(self.spin_limit_log2)
         o.test_drop_blocks = int(self.test_drop_blocks)
         o.profile_sweeps = int(bool(self.profile_sweeps))
+        o.pair_fields = int(bool(self.pair_fields))
         return o
 
 

@@ -14,6 +14,7 @@
 #include <limits>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -85,14 +86,14 @@ bool locate(double x, double x0, double d, int n, int *cell, double *offset) {
 }
 
 struct Workspace {
-    DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners;
+    DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, pairs;
     PinnedBuf stage;
     std::vector<int> orderKey;   // (tilesY, tilesZ, nFields, dim) of the uploaded order table
 };
 
 struct ScheduleKey {
     int dim = 0, precision = -1, nFields = 0, nx = 0, ny = 0, nz = 0, nSweeps = -1, radius = 0,
-        initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0;
+        initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0;
     double tol = 0, h = 0, dx = 0, dy = 0, dz = 0;
     unsigned long long spin = 0;
     const void *tt = nullptr, *sp = nullptr, *srcs = nullptr, *corners = nullptr;
@@ -278,17 +279,24 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
         spadValid = true;
     }
 
+    // geometry in the sweep type (include/private/solver3d.hpp:31-44, solver2d.hpp:29-46)
+    const double eps = std::numeric_limits<T>::epsilon() * 100;
+    const bool uniform = DIM == 3 ? (std::abs(dx - dy) < eps && std::abs(dx - dz) < eps) : (std::abs(dx - dz) < eps);
+    // FP32 uniform 3D batches run two fields per lane (the paired kernel)
+    const bool paired = DIM == 3 && P == EIKX_F32 && uniform && nSrc >= 2 && o.pair_fields;
+    const int nUnits = paired ? (nSrc + 1) / 2 : nSrc;   // work units: fields or field pairs
+
     // workspace
     const int ly = DIM == 3 ? eikx::LY3 : 1, lz = DIM == 3 ? eikx::LZ3 : eikx::LZ2;
     const int tilesY = DIM == 3 ? (ny + ly - 1) / ly : 1;
     const int tilesZ = (nz + lz - 1) / lz;
-    const int nProgress = nSrc * tilesY * tilesZ;
+    const int nProgress = nUnits * tilesY * tilesZ;
     const int nSweepKinds = DIM == 3 ? 8 : 4;
     const int nSweeps = std::max(0, o.n_sweeps);
     const int resStride = nSweepKinds * (1 + nSweeps);
     Workspace &w = c->ws;
     const size_t ttBytes = static_cast<size_t>(fieldStride) * nSrc * sizeof(T);
-    const int mailWords = static_cast<int>(sizeof(T) / 4);   // tagged 64-bit words per value
+    const int mailWords = paired ? 2 : static_cast<int>(sizeof(T) / 4);   // tagged 64-bit words per unit
     const size_t mboxBytes = static_cast<size_t>(nProgress) * (DIM == 3 ? ly + lz : 1) * Px * mailWords * 8;
     const void *before[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
                             w.iterations.p, w.order.p, w.srcs.p, w.corners.p};
@@ -310,20 +318,29 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     EIKX_CUDA(w.order.ensure(static_cast<size_t>(nProgress) * 16));
     EIKX_CUDA(w.srcs.ensure(static_cast<size_t>(nSrc) * sizeof(eikx::SourceT<T>)));
     EIKX_CUDA(w.corners.ensure(static_cast<size_t>(nSrc) * sizeof(eikx::Corner3)));
+    EIKX_CUDA(w.pairs.ensure(static_cast<size_t>(nUnits) * sizeof(int2)));
     const void *after[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
                            w.iterations.p, w.order.p, w.srcs.p, w.corners.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) dropGraph(c);
 
     // small uploads through pinned staging
-    std::vector<int> key = {tilesY, tilesZ, nSrc, DIM};
+    std::vector<int> key = {tilesY, tilesZ, nUnits, DIM};
     const bool newOrder = key != w.orderKey;
     std::vector<int> order;
-    if (newOrder) order = buildOrder(tilesY, tilesZ, nSrc, ly, lz);
+    if (newOrder) order = buildOrder(tilesY, tilesZ, nUnits, ly, lz);
+    std::vector<int> pairs;
+    if (paired) {
+        for (int i = 0; i < nUnits; ++i) {
+            pairs.push_back(2 * i);
+            pairs.push_back(std::min(2 * i + 1, nSrc - 1));   // an odd batch pairs its last field with itself
+        }
+    }
+    const size_t pairBytes = pairs.size() * sizeof(int);
     const size_t srcBytes = srcT.size() * sizeof(eikx::SourceT<T>);
     const size_t cornerBytes = corners.size() * sizeof(eikx::Corner3);
     const size_t orderBytes = order.size() * sizeof(int);
     EIKX_CUDA(cudaStreamSynchronize(c->stream));  // staging buffer reuse
-    EIKX_CUDA(w.stage.ensure(srcBytes + cornerBytes + orderBytes + 64));
+    EIKX_CUDA(w.stage.ensure(srcBytes + cornerBytes + orderBytes + pairBytes + 64));
     char *stage = static_cast<char *>(w.stage.p);
     std::memcpy(stage, srcT.data(), srcBytes);
     std::memcpy(stage + srcBytes, corners.data(), cornerBytes);
@@ -334,6 +351,11 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
         EIKX_CUDA(cudaMemcpyAsync(w.order.p, stage + srcBytes + cornerBytes, orderBytes, cudaMemcpyHostToDevice,
                                   c->stream));
         w.orderKey = key;
+    }
+    if (paired) {
+        char *pstage = stage + srcBytes + cornerBytes + orderBytes;
+        std::memcpy(pstage, pairs.data(), pairBytes);
+        EIKX_CUDA(cudaMemcpyAsync(w.pairs.p, pstage, pairBytes, cudaMemcpyHostToDevice, c->stream));
     }
 
     const int nSweepLaunches = nSweepKinds * ((o.init_sweeps ? 1 : 0) + nSweeps);
@@ -355,10 +377,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     const int spinLog2 = o.spin_limit_log2 > 0 ? std::min(o.spin_limit_log2, 40) : 22;
     st.spinLimit = 1ull << spinLog2;
 
-    // geometry in the sweep type (include/private/solver3d.hpp:31-44, solver2d.hpp:29-46)
-    const double eps = std::numeric_limits<T>::epsilon() * 100;
-    const bool uniform = DIM == 3 ? (std::abs(dx - dy) < eps && std::abs(dx - dz) < eps) : (std::abs(dx - dz) < eps);
-    const int perSM = DIM == 3 ? eikx::sweep3BlocksPerSM<T>(uniform) : eikx::sweep2BlocksPerSM<T>(uniform);
+    const int perSM = paired ? eikx::sweep3PairBlocksPerSM()
+                             : (DIM == 3 ? eikx::sweep3BlocksPerSM<T>(uniform) : eikx::sweep2BlocksPerSM<T>(uniform));
     int blocks = std::min(c->numSMs * perSM, (nProgress + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock);
     blocks = std::max(blocks, 1);
 
@@ -367,6 +387,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     sk.nSweeps = nSweeps; sk.radius = o.factored_radius; sk.initSweeps = o.init_sweeps ? 1 : 0;
     sk.initFp64 = o.init_fp64 ? 1 : 0; sk.uniform = uniform; sk.blocks = blocks; sk.tol = o.tolerance;
     sk.h = dx; sk.dx = dx; sk.dy = dy; sk.dz = dz; sk.spin = st.spinLimit; sk.dropBlocks = drop;
+    sk.paired = paired ? 1 : 0;
     sk.tt = w.tt.p; sk.sp = spad[0].p; sk.srcs = w.srcs.p; sk.corners = w.corners.p;
 
     int launches = 0;
@@ -414,7 +435,13 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
                 g.dy2_p_dz2_inv = 1 / (tdy * tdy + tdz * tdz);
                 g.dx2_p_dy2_inv = 1 / (tdx * tdx + tdy * tdy);
                 a.sp3 = g;
-                EIKX_CUDA(eikx::launchSweep3<T>(a, uniform, blocks, c->stream));
+                a.pairs = w.pairs.as<int2>();
+                if constexpr (std::is_same<T, float>::value) {
+                    if (paired) EIKX_CUDA(eikx::launchSweep3Pair(a, blocks, c->stream));
+                    else EIKX_CUDA(eikx::launchSweep3<T>(a, uniform, blocks, c->stream));
+                } else {
+                    EIKX_CUDA(eikx::launchSweep3<T>(a, uniform, blocks, c->stream));
+                }
             } else {
                 eikx::Sweep2Args<T> a{};
                 a.tt = w.tt.as<T>(); a.fieldStride = fieldStride; a.pitch = Px;
@@ -549,6 +576,7 @@ void eikx_options_default(eikx_options *opt) {
     opt->init_sweeps = 1;
     opt->init_fp64 = 1;
     opt->spin_limit_log2 = 22;
+    opt->pair_fields = 1;
 }
 
 const char *eikx_last_error(void) { return gLastError.c_str(); }

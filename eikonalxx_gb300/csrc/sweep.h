@@ -49,6 +49,7 @@ template <class T> struct Sweep3Args {
     int radius;               // factored-eikonal radius
     T h;                      // uniform spacing
     Spacing3<T> sp3;          // non-uniform constants
+    const int2 *pairs;        // field pairs of the paired kernel (work items index pairs)
 };
 
 template <class T> struct Sweep2Args {
@@ -77,6 +78,10 @@ template <class T>
 cudaError_t launchSweep3(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s);
 template <class T>
 cudaError_t launchSweep2(const Sweep2Args<T> &a, bool uniform, int blocks, cudaStream_t s);
+// Paired 3D kernel (sweep_pair.cu): FP32, uniform grid, two fields of one model per lane.
+cudaError_t launchSweep3Pair(const Sweep3Args<float> &a, int blocks, cudaStream_t s);
+int sweep3PairBlocksPerSM();
+size_t sweep3PairSmemBytes();
 // Resident blocks per SM of the sweep kernels (for the persistent grid size).
 template <class T> int sweep3BlocksPerSM(bool uniform);
 template <class T> int sweep2BlocksPerSM(bool uniform);

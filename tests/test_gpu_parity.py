@@ -174,3 +174,25 @@ def test_bounded_wait_times_out_and_context_survives(ctx, oracle):
     t = ctx.solve3d([pos], ex.Options(n_sweeps=1, tolerance=-1), ex.F32)[0]
     t_or = oracle.solve3d(s, shape, cell, off, n_sweeps=1, radius=3)
     assert np.array_equal(_bits(t), _bits(t_or))
+
+
+@pytest.mark.parametrize("n_src", [2, 5, 8])
+def test_paired_fields_converge_independently(ctx, oracle, n_src):
+    """Two fields per lane (FP32, uniform grid): fields of one pair converge at different
+    iterations and each must still stop exactly where the oracle stops."""
+    rng = np.random.default_rng(100 + n_src)
+    shape = (37, 29, 21, 60., 60., 60.)
+    nx, ny, nz = shape[:3]
+    s = random_slowness(rng, (nz - 1) * (ny - 1) * (nx - 1), dtype=np.float32)
+    ctx.set_grid3d(*shape)
+    ctx.set_slowness3d(s)
+    srcs = [_src(rng, (nx, ny, nz), shape[3:]) for _ in range(n_src)]
+    pos = [p for p, _, _ in srcs]
+    outs = {}
+    for pair in (True, False):
+        opt = ex.Options(n_sweeps=12, tolerance=1e-6, factored_radius=3, pair_fields=pair)
+        outs[pair] = ctx.solve3d(pos, opt, ex.F32)
+    for i, (_, cell, off) in enumerate(srcs):
+        t_or = oracle.solve3d(s, shape, cell, off, n_sweeps=12, radius=3, tol=1e-6)
+        assert np.array_equal(_bits(outs[True][i]), _bits(t_or)), i
+        assert np.array_equal(_bits(outs[False][i]), _bits(t_or)), i
