@@ -148,7 +148,7 @@ class Options:
     spin_limit_log2: int = 22
     test_drop_blocks: int = 0   # test hook only (see eikx_options.test_drop_blocks)
     profile_sweeps: bool = False  # time each sweep kernel with CUDA events (no graph)
-    pair_fields: bool = True      # two fields per GPU lane for FP32 uniform batches
+    pair_fields: bool = False     # two fields per GPU lane for FP32 uniform batches
 
     def _c(self):
         o = _Options()

@@ -576,7 +576,7 @@ void eikx_options_default(eikx_options *opt) {
     opt->init_sweeps = 1;
     opt->init_fp64 = 1;
     opt->spin_limit_log2 = 22;
-    opt->pair_fields = 1;
+    opt->pair_fields = 0;
 }
 
 const char *eikx_last_error(void) { return gLastError.c_str(); }

@@ -63,9 +63,11 @@ typedef struct {
                               usable).  Exercises failure detection without a GPU fault. */
     int profile_sweeps;    /* 1 = run the schedule without the CUDA graph and time every sweep
                               kernel with CUDA events (eikx_stats.sweep_ms); 0 = graph replay */
-    int pair_fields;       /* 1 (default) = FP32 uniform-grid batches of >= 2 fields run two
-                              fields per GPU lane (shared slowness work, packed FP32 math);
-                              0 = one field per lane.  Both give identical travel times. */
+    int pair_fields;       /* 1 = FP32 uniform-grid batches of >= 2 fields run two fields per
+                              GPU lane (shared slowness work, packed FP32 math); 0 (default)
+                              = one field per lane, measured faster on GB300 at every batch
+                              size (the paired kernel needs 168 registers per thread, which
+                              leaves 12 resident warps per SM).  Both give identical times. */
     int reserved[3];
 } eikx_options;
 
