@@ -34,6 +34,7 @@ NX, NY, NZ, H = 256, 256, 128, 50.0
 MODEL_SEED, SOURCE_SEED = 20240601, 7
 N_SWEEPS_MAX, TOL, RADIUS = 10, 1e-5, 3
 PAIR = [False]  # pair_fields option of the GPU arm (set from the command line)
+KERNEL = [0]    # sweep_kernel option of the GPU arm: 0 default, 1 node-step, 2 chunk-step
 L2_BYTES = 129 * 2 ** 20
 BYTES_PER_NODE_SWEEP = 12          # FP32: read T, read slowness, write T
 
@@ -137,7 +138,7 @@ def run_gpu(args):
     ctx.set_grid3d(NX, NY, NZ, H, H, H)
     v_host = torch.from_numpy(v.ravel()).pin_memory()
     ctx.set_nodal_velocity3d(v_host)
-    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, pair_fields=PAIR[0])
+    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, pair_fields=PAIR[0], sweep_kernel=KERNEL[0])
     out_dev = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device=f"cuda:{dev}")
     out_host = torch.empty((fields, NZ, NY, NX), dtype=torch.float32).pin_memory()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -183,7 +184,7 @@ def run_gpu(args):
 
     # roofline of the sweep kernel: per-launch durations from CUDA events around each sweep
     prof = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True,
-                      pair_fields=PAIR[0])
+                      pair_fields=PAIR[0], sweep_kernel=KERNEL[0])
     ctx.solve3d(src, prof, ex.F32, out=out_dev)
     pst = ctx.stats()
     sweep_launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
@@ -215,7 +216,8 @@ def run_gpu(args):
                    "l2": "flushed (write of 2x L2) between timed steps; per-step fields exceed L2",
                    "parallelism": f"replicas x{world} (sources sharded, no collective)"},
         "roofline": {"bound": "hbm", "kernel": ("sweep3PairKernel" if PAIR[0] and fields >= 2
-                                                else "sweep3Kernel<float,uniform>"), "achieved": achieved,
+                                                else "sweep3Kernel<float,uniform>" if KERNEL[0] == 1
+                                                else "sweep3ChunkKernel<float,uniform>"), "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "bytes_per_launch": bytes_per_launch, "launch_ms": sweep_launch_ms,
                      "traffic": (tr["dram_bytes_per_launch"] if tr else None)},
@@ -239,7 +241,7 @@ def profile_case(fields):
     ctx = ex.Context(torch.cuda.current_device())
     ctx.set_grid3d(NX, NY, NZ, H, H, H)
     ctx.set_nodal_velocity3d(v.ravel())
-    opt = ex.Options(n_sweeps=1, tolerance=-1, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0])
+    opt = ex.Options(n_sweeps=1, tolerance=-1, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0], sweep_kernel=KERNEL[0])
     out = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device="cuda")
     ctx.solve3d(src, opt, ex.F32, out=out)
     st = ctx.stats()
@@ -362,12 +364,15 @@ def main():
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--sweep-kernel", type=int, default=0, choices=[0, 1, 2],
+                    help="3D sweep kernel: 0 default (chunk-step), 1 node-step, 2 chunk-step")
     ap.add_argument("--pair-fields", action="store_true",
                     help="sweep two fields per lane (the paired FP32 kernel) instead of one")
     ap.add_argument("--profile-case", action="store_true",
                     help="one solve of the workload (1 refinement iteration) for ncu captures")
     args = ap.parse_args()
     PAIR[0] = args.pair_fields
+    KERNEL[0] = args.sweep_kernel
     if args.profile_case:
         profile_case(args.fields)
         return

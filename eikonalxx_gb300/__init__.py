@@ -63,7 +63,8 @@ class _Options(ctypes.Structure):
                 ("factored_radius", ctypes.c_int), ("init_sweeps", ctypes.c_int),
                 ("init_fp64", ctypes.c_int), ("spin_limit_log2", ctypes.c_int),
                 ("test_drop_blocks", ctypes.c_int), ("profile_sweeps", ctypes.c_int),
-                ("pair_fields", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("pair_fields", ctypes.c_int), ("sweep_kernel", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class _Stats(ctypes.Structure):
@@ -149,6 +150,7 @@ class Options:
     test_drop_blocks: int = 0   # test hook only (see eikx_options.test_drop_blocks)
     profile_sweeps: bool = False  # time each sweep kernel with CUDA events (no graph)
     pair_fields: bool = False     # two fields per GPU lane for FP32 uniform batches
+    sweep_kernel: int = 0         # 3D: 0 = default (chunk-step), 1 = node-step, 2 = chunk-step
 
     def _c(self):
         o = _Options()
@@ -161,6 +163,7 @@ class Options:
         o.test_drop_blocks = int(self.test_drop_blocks)
         o.profile_sweeps = int(bool(self.profile_sweeps))
         o.pair_fields = int(bool(self.pair_fields))
+        o.sweep_kernel = int(self.sweep_kernel)
         return o
 
 

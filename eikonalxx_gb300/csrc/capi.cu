@@ -93,7 +93,7 @@ struct Workspace {
 
 struct ScheduleKey {
     int dim = 0, precision = -1, nFields = 0, nx = 0, ny = 0, nz = 0, nSweeps = -1, radius = 0,
-        initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0;
+        initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0, variant = 0;
     double tol = 0, h = 0, dx = 0, dy = 0, dz = 0;
     unsigned long long spin = 0;
     const void *tt = nullptr, *sp = nullptr, *srcs = nullptr, *corners = nullptr;
@@ -377,8 +377,11 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     const int spinLog2 = o.spin_limit_log2 > 0 ? std::min(o.spin_limit_log2, 40) : 22;
     st.spinLimit = 1ull << spinLog2;
 
+    const int variant = o.sweep_kernel == eikx::kNodeStep ? eikx::kNodeStep : eikx::kChunkStep;
     const int perSM = paired ? eikx::sweep3PairBlocksPerSM()
-                             : (DIM == 3 ? eikx::sweep3BlocksPerSM<T>(uniform) : eikx::sweep2BlocksPerSM<T>(uniform));
+                      : DIM == 2 ? eikx::sweep2BlocksPerSM<T>(uniform)
+                      : variant == eikx::kChunkStep ? eikx::sweep3ChunkBlocksPerSM<T>(uniform)
+                                                    : eikx::sweep3BlocksPerSM<T>(uniform);
     int blocks = std::min(c->numSMs * perSM, (nProgress + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock);
     blocks = std::max(blocks, 1);
 
@@ -388,6 +391,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     sk.initFp64 = o.init_fp64 ? 1 : 0; sk.uniform = uniform; sk.blocks = blocks; sk.tol = o.tolerance;
     sk.h = dx; sk.dx = dx; sk.dy = dy; sk.dz = dz; sk.spin = st.spinLimit; sk.dropBlocks = drop;
     sk.paired = paired ? 1 : 0;
+    sk.variant = variant;
     sk.tt = w.tt.p; sk.sp = spad[0].p; sk.srcs = w.srcs.p; sk.corners = w.corners.p;
 
     int launches = 0;
@@ -436,11 +440,16 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
                 g.dx2_p_dy2_inv = 1 / (tdx * tdx + tdy * tdy);
                 a.sp3 = g;
                 a.pairs = w.pairs.as<int2>();
+                bool done = false;
                 if constexpr (std::is_same<T, float>::value) {
-                    if (paired) EIKX_CUDA(eikx::launchSweep3Pair(a, blocks, c->stream));
+                    if (paired) {
+                        EIKX_CUDA(eikx::launchSweep3Pair(a, blocks, c->stream));
+                        done = true;
+                    }
+                }
+                if (!done) {
+                    if (variant == eikx::kChunkStep) EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, blocks, c->stream));
                     else EIKX_CUDA(eikx::launchSweep3<T>(a, uniform, blocks, c->stream));
-                } else {
-                    EIKX_CUDA(eikx::launchSweep3<T>(a, uniform, blocks, c->stream));
                 }
             } else {
                 eikx::Sweep2Args<T> a{};

@@ -77,27 +77,32 @@ template <class T> struct Stencil3 {
     T t1, t2, t3, t4, t5, t6, t7;
 };
 
-// 3D uniform-grid update (solverUtilities3d.hpp:258-558).  The factored branch is the
-// reference's as shipped: T0 built from the home-cell slowness s0.
-template <class T>
-__device__ __forceinline__ T fd3Uniform(int radius, T h, const SourceT<T> &src,
-                                        const SweepSigns &sg, int ix, int iy, int iz,
-                                        const Stencil3<T> &n) {
-    const T huge = static_cast<T>(1.e10);
-    const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7;
-    const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7;
-    T tUpd;
-    T minS0S3 = dmin(s0, s3);
-    T minS0S1 = dmin(s0, s1);
-    T minS0S4 = dmin(s0, s4);
-    T t1d1 = t1 + h * dmin(minS0S3, dmin(s4, s7));
-    T t1d2 = t3 + h * dmin(minS0S4, dmin(s1, s5));
-    T t1d3 = t4 + h * dmin(minS0S1, dmin(s2, s3));
-    T t1d = dmin(dmin(t1d1, t1d2), t1d3);
-    T hs03 = h * minS0S3;
-    T hs01 = h * minS0S1;
+// 3D uniform-grid update (solverUtilities3d.hpp:258-558), split at the reference's
+// branch on the factored radius (:286-300): fd3UniformFar is the Cartesian branch, taken
+// when the node is more than `radius` cells from the source cell along some axis;
+// fd3UniformNear is the factored branch, the reference's as shipped (T0 built from the
+// home-cell slowness s0).  Both evaluate the common head-wave prefix first, exactly as
+// the reference does before it branches.
+#define EIKX_FD3_UNIFORM_PREFIX                                                        \
+    const T huge = static_cast<T>(1.e10);                                              \
+    const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7; \
+    const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7; \
+    T tUpd;                                                                            \
+    T minS0S3 = dmin(s0, s3);                                                          \
+    T minS0S1 = dmin(s0, s1);                                                          \
+    T minS0S4 = dmin(s0, s4);                                                          \
+    T t1d1 = t1 + h * dmin(minS0S3, dmin(s4, s7));                                     \
+    T t1d2 = t3 + h * dmin(minS0S4, dmin(s1, s5));                                     \
+    T t1d3 = t4 + h * dmin(minS0S1, dmin(s2, s3));                                     \
+    T t1d = dmin(dmin(t1d1, t1d2), t1d3);                                              \
+    T hs03 = h * minS0S3;                                                              \
+    T hs01 = h * minS0S1;                                                              \
     T hs04 = h * minS0S4;
-    if (abs(src.isx - ix) > radius || abs(src.isy - iy) > radius || abs(src.isz - iz) > radius) {
+
+template <class T>
+__device__ __forceinline__ T fd3UniformFar(T h, const Stencil3<T> &n) {
+    EIKX_FD3_UNIFORM_PREFIX
+    {
         // 2D critically refracted (diagonal) operators in the XZ, YZ and XY planes.
         // Evaluated branch-free: every lane runs the same instructions and a failed
         // condition selects `huge`; a taken operator rounds exactly as the reference's.
@@ -129,7 +134,15 @@ __device__ __forceinline__ T fd3Uniform(int radius, T h, const SourceT<T> &src,
         const T r3 = dsqrt(c3 ? det : one);
         T t3d = c3 ? third * ((Tx + Ty + Tz) + r3) : huge;
         tUpd = dmin(t1d, dmin(t2d, t3d));
-    } else {
+    }
+    return tUpd;
+}
+
+template <class T>
+__device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const SweepSigns &sg,
+                                            int ix, int iy, int iz, const Stencil3<T> &n) {
+    EIKX_FD3_UNIFORM_PREFIX
+    {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
         T t0, dt0dx, dt0dy, dt0dz;
         analyticTG3(ix, iy, iz, h, h, h, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
@@ -200,6 +213,19 @@ __device__ __forceinline__ T fd3Uniform(int radius, T h, const SourceT<T> &src,
     }
     return tUpd;
 }
+#undef EIKX_FD3_UNIFORM_PREFIX
+
+__device__ __forceinline__ bool nearSource(int radius, int isx, int isy, int isz, int ix, int iy, int iz) {
+    return !(abs(isx - ix) > radius || abs(isy - iy) > radius || abs(isz - iz) > radius);
+}
+
+template <class T>
+__device__ __forceinline__ T fd3Uniform(int radius, T h, const SourceT<T> &src,
+                                        const SweepSigns &sg, int ix, int iy, int iz,
+                                        const Stencil3<T> &n) {
+    if (!nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) return fd3UniformFar(h, n);
+    return fd3UniformNear(h, src, sg, ix, iy, iz, n);
+}
 
 // Grid constants of the non-uniform 3D solver (include/private/solver3d.hpp:247-261),
 // computed on the host in the field type and passed by value.
@@ -209,24 +235,26 @@ template <class T> struct Spacing3 {
     T dx2_p_dz2_inv, dy2_p_dz2_inv, dx2_p_dy2_inv;
 };
 
-// 3D non-uniform update (solverUtilities3d.hpp:562-824).
-template <class T>
-__device__ __forceinline__ T fd3NonUniform(int radius, const Spacing3<T> &g, const SourceT<T> &src,
-                                           const SweepSigns &sg, int ix, int iy, int iz,
-                                           const Stencil3<T> &n) {
-    const T huge = static_cast<T>(1.e10);
-    const T dx = g.dx, dy = g.dy, dz = g.dz;
-    const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7;
-    const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7;
-    T tUpd;
-    T minS0S3 = dmin(s0, s3);
-    T minS0S1 = dmin(s0, s1);
-    T minS0S4 = dmin(s0, s4);
-    T t1d1 = t1 + dx * dmin(minS0S3, dmin(s4, s7));
-    T t1d2 = t3 + dy * dmin(minS0S4, dmin(s1, s5));
-    T t1d3 = t4 + dz * dmin(minS0S1, dmin(s2, s3));
+// 3D non-uniform update (solverUtilities3d.hpp:562-824), split at the factored-radius
+// branch like the uniform solver.
+#define EIKX_FD3_NONUNIFORM_PREFIX                                                     \
+    const T huge = static_cast<T>(1.e10);                                              \
+    const T dx = g.dx, dy = g.dy, dz = g.dz;                                           \
+    const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7; \
+    const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7; \
+    T tUpd;                                                                            \
+    T minS0S3 = dmin(s0, s3);                                                          \
+    T minS0S1 = dmin(s0, s1);                                                          \
+    T minS0S4 = dmin(s0, s4);                                                          \
+    T t1d1 = t1 + dx * dmin(minS0S3, dmin(s4, s7));                                    \
+    T t1d2 = t3 + dy * dmin(minS0S4, dmin(s1, s5));                                    \
+    T t1d3 = t4 + dz * dmin(minS0S1, dmin(s2, s3));                                    \
     T t1d = dmin(dmin(t1d1, t1d2), t1d3);
-    if (abs(src.isx - ix) > radius || abs(src.isy - iy) > radius || abs(src.isz - iz) > radius) {
+
+template <class T>
+__device__ __forceinline__ T fd3NonUniformFar(const Spacing3<T> &g, const Stencil3<T> &n) {
+    EIKX_FD3_NONUNIFORM_PREFIX
+    {
         T dXZ = t1 - t4;
         T detXZ = (dx * dx + dz * dz) * (minS0S3 * minS0S3) - dXZ * dXZ;
         T t2d = huge;
@@ -271,7 +299,16 @@ __device__ __forceinline__ T fd3NonUniform(int radius, const Spacing3<T> &g, con
                       (g.dx2Inv + g.dy2Inv + g.dz2Inv);
         }
         tUpd = dmin(t1d, dmin(t2d, t3d));
-    } else {
+    }
+    return tUpd;
+}
+
+template <class T>
+__device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const SourceT<T> &src,
+                                               const SweepSigns &sg, int ix, int iy, int iz,
+                                               const Stencil3<T> &n) {
+    EIKX_FD3_NONUNIFORM_PREFIX
+    {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
         T t0, dt0dx, dt0dy, dt0dz;
         analyticTG3(ix, iy, iz, dx, dy, dz, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
@@ -345,6 +382,15 @@ __device__ __forceinline__ T fd3NonUniform(int radius, const Spacing3<T> &g, con
         tUpd = dmin(t1d, dmin(t2d, t3d));
     }
     return tUpd;
+}
+#undef EIKX_FD3_NONUNIFORM_PREFIX
+
+template <class T>
+__device__ __forceinline__ T fd3NonUniform(int radius, const Spacing3<T> &g, const SourceT<T> &src,
+                                           const SweepSigns &sg, int ix, int iy, int iz,
+                                           const Stencil3<T> &n) {
+    if (!nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) return fd3NonUniformFar(g, n);
+    return fd3NonUniformNear(g, src, sg, ix, iy, iz, n);
 }
 
 // ---------------------------------------------------------------------------- 2D

@@ -78,6 +78,14 @@ template <class T>
 cudaError_t launchSweep3(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s);
 template <class T>
 cudaError_t launchSweep2(const Sweep2Args<T> &a, bool uniform, int blocks, cudaStream_t s);
+// Chunk-step 3D kernel (sweep_chunk.cu): a lane updates one 16-byte chunk of its pencil
+// per wavefront step.
+template <class T>
+cudaError_t launchSweep3Chunk(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s);
+template <class T> int sweep3ChunkBlocksPerSM(bool uniform);
+size_t sweep3ChunkSmemBytes();
+// 3D sweep kernel variants (eikx_options.sweep_kernel).
+enum Sweep3Variant { kNodeStep = 1, kChunkStep = 2 };
 // Paired 3D kernel (sweep_pair.cu): FP32, uniform grid, two fields of one model per lane.
 cudaError_t launchSweep3Pair(const Sweep3Args<float> &a, int blocks, cudaStream_t s);
 int sweep3PairBlocksPerSM();

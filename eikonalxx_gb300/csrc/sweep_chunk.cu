@@ -1,0 +1,396 @@
+// Chunk-step 3D level-set sweep kernel for sm_103a.
+//
+// The same warp-block wavefront as sweep3Kernel (wavefront.cuh), with the unit of a
+// step widened from one node to one 16-byte chunk of V = 16 / sizeof(T) consecutive
+// x'-nodes (4 in FP32, 2 in FP64).  At step s lane (ly, lz) updates chunk
+// k = s - ly - lz of its pencil, its V nodes in walk order: node e of the chunk reads
+// node e-1 just updated, so the chunk reproduces the serial x-loop of the reference
+// (include/private/solver3d.hpp:186-243) node for node, and every value it reads from
+// another lane lies on an earlier level.
+//
+// What a step costs is paid once per chunk instead of once per node:
+//   * the y'-, z'- and yz'-upwind lanes' chunks (travel times and cell slowness) come
+//     from the per-warp ring as six 16-byte shared-memory loads; their x'-1 values are
+//     the last elements of the chunks the lane read the step before (register carries);
+//   * the own pencil streams as one 16-byte load of travel times and one of slowness per
+//     step (fetched a step ahead), and a chunk is stored back with one 16-byte store
+//     when any of its nodes decreased;
+//   * halo values cross warp blocks as 32-byte mailbox chunks (four tagged 64-bit words:
+//     one per FP32 value, two per FP64 value), read with two 16-byte relaxed loads that
+//     are issued a step before they are needed.
+// Near-source nodes (factored branch) are evaluated by an out-of-line call, so the V
+// inlined copies of the update are the Cartesian operators only.
+#include "sweep.h"
+#include "wavefront.cuh"
+
+namespace eikx {
+
+namespace {
+
+constexpr int HY = LY3 + 1, HZ = LZ3 + 1;          // ring plane incl. halo row/column
+constexpr int kPlane = HY * HZ;
+constexpr int kRingC = 4;                           // ring depth in steps (reads go back 2)
+constexpr int kThreads = 32 * kWarpsPerBlock;
+
+template <class T> struct alignas(16) Vec {
+    static constexpr int N = 16 / sizeof(T);
+    T v[N];
+};
+template <class T> __device__ __forceinline__ Vec<T> ldVec(const T *p) {
+    Vec<T> r;
+    *reinterpret_cast<uint4 *>(r.v) = *reinterpret_cast<const uint4 *>(p);
+    return r;
+}
+template <class T> __device__ __forceinline__ void stVec(T *p, const Vec<T> &a) {
+    *reinterpret_cast<uint4 *>(p) = *reinterpret_cast<const uint4 *>(a.v);
+}
+template <class T> __device__ __forceinline__ Vec<T> splat(T x) {
+    Vec<T> r;
+#pragma unroll
+    for (int e = 0; e < Vec<T>::N; ++e) r.v[e] = x;
+    return r;
+}
+template <class T> __device__ __forceinline__ Vec<T> reversed(const Vec<T> &a) {
+    Vec<T> r;
+#pragma unroll
+    for (int e = 0; e < Vec<T>::N; ++e) r.v[e] = a.v[Vec<T>::N - 1 - e];
+    return r;
+}
+
+__device__ __forceinline__ void ldRelaxed2(const unsigned long long *p, unsigned long long &a,
+                                           unsigned long long &b) {
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p));
+}
+__device__ __forceinline__ void stRelaxed2(unsigned long long *p, unsigned long long a, unsigned long long b) {
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b));
+}
+
+// One chunk in the mailbox: four tagged words.  Each 64-bit word is written and read
+// single-copy atomically and carries the tag of the sweep that wrote it, so a reader
+// knows word by word whether the value is this sweep's.
+template <class T> struct MailChunk {
+    unsigned long long w[4];
+    __device__ __forceinline__ void issue(const unsigned long long *p) {
+        ldRelaxed2(p, w[0], w[1]);
+        ldRelaxed2(p + 2, w[2], w[3]);
+    }
+    __device__ __forceinline__ bool ready(unsigned tag) const {
+        return static_cast<unsigned>(w[0] >> 32) == tag && static_cast<unsigned>(w[1] >> 32) == tag &&
+               static_cast<unsigned>(w[2] >> 32) == tag && static_cast<unsigned>(w[3] >> 32) == tag;
+    }
+    __device__ __forceinline__ Vec<T> value() const {
+        Vec<T> r;
+        if constexpr (sizeof(T) == 4) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) r.v[e] = __uint_as_float(static_cast<unsigned>(w[e]));
+        } else {
+#pragma unroll
+            for (int e = 0; e < 2; ++e)
+                r.v[e] = __longlong_as_double(
+                    static_cast<long long>((w[2 * e + 1] << 32) | (w[2 * e] & 0xffffffffull)));
+        }
+        return r;
+    }
+    // Wait (bounded) until all four words carry `tag`, re-reading them.
+    __device__ __forceinline__ bool take(const unsigned long long *p, unsigned tag, int *abortFlag,
+                                         unsigned long long spinLimit) {
+        unsigned long long it = 0;
+        while (!ready(tag)) {
+            if ((++it & 31ull) == 0) {
+                if (ldVolatile(abortFlag)) return false;
+                if (it > spinLimit) {
+                    atomicExch(abortFlag, 1);
+                    return false;
+                }
+            }
+            __nanosleep(32);
+            issue(p);
+        }
+        return true;
+    }
+};
+template <class T>
+__device__ __forceinline__ void putChunk(unsigned long long *p, unsigned tag, const Vec<T> &v) {
+    const unsigned long long t = static_cast<unsigned long long>(tag) << 32;
+    unsigned long long w[4];
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) w[e] = t | __float_as_uint(v.v[e]);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v.v[e]));
+            w[2 * e] = t | (b & 0xffffffffull);
+            w[2 * e + 1] = t | (b >> 32);
+        }
+    }
+    stRelaxed2(p, w[0], w[1]);
+    stRelaxed2(p + 2, w[2], w[3]);
+}
+
+// Factored (near-source) updates, out of line: taken by a few hundred nodes per field.
+template <class T>
+__device__ __noinline__ T nearUniform(T h, const SourceT<T> src, const SweepSigns sg, int ix, int iy, int iz,
+                                      const Stencil3<T> n) {
+    return fd3UniformNear(h, src, sg, ix, iy, iz, n);
+}
+template <class T>
+__device__ __noinline__ T nearNonUniform(const Spacing3<T> g, const SourceT<T> src, const SweepSigns sg, int ix,
+                                         int iy, int iz, const Stencil3<T> n) {
+    return fd3NonUniformNear(g, src, sg, ix, iy, iz, n);
+}
+
+__device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *st.queue[buf ^ 1] = 0u;
+}
+
+template <class T, bool UNIFORM, bool REV>
+__global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T> a) {
+    constexpr int V = Vec<T>::N;
+    constexpr int W = sizeof(T) / 4;                // mailbox words per value
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ly = lane % LY3, lz = lane / LY3;
+    Vec<T> *tring = reinterpret_cast<Vec<T> *>(smemRaw) + warp * (2 * kRingC * kPlane);
+    Vec<T> *sring = tring + kRingC * kPlane;
+    const SolveState &st = a.st;
+    clearNextQueue(st, a.buf);
+    if (ldVolatile(st.abortFlag)) return;
+    const unsigned tag = *st.epoch + static_cast<unsigned>(a.sweepIndex);
+
+    const int fy = (a.sweep >> 1) & 1, fz = (a.sweep >> 2) & 1;
+    SweepSigns sg;
+    sg.ixShift = REV ? 1 : -1; sg.iyShift = fy ? 1 : -1; sg.izShift = fz ? 1 : -1;
+    sg.signX = REV ? -1 : 1; sg.signY = fy ? -1 : 1; sg.signZ = fz ? -1 : 1;
+    const int Px = a.pitch;
+    const int nChunks = Px / V;
+    const int nSteps = nChunks + LY3 + LZ3 - 2;
+    const T *sp = REV ? a.spNeg : a.spPos;
+    const T huge = static_cast<T>(1.e10);
+    const long long faceWords = static_cast<long long>(LY3 + LZ3) * Px * W;
+
+    // helper lanes stand in for the virtual upwind lanes of the halo row/column
+    const bool helper = lane < HZ + LY3;
+    const int vly = lane < HZ ? -1 : lane - HZ;
+    const int vlz = lane < HZ ? lane - 1 : -1;
+    const int vslot = (vlz + 1) * HY + (vly + 1);
+    const int myslot = (lz + 1) * HY + (ly + 1);
+
+    // chunk k of a row in walk order: forward rows start at the row, reversed rows end there
+    auto tChunk = [&](T *row, int k) { return REV ? row + Px - (k + 1) * V : row + k * V; };
+    auto sChunk = [&](const T *srow, int k) { return REV ? srow + Px - (k + 1) * V : srow + (k + 1) * V; };
+    auto walk = [&](const Vec<T> &m) { return REV ? reversed(m) : m; };   // memory <-> walk order
+
+    while (true) {
+        unsigned q = 0;
+        if (lane == 0) q = atomicAdd(st.queue[a.buf], 1u);
+        q = __shfl_sync(kFull, q, 0);
+        if (q >= static_cast<unsigned>(st.totalItems)) break;
+        const int4 item = st.order[q];
+        const int f = item.x, b = item.y, c = item.z;
+        if (st.converged[f]) continue;
+        const SourceT<T> src = a.srcs[f];
+        const int y0 = b * LY3, z0 = c * LZ3;
+        const int yp = y0 + ly, zp = z0 + lz;
+        const bool laneValid = yp < a.ny && zp < a.nz;
+        const int ya = laneValid ? reflect(yp, a.ny, fy) : 0;
+        const int za = laneValid ? reflect(zp, a.nz, fz) : 0;
+        int xlo, xhi, ylo, yhi, zlo, zhi;
+        axisBounds(a.nx, REV, a.init, src.isx, xlo, xhi);
+        axisBounds(a.ny, fy, a.init, src.isy, ylo, yhi);
+        axisBounds(a.nz, fz, a.init, src.isz, zlo, zhi);
+        const bool yzUpd = laneValid && ya >= ylo && ya <= yhi && za >= zlo && za <= zhi;
+        // the factored branch applies within `radius` cells of the source cell on every axis
+        const bool yzNear = abs(src.isy - ya) <= a.radius && abs(src.isz - za) <= a.radius;
+        T *row = a.tt + static_cast<long long>(f) * a.fieldStride + (static_cast<long long>(za) * a.ny + ya) * Px;
+        const T *srow = sp + static_cast<long long>(za + (fz ? 0 : 1)) * a.spPlane +
+                        static_cast<long long>(ya + (fy ? 0 : 1)) * a.spPitch;
+        Vec<T> tNext = splat(huge), sNext = splat(huge);
+        if (laneValid) {
+            tNext = ldVec(tChunk(row, 0));
+            sNext = ldVec(sChunk(srow, 0));
+        }
+
+        // mailbox: this block's faces, and the upstream face row a helper lane reads
+        const long long tileId = (static_cast<long long>(f) * a.tilesZ + c) * a.tilesY + b;
+        unsigned long long *box = st.mbox + tileId * faceWords;
+        unsigned long long *yFace = box + static_cast<long long>(lz) * Px * W;          // ly == LY-1
+        unsigned long long *zFace = box + static_cast<long long>(LZ3 + ly) * Px * W;    // lz == LZ-1
+        const int vyp = y0 + vly, vzp = z0 + vlz;
+        const bool vValid = helper && vyp >= 0 && vzp >= 0 && vyp < a.ny && vzp < a.nz;
+        const unsigned long long *vbox = st.mbox;
+        const T *vsrow = sp;
+        if (vValid) {
+            const int vya = reflect(vyp, a.ny, fy), vza = reflect(vzp, a.nz, fz);
+            if (vly < 0) {
+                const long long up = vlz >= 0 ? tileId - 1 : tileId - a.tilesY - 1;
+                vbox = st.mbox + up * faceWords + static_cast<long long>(vlz >= 0 ? vlz : LZ3 - 1) * Px * W;
+            } else {
+                vbox = st.mbox + (tileId - a.tilesY) * faceWords + static_cast<long long>(LZ3 + vly) * Px * W;
+            }
+            vsrow = sp + static_cast<long long>(vza + (fz ? 0 : 1)) * a.spPlane +
+                    static_cast<long long>(vya + (fy ? 0 : 1)) * a.spPitch;
+        }
+
+        // Halo pipeline: the chunk a virtual lane produces at step sv goes into ring slot
+        // sv; its mailbox words are loaded one step ahead and checked at step sv.
+        auto haloChunk = [&](int sv) { return sv - vly - vlz; };
+        auto haloValid = [&](int kv) { return vValid && kv >= 0 && kv < nChunks; };
+        auto haloStore = [&](int sv, const Vec<T> &tv, const Vec<T> &sv_) {
+            const int slot = (sv & (kRingC - 1)) * kPlane + vslot;
+            tring[slot] = tv;
+            sring[slot] = sv_;
+        };
+        MailChunk<T> mslot;
+        Vec<T> sslot = splat(huge);
+        auto issue = [&](int sv) {
+            const int kv = haloChunk(sv);
+            if (helper && haloValid(kv)) {
+                mslot.issue(vbox + static_cast<long long>(kv) * V * W);
+                sslot = ldVec(sChunk(vsrow, kv));
+            }
+        };
+        auto consume = [&](int sv) -> bool {
+            bool good = true;
+            if (helper) {
+                const int kv = haloChunk(sv);
+                Vec<T> tv = splat(huge), svv = splat(huge);
+                if (haloValid(kv)) {
+                    good = mslot.take(vbox + static_cast<long long>(kv) * V * W, tag, st.abortFlag, st.spinLimit);
+                    tv = mslot.value();
+                    svv = walk(sslot);
+                }
+                haloStore(sv, tv, svv);
+            }
+            return __all_sync(kFull, good);
+        };
+
+        issue(-2);
+        bool ok = consume(-2);
+        if (ok) {
+            issue(-1);
+            ok = consume(-1);
+        }
+        if (ok) issue(0);
+        // x'-1 values of the chunks read the step before (walk position k*V - 1)
+        T cT1 = huge, cT3 = huge, cT4 = huge, cT7 = huge;
+        T cS1 = huge, cS2 = huge, cS5 = huge, cS7 = huge;
+        T res = 0;
+        for (int s = 0; s < nSteps && ok; ++s) {
+            ok = consume(s);
+            if (!ok) break;
+            issue(s + 1);
+            const int k = s - ly - lz;
+            const bool active = laneValid && k >= 0 && k < nChunks;
+            Vec<T> tOwn = splat(huge), sOwn = splat(huge);
+            if (active) {
+                tOwn = walk(tNext);
+                sOwn = walk(sNext);
+                if (k + 1 < nChunks) {
+                    tNext = ldVec(tChunk(row, k + 1));
+                    sNext = ldVec(sChunk(srow, k + 1));
+                }
+            }
+            const int cur = (s & (kRingC - 1)) * kPlane;
+            const int p1 = ((s - 1) & (kRingC - 1)) * kPlane;
+            const int p2 = ((s - 2) & (kRingC - 1)) * kPlane;
+            sring[cur + myslot] = sOwn;
+            __syncwarp();
+            const Vec<T> tY = tring[p1 + myslot - 1];          // lane (ly-1, lz): same chunk
+            const Vec<T> tZ = tring[p1 + myslot - HY];         // lane (ly, lz-1)
+            const Vec<T> tYZ = tring[p2 + myslot - HY - 1];    // lane (ly-1, lz-1)
+            const Vec<T> sY = sring[p1 + myslot - 1];
+            const Vec<T> sZ = sring[p1 + myslot - HY];
+            const Vec<T> sYZ = sring[p2 + myslot - HY - 1];
+            Vec<T> out = tOwn;
+            bool changed = false;
+#pragma unroll
+            for (int e = 0; e < V; ++e) {
+                const int xp = k * V + e;
+                const int xa = REV ? Px - 1 - xp : xp;
+                if (active && yzUpd && xa >= xlo && xa <= xhi) {
+                    Stencil3<T> n;
+                    n.t1 = e ? out.v[e - 1] : cT1;
+                    n.t3 = tY.v[e];
+                    n.t2 = e ? tY.v[e - 1] : cT3;
+                    n.t4 = tZ.v[e];
+                    n.t5 = e ? tZ.v[e - 1] : cT4;
+                    n.t7 = tYZ.v[e];
+                    n.t6 = e ? tYZ.v[e - 1] : cT7;
+                    n.s0 = e ? sYZ.v[e - 1] : cS1;
+                    n.s1 = sYZ.v[e];
+                    n.s2 = sZ.v[e];
+                    n.s3 = e ? sZ.v[e - 1] : cS2;
+                    n.s4 = e ? sY.v[e - 1] : cS5;
+                    n.s5 = sY.v[e];
+                    n.s7 = e ? sOwn.v[e - 1] : cS7;
+                    const bool near = yzNear && abs(src.isx - xa) <= a.radius;
+                    T tu;
+                    if (UNIFORM) tu = near ? nearUniform<T>(a.h, src, sg, xa, ya, za, n) : fd3UniformFar<T>(a.h, n);
+                    else tu = near ? nearNonUniform<T>(a.sp3, src, sg, xa, ya, za, n) : fd3NonUniformFar<T>(a.sp3, n);
+                    const T t0 = out.v[e];
+                    if (tu < t0) {
+                        out.v[e] = tu;
+                        changed = true;
+                        res = dmax(res, t0 - tu);
+                    }
+                }
+            }
+            tring[cur + myslot] = out;
+            if (active) {
+                if (changed) stVec(tChunk(row, k), walk(out));
+                if (ly == LY3 - 1) putChunk(yFace + static_cast<long long>(k) * V * W, tag, out);
+                if (lz == LZ3 - 1) putChunk(zFace + static_cast<long long>(k) * V * W, tag, out);
+            }
+            cT1 = out.v[V - 1]; cT3 = tY.v[V - 1]; cT4 = tZ.v[V - 1]; cT7 = tYZ.v[V - 1];
+            cS1 = sYZ.v[V - 1]; cS2 = sZ.v[V - 1]; cS5 = sY.v[V - 1]; cS7 = sOwn.v[V - 1];
+        }
+        if (!ok) break;
+        const double r = warpMax(static_cast<double>(res));
+        if (lane == 0 && r > 0)
+            atomicMax(st.residual + static_cast<long long>(f) * st.residualStride + a.residualSlot,
+                      static_cast<unsigned long long>(__double_as_longlong(r)));
+    }
+}
+
+template <class T, bool U, bool R> void *chunkKernel() {
+    return reinterpret_cast<void *>(sweep3ChunkKernel<T, U, R>);
+}
+
+}  // namespace
+
+size_t sweep3ChunkSmemBytes() { return 2 * kRingC * kPlane * 16 * kWarpsPerBlock; }
+
+template <class T>
+cudaError_t launchSweep3Chunk(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s) {
+    const size_t smem = sweep3ChunkSmemBytes();
+    const bool rev = (a.sweep & 1) != 0;
+    if (uniform) {
+        if (rev) sweep3ChunkKernel<T, true, true><<<blocks, kThreads, smem, s>>>(a);
+        else sweep3ChunkKernel<T, true, false><<<blocks, kThreads, smem, s>>>(a);
+    } else {
+        if (rev) sweep3ChunkKernel<T, false, true><<<blocks, kThreads, smem, s>>>(a);
+        else sweep3ChunkKernel<T, false, false><<<blocks, kThreads, smem, s>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+template <class T> int sweep3ChunkBlocksPerSM(bool uniform) {
+    // the four instantiations of a precision share their resource use; take the least
+    int best = 1 << 30;
+    void *k[2] = {uniform ? chunkKernel<T, true, false>() : chunkKernel<T, false, false>(),
+                  uniform ? chunkKernel<T, true, true>() : chunkKernel<T, false, true>()};
+    for (void *f : k) {
+        int n = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kThreads, sweep3ChunkSmemBytes());
+        best = n < best ? n : best;
+    }
+    return best > 0 ? best : 1;
+}
+
+template cudaError_t launchSweep3Chunk<float>(const Sweep3Args<float> &, bool, int, cudaStream_t);
+template cudaError_t launchSweep3Chunk<double>(const Sweep3Args<double> &, bool, int, cudaStream_t);
+template int sweep3ChunkBlocksPerSM<float>(bool);
+template int sweep3ChunkBlocksPerSM<double>(bool);
+
+}  // namespace eikx

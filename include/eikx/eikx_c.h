@@ -68,7 +68,11 @@ typedef struct {
                               = one field per lane, measured faster on GB300 at every batch
                               size (the paired kernel needs 168 registers per thread, which
                               leaves 12 resident warps per SM).  Both give identical times. */
-    int reserved[3];
+    int sweep_kernel;      /* 3D sweep kernel: 0 (default) = chunk-step, 1 = node-step (a
+                              lane updates one node per wavefront step), 2 = chunk-step (a
+                              lane updates one 16-byte chunk, 4 FP32 / 2 FP64 nodes, per
+                              step).  All give identical travel times. */
+    int reserved[2];
 } eikx_options;
 
 /* Fills *opt with the defaults above. */
