@@ -192,6 +192,14 @@ def run_gpu(args):
     achieved = bytes_per_launch / (sweep_launch_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
     tr = _traffic()
+    kernel_name = ("sweep3PairKernel" if PAIR[0] and fields >= 2 else
+                   "sweep3Kernel<float,uniform>" if KERNEL[0] == 1 else "sweep3ChunkKernel<float,uniform>")
+    traffic, traffic_src = None, None
+    if tr and tr.get("kernel") == kernel_name:
+        # DRAM bytes of one full sweep from the committed ncu capture, scaled by the
+        # fields per launch (traffic grows in proportion to the fields swept)
+        traffic = tr["dram_bytes_per_launch"] * fields / tr["fields"]
+        traffic_src = f"profiles/sweep3d_traffic.json ({tr['fields']} fields, scaled to {fields})"
 
     # end to end through the public API with host buffers every step
     e2e_ms = []
@@ -215,12 +223,10 @@ def run_gpu(args):
                    "factored_radius": RADIUS, "tolerance_s": TOL, "max_iterations": N_SWEEPS_MAX,
                    "l2": "flushed (write of 2x L2) between timed steps; per-step fields exceed L2",
                    "parallelism": f"replicas x{world} (sources sharded, no collective)"},
-        "roofline": {"bound": "hbm", "kernel": ("sweep3PairKernel" if PAIR[0] and fields >= 2
-                                                else "sweep3Kernel<float,uniform>" if KERNEL[0] == 1
-                                                else "sweep3ChunkKernel<float,uniform>"), "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "bytes_per_launch": bytes_per_launch, "launch_ms": sweep_launch_ms,
-                     "traffic": (tr["dram_bytes_per_launch"] if tr else None)},
+                     "traffic": traffic, "traffic_source": traffic_src},
         "e2e": {"value": e2e, "unit": "grids/s", "h2d_bytes_per_step": int(v.nbytes + 24 * fields),
                 "d2h_bytes_per_step": int(4 * n_nodes * fields), "ms_per_step": float(np.mean(e2e_ms))},
         "gpu_launches": int(launches), "clocks": clk.summary(),
@@ -312,8 +318,9 @@ def cpu_sweep_rate(seconds, threads):
 def _sweeps_per_grid(iterations=None):
     """Sweeps one grid of this workload takes (init pass + refinement iterations), for
     the CPU extrapolation: the GPU arm passes the iterations it measured; otherwise the
-    count the workload converges in (4 iterations, measured on GB300)."""
-    return 8 * (1 + (iterations if iterations else 4))
+    count the FP32 workload converges in at tolerance 1e-5 s (7 refinement iterations,
+    measured on GB300 with 8 to 32 sources)."""
+    return 8 * (1 + (iterations if iterations else 7))
 
 
 def cpu_baseline(seconds, threads=1, sweeps_per_grid=None):
@@ -358,7 +365,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--fields", type=int, default=8, help="independent sources per step per GPU")
+    ap.add_argument("--fields", type=int, default=32, help="independent sources per step per GPU")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cpu-threads", type=int, default=0)
