@@ -122,6 +122,7 @@ def make_workload(fields):
 def run_gpu(args):
     import torch
     import eikonalxx_gb300 as ex
+    from eikonalxx_gb300 import sharding
 
     world, rank = _dist()
     if world > 1:
@@ -131,7 +132,7 @@ def run_gpu(args):
     dev = torch.cuda.current_device()
     fields = args.fields
     v, src_all = make_workload(fields * world)
-    src = src_all[rank * fields:(rank + 1) * fields]   # weak scaling: each rank its own fields
+    src = src_all[sharding.shard(fields * world, world, rank)]   # weak scaling: each rank its own fields
     n_nodes = NX * NY * NZ
 
     ctx = ex.Context(dev)
@@ -160,9 +161,8 @@ def run_gpu(args):
 
     for _ in range(args.warmup):
         step_device()
-    if world > 1:
-        torch.distributed.barrier()
     torch.cuda.synchronize()
+    sharding.barrier()
     per_step_ms, iters, launches, wall = [], [], 0, []
     with ClockSampler(dev) as clk:
         for _ in range(args.steps):
@@ -175,11 +175,8 @@ def run_gpu(args):
             iters.append(st["iterations_max"])
             launches += st["kernel_launches"]
     torch.cuda.synchronize()
-    ms = float(np.mean(per_step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    sharding.barrier()
+    ms = sharding.max_over_ranks(float(np.mean(per_step_ms)), device=f"cuda:{dev}")
     value = fields * world / (ms / 1e3)
 
     # roofline of the sweep kernel: per-launch durations from CUDA events around each sweep
