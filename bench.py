@@ -33,6 +33,7 @@ METRIC = "3D travel-time grids/s at max err <=1e-4 s vs FP64; batched+learned vs
 NX, NY, NZ, H = 256, 256, 128, 50.0
 MODEL_SEED, SOURCE_SEED = 20240601, 7
 N_SWEEPS_MAX, TOL, RADIUS = 10, 1e-5, 3
+SURFACE = [False]  # sources on the top surface (station tables by reciprocity)
 PAIR = [False]  # pair_fields option of the GPU arm (set from the command line)
 KERNEL = [0]    # sweep_kernel option of the GPU arm: 0 default, 1 node-step, 2 chunk-step
 L2_BYTES = 129 * 2 ** 20
@@ -115,7 +116,7 @@ class ClockSampler:
 def make_workload(fields):
     from eikonalxx_gb300 import synthetic
     v = synthetic.layered_grf_model(NX, NY, NZ, H, MODEL_SEED)
-    src = synthetic.uniform_sources(fields, NX, NY, NZ, H, SOURCE_SEED)
+    src = synthetic.uniform_sources(fields, NX, NY, NZ, H, SOURCE_SEED, surface=SURFACE[0])
     return v, src
 
 
@@ -214,8 +215,10 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered+GRF model, seeded sources)",
-        "config": {"workload": f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, "
-                               f"{fields} independent sources per step per GPU",
+        "config": {"workload": (f"station tables, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, {fields} sources on the "
+                                f"top surface per step per GPU, one persistent launch per sweep" if SURFACE[0] else
+                                f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, "
+                                f"{fields} independent sources per step per GPU"),
                    "grid": [NX, NY, NZ], "h_m": H, "fields_per_step": fields, "precision": "fp32 sweeps, fp64 init",
                    "factored_radius": RADIUS, "tolerance_s": TOL, "max_iterations": N_SWEEPS_MAX,
                    "l2": "flushed (write of 2x L2) between timed steps; per-step fields exceed L2",
@@ -231,6 +234,100 @@ def run_gpu(args):
         "wall_ms_per_step": float(np.mean(wall)), "accuracy": acc,
         "cpu_baseline": (cpu_baseline(args.cpu_seconds, 1, _sweeps_per_grid(max(iters)))
                          if not args.skip_cpu else None),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_models(args):
+    """Many models of uneven size in one schedule: `fields` layered+GRF models with nx, ny
+    uniform in [64, 256], nz in [32, 128], h = 100 m, one seeded source each."""
+    import torch
+    import eikonalxx_gb300 as ex
+    from eikonalxx_gb300 import sharding, synthetic
+
+    world, rank = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.cuda.current_device()
+    n = args.fields
+    everything = synthetic.uneven_models(n * world, MODEL_SEED + 1)
+    mine = everything[sharding.shard(n * world, world, rank)]
+    nodes = sum(m["grid"][0] * m["grid"][1] * m["grid"][2] for m in mine)
+    ctx = ex.Context(dev)
+    dev_models = [{"grid": m["grid"], "model": torch.from_numpy(m["v"]).to(f"cuda:{dev}"), "nodal": True,
+                   "sources": [m["source"]],
+                   "out": torch.empty((1,) + m["v"].shape, dtype=torch.float32, device=f"cuda:{dev}")} for m in mine]
+    host_models = [{"grid": m["grid"], "model": torch.from_numpy(m["v"]).pin_memory(), "nodal": True,
+                    "sources": [m["source"]],
+                    "out": torch.empty((1,) + m["v"].shape, dtype=torch.float32).pin_memory()} for m in mine]
+    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+
+    acc = {}
+    if rank == 0 and not args.skip_accuracy:
+        t32 = ctx.solve3d_batch(dev_models, opt, ex.F32)
+        t32 = [t.cpu().numpy().astype(np.float64) for t in t32]
+        o64 = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=1e-9, factored_radius=RADIUS)
+        t64 = ctx.solve3d_batch([dict(m, out=None) for m in dev_models], o64, ex.F64)
+        d = np.concatenate([np.abs(a - b).ravel() for a, b in zip(t32, t64)])
+        acc = {"max_err_vs_fp64_s": float(d.max()), "rms_err_vs_fp64_s": float(np.sqrt(np.mean(d ** 2)))}
+
+    for _ in range(args.warmup):
+        ctx.solve3d_batch(dev_models, opt, ex.F32)
+    torch.cuda.synchronize()
+    sharding.barrier()
+    per_step, iters, launches = [], [], 0
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            ctx.solve3d_batch(dev_models, opt, ex.F32)
+            st = ctx.stats()
+            per_step.append(st["device_ms"])
+            iters.append(st["iterations_max"])
+            launches += st["kernel_launches"]
+    torch.cuda.synchronize()
+    sharding.barrier()
+    ms = sharding.max_over_ranks(float(np.mean(per_step)), device=f"cuda:{dev}")
+    value = n * world / (ms / 1e3)
+
+    prof = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True)
+    ctx.solve3d_batch(dev_models, prof, ex.F32)
+    pst = ctx.stats()
+    launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
+    bytes_per_launch = BYTES_PER_NODE_SWEEP * nodes
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+
+    e2e_ms = []
+    for i in range(max(1, args.warmup) + args.steps):
+        t0 = time.perf_counter()
+        ctx.solve3d_batch(host_models, opt, ex.F32)
+        if i >= max(1, args.warmup):
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e = n * world / (float(np.mean(e2e_ms)) / 1e3)
+    if rank != 0:
+        return
+    grids = [m["grid"][:3] for m in mine]
+    line = {
+        "metric": METRIC, "value": value, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered+GRF models, seeded sources)",
+        "config": {"workload": f"{n} models of uneven size (nx, ny in [64, 256], nz in [32, 128], h=100 m) "
+                               f"per step per GPU, one source each, one schedule",
+                   "nodes_per_step": nodes, "grids_min": min(grids), "grids_max": max(grids),
+                   "precision": "fp32 sweeps, fp64 init", "factored_radius": RADIUS, "tolerance_s": TOL,
+                   "max_iterations": N_SWEEPS_MAX, "l2": "flushed (write of 2x L2) between timed steps",
+                   "parallelism": f"replicas x{world} (models sharded, no collective)"},
+        "roofline": {"bound": "hbm", "kernel": "sweep3ChunkKernel<float,uniform,batch>", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms, "traffic": None},
+        "e2e": {"value": e2e, "unit": "grids/s", "h2d_bytes_per_step": int(sum(m["v"].nbytes for m in mine)),
+                "d2h_bytes_per_step": int(4 * nodes), "ms_per_step": float(np.mean(e2e_ms))},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "iterations": {"max": int(max(iters)), "min": int(min(iters))}, "accuracy": acc,
     }
     print(json.dumps(line), flush=True)
 
@@ -362,7 +459,11 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--fields", type=int, default=32, help="independent sources per step per GPU")
+    ap.add_argument("--workload", default="plain", choices=["plain", "stations", "models"],
+                    help="plain: 256x256x128 h=50 m, independent sources; stations: 200x200x100 h=100 m, "
+                         "sources on the top surface; models: uneven models, one source each")
+    ap.add_argument("--fields", type=int, default=None,
+                    help="sources (plain: 32, stations: 64) or models (models: 32) per step per GPU")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -375,6 +476,12 @@ def main():
     ap.add_argument("--profile-case", action="store_true",
                     help="one solve of the workload (1 refinement iteration) for ncu captures")
     args = ap.parse_args()
+    global NX, NY, NZ, H
+    if args.workload == "stations":
+        NX, NY, NZ, H = 200, 200, 100, 100.0
+        SURFACE[0] = True
+    if args.fields is None:
+        args.fields = 64 if args.workload == "stations" else 32
     PAIR[0] = args.pair_fields
     KERNEL[0] = args.sweep_kernel
     if args.profile_case:
@@ -384,6 +491,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "models":
+        run_models(args)
     else:
         run_gpu(args)
 

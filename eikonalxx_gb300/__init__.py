@@ -34,8 +34,9 @@ EXPORTED = [
     "eikx_set_grid3d", "eikx_set_slowness3d", "eikx_set_nodal_velocity3d", "eikx_get_slowness3d",
     "eikx_solve3d", "eikx_set_grid2d", "eikx_set_slowness2d", "eikx_set_nodal_velocity2d",
     "eikx_solve2d", "eikx_graph3d_tables", "eikx_levels2d", "eikx_analytic3d", "eikx_analytic2d",
-    "eikx_solve3d_noalloc",
+    "eikx_solve3d_noalloc", "eikx_solve3d_batch",
 ]
+CELL_SLOWNESS, NODAL_VELOCITY = 0, 1
 
 
 class EikxError(RuntimeError):
@@ -82,6 +83,15 @@ class _Src2(ctypes.Structure):
     _fields_ = [("x", ctypes.c_double), ("z", ctypes.c_double)]
 
 
+class _Model3(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("x0", ctypes.c_double), ("y0", ctypes.c_double), ("z0", ctypes.c_double),
+                ("model", ctypes.c_void_p), ("model_kind", ctypes.c_int), ("dtype", ctypes.c_int),
+                ("ordering", ctypes.c_int), ("where", ctypes.c_int), ("n_src", ctypes.c_int),
+                ("src", ctypes.POINTER(_Src3)), ("t_out", ctypes.c_void_p), ("t_where", ctypes.c_int)]
+
+
 _lib = None
 
 
@@ -116,6 +126,7 @@ def load(path=None):
     lib.eikx_levels2d.argtypes = [c_int, c_int, c_int, ip, ip, ip]
     lib.eikx_analytic3d.argtypes = [vp, ctypes.POINTER(_Src3), c_double, c_double, vp, c_int]
     lib.eikx_analytic2d.argtypes = [vp, ctypes.POINTER(_Src2), c_double, c_double, vp, c_int]
+    lib.eikx_solve3d_batch.argtypes = [vp, ctypes.POINTER(_Model3), c_int, ctypes.POINTER(_Options), c_int]
     for name in EXPORTED:
         if name not in ("eikx_options_default", "eikx_last_error", "eikx_levels2d", "eikx_graph3d_tables"):
             getattr(lib, name).restype = c_int
@@ -249,6 +260,36 @@ class Context:
         o = (options or Options())._c()
         _check(self._lib.eikx_solve3d(self._h, arr, n, ctypes.byref(o), precision, p, where))
         return out
+
+    def solve3d_batch(self, models, options=None, precision=F32):
+        """Solve many models, each with its own sources, in one schedule.
+
+        `models` is a sequence of dicts with keys ``grid`` = (nx, ny, nz, dx, dy, dz[, x0,
+        y0, z0]), ``model`` (cell slowness of (nz-1, ny-1, nx-1) values or, with
+        ``nodal=True``, nodal velocity of (nz, ny, nx) values; numpy or torch, host or
+        CUDA), ``sources`` (sequence of (x, y, z)) and optionally ``out`` (n_src, nz, ny,
+        nx). Returns the list of output arrays, one per model."""
+        n = len(models)
+        arr = (_Model3 * n)()
+        keep, outs = [], []
+        for i, m in enumerate(models):
+            g = tuple(m["grid"]) + (0.0,) * (9 - len(m["grid"]))
+            nx, ny, nz = (int(v) for v in g[:3])
+            src = np.atleast_2d(np.asarray(m["sources"], dtype=np.float64))
+            sarr = (_Src3 * len(src))(*[_Src3(*map(float, q)) for q in src])
+            out = m.get("out")
+            if out is None:
+                out = np.empty((len(src), nz, ny, nx), dtype=np.float32 if precision == F32 else np.float64)
+            mp, mwhere = _ptr(m["model"])
+            op, owhere = _ptr(out)
+            arr[i] = _Model3(nx, ny, nz, *map(float, g[3:9]), mp,
+                             NODAL_VELOCITY if m.get("nodal") else CELL_SLOWNESS, _dtype_code(m["model"]),
+                             int(m.get("ordering", NATURAL)), mwhere, len(src), sarr, op, owhere)
+            keep.append(sarr)
+            outs.append(out)
+        o = (options or Options())._c()
+        _check(self._lib.eikx_solve3d_batch(self._h, arr, n, ctypes.byref(o), precision))
+        return outs
 
     # ---- 2D ---------------------------------------------------------------
     def set_grid2d(self, nx, nz, dx, dz, x0=0.0, z0=0.0):

@@ -7,6 +7,7 @@
 // initialisation, the source-limited pass, nSweeps refinement iterations each
 // followed by the convergence check -- and copy the fields out with one pitched copy.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -91,6 +92,23 @@ struct Workspace {
     std::vector<int> orderKey;   // (tilesY, tilesZ, nFields, dim) of the uploaded order table
 };
 
+// Buffers of multi-model batches (eikx_solve3d_batch): every model's fields, padded
+// slowness and mailbox packed into one allocation each, plus the cached schedule graph.
+struct BatchWorkspace {
+    DevBuf tt, sp, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, units,
+        slow64, input, badFlag;
+    PinnedBuf stage, srcCells;
+    std::vector<double> key;                 // what the cached graph was captured for
+    cudaGraphExec_t exec = nullptr;
+    int launches = 0;
+    void dropGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key.clear();
+    }
+    ~BatchWorkspace() { dropGraph(); }
+};
+
 struct ScheduleKey {
     int dim = 0, precision = -1, nFields = 0, nx = 0, ny = 0, nz = 0, nSweeps = -1, radius = 0,
         initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0, variant = 0;
@@ -126,6 +144,7 @@ struct eikx_ctx {
     bool spadValid2[2] = {false, false};
     DevBuf scratch;                // staging for host inputs and analytic fields
     Workspace ws;
+    BatchWorkspace bw;
     eikx_stats stats{};
     // cached schedule graph
     ScheduleKey graphKey;
@@ -565,6 +584,397 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     return EIKX_OK;
 }
 
+// Spacing constants of the non-uniform 3D solver in the field type
+// (include/private/solver3d.hpp:247-261).
+template <class T> eikx::Spacing3<T> spacing3(double dx, double dy, double dz) {
+    const T tdx = static_cast<T>(dx), tdy = static_cast<T>(dy), tdz = static_cast<T>(dz);
+    eikx::Spacing3<T> g;
+    g.dx = tdx; g.dy = tdy; g.dz = tdz;
+    g.dxInv = 1 / tdx; g.dyInv = 1 / tdy; g.dzInv = 1 / tdz;
+    g.dx2Inv = 1 / (tdx * tdx); g.dy2Inv = 1 / (tdy * tdy); g.dz2Inv = 1 / (tdz * tdz);
+    g.dx_dz = tdx / tdz; g.dz_dx = tdz / tdx; g.dy_dz = tdy / tdz; g.dz_dy = tdz / tdy;
+    g.dx_dy = tdx / tdy; g.dy_dx = tdy / tdx;
+    g.dx2_p_dz2_inv = 1 / (tdx * tdx + tdz * tdz);
+    g.dy2_p_dz2_inv = 1 / (tdy * tdy + tdz * tdz);
+    g.dx2_p_dy2_inv = 1 / (tdx * tdx + tdy * tdy);
+    return g;
+}
+
+bool uniformSpacing3(double dx, double dy, double dz, double eps) {
+    return std::abs(dx - dy) < eps && std::abs(dx - dz) < eps;
+}
+
+// Checks one model of a batch; returns an error message or "".
+std::string checkModel(const eikx_model3d &m, int i) {
+    const std::string who = "model " + std::to_string(i) + ": ";
+    if (m.nx < 3 || m.ny < 3 || m.nz < 3) return who + "grid needs at least 3 points in each direction";
+    if (!(m.dx > 0) || !(m.dy > 0) || !(m.dz > 0)) return who + "grid spacing must be positive";
+    if (!m.model) return who + "model is NULL";
+    if (m.model_kind != EIKX_CELL_SLOWNESS && m.model_kind != EIKX_NODAL_VELOCITY)
+        return who + "model_kind must be EIKX_CELL_SLOWNESS or EIKX_NODAL_VELOCITY";
+    if (m.dtype != EIKX_F32 && m.dtype != EIKX_F64) return who + "dtype must be EIKX_F32 or EIKX_F64";
+    if (m.ordering != 0 && m.ordering != 1) return who + "ordering must be 0 (natural) or 1";
+    if (m.where != EIKX_HOST && m.where != EIKX_DEVICE) return who + "where must be EIKX_HOST or EIKX_DEVICE";
+    if (m.n_src < 1 || !m.src) return who + "needs at least one source";
+    if (!m.t_out) return who + "t_out is NULL";
+    if (m.t_where != EIKX_HOST && m.t_where != EIKX_DEVICE) return who + "t_where must be EIKX_HOST or EIKX_DEVICE";
+    return "";
+}
+
+// One schedule over the selected models of a batch (all with uniform or all with
+// non-uniform spacing).  Statistics are accumulated into `agg`.
+template <class T>
+eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vector<int> &sel, bool uniform,
+                        const eikx_options &o, eikx_stats &agg) {
+    BatchWorkspace &w = c->bw;
+    constexpr int V = 16 / sizeof(T);
+    constexpr int W = sizeof(T) / 4;
+    const int ly = eikx::LY3, lz = eikx::LZ3;
+    const int nM = static_cast<int>(sel.size());
+    struct Layout {
+        int nx, ny, nz, Px, spPitch, tilesY, tilesZ, firstUnit, nSrc;
+        long long fieldStride, spPlane, spElems, faceWords;
+        size_t ttOff, spOff, mboxOff;
+    };
+    std::vector<Layout> L(nM);
+    size_t ttElems = 0, spElems = 0, mboxWords = 0, maxCells = 0, maxInBytes = 0, nItems = 0;
+    int nUnits = 0;
+    for (int i = 0; i < nM; ++i) {
+        const eikx_model3d &m = models[sel[i]];
+        Layout &l = L[i];
+        l.nx = m.nx; l.ny = m.ny; l.nz = m.nz;
+        l.Px = roundUp(m.nx, 4);
+        l.spPitch = l.Px + 8;
+        l.tilesY = (m.ny + ly - 1) / ly;
+        l.tilesZ = (m.nz + lz - 1) / lz;
+        l.nSrc = m.n_src;
+        l.firstUnit = nUnits;
+        l.fieldStride = static_cast<long long>(l.Px) * m.ny * m.nz;
+        l.spPlane = static_cast<long long>(l.spPitch) * (m.ny + 1);
+        l.spElems = l.spPlane * (m.nz + 1);
+        l.faceWords = static_cast<long long>(ly + lz) * l.Px * W;
+        l.ttOff = ttElems;
+        ttElems += static_cast<size_t>(l.fieldStride) * m.n_src;
+        l.spOff = spElems;
+        spElems += 2 * static_cast<size_t>(l.spElems);
+        l.mboxOff = mboxWords;
+        mboxWords += static_cast<size_t>(m.n_src) * l.tilesY * l.tilesZ * l.faceWords;
+        nUnits += m.n_src;
+        nItems += static_cast<size_t>(m.n_src) * l.tilesY * l.tilesZ;
+        const size_t cells = static_cast<size_t>(m.nx - 1) * (m.ny - 1) * (m.nz - 1);
+        const size_t nIn = m.model_kind == EIKX_NODAL_VELOCITY ? static_cast<size_t>(m.nx) * m.ny * m.nz : cells;
+        maxCells = std::max(maxCells, cells);
+        maxInBytes = std::max(maxInBytes, nIn * (m.dtype == EIKX_F64 ? 8 : 4));
+    }
+    if (nItems > static_cast<size_t>(std::numeric_limits<int>::max()))
+        return fail(EIKX_ERR_INVALID, "batch has too many warp blocks");
+    const int nSweepKinds = 8;
+    const int nSweeps = std::max(0, o.n_sweeps);
+    const int resStride = nSweepKinds * (1 + nSweeps);
+
+    const void *before[] = {w.tt.p, w.sp.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p, w.iterations.p,
+                            w.order.p, w.srcs.p, w.corners.p, w.units.p};
+    EIKX_CUDA(w.tt.ensure(ttElems * sizeof(T)));
+    EIKX_CUDA(w.sp.ensure(spElems * sizeof(T)));
+    if (w.mbox.bytes < mboxWords * 8 || !w.mbox.p) {
+        // fresh words carry tag 0, which no sweep uses
+        EIKX_CUDA(w.mbox.ensure(mboxWords * 8));
+        EIKX_CUDA(cudaMemsetAsync(w.mbox.p, 0, w.mbox.bytes, c->stream));
+    }
+    if (!w.epoch.p) {
+        EIKX_CUDA(w.epoch.ensure(sizeof(unsigned)));
+        EIKX_CUDA(cudaMemsetAsync(w.epoch.p, 0, sizeof(unsigned), c->stream));
+    }
+    EIKX_CUDA(w.queue.ensure(2 * sizeof(unsigned)));
+    EIKX_CUDA(w.residual.ensure(static_cast<size_t>(nUnits) * resStride * 8));
+    EIKX_CUDA(w.converged.ensure(static_cast<size_t>(nUnits) * 4));
+    EIKX_CUDA(w.iterations.ensure(static_cast<size_t>(nUnits) * 4));
+    EIKX_CUDA(w.abortFlag.ensure(sizeof(int)));
+    EIKX_CUDA(w.order.ensure(nItems * 16));
+    EIKX_CUDA(w.srcs.ensure(static_cast<size_t>(nUnits) * sizeof(eikx::SourceT<T>)));
+    EIKX_CUDA(w.corners.ensure(static_cast<size_t>(nUnits) * sizeof(eikx::Corner3)));
+    EIKX_CUDA(w.units.ensure(static_cast<size_t>(nUnits) * sizeof(eikx::Grid3Unit<T>)));
+    EIKX_CUDA(w.slow64.ensure(maxCells * sizeof(double)));
+    EIKX_CUDA(w.input.ensure(maxInBytes));
+    EIKX_CUDA(w.badFlag.ensure(sizeof(int)));
+    EIKX_CUDA(w.srcCells.ensure(static_cast<size_t>(nUnits) * sizeof(double) + sizeof(int)));
+    const void *after[] = {w.tt.p, w.sp.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p, w.iterations.p,
+                           w.order.p, w.srcs.p, w.corners.p, w.units.p};
+    if (std::memcmp(before, after, sizeof(before)) != 0) w.dropGraph();
+
+    // models -> cell slowness (FP64, natural) -> two padded copies in the sweep precision;
+    // sources located on each model as eikx_solve3d does.  The whole batch is one stream
+    // of work with a single synchronisation: positivity is checked on the device into one
+    // flag and only the source cells' slowness comes back to the host.
+    std::vector<eikx::SourceT<T>> srcT(nUnits);
+    std::vector<eikx::Corner3> corners(nUnits);
+    std::vector<eikx::Grid3Unit<T>> units(nUnits);
+    std::vector<std::array<double, 3>> offs(nUnits);
+    T *ttBase = w.tt.as<T>();
+    T *spBase = w.sp.as<T>();
+    unsigned long long *mbBase = w.mbox.as<unsigned long long>();
+    double *srcCell = static_cast<double *>(w.srcCells.p);
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));   // pinned staging of a previous call is free
+    EIKX_CUDA(cudaMemsetAsync(w.badFlag.p, 0, sizeof(int), c->stream));
+    for (int i = 0; i < nM; ++i) {
+        const eikx_model3d &m = models[sel[i]];
+        const Layout &l = L[i];
+        // locate the sources first: the cell slowness they need is copied out below
+        for (int j = 0; j < m.n_src; ++j) {
+            const int u = l.firstUnit + j;
+            int cx, cy, cz;
+            double ox, oy, oz;
+            if (!locate(m.src[j].x, m.x0, m.dx, m.nx, &cx, &ox) || !locate(m.src[j].y, m.y0, m.dy, m.ny, &cy, &oy) ||
+                !locate(m.src[j].z, m.z0, m.dz, m.nz, &cz, &oz))
+                return fail(EIKX_ERR_INVALID, "model " + std::to_string(sel[i]) + ": source " + std::to_string(j) +
+                                                  " lies outside the grid");
+            srcT[u].isx = cx; srcT[u].isy = cy; srcT[u].isz = cz;
+            offs[u] = {ox, oy, oz};
+        }
+        const bool nodal = m.model_kind == EIKX_NODAL_VELOCITY;
+        const size_t nCell = static_cast<size_t>(m.nx - 1) * (m.ny - 1) * (m.nz - 1);
+        const size_t nIn = nodal ? static_cast<size_t>(m.nx) * m.ny * m.nz : nCell;
+        const size_t inBytes = nIn * (m.dtype == EIKX_F64 ? 8 : 4);
+        const void *d = m.model;
+        if (m.where == EIKX_HOST) {
+            EIKX_CUDA(cudaMemcpyAsync(w.input.p, m.model, inBytes, cudaMemcpyHostToDevice, c->stream));
+            d = w.input.p;
+        }
+        double *slow = w.slow64.as<double>();
+        if (m.dtype == EIKX_F32) {
+            const float *f = static_cast<const float *>(d);
+            if (nodal) EIKX_CUDA(eikx::launchNodalToCell3<float>(slow, f, m.nx, m.ny, m.nz, m.ordering, c->stream));
+            else EIKX_CUDA(eikx::launchCellsToNatural3<float>(slow, f, m.nx, m.ny, m.nz, m.ordering, c->stream));
+        } else {
+            const double *f = static_cast<const double *>(d);
+            if (nodal) EIKX_CUDA(eikx::launchNodalToCell3<double>(slow, f, m.nx, m.ny, m.nz, m.ordering, c->stream));
+            else EIKX_CUDA(eikx::launchCellsToNatural3<double>(slow, f, m.nx, m.ny, m.nz, m.ordering, c->stream));
+        }
+        EIKX_CUDA(eikx::launchCheckPositive(slow, static_cast<long long>(nCell), w.badFlag.as<int>(), c->stream));
+        EIKX_CUDA((eikx::launchPadSlowness3<T, double>(spBase + l.spOff, l.spPitch, V - 1, slow, m.nx, m.ny, m.nz,
+                                                       c->stream)));
+        EIKX_CUDA((eikx::launchPadSlowness3<T, double>(spBase + l.spOff + l.spElems, l.spPitch, 0, slow, m.nx, m.ny,
+                                                       m.nz, c->stream)));
+        for (int j = 0; j < m.n_src; ++j) {
+            const int u = l.firstUnit + j;
+            const size_t cell = (static_cast<size_t>(srcT[u].isz) * (m.ny - 1) + srcT[u].isy) * (m.nx - 1) + srcT[u].isx;
+            EIKX_CUDA(cudaMemcpyAsync(srcCell + u, slow + cell, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        }
+        const eikx::Spacing3<T> g = spacing3<T>(m.dx, m.dy, m.dz);
+        for (int j = 0; j < m.n_src; ++j) {
+            eikx::Grid3Unit<T> &gu = units[l.firstUnit + j];
+            gu.tt = ttBase + l.ttOff + static_cast<size_t>(j) * l.fieldStride;
+            gu.spPos = spBase + l.spOff;
+            gu.spNeg = spBase + l.spOff + l.spElems;
+            gu.mbox = mbBase + l.mboxOff + static_cast<size_t>(j) * l.tilesY * l.tilesZ * l.faceWords;
+            gu.spPlane = l.spPlane;
+            gu.spPitch = l.spPitch;
+            gu.Px = l.Px; gu.nx = m.nx; gu.ny = m.ny; gu.nz = m.nz;
+            gu.tilesY = l.tilesY; gu.tilesZ = l.tilesZ; gu.pad = 0;
+            gu.h = static_cast<T>(m.dx);
+            gu.sp3 = g;
+        }
+    }
+    int *bad = reinterpret_cast<int *>(srcCell + nUnits);
+    EIKX_CUDA(cudaMemcpyAsync(bad, w.badFlag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));
+    if (*bad) return fail(EIKX_ERR_INVALID, "Non-positive velocities detected");
+    for (int u = 0; u < nUnits; ++u) {
+        const double sc = srcCell[u];
+        srcT[u].xs = static_cast<T>(offs[u][0]);
+        srcT[u].ys = static_cast<T>(offs[u][1]);
+        srcT[u].zs = static_cast<T>(offs[u][2]);
+        srcT[u].sSrc = static_cast<T>(sc);
+        corners[u] = eikx::Corner3{srcT[u].isx, srcT[u].isy, srcT[u].isz, offs[u][0], offs[u][1], offs[u][2],
+                                   static_cast<double>(static_cast<T>(sc))};
+    }
+
+    // work order: every unit's warp blocks, sorted by the step at which they can start
+    struct Item { int key, u, b, c; };
+    std::vector<Item> items;
+    items.reserve(nItems);
+    for (int i = 0; i < nM; ++i)
+        for (int j = 0; j < L[i].nSrc; ++j)
+            for (int cc = 0; cc < L[i].tilesZ; ++cc)
+                for (int bb = 0; bb < L[i].tilesY; ++bb) items.push_back({bb * ly + cc * lz, L[i].firstUnit + j, bb, cc});
+    std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) {
+        if (a.key != b.key) return a.key < b.key;
+        if (a.u != b.u) return a.u < b.u;
+        return a.b < b.b;
+    });
+    const size_t srcBytes = srcT.size() * sizeof(eikx::SourceT<T>);
+    const size_t cornerBytes = corners.size() * sizeof(eikx::Corner3);
+    const size_t unitBytes = units.size() * sizeof(eikx::Grid3Unit<T>);
+    const size_t orderBytes = items.size() * 16;
+    EIKX_CUDA(w.stage.ensure(srcBytes + cornerBytes + unitBytes + orderBytes + 64));
+    char *stage = static_cast<char *>(w.stage.p);
+    std::memcpy(stage, srcT.data(), srcBytes);
+    std::memcpy(stage + srcBytes, corners.data(), cornerBytes);
+    std::memcpy(stage + srcBytes + cornerBytes, units.data(), unitBytes);
+    int *ord = reinterpret_cast<int *>(stage + srcBytes + cornerBytes + unitBytes);
+    for (size_t k = 0; k < items.size(); ++k) {
+        ord[4 * k] = items[k].u; ord[4 * k + 1] = items[k].b; ord[4 * k + 2] = items[k].c; ord[4 * k + 3] = 0;
+    }
+    EIKX_CUDA(cudaMemcpyAsync(w.srcs.p, stage, srcBytes, cudaMemcpyHostToDevice, c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(w.corners.p, stage + srcBytes, cornerBytes, cudaMemcpyHostToDevice, c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(w.units.p, stage + srcBytes + cornerBytes, unitBytes, cudaMemcpyHostToDevice, c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(w.order.p, ord, orderBytes, cudaMemcpyHostToDevice, c->stream));
+
+    const int nSweepLaunches = nSweepKinds * ((o.init_sweeps ? 1 : 0) + nSweeps);
+    eikx::SolveState st{};
+    st.queue[0] = w.queue.as<unsigned>();
+    st.queue[1] = w.queue.as<unsigned>() + 1;
+    st.mbox = w.mbox.as<unsigned long long>();
+    st.epoch = w.epoch.as<unsigned>();
+    st.epochStride = nSweepLaunches + 1;
+    st.residual = w.residual.as<unsigned long long>();
+    st.residualStride = resStride;
+    st.converged = w.converged.as<int>();
+    st.iterations = w.iterations.as<int>();
+    st.abortFlag = w.abortFlag.as<int>();
+    st.order = w.order.as<int4>();
+    st.totalItems = static_cast<int>(nItems);
+    const int spinLog2 = o.spin_limit_log2 > 0 ? std::min(o.spin_limit_log2, 40) : 22;
+    st.spinLimit = 1ull << spinLog2;
+    const int perSM = eikx::sweep3ChunkBlocksPerSM<T>(uniform, true);
+    const int blocks = std::max(1, static_cast<int>(std::min<size_t>(
+                                       static_cast<size_t>(c->numSMs) * perSM,
+                                       (nItems + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock)));
+
+    int launches = 0, sweepsLaunched = 0;
+    const bool profile = o.profile_sweeps != 0;
+    if (profile) {
+        while (static_cast<int>(c->sweepEv.size()) < 2 * nSweepLaunches) {
+            cudaEvent_t e;
+            EIKX_CUDA(cudaEventCreate(&e));
+            c->sweepEv.push_back(e);
+        }
+    }
+    auto enqueue = [&]() -> eikx_status {
+        launches = 0;
+        sweepsLaunched = 0;
+        int buf = 0;
+        EIKX_CUDA(eikx::launchResetState(st, nUnits, buf, c->stream));
+        ++launches;
+        for (int i = 0; i < nM; ++i) {
+            const eikx_model3d &m = models[sel[i]];
+            EIKX_CUDA(eikx::launchInit3<T>(ttBase + L[i].ttOff, L[i].nSrc, L[i].fieldStride, L[i].Px, m.nx, m.ny, m.nz,
+                                           m.dx, m.dy, m.dz, w.corners.as<eikx::Corner3>() + L[i].firstUnit,
+                                           o.init_fp64 ? 1 : 0, c->stream));
+            ++launches;
+        }
+        auto sweep = [&](int e, int init, int slot) -> eikx_status {
+            if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched], c->stream));
+            eikx::Sweep3Args<T> a{};
+            a.srcs = w.srcs.as<eikx::SourceT<T>>(); a.st = st; a.buf = buf; a.residualSlot = slot;
+            a.sweepIndex = sweepsLaunched;
+            a.sweep = e; a.init = init; a.radius = o.factored_radius;
+            a.units = w.units.as<eikx::Grid3Unit<T>>();
+            EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, blocks, c->stream));
+            if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched + 1], c->stream));
+            buf ^= 1;
+            ++launches;
+            ++sweepsLaunched;
+            return EIKX_OK;
+        };
+        if (o.init_sweeps)
+            for (int e = 0; e < nSweepKinds; ++e)
+                if (eikx_status r = sweep(e, 1, e); r != EIKX_OK) return r;
+        for (int k = 0; k < nSweeps; ++k) {
+            for (int e = 0; e < nSweepKinds; ++e)
+                if (eikx_status r = sweep(e, 0, nSweepKinds * (1 + k) + e); r != EIKX_OK) return r;
+            EIKX_CUDA(eikx::launchCheckConvergence(st, nUnits, nSweepKinds * (1 + k), nSweepKinds, k, o.tolerance,
+                                                   c->stream));
+            ++launches;
+        }
+        return EIKX_OK;
+    };
+
+    // graph key: everything the captured launches depend on
+    std::vector<double> key = {static_cast<double>(sizeof(T)), uniform ? 1.0 : 0.0, static_cast<double>(nM),
+                               static_cast<double>(o.n_sweeps), static_cast<double>(o.factored_radius),
+                               static_cast<double>(o.init_sweeps), static_cast<double>(o.init_fp64), o.tolerance,
+                               static_cast<double>(st.spinLimit), static_cast<double>(blocks)};
+    for (int i = 0; i < nM; ++i) {
+        const eikx_model3d &m = models[sel[i]];
+        for (double v : {static_cast<double>(m.nx), static_cast<double>(m.ny), static_cast<double>(m.nz), m.dx, m.dy,
+                         m.dz, static_cast<double>(m.n_src)})
+            key.push_back(v);
+    }
+    for (const void *p : after) key.push_back(static_cast<double>(reinterpret_cast<uintptr_t>(p)));
+
+    EIKX_CUDA(cudaEventRecord(c->ev0, c->stream));
+    if (c->useGraphs && !profile) {
+        if (!(w.exec && w.key == key)) {
+            w.dropGraph();
+            cudaGraph_t graph = nullptr;
+            EIKX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            eikx_status r = enqueue();
+            cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+            if (r != EIKX_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return r;
+            }
+            EIKX_CUDA(ce);
+            cudaError_t ie = cudaGraphInstantiate(&w.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            EIKX_CUDA(ie);
+            w.key = key;
+            w.launches = launches;
+        }
+        EIKX_CUDA(cudaGraphLaunch(w.exec, c->stream));
+        launches = w.launches;
+        sweepsLaunched = nSweepLaunches;
+    } else {
+        if (eikx_status r = enqueue(); r != EIKX_OK) return r;
+    }
+    for (int i = 0; i < nM; ++i) {
+        const eikx_model3d &m = models[sel[i]];
+        const cudaMemcpyKind kind = m.t_where == EIKX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        EIKX_CUDA(cudaMemcpy2DAsync(m.t_out, static_cast<size_t>(m.nx) * sizeof(T), ttBase + L[i].ttOff,
+                                    static_cast<size_t>(L[i].Px) * sizeof(T), static_cast<size_t>(m.nx) * sizeof(T),
+                                    static_cast<size_t>(m.ny) * m.nz * m.n_src, kind, c->stream));
+    }
+    EIKX_CUDA(cudaEventRecord(c->ev1, c->stream));
+    std::vector<int> iters(nUnits);
+    int aborted = 0;
+    EIKX_CUDA(cudaMemcpyAsync(iters.data(), w.iterations.p, nUnits * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(&aborted, w.abortFlag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<unsigned long long> res;
+    if (nSweeps > 0) {
+        res.resize(static_cast<size_t>(nUnits) * resStride);
+        EIKX_CUDA(cudaMemcpyAsync(res.data(), w.residual.p, res.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    for (int u = 0; u < nUnits; ++u) {
+        agg.iterations_max = std::max(agg.iterations_max, iters[u]);
+        agg.iterations_min = std::min(agg.iterations_min, iters[u]);
+        if (iters[u] > 0)
+            for (int e = 0; e < nSweepKinds; ++e) {
+                double r;
+                std::memcpy(&r, &res[static_cast<size_t>(u) * resStride + nSweepKinds * iters[u] + e], sizeof(r));
+                agg.residual_last = std::max(agg.residual_last, r);
+            }
+    }
+    agg.n_fields += nUnits;
+    agg.sweeps_launched += sweepsLaunched;
+    agg.kernel_launches += launches;
+    agg.device_ms += ms;
+    if (profile) {
+        double tot = 0;
+        for (int i = 0; i < sweepsLaunched; ++i) {
+            float m = 0;
+            cudaEventElapsedTime(&m, c->sweepEv[2 * i], c->sweepEv[2 * i + 1]);
+            tot += m;
+        }
+        agg.sweep_ms = (agg.sweep_ms < 0 ? 0 : agg.sweep_ms) + tot;
+    }
+    if (aborted) return fail(EIKX_ERR_TIMEOUT, "a bounded inter-tile wait ran out; the fields are not valid");
+    return EIKX_OK;
+}
+
 eikx_status fillOptions(const eikx_options *in, eikx_options *out) {
     if (in) *out = *in; else eikx_options_default(out);
     if (out->n_sweeps < 0) return fail(EIKX_ERR_INVALID, "n_sweeps must be non-negative");
@@ -762,6 +1172,37 @@ eikx_status eikx_solve3d(eikx_ctx *c, const eikx_source3d *src, int nSrc, const 
     if (precision == EIKX_F32) return solveImpl<float, 3>(c, xyz.data(), nSrc, o, tOut, where);
     if (precision == EIKX_F64) return solveImpl<double, 3>(c, xyz.data(), nSrc, o, tOut, where);
     return fail(EIKX_ERR_INVALID, "precision must be EIKX_F32 or EIKX_F64");
+}
+
+eikx_status eikx_solve3d_batch(eikx_ctx *c, const eikx_model3d *models, int nModels, const eikx_options *opt,
+                               int precision) {
+    if (eikx_status r = checkCtx(c); r) return r;
+    if (!models || nModels <= 0) return fail(EIKX_ERR_INVALID, "batch has no models");
+    if (precision != EIKX_F32 && precision != EIKX_F64)
+        return fail(EIKX_ERR_INVALID, "precision must be EIKX_F32 or EIKX_F64");
+    eikx_options o;
+    if (eikx_status r = fillOptions(opt, &o); r) return r;
+    for (int i = 0; i < nModels; ++i)
+        if (std::string e = checkModel(models[i], i); !e.empty()) return fail(EIKX_ERR_INVALID, e);
+    EIKX_CUDA(cudaSetDevice(c->device));
+    // uniform-grid and non-uniform-grid models run different local solvers: one schedule each
+    const double eps = (precision == EIKX_F32 ? std::numeric_limits<float>::epsilon()
+                                              : std::numeric_limits<double>::epsilon()) * 100;
+    std::vector<int> uni, non;
+    for (int i = 0; i < nModels; ++i)
+        (uniformSpacing3(models[i].dx, models[i].dy, models[i].dz, eps) ? uni : non).push_back(i);
+    eikx_stats agg{};
+    agg.iterations_min = 1 << 30;
+    agg.sweep_ms = -1;
+    for (int pass = 0; pass < 2; ++pass) {
+        const std::vector<int> &sel = pass == 0 ? uni : non;
+        if (sel.empty()) continue;
+        eikx_status r = precision == EIKX_F32 ? solveBatch3<float>(c, models, sel, pass == 0, o, agg)
+                                              : solveBatch3<double>(c, models, sel, pass == 0, o, agg);
+        if (r != EIKX_OK) return r;
+    }
+    c->stats = agg;
+    return EIKX_OK;
 }
 
 eikx_status eikx_solve2d(eikx_ctx *c, const eikx_source2d *src, int nSrc, const eikx_options *opt, int precision,

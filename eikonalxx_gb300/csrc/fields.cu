@@ -20,6 +20,18 @@ inline int gridFor(long long n, int threads = kThreads) {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return max(lo, min(hi, v)); }
 
+// Raises *flag when a slowness is not a positive finite number (Model3D rejects
+// non-positive velocities, src/model3d.cpp:301-305).
+__global__ void positiveKernel(const double *s, long long n, int *flag) {
+    bool bad = false;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const double v = s[i];
+        bad = bad || !(v > 0) || !isfinite(v);
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
 // Travel-time initialisation (Solver3D::initializeTravelTimes, src/solver3d.cpp:21-84):
 // every node := HUGE, the 8 corners of the source cell := s_src * |x - x_s|, the
 // distance and product evaluated in FP64 (fp64 = 1) or in the field type.
@@ -331,6 +343,11 @@ cudaError_t launchResetState(const SolveState &st, int nFields, int buf, cudaStr
     resetKernel<<<gridFor(static_cast<long long>(nFields) * st.residualStride), kThreads, 0, s>>>(st, nFields, buf);
     return cudaGetLastError();
 }
+cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st) {
+    positiveKernel<<<gridFor(n), kThreads, 0, st>>>(s, n, flag);
+    return cudaGetLastError();
+}
+
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots, int iteration,
                                    double tol, cudaStream_t s) {
     checkKernel<<<gridFor(nFields, 128), 128, 0, s>>>(st, nFields, firstSlot, nSlots, iteration, tol);

@@ -29,6 +29,18 @@ struct SolveState {
     unsigned long long spinLimit;   // polls before a wait gives up
 };
 
+// Geometry of one work unit (one field on one model) of a multi-model batch: the grids of
+// a batch may differ in size and spacing; a warp reads its unit's entry per work item.
+template <class T> struct Grid3Unit {
+    T *tt;                        // this field's travel times, row pitch Px
+    const T *spPos, *spNeg;       // the model's padded slowness copies
+    unsigned long long *mbox;     // this field's mailbox (tilesY * tilesZ warp blocks)
+    long long spPlane;            // spPitch * (ny + 1)
+    int spPitch, Px, nx, ny, nz, tilesY, tilesZ, pad;
+    T h;                          // uniform spacing
+    Spacing3<T> sp3;              // non-uniform constants
+};
+
 template <class T> struct Sweep3Args {
     T *tt;                    // travel-time fields, row pitch `pitch`, rows (y,z) natural
     long long fieldStride;    // elements per field
@@ -50,6 +62,7 @@ template <class T> struct Sweep3Args {
     T h;                      // uniform spacing
     Spacing3<T> sp3;          // non-uniform constants
     const int2 *pairs;        // field pairs of the paired kernel (work items index pairs)
+    const Grid3Unit<T> *units;  // multi-model batch: per-unit geometry (chunk-step kernel only)
 };
 
 template <class T> struct Sweep2Args {
@@ -80,9 +93,11 @@ template <class T>
 cudaError_t launchSweep2(const Sweep2Args<T> &a, bool uniform, int blocks, cudaStream_t s);
 // Chunk-step 3D kernel (sweep_chunk.cu): a lane updates one 16-byte chunk of its pencil
 // per wavefront step.
+// With a.units set, a work item's field index is a unit of a multi-model batch and the
+// grid, slowness, mailbox and spacing come from a.units[unit].
 template <class T>
 cudaError_t launchSweep3Chunk(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s);
-template <class T> int sweep3ChunkBlocksPerSM(bool uniform);
+template <class T> int sweep3ChunkBlocksPerSM(bool uniform, bool batch = false);
 size_t sweep3ChunkSmemBytes();
 // 3D sweep kernel variants (eikx_options.sweep_kernel).
 enum Sweep3Variant { kNodeStep = 1, kChunkStep = 2 };
@@ -125,6 +140,8 @@ cudaError_t launchCellsToNatural3(double *slow, const U *c, int nx, int ny, int 
 template <class U>
 cudaError_t launchCellsToNatural2(double *slow, const U *c, int nx, int nz, int ordering, cudaStream_t s);
 cudaError_t launchResetState(const SolveState &st, int nFields, int buf, cudaStream_t s);
+// Sets *flag (ORs 1) if any of the n slownesses is not positive and finite.
+cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st);
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,
                                    int iteration, double tol, cudaStream_t s);
 cudaError_t launchAnalytic3(double *t, int nx, int ny, int nz, double dx, double dy, double dz,

@@ -128,7 +128,8 @@ __device__ __forceinline__ void putChunk(unsigned long long *p, unsigned tag, co
     stRelaxed2(p + 2, w[2], w[3]);
 }
 
-// Factored (near-source) updates, out of line: taken by a few hundred nodes per field.
+// Factored (near-source) updates, out of line: taken by a few hundred nodes per field,
+// so the V inlined copies of the update hold only the Cartesian operators.
 template <class T>
 __device__ __noinline__ T nearUniform(T h, const SourceT<T> src, const SweepSigns sg, int ix, int iy, int iz,
                                       const Stencil3<T> n) {
@@ -144,7 +145,7 @@ __device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *st.queue[buf ^ 1] = 0u;
 }
 
-template <class T, bool UNIFORM, bool REV>
+template <class T, bool UNIFORM, bool REV, bool BATCH>
 __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T> a) {
     constexpr int V = Vec<T>::N;
     constexpr int W = sizeof(T) / 4;                // mailbox words per value
@@ -162,12 +163,7 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
     SweepSigns sg;
     sg.ixShift = REV ? 1 : -1; sg.iyShift = fy ? 1 : -1; sg.izShift = fz ? 1 : -1;
     sg.signX = REV ? -1 : 1; sg.signY = fy ? -1 : 1; sg.signZ = fz ? -1 : 1;
-    const int Px = a.pitch;
-    const int nChunks = Px / V;
-    const int nSteps = nChunks + LY3 + LZ3 - 2;
-    const T *sp = REV ? a.spNeg : a.spPos;
     const T huge = static_cast<T>(1.e10);
-    const long long faceWords = static_cast<long long>(LY3 + LZ3) * Px * W;
 
     // helper lanes stand in for the virtual upwind lanes of the halo row/column
     const bool helper = lane < HZ + LY3;
@@ -175,11 +171,6 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
     const int vlz = lane < HZ ? lane - 1 : -1;
     const int vslot = (vlz + 1) * HY + (vly + 1);
     const int myslot = (lz + 1) * HY + (ly + 1);
-
-    // chunk k of a row in walk order: forward rows start at the row, reversed rows end there
-    auto tChunk = [&](T *row, int k) { return REV ? row + Px - (k + 1) * V : row + k * V; };
-    auto sChunk = [&](const T *srow, int k) { return REV ? srow + Px - (k + 1) * V : srow + (k + 1) * V; };
-    auto walk = [&](const Vec<T> &m) { return REV ? reversed(m) : m; };   // memory <-> walk order
 
     while (true) {
         unsigned q = 0;
@@ -190,21 +181,42 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
         const int f = item.x, b = item.y, c = item.z;
         if (st.converged[f]) continue;
         const SourceT<T> src = a.srcs[f];
+
+        // grid of this work item: the launch's (one model) or the unit's (batch)
+        const Grid3Unit<T> *unit = BATCH ? a.units + f : nullptr;
+        const int Px = BATCH ? unit->Px : a.pitch;
+        const int nx = BATCH ? unit->nx : a.nx, ny = BATCH ? unit->ny : a.ny, nz = BATCH ? unit->nz : a.nz;
+        const int tilesY = BATCH ? unit->tilesY : a.tilesY;
+        const int spPitch = BATCH ? unit->spPitch : a.spPitch;
+        const long long spPlane = BATCH ? unit->spPlane : a.spPlane;
+        const T *sp = BATCH ? (REV ? unit->spNeg : unit->spPos) : (REV ? a.spNeg : a.spPos);
+        T *field = BATCH ? unit->tt : a.tt + static_cast<long long>(f) * a.fieldStride;
+        const long long faceWords = static_cast<long long>(LY3 + LZ3) * Px * W;
+        unsigned long long *fieldBox =
+            BATCH ? unit->mbox : st.mbox + static_cast<long long>(f) * a.tilesZ * a.tilesY * faceWords;
+        const T h = BATCH ? unit->h : a.h;
+        const int nChunks = Px / V;
+        const int nSteps = nChunks + LY3 + LZ3 - 2;
+
         const int y0 = b * LY3, z0 = c * LZ3;
         const int yp = y0 + ly, zp = z0 + lz;
-        const bool laneValid = yp < a.ny && zp < a.nz;
-        const int ya = laneValid ? reflect(yp, a.ny, fy) : 0;
-        const int za = laneValid ? reflect(zp, a.nz, fz) : 0;
+        const bool laneValid = yp < ny && zp < nz;
+        const int ya = laneValid ? reflect(yp, ny, fy) : 0;
+        const int za = laneValid ? reflect(zp, nz, fz) : 0;
         int xlo, xhi, ylo, yhi, zlo, zhi;
-        axisBounds(a.nx, REV, a.init, src.isx, xlo, xhi);
-        axisBounds(a.ny, fy, a.init, src.isy, ylo, yhi);
-        axisBounds(a.nz, fz, a.init, src.isz, zlo, zhi);
+        axisBounds(nx, REV, a.init, src.isx, xlo, xhi);
+        axisBounds(ny, fy, a.init, src.isy, ylo, yhi);
+        axisBounds(nz, fz, a.init, src.isz, zlo, zhi);
         const bool yzUpd = laneValid && ya >= ylo && ya <= yhi && za >= zlo && za <= zhi;
         // the factored branch applies within `radius` cells of the source cell on every axis
         const bool yzNear = abs(src.isy - ya) <= a.radius && abs(src.isz - za) <= a.radius;
-        T *row = a.tt + static_cast<long long>(f) * a.fieldStride + (static_cast<long long>(za) * a.ny + ya) * Px;
-        const T *srow = sp + static_cast<long long>(za + (fz ? 0 : 1)) * a.spPlane +
-                        static_cast<long long>(ya + (fy ? 0 : 1)) * a.spPitch;
+        T *row = field + (static_cast<long long>(za) * ny + ya) * Px;
+        const T *srow = sp + static_cast<long long>(za + (fz ? 0 : 1)) * spPlane +
+                        static_cast<long long>(ya + (fy ? 0 : 1)) * spPitch;
+        // chunk k of a row in walk order: forward rows start at the row, reversed rows end there
+        auto tChunk = [&](T *r, int k) { return REV ? r + Px - (k + 1) * V : r + k * V; };
+        auto sChunk = [&](const T *r, int k) { return REV ? r + Px - (k + 1) * V : r + (k + 1) * V; };
+        auto walk = [&](const Vec<T> &m) { return REV ? reversed(m) : m; };   // memory <-> walk order
         Vec<T> tNext = splat(huge), sNext = splat(huge);
         if (laneValid) {
             tNext = ldVec(tChunk(row, 0));
@@ -212,24 +224,25 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
         }
 
         // mailbox: this block's faces, and the upstream face row a helper lane reads
-        const long long tileId = (static_cast<long long>(f) * a.tilesZ + c) * a.tilesY + b;
-        unsigned long long *box = st.mbox + tileId * faceWords;
+        unsigned long long *box = fieldBox + (static_cast<long long>(c) * tilesY + b) * faceWords;
         unsigned long long *yFace = box + static_cast<long long>(lz) * Px * W;          // ly == LY-1
         unsigned long long *zFace = box + static_cast<long long>(LZ3 + ly) * Px * W;    // lz == LZ-1
         const int vyp = y0 + vly, vzp = z0 + vlz;
-        const bool vValid = helper && vyp >= 0 && vzp >= 0 && vyp < a.ny && vzp < a.nz;
-        const unsigned long long *vbox = st.mbox;
+        const bool vValid = helper && vyp >= 0 && vzp >= 0 && vyp < ny && vzp < nz;
+        const unsigned long long *vbox = box;
         const T *vsrow = sp;
         if (vValid) {
-            const int vya = reflect(vyp, a.ny, fy), vza = reflect(vzp, a.nz, fz);
+            const int vya = reflect(vyp, ny, fy), vza = reflect(vzp, nz, fz);
             if (vly < 0) {
-                const long long up = vlz >= 0 ? tileId - 1 : tileId - a.tilesY - 1;
-                vbox = st.mbox + up * faceWords + static_cast<long long>(vlz >= 0 ? vlz : LZ3 - 1) * Px * W;
+                // block (b-1, c), or the corner block (b-1, c-1): its y' face row
+                vbox = box - (vlz >= 0 ? faceWords : (tilesY + 1) * faceWords) +
+                       static_cast<long long>(vlz >= 0 ? vlz : LZ3 - 1) * Px * W;
             } else {
-                vbox = st.mbox + (tileId - a.tilesY) * faceWords + static_cast<long long>(LZ3 + vly) * Px * W;
+                // block (b, c-1): its z' face row
+                vbox = box - tilesY * faceWords + static_cast<long long>(LZ3 + vly) * Px * W;
             }
-            vsrow = sp + static_cast<long long>(vza + (fz ? 0 : 1)) * a.spPlane +
-                    static_cast<long long>(vya + (fy ? 0 : 1)) * a.spPitch;
+            vsrow = sp + static_cast<long long>(vza + (fz ? 0 : 1)) * spPlane +
+                    static_cast<long long>(vya + (fy ? 0 : 1)) * spPitch;
         }
 
         // Halo pipeline: the chunk a virtual lane produces at step sv goes into ring slot
@@ -326,8 +339,12 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
                     n.s7 = e ? sOwn.v[e - 1] : cS7;
                     const bool near = yzNear && abs(src.isx - xa) <= a.radius;
                     T tu;
-                    if (UNIFORM) tu = near ? nearUniform<T>(a.h, src, sg, xa, ya, za, n) : fd3UniformFar<T>(a.h, n);
-                    else tu = near ? nearNonUniform<T>(a.sp3, src, sg, xa, ya, za, n) : fd3NonUniformFar<T>(a.sp3, n);
+                    if (UNIFORM) {
+                        tu = near ? nearUniform<T>(h, src, sg, xa, ya, za, n) : fd3UniformFar<T>(h, n);
+                    } else {
+                        const Spacing3<T> &g = BATCH ? unit->sp3 : a.sp3;
+                        tu = near ? nearNonUniform<T>(g, src, sg, xa, ya, za, n) : fd3NonUniformFar<T>(g, n);
+                    }
                     const T t0 = out.v[e];
                     if (tu < t0) {
                         out.v[e] = tu;
@@ -353,8 +370,19 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
     }
 }
 
-template <class T, bool U, bool R> void *chunkKernel() {
-    return reinterpret_cast<void *>(sweep3ChunkKernel<T, U, R>);
+template <class T, bool U, bool R, bool B> void *chunkKernel() {
+    return reinterpret_cast<void *>(sweep3ChunkKernel<T, U, R, B>);
+}
+
+template <class T, bool B>
+void launchChunk(const Sweep3Args<T> &a, bool uniform, bool rev, int blocks, size_t smem, cudaStream_t s) {
+    if (uniform) {
+        if (rev) sweep3ChunkKernel<T, true, true, B><<<blocks, kThreads, smem, s>>>(a);
+        else sweep3ChunkKernel<T, true, false, B><<<blocks, kThreads, smem, s>>>(a);
+    } else {
+        if (rev) sweep3ChunkKernel<T, false, true, B><<<blocks, kThreads, smem, s>>>(a);
+        else sweep3ChunkKernel<T, false, false, B><<<blocks, kThreads, smem, s>>>(a);
+    }
 }
 
 }  // namespace
@@ -365,21 +393,22 @@ template <class T>
 cudaError_t launchSweep3Chunk(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s) {
     const size_t smem = sweep3ChunkSmemBytes();
     const bool rev = (a.sweep & 1) != 0;
-    if (uniform) {
-        if (rev) sweep3ChunkKernel<T, true, true><<<blocks, kThreads, smem, s>>>(a);
-        else sweep3ChunkKernel<T, true, false><<<blocks, kThreads, smem, s>>>(a);
-    } else {
-        if (rev) sweep3ChunkKernel<T, false, true><<<blocks, kThreads, smem, s>>>(a);
-        else sweep3ChunkKernel<T, false, false><<<blocks, kThreads, smem, s>>>(a);
-    }
+    if (a.units) launchChunk<T, true>(a, uniform, rev, blocks, smem, s);
+    else launchChunk<T, false>(a, uniform, rev, blocks, smem, s);
     return cudaGetLastError();
 }
 
-template <class T> int sweep3ChunkBlocksPerSM(bool uniform) {
-    // the four instantiations of a precision share their resource use; take the least
+template <class T> int sweep3ChunkBlocksPerSM(bool uniform, bool batch) {
+    // the instantiations of one kind differ only in the sweep direction; take the least
+    void *k[2];
+    if (batch) {
+        k[0] = uniform ? chunkKernel<T, true, false, true>() : chunkKernel<T, false, false, true>();
+        k[1] = uniform ? chunkKernel<T, true, true, true>() : chunkKernel<T, false, true, true>();
+    } else {
+        k[0] = uniform ? chunkKernel<T, true, false, false>() : chunkKernel<T, false, false, false>();
+        k[1] = uniform ? chunkKernel<T, true, true, false>() : chunkKernel<T, false, true, false>();
+    }
     int best = 1 << 30;
-    void *k[2] = {uniform ? chunkKernel<T, true, false>() : chunkKernel<T, false, false>(),
-                  uniform ? chunkKernel<T, true, true>() : chunkKernel<T, false, true>()};
     for (void *f : k) {
         int n = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kThreads, sweep3ChunkSmemBytes());
@@ -390,7 +419,7 @@ template <class T> int sweep3ChunkBlocksPerSM(bool uniform) {
 
 template cudaError_t launchSweep3Chunk<float>(const Sweep3Args<float> &, bool, int, cudaStream_t);
 template cudaError_t launchSweep3Chunk<double>(const Sweep3Args<double> &, bool, int, cudaStream_t);
-template int sweep3ChunkBlocksPerSM<float>(bool);
-template int sweep3ChunkBlocksPerSM<double>(bool);
+template int sweep3ChunkBlocksPerSM<float>(bool, bool);
+template int sweep3ChunkBlocksPerSM<double>(bool, bool);
 
 }  // namespace eikx

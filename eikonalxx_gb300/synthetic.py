@@ -44,3 +44,19 @@ def uniform_sources(n, nx, ny, nz, h, seed, surface=False):
     xyz = np.column_stack([rng.uniform(0, (nx - 1) * h, n), rng.uniform(0, (ny - 1) * h, n),
                            np.zeros(n) if surface else rng.uniform(0, (nz - 1) * h, n)])
     return xyz
+
+
+def uneven_models(n, seed, h=100.0, nxy=(64, 256), nz=(32, 128), dtype=np.float32):
+    """n independent models of uneven size: nx, ny uniform in `nxy`, nz uniform in `nz`,
+    spacing h, each a layered + GRF model with one source uniform in its domain.
+    Returns a list of dicts with ``grid`` (nx, ny, nz, h, h, h), ``v`` (nodal, (nz, ny, nx))
+    and ``source`` (x, y, z)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        gx, gy = (int(v) for v in rng.integers(nxy[0], nxy[1] + 1, 2))
+        gz = int(rng.integers(nz[0], nz[1] + 1))
+        v = layered_grf_model(gx, gy, gz, h, int(rng.integers(1 << 31)), dtype=dtype)
+        src = uniform_sources(1, gx, gy, gz, h, int(rng.integers(1 << 31)))[0]
+        out.append({"grid": (gx, gy, gz, h, h, h), "v": v, "source": tuple(float(c) for c in src)})
+    return out

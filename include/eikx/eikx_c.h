@@ -135,6 +135,36 @@ eikx_status eikx_solve3d(eikx_ctx *ctx, const eikx_source3d *src, int n_src,
                          const eikx_options *opt, int precision, void *t_out, int where);
 
 /* ---- 2D ---------------------------------------------------------------- */
+/* ---- multi-model batch ------------------------------------------------- */
+
+/* One model of a multi-model batch and the sources to solve on it. */
+typedef struct {
+    int nx, ny, nz;               /* grid points (>= 3 each) */
+    double dx, dy, dz;            /* spacing (m, > 0) */
+    double x0, y0, z0;            /* origin (m) */
+    const void *model;            /* cell slowness ((nx-1)(ny-1)(nz-1) values, s/m) or nodal
+                                     velocity (nx*ny*nz values, m/s), as model_kind says */
+    int model_kind;               /* EIKX_CELL_SLOWNESS or EIKX_NODAL_VELOCITY */
+    int dtype;                    /* EIKX_F32 / EIKX_F64 of `model` */
+    int ordering;                 /* EIKX_ORDER_NATURAL / EIKX_ORDER_TRANSPOSED of `model` */
+    int where;                    /* EIKX_HOST / EIKX_DEVICE of `model` */
+    int n_src;                    /* sources on this model (>= 1) */
+    const eikx_source3d *src;     /* host array of n_src source positions (m) */
+    void *t_out;                  /* n_src * nx*ny*nz values of the solve precision, natural order */
+    int t_where;                  /* EIKX_HOST / EIKX_DEVICE of t_out */
+} eikx_model3d;
+enum { EIKX_CELL_SLOWNESS = 0, EIKX_NODAL_VELOCITY = 1 };
+
+/* No single counterpart in the reference: a loop of Solver3D::setVelocityModel +
+ * setSource + solve (src/solver3d.cpp:197-249, :351-525) over many models, run as one
+ * schedule.  Every (model, source) field of the batch is a work unit of the same
+ * persistent sweep launches, whatever the grid sizes; models with uniform spacing and
+ * models with non-uniform spacing run as two schedules.  Fields are identical to
+ * eikx_solve3d on each model alone.  Uses the chunk-step sweep kernel; the context's own
+ * model (eikx_set_slowness3d) is not touched.  eikx_get_stats reports the batch. */
+eikx_status eikx_solve3d_batch(eikx_ctx *ctx, const eikx_model3d *models, int n_models,
+                               const eikx_options *opt, int precision);
+
 /* Replaces Solver2D::initialize (src/solver2d.cpp:291-343). */
 eikx_status eikx_set_grid2d(eikx_ctx *ctx, int nx, int nz, double dx, double dz, double x0,
                             double z0);
