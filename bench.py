@@ -145,6 +145,11 @@ def run_gpu(args):
     out_host = torch.empty((fields, NZ, NY, NX), dtype=torch.float32).pin_memory()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
 
+    # autotuning (outside the timed region): kernel variant, warp-block shape, grid size
+    tuning = None
+    if not args.no_autotune and KERNEL[0] == 0 and not PAIR[0]:
+        tuning = ctx.autotune3d(src, ex.F32)
+
     def step_device():
         ctx.solve3d(src, opt, ex.F32, out=out_dev)
         return ctx.stats()
@@ -190,10 +195,16 @@ def run_gpu(args):
     achieved = bytes_per_launch / (sweep_launch_ms / 1e3) / 1e9
     peak, peak_kind = _peaks()
     tr = _traffic()
-    kernel_name = ("sweep3PairKernel" if PAIR[0] and fields >= 2 else
-                   "sweep3Kernel<float,uniform>" if KERNEL[0] == 1 else "sweep3ChunkKernel<float,uniform>")
+    shapes = {1: "8x4", 2: "4x8", 3: "16x2"}
+    if tuning:
+        kernel_name = ("sweep3PairKernel" if tuning["pair_fields"] else "sweep3Kernel<float,uniform>"
+                       if tuning["sweep_kernel"] == 1 else
+                       f"sweep3ChunkKernel<float,uniform,{shapes[tuning['block_shape']]}>")
+    else:
+        kernel_name = ("sweep3PairKernel" if PAIR[0] and fields >= 2 else
+                       "sweep3Kernel<float,uniform>" if KERNEL[0] == 1 else "sweep3ChunkKernel<float,uniform,8x4>")
     traffic, traffic_src = None, None
-    if tr and tr.get("kernel") == kernel_name:
+    if tr and tr.get("kernel") == kernel_name.replace(",8x4", ""):
         # DRAM bytes of one full sweep from the committed ncu capture, scaled by the
         # fields per launch (traffic grows in proportion to the fields swept)
         traffic = tr["dram_bytes_per_launch"] * fields / tr["fields"]
@@ -231,7 +242,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(4 * n_nodes * fields), "ms_per_step": float(np.mean(e2e_ms))},
         "gpu_launches": int(launches), "clocks": clk.summary(),
         "iterations": {"max": int(max(iters)), "min": int(min(iters))},
-        "wall_ms_per_step": float(np.mean(wall)), "accuracy": acc,
+        "wall_ms_per_step": float(np.mean(wall)), "accuracy": acc, "tuning": tuning,
         "cpu_baseline": (cpu_baseline(args.cpu_seconds, 1, _sweeps_per_grid(max(iters)))
                          if not args.skip_cpu else None),
     }
@@ -471,6 +482,8 @@ def main():
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--sweep-kernel", type=int, default=0, choices=[0, 1, 2],
                     help="3D sweep kernel: 0 default (chunk-step), 1 node-step, 2 chunk-step")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip eikx_autotune3d before timing (default chunk-step 8x4 configuration)")
     ap.add_argument("--pair-fields", action="store_true",
                     help="sweep two fields per lane (the paired FP32 kernel) instead of one")
     ap.add_argument("--profile-case", action="store_true",

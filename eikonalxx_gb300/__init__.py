@@ -34,7 +34,7 @@ EXPORTED = [
     "eikx_set_grid3d", "eikx_set_slowness3d", "eikx_set_nodal_velocity3d", "eikx_get_slowness3d",
     "eikx_solve3d", "eikx_set_grid2d", "eikx_set_slowness2d", "eikx_set_nodal_velocity2d",
     "eikx_solve2d", "eikx_graph3d_tables", "eikx_levels2d", "eikx_analytic3d", "eikx_analytic2d",
-    "eikx_solve3d_noalloc", "eikx_solve3d_batch",
+    "eikx_solve3d_noalloc", "eikx_solve3d_batch", "eikx_autotune3d", "eikx_tuning_save", "eikx_tuning_load",
 ]
 CELL_SLOWNESS, NODAL_VELOCITY = 0, 1
 
@@ -65,6 +65,7 @@ class _Options(ctypes.Structure):
                 ("init_fp64", ctypes.c_int), ("spin_limit_log2", ctypes.c_int),
                 ("test_drop_blocks", ctypes.c_int), ("profile_sweeps", ctypes.c_int),
                 ("pair_fields", ctypes.c_int), ("sweep_kernel", ctypes.c_int),
+                ("block_shape", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("reserved", ctypes.c_int * 2)]
 
 
@@ -81,6 +82,12 @@ class _Src3(ctypes.Structure):
 
 class _Src2(ctypes.Structure):
     _fields_ = [("x", ctypes.c_double), ("z", ctypes.c_double)]
+
+
+class _Tuning(ctypes.Structure):
+    _fields_ = [("sweep_kernel", ctypes.c_int), ("pair_fields", ctypes.c_int), ("block_shape", ctypes.c_int),
+                ("blocks_per_sm", ctypes.c_int), ("ms_per_sweep", ctypes.c_double),
+                ("default_ms_per_sweep", ctypes.c_double), ("candidates", ctypes.c_int)]
 
 
 class _Model3(ctypes.Structure):
@@ -127,6 +134,9 @@ def load(path=None):
     lib.eikx_analytic3d.argtypes = [vp, ctypes.POINTER(_Src3), c_double, c_double, vp, c_int]
     lib.eikx_analytic2d.argtypes = [vp, ctypes.POINTER(_Src2), c_double, c_double, vp, c_int]
     lib.eikx_solve3d_batch.argtypes = [vp, ctypes.POINTER(_Model3), c_int, ctypes.POINTER(_Options), c_int]
+    lib.eikx_autotune3d.argtypes = [vp, ctypes.POINTER(_Src3), c_int, c_int, ctypes.POINTER(_Tuning)]
+    lib.eikx_tuning_save.argtypes = [vp, ctypes.c_char_p]
+    lib.eikx_tuning_load.argtypes = [vp, ctypes.c_char_p]
     for name in EXPORTED:
         if name not in ("eikx_options_default", "eikx_last_error", "eikx_levels2d", "eikx_graph3d_tables"):
             getattr(lib, name).restype = c_int
@@ -161,7 +171,9 @@ class Options:
     test_drop_blocks: int = 0   # test hook only (see eikx_options.test_drop_blocks)
     profile_sweeps: bool = False  # time each sweep kernel with CUDA events (no graph)
     pair_fields: bool = False     # two fields per GPU lane for FP32 uniform batches
-    sweep_kernel: int = 0         # 3D: 0 = default (chunk-step), 1 = node-step, 2 = chunk-step
+    sweep_kernel: int = 0         # 3D: 0 = tuned or chunk-step, 1 = node-step, 2 = chunk-step
+    block_shape: int = 0          # 3D chunk-step warp block: 0 = tuned or 8x4, 1 = 8x4, 2 = 4x8, 3 = 16x2
+    blocks_per_sm: int = 0        # persistent grid: 0 = as many as fit (or tuned)
 
     def _c(self):
         o = _Options()
@@ -175,6 +187,8 @@ class Options:
         o.profile_sweeps = int(bool(self.profile_sweeps))
         o.pair_fields = int(bool(self.pair_fields))
         o.sweep_kernel = int(self.sweep_kernel)
+        o.block_shape = int(self.block_shape)
+        o.blocks_per_sm = int(self.blocks_per_sm)
         return o
 
 
@@ -260,6 +274,22 @@ class Context:
         o = (options or Options())._c()
         _check(self._lib.eikx_solve3d(self._h, arr, n, ctypes.byref(o), precision, p, where))
         return out
+
+    def autotune3d(self, sources, precision=F32):
+        """Time the kernel variants, warp-block shapes and grid sizes on this model and these
+        sources; later solves of the same grid class with default options use the fastest.
+        Returns the choice as a dict."""
+        src = np.atleast_2d(np.asarray(sources, dtype=np.float64))
+        arr = (_Src3 * len(src))(*[_Src3(*map(float, q)) for q in src])
+        t = _Tuning()
+        _check(self._lib.eikx_autotune3d(self._h, arr, len(src), precision, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in _Tuning._fields_}
+
+    def save_tuning(self, path):
+        _check(self._lib.eikx_tuning_save(self._h, os.fsencode(path)))
+
+    def load_tuning(self, path):
+        _check(self._lib.eikx_tuning_load(self._h, os.fsencode(path)))
 
     def solve3d_batch(self, models, options=None, precision=F32):
         """Solve many models, each with its own sources, in one schedule.

@@ -12,9 +12,13 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <sstream>
 #include <limits>
+#include <map>
 #include <memory>
 #include <string>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -111,12 +115,26 @@ struct BatchWorkspace {
 
 struct ScheduleKey {
     int dim = 0, precision = -1, nFields = 0, nx = 0, ny = 0, nz = 0, nSweeps = -1, radius = 0,
-        initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0, variant = 0;
+        initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0, variant = 0, shape = 0;
     double tol = 0, h = 0, dx = 0, dy = 0, dz = 0;
     unsigned long long spin = 0;
     const void *tt = nullptr, *sp = nullptr, *srcs = nullptr, *corners = nullptr;
     bool operator==(const ScheduleKey &o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
 };
+
+// Grid class of the tuning table: precision, uniform spacing, extents rounded up to
+// multiples of 32, source count rounded up to a power of two.
+struct TuneKey {
+    int precision, uniform, nx, ny, nz, nsrc;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(precision, uniform, nx, ny, nz, nsrc) < std::tie(o.precision, o.uniform, o.nx, o.ny, o.nz, o.nsrc);
+    }
+};
+TuneKey tuneKey(int precision, bool uniform, int nx, int ny, int nz, int nSrc) {
+    int p2 = 1;
+    while (p2 < nSrc) p2 <<= 1;
+    return TuneKey{precision, uniform ? 1 : 0, (nx + 31) / 32 * 32, (ny + 31) / 32 * 32, (nz + 31) / 32 * 32, p2};
+}
 
 }  // namespace
 
@@ -145,6 +163,8 @@ struct eikx_ctx {
     DevBuf scratch;                // staging for host inputs and analytic fields
     Workspace ws;
     BatchWorkspace bw;
+    std::map<TuneKey, eikx_tuning> tuning;   // eikx_autotune3d results per grid class
+    DevBuf tuneOut;                          // fields written while tuning
     eikx_stats stats{};
     // cached schedule graph
     ScheduleKey graphKey;
@@ -239,7 +259,7 @@ template <> int precOf<double>() { return EIKX_F64; }
 
 // Shared solve driver for 2D and 3D.
 template <class T, int DIM>
-eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_options &o, void *tOut,
+eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options o, void *tOut,
                       int where) {
     const int P = precOf<T>();
     const int nx = DIM == 3 ? c->nx : c->nx2;
@@ -301,12 +321,27 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     // geometry in the sweep type (include/private/solver3d.hpp:31-44, solver2d.hpp:29-46)
     const double eps = std::numeric_limits<T>::epsilon() * 100;
     const bool uniform = DIM == 3 ? (std::abs(dx - dy) < eps && std::abs(dx - dz) < eps) : (std::abs(dx - dz) < eps);
+    // options left at "auto" take the tuned configuration of this grid class
+    if (DIM == 3 && o.sweep_kernel == 0 && o.block_shape == 0 && o.blocks_per_sm == 0 && !o.pair_fields) {
+        auto it = c->tuning.find(tuneKey(P, uniform, nx, ny, nz, nSrc));
+        if (it != c->tuning.end()) {
+            o.sweep_kernel = it->second.sweep_kernel;
+            o.pair_fields = it->second.pair_fields;
+            o.block_shape = it->second.block_shape;
+            o.blocks_per_sm = it->second.blocks_per_sm;
+        }
+    }
     // FP32 uniform 3D batches run two fields per lane (the paired kernel)
     const bool paired = DIM == 3 && P == EIKX_F32 && uniform && nSrc >= 2 && o.pair_fields;
     const int nUnits = paired ? (nSrc + 1) / 2 : nSrc;   // work units: fields or field pairs
 
+    // sweep kernel and warp-block shape
+    const int variant = o.sweep_kernel == eikx::kNodeStep ? eikx::kNodeStep : eikx::kChunkStep;
+    const bool chunkStep = DIM == 3 && !paired && variant == eikx::kChunkStep;
+    const int shape = chunkStep && o.block_shape > 0 ? o.block_shape - 1 : eikx::kShape8x4;
+
     // workspace
-    const int ly = DIM == 3 ? eikx::LY3 : 1, lz = DIM == 3 ? eikx::LZ3 : eikx::LZ2;
+    const int ly = DIM == 3 ? eikx::shapeLY(shape) : 1, lz = DIM == 3 ? eikx::shapeLZ(shape) : eikx::LZ2;
     const int tilesY = DIM == 3 ? (ny + ly - 1) / ly : 1;
     const int tilesZ = (nz + lz - 1) / lz;
     const int nProgress = nUnits * tilesY * tilesZ;
@@ -343,7 +378,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     if (std::memcmp(before, after, sizeof(before)) != 0) dropGraph(c);
 
     // small uploads through pinned staging
-    std::vector<int> key = {tilesY, tilesZ, nUnits, DIM};
+    std::vector<int> key = {tilesY, tilesZ, nUnits, DIM, ly};
     const bool newOrder = key != w.orderKey;
     std::vector<int> order;
     if (newOrder) order = buildOrder(tilesY, tilesZ, nUnits, ly, lz);
@@ -396,11 +431,11 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     const int spinLog2 = o.spin_limit_log2 > 0 ? std::min(o.spin_limit_log2, 40) : 22;
     st.spinLimit = 1ull << spinLog2;
 
-    const int variant = o.sweep_kernel == eikx::kNodeStep ? eikx::kNodeStep : eikx::kChunkStep;
-    const int perSM = paired ? eikx::sweep3PairBlocksPerSM()
-                      : DIM == 2 ? eikx::sweep2BlocksPerSM<T>(uniform)
-                      : variant == eikx::kChunkStep ? eikx::sweep3ChunkBlocksPerSM<T>(uniform)
-                                                    : eikx::sweep3BlocksPerSM<T>(uniform);
+    int perSM = paired ? eikx::sweep3PairBlocksPerSM()
+                : DIM == 2 ? eikx::sweep2BlocksPerSM<T>(uniform)
+                : chunkStep ? eikx::sweep3ChunkBlocksPerSM<T>(uniform, false, shape)
+                            : eikx::sweep3BlocksPerSM<T>(uniform);
+    if (o.blocks_per_sm > 0) perSM = std::min(perSM, o.blocks_per_sm);
     int blocks = std::min(c->numSMs * perSM, (nProgress + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock);
     blocks = std::max(blocks, 1);
 
@@ -411,6 +446,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
     sk.h = dx; sk.dx = dx; sk.dy = dy; sk.dz = dz; sk.spin = st.spinLimit; sk.dropBlocks = drop;
     sk.paired = paired ? 1 : 0;
     sk.variant = variant;
+    sk.shape = shape;
     sk.tt = w.tt.p; sk.sp = spad[0].p; sk.srcs = w.srcs.p; sk.corners = w.corners.p;
 
     int launches = 0;
@@ -467,7 +503,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, const eikx_op
                     }
                 }
                 if (!done) {
-                    if (variant == eikx::kChunkStep) EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, blocks, c->stream));
+                    if (chunkStep) EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, shape, blocks, c->stream));
                     else EIKX_CUDA(eikx::launchSweep3<T>(a, uniform, blocks, c->stream));
                 }
             } else {
@@ -629,7 +665,8 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     BatchWorkspace &w = c->bw;
     constexpr int V = 16 / sizeof(T);
     constexpr int W = sizeof(T) / 4;
-    const int ly = eikx::LY3, lz = eikx::LZ3;
+    const int shape = o.block_shape > 0 ? o.block_shape - 1 : eikx::kShape8x4;
+    const int ly = eikx::shapeLY(shape), lz = eikx::shapeLZ(shape);
     const int nM = static_cast<int>(sel.size());
     struct Layout {
         int nx, ny, nz, Px, spPitch, tilesY, tilesZ, firstUnit, nSrc;
@@ -836,7 +873,8 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     st.totalItems = static_cast<int>(nItems);
     const int spinLog2 = o.spin_limit_log2 > 0 ? std::min(o.spin_limit_log2, 40) : 22;
     st.spinLimit = 1ull << spinLog2;
-    const int perSM = eikx::sweep3ChunkBlocksPerSM<T>(uniform, true);
+    int perSM = eikx::sweep3ChunkBlocksPerSM<T>(uniform, true, shape);
+    if (o.blocks_per_sm > 0) perSM = std::min(perSM, o.blocks_per_sm);
     const int blocks = std::max(1, static_cast<int>(std::min<size_t>(
                                        static_cast<size_t>(c->numSMs) * perSM,
                                        (nItems + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock)));
@@ -870,7 +908,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
             a.sweepIndex = sweepsLaunched;
             a.sweep = e; a.init = init; a.radius = o.factored_radius;
             a.units = w.units.as<eikx::Grid3Unit<T>>();
-            EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, blocks, c->stream));
+            EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, shape, blocks, c->stream));
             if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched + 1], c->stream));
             buf ^= 1;
             ++launches;
@@ -894,7 +932,8 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     std::vector<double> key = {static_cast<double>(sizeof(T)), uniform ? 1.0 : 0.0, static_cast<double>(nM),
                                static_cast<double>(o.n_sweeps), static_cast<double>(o.factored_radius),
                                static_cast<double>(o.init_sweeps), static_cast<double>(o.init_fp64), o.tolerance,
-                               static_cast<double>(st.spinLimit), static_cast<double>(blocks)};
+                               static_cast<double>(st.spinLimit), static_cast<double>(blocks),
+                               static_cast<double>(shape)};
     for (int i = 0; i < nM; ++i) {
         const eikx_model3d &m = models[sel[i]];
         for (double v : {static_cast<double>(m.nx), static_cast<double>(m.ny), static_cast<double>(m.nz), m.dx, m.dy,
@@ -975,10 +1014,68 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     return EIKX_OK;
 }
 
+template <class T>
+eikx_status autotune3(eikx_ctx *c, const std::vector<double> &xyz, int nSrc, eikx_tuning *res) {
+    const int P = precOf<T>();
+    const size_t n = static_cast<size_t>(c->nx) * c->ny * c->nz;
+    EIKX_CUDA(c->tuneOut.ensure(n * nSrc * sizeof(T)));
+    const double eps = std::numeric_limits<T>::epsilon() * 100;
+    const bool uniform = uniformSpacing3(c->dx, c->dy, c->dz, eps);
+    eikx_options base;
+    eikx_options_default(&base);
+    base.n_sweeps = 1;
+    base.tolerance = -1;
+    base.profile_sweeps = 1;
+    std::vector<eikx_options> cands;
+    auto add = [&](int kernel, int pair, int shape, int perSM) {
+        eikx_options o = base;
+        o.sweep_kernel = kernel;
+        o.pair_fields = pair;
+        o.block_shape = shape;
+        o.blocks_per_sm = perSM;
+        cands.push_back(o);
+    };
+    for (int shape = 0; shape < eikx::kNumShapes; ++shape) {
+        const int mx = eikx::sweep3ChunkBlocksPerSM<T>(uniform, false, shape);
+        add(eikx::kChunkStep, 0, shape + 1, mx);
+        if (mx / 2 >= 1 && mx / 2 < mx) add(eikx::kChunkStep, 0, shape + 1, mx / 2);
+    }
+    add(eikx::kNodeStep, 0, 1, eikx::sweep3BlocksPerSM<T>(uniform));
+    if (std::is_same<T, float>::value && uniform && nSrc >= 2) add(eikx::kChunkStep, 1, 1, eikx::sweep3PairBlocksPerSM());
+    double best = 1e300, dflt = -1;
+    eikx_tuning pick{};
+    for (size_t i = 0; i < cands.size(); ++i) {
+        double ms = 0;
+        for (int rep = 0; rep < 2; ++rep) {
+            if (eikx_status r = solveImpl<T, 3>(c, xyz.data(), nSrc, cands[i], c->tuneOut.p, EIKX_DEVICE); r)
+                return r;
+            ms = c->stats.sweep_ms / std::max(1, c->stats.sweeps_launched);
+        }
+        if (i == 0) dflt = ms;   // chunk-step, 8x4, full grid: the untuned default
+        if (ms < best) {
+            best = ms;
+            pick.sweep_kernel = cands[i].sweep_kernel;
+            pick.pair_fields = cands[i].pair_fields;
+            pick.block_shape = cands[i].block_shape;
+            pick.blocks_per_sm = cands[i].blocks_per_sm;
+        }
+    }
+    pick.ms_per_sweep = best;
+    pick.default_ms_per_sweep = dflt;
+    pick.candidates = static_cast<int>(cands.size());
+    c->tuning[tuneKey(P, uniform, c->nx, c->ny, c->nz, nSrc)] = pick;
+    if (res) *res = pick;
+    return EIKX_OK;
+}
+
 eikx_status fillOptions(const eikx_options *in, eikx_options *out) {
     if (in) *out = *in; else eikx_options_default(out);
     if (out->n_sweeps < 0) return fail(EIKX_ERR_INVALID, "n_sweeps must be non-negative");
     if (out->factored_radius < 0) out->factored_radius = 0;
+    if (out->block_shape < 0 || out->block_shape > eikx::kNumShapes)
+        return fail(EIKX_ERR_INVALID, "block_shape must be 0..3");
+    if (out->sweep_kernel < 0 || out->sweep_kernel > 2) return fail(EIKX_ERR_INVALID, "sweep_kernel must be 0..2");
+    if (out->blocks_per_sm < 0) return fail(EIKX_ERR_INVALID, "blocks_per_sm must be >= 0");
     return EIKX_OK;
 }
 
@@ -1202,6 +1299,67 @@ eikx_status eikx_solve3d_batch(eikx_ctx *c, const eikx_model3d *models, int nMod
         if (r != EIKX_OK) return r;
     }
     c->stats = agg;
+    return EIKX_OK;
+}
+
+eikx_status eikx_autotune3d(eikx_ctx *c, const eikx_source3d *src, int nSrc, int precision, eikx_tuning *out) {
+    if (eikx_status r = checkCtx(c); r) return r;
+    if (!c->haveGrid3) return fail(EIKX_ERR_STATE, "Class not initialized");
+    if (!c->haveSlow3) return fail(EIKX_ERR_STATE, "Velocity model not set");
+    if (!src || nSrc <= 0) return fail(EIKX_ERR_STATE, "Source location not set");
+    EIKX_CUDA(cudaSetDevice(c->device));
+    std::vector<double> xyz(3 * static_cast<size_t>(nSrc));
+    for (int i = 0; i < nSrc; ++i) { xyz[3 * i] = src[i].x; xyz[3 * i + 1] = src[i].y; xyz[3 * i + 2] = src[i].z; }
+    if (precision == EIKX_F32) return autotune3<float>(c, xyz, nSrc, out);
+    if (precision == EIKX_F64) return autotune3<double>(c, xyz, nSrc, out);
+    return fail(EIKX_ERR_INVALID, "precision must be EIKX_F32 or EIKX_F64");
+}
+
+eikx_status eikx_tuning_save(const eikx_ctx *c, const char *path) {
+    if (eikx_status r = checkCtx(c); r) return r;
+    if (!path) return fail(EIKX_ERR_INVALID, "path is NULL");
+    std::ofstream f(path);
+    if (!f) return fail(EIKX_ERR_INVALID, std::string("cannot write ") + path);
+    for (const auto &kv : c->tuning) {
+        const TuneKey &k = kv.first;
+        const eikx_tuning &t = kv.second;
+        f << "{\"precision\": " << k.precision << ", \"uniform\": " << k.uniform << ", \"nx\": " << k.nx
+          << ", \"ny\": " << k.ny << ", \"nz\": " << k.nz << ", \"nsrc\": " << k.nsrc
+          << ", \"sweep_kernel\": " << t.sweep_kernel << ", \"pair_fields\": " << t.pair_fields
+          << ", \"block_shape\": " << t.block_shape << ", \"blocks_per_sm\": " << t.blocks_per_sm
+          << ", \"ms_per_sweep\": " << t.ms_per_sweep << ", \"default_ms_per_sweep\": " << t.default_ms_per_sweep
+          << ", \"candidates\": " << t.candidates << "}\n";
+    }
+    return f ? EIKX_OK : fail(EIKX_ERR_INVALID, std::string("cannot write ") + path);
+}
+
+eikx_status eikx_tuning_load(eikx_ctx *c, const char *path) {
+    if (eikx_status r = checkCtx(c); r) return r;
+    if (!path) return fail(EIKX_ERR_INVALID, "path is NULL");
+    std::ifstream f(path);
+    if (!f) return fail(EIKX_ERR_INVALID, std::string("cannot read ") + path);
+    std::string line;
+    int lineNo = 0;
+    std::map<TuneKey, eikx_tuning> add;
+    while (std::getline(f, line)) {
+        ++lineNo;
+        if (line.find_first_not_of(" \t\r") == std::string::npos) continue;
+        TuneKey k{};
+        eikx_tuning t{};
+        const int got = std::sscanf(line.c_str(),
+                                    " {\"precision\": %d, \"uniform\": %d, \"nx\": %d, \"ny\": %d, \"nz\": %d, "
+                                    "\"nsrc\": %d, \"sweep_kernel\": %d, \"pair_fields\": %d, \"block_shape\": %d, "
+                                    "\"blocks_per_sm\": %d, \"ms_per_sweep\": %lf, \"default_ms_per_sweep\": %lf, "
+                                    "\"candidates\": %d}",
+                                    &k.precision, &k.uniform, &k.nx, &k.ny, &k.nz, &k.nsrc, &t.sweep_kernel,
+                                    &t.pair_fields, &t.block_shape, &t.blocks_per_sm, &t.ms_per_sweep,
+                                    &t.default_ms_per_sweep, &t.candidates);
+        if (got != 13 || t.sweep_kernel < 1 || t.sweep_kernel > 2 || t.block_shape < 1 ||
+            t.block_shape > eikx::kNumShapes || t.blocks_per_sm < 0)
+            return fail(EIKX_ERR_INVALID, std::string(path) + ":" + std::to_string(lineNo) + ": not a tuning entry");
+        add[k] = t;
+    }
+    for (const auto &kv : add) c->tuning[kv.first] = kv.second;
     return EIKX_OK;
 }
 

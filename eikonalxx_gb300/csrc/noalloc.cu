@@ -188,7 +188,8 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     const double eps = std::numeric_limits<float>::epsilon() * 100;
     const bool uniform = std::abs(dx - dy) < eps && std::abs(dx - dz) < eps;
     const bool chunk = o.sweep_kernel != eikx::kNodeStep;
-    const int perSM = chunk ? eikx::sweep3ChunkBlocksPerSM<float>(uniform) : eikx::sweep3BlocksPerSM<float>(uniform);
+    const int perSM = chunk ? eikx::sweep3ChunkBlocksPerSM<float>(uniform, false, eikx::kShape8x4)
+                            : eikx::sweep3BlocksPerSM<float>(uniform);
     const int blocks = std::max(1, std::min(numSMs * perSM, (nTiles + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock));
 
     eikx::SolveState st{};
@@ -236,7 +237,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
         a.nx = nx; a.ny = ny; a.nz = nz; a.tilesY = tilesY; a.tilesZ = tilesZ;
         a.srcs = srcDev; a.st = st; a.buf = buf; a.sweepIndex = launched; a.residualSlot = slot;
         a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = fdx; a.sp3 = g;
-        if (chunk) NOALLOC_CUDA(eikx::launchSweep3Chunk<float>(a, uniform, blocks, stream));
+        if (chunk) NOALLOC_CUDA(eikx::launchSweep3Chunk<float>(a, uniform, eikx::kShape8x4, blocks, stream));
         else NOALLOC_CUDA(eikx::launchSweep3<float>(a, uniform, blocks, stream));
         buf ^= 1;
         ++launched;

@@ -91,14 +91,33 @@ template <class T>
 cudaError_t launchSweep3(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s);
 template <class T>
 cudaError_t launchSweep2(const Sweep2Args<T> &a, bool uniform, int blocks, cudaStream_t s);
-// Chunk-step 3D kernel (sweep_chunk.cu): a lane updates one 16-byte chunk of its pencil
-// per wavefront step.
-// With a.units set, a work item's field index is a unit of a multi-model batch and the
-// grid, slowness, mailbox and spacing come from a.units[unit].
+// Chunk-step 3D kernel (sweep_chunk.cuh): a lane updates one 16-byte chunk of its pencil
+// per wavefront step.  With a.units set, a work item's field index is a unit of a
+// multi-model batch and the grid, slowness, mailbox and spacing come from a.units[unit].
+// Warp-block shapes (pencils per warp along y' x z'), one translation unit each.
+enum ChunkShape { kShape8x4 = 0, kShape4x8 = 1, kShape16x2 = 2, kNumShapes = 3 };
+constexpr int shapeLY(int shape) { return shape == kShape4x8 ? 4 : shape == kShape16x2 ? 16 : 8; }
+constexpr int shapeLZ(int shape) { return shape == kShape4x8 ? 8 : shape == kShape16x2 ? 2 : 4; }
+#define EIKX_DECLARE_CHUNK_SHAPE(LY_, LZ_)                                                        \
+    template <class T>                                                                            \
+    cudaError_t launchSweep3Chunk_##LY_##x##LZ_(const Sweep3Args<T> &a, bool uniform, int blocks, \
+                                                cudaStream_t s);                                  \
+    template <class T> int sweep3ChunkBlocksPerSM_##LY_##x##LZ_(bool uniform, bool batch);
+EIKX_DECLARE_CHUNK_SHAPE(8, 4)
+EIKX_DECLARE_CHUNK_SHAPE(4, 8)
+EIKX_DECLARE_CHUNK_SHAPE(16, 2)
+#undef EIKX_DECLARE_CHUNK_SHAPE
 template <class T>
-cudaError_t launchSweep3Chunk(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s);
-template <class T> int sweep3ChunkBlocksPerSM(bool uniform, bool batch = false);
-size_t sweep3ChunkSmemBytes();
+inline cudaError_t launchSweep3Chunk(const Sweep3Args<T> &a, bool uniform, int shape, int blocks, cudaStream_t s) {
+    if (shape == kShape4x8) return launchSweep3Chunk_4x8<T>(a, uniform, blocks, s);
+    if (shape == kShape16x2) return launchSweep3Chunk_16x2<T>(a, uniform, blocks, s);
+    return launchSweep3Chunk_8x4<T>(a, uniform, blocks, s);
+}
+template <class T> inline int sweep3ChunkBlocksPerSM(bool uniform, bool batch, int shape) {
+    if (shape == kShape4x8) return sweep3ChunkBlocksPerSM_4x8<T>(uniform, batch);
+    if (shape == kShape16x2) return sweep3ChunkBlocksPerSM_16x2<T>(uniform, batch);
+    return sweep3ChunkBlocksPerSM_8x4<T>(uniform, batch);
+}
 // 3D sweep kernel variants (eikx_options.sweep_kernel).
 enum Sweep3Variant { kNodeStep = 1, kChunkStep = 2 };
 // Paired 3D kernel (sweep_pair.cu): FP32, uniform grid, two fields of one model per lane.

@@ -20,17 +20,19 @@
 //     are issued a step before they are needed.
 // Near-source nodes (factored branch) are evaluated by an out-of-line call, so the V
 // inlined copies of the update are the Cartesian operators only.
+//
+// The warp-block shape LY x LZ (pencils per warp, LY * LZ = 32) is a template parameter;
+// each shape is instantiated in its own translation unit (sweep_chunk_<LY>x<LZ>.cu).
+#pragma once
 #include "sweep.h"
 #include "wavefront.cuh"
 
 namespace eikx {
 
-namespace {
+namespace chunk {
 
-constexpr int HY = LY3 + 1, HZ = LZ3 + 1;          // ring plane incl. halo row/column
-constexpr int kPlane = HY * HZ;
 constexpr int kRingC = 4;                           // ring depth in steps (reads go back 2)
-constexpr int kThreads = 32 * kWarpsPerBlock;
+constexpr int kThreadsC = 32 * kWarpsPerBlock;
 
 template <class T> struct alignas(16) Vec {
     static constexpr int N = 16 / sizeof(T);
@@ -145,13 +147,16 @@ __device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *st.queue[buf ^ 1] = 0u;
 }
 
-template <class T, bool UNIFORM, bool REV, bool BATCH>
-__global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T> a) {
+template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ>
+__global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<T> a) {
+    static_assert(LY * LZ == 32 && LZ + 1 + LY <= 32, "a warp holds 32 pencils and its halo helpers");
+    constexpr int HY = LY + 1, HZ = LZ + 1;          // ring plane incl. halo row/column
+    constexpr int kPlane = HY * HZ;
     constexpr int V = Vec<T>::N;
     constexpr int W = sizeof(T) / 4;                // mailbox words per value
     extern __shared__ __align__(16) unsigned char smemRaw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ly = lane % LY3, lz = lane / LY3;
+    const int ly = lane % LY, lz = lane / LY;
     Vec<T> *tring = reinterpret_cast<Vec<T> *>(smemRaw) + warp * (2 * kRingC * kPlane);
     Vec<T> *sring = tring + kRingC * kPlane;
     const SolveState &st = a.st;
@@ -166,7 +171,7 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
     const T huge = static_cast<T>(1.e10);
 
     // helper lanes stand in for the virtual upwind lanes of the halo row/column
-    const bool helper = lane < HZ + LY3;
+    const bool helper = lane < HZ + LY;
     const int vly = lane < HZ ? -1 : lane - HZ;
     const int vlz = lane < HZ ? lane - 1 : -1;
     const int vslot = (vlz + 1) * HY + (vly + 1);
@@ -191,14 +196,14 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
         const long long spPlane = BATCH ? unit->spPlane : a.spPlane;
         const T *sp = BATCH ? (REV ? unit->spNeg : unit->spPos) : (REV ? a.spNeg : a.spPos);
         T *field = BATCH ? unit->tt : a.tt + static_cast<long long>(f) * a.fieldStride;
-        const long long faceWords = static_cast<long long>(LY3 + LZ3) * Px * W;
+        const long long faceWords = static_cast<long long>(LY + LZ) * Px * W;
         unsigned long long *fieldBox =
             BATCH ? unit->mbox : st.mbox + static_cast<long long>(f) * a.tilesZ * a.tilesY * faceWords;
         const T h = BATCH ? unit->h : a.h;
         const int nChunks = Px / V;
-        const int nSteps = nChunks + LY3 + LZ3 - 2;
+        const int nSteps = nChunks + LY + LZ - 2;
 
-        const int y0 = b * LY3, z0 = c * LZ3;
+        const int y0 = b * LY, z0 = c * LZ;
         const int yp = y0 + ly, zp = z0 + lz;
         const bool laneValid = yp < ny && zp < nz;
         const int ya = laneValid ? reflect(yp, ny, fy) : 0;
@@ -226,7 +231,7 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
         // mailbox: this block's faces, and the upstream face row a helper lane reads
         unsigned long long *box = fieldBox + (static_cast<long long>(c) * tilesY + b) * faceWords;
         unsigned long long *yFace = box + static_cast<long long>(lz) * Px * W;          // ly == LY-1
-        unsigned long long *zFace = box + static_cast<long long>(LZ3 + ly) * Px * W;    // lz == LZ-1
+        unsigned long long *zFace = box + static_cast<long long>(LZ + ly) * Px * W;    // lz == LZ-1
         const int vyp = y0 + vly, vzp = z0 + vlz;
         const bool vValid = helper && vyp >= 0 && vzp >= 0 && vyp < ny && vzp < nz;
         const unsigned long long *vbox = box;
@@ -236,10 +241,10 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
             if (vly < 0) {
                 // block (b-1, c), or the corner block (b-1, c-1): its y' face row
                 vbox = box - (vlz >= 0 ? faceWords : (tilesY + 1) * faceWords) +
-                       static_cast<long long>(vlz >= 0 ? vlz : LZ3 - 1) * Px * W;
+                       static_cast<long long>(vlz >= 0 ? vlz : LZ - 1) * Px * W;
             } else {
                 // block (b, c-1): its z' face row
-                vbox = box - tilesY * faceWords + static_cast<long long>(LZ3 + vly) * Px * W;
+                vbox = box - tilesY * faceWords + static_cast<long long>(LZ + vly) * Px * W;
             }
             vsrow = sp + static_cast<long long>(vza + (fz ? 0 : 1)) * spPlane +
                     static_cast<long long>(vya + (fy ? 0 : 1)) * spPitch;
@@ -356,8 +361,8 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
             tring[cur + myslot] = out;
             if (active) {
                 if (changed) stVec(tChunk(row, k), walk(out));
-                if (ly == LY3 - 1) putChunk(yFace + static_cast<long long>(k) * V * W, tag, out);
-                if (lz == LZ3 - 1) putChunk(zFace + static_cast<long long>(k) * V * W, tag, out);
+                if (ly == LY - 1) putChunk(yFace + static_cast<long long>(k) * V * W, tag, out);
+                if (lz == LZ - 1) putChunk(zFace + static_cast<long long>(k) * V * W, tag, out);
             }
             cT1 = out.v[V - 1]; cT3 = tY.v[V - 1]; cT4 = tZ.v[V - 1]; cT7 = tYZ.v[V - 1];
             cS1 = sYZ.v[V - 1]; cS2 = sZ.v[V - 1]; cS5 = sY.v[V - 1]; cS7 = sOwn.v[V - 1];
@@ -370,56 +375,62 @@ __global__ void __launch_bounds__(kThreads) sweep3ChunkKernel(const Sweep3Args<T
     }
 }
 
-template <class T, bool U, bool R, bool B> void *chunkKernel() {
-    return reinterpret_cast<void *>(sweep3ChunkKernel<T, U, R, B>);
+template <int LY, int LZ> constexpr size_t smemBytes() {
+    return 2 * kRingC * (LY + 1) * (LZ + 1) * 16 * kWarpsPerBlock;
 }
 
-template <class T, bool B>
-void launchChunk(const Sweep3Args<T> &a, bool uniform, bool rev, int blocks, size_t smem, cudaStream_t s) {
+template <class T, bool B, int LY, int LZ>
+void launchShape(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s) {
+    const size_t smem = smemBytes<LY, LZ>();
+    const bool rev = (a.sweep & 1) != 0;
     if (uniform) {
-        if (rev) sweep3ChunkKernel<T, true, true, B><<<blocks, kThreads, smem, s>>>(a);
-        else sweep3ChunkKernel<T, true, false, B><<<blocks, kThreads, smem, s>>>(a);
+        if (rev) sweep3ChunkKernel<T, true, true, B, LY, LZ><<<blocks, kThreadsC, smem, s>>>(a);
+        else sweep3ChunkKernel<T, true, false, B, LY, LZ><<<blocks, kThreadsC, smem, s>>>(a);
     } else {
-        if (rev) sweep3ChunkKernel<T, false, true, B><<<blocks, kThreads, smem, s>>>(a);
-        else sweep3ChunkKernel<T, false, false, B><<<blocks, kThreads, smem, s>>>(a);
+        if (rev) sweep3ChunkKernel<T, false, true, B, LY, LZ><<<blocks, kThreadsC, smem, s>>>(a);
+        else sweep3ChunkKernel<T, false, false, B, LY, LZ><<<blocks, kThreadsC, smem, s>>>(a);
     }
 }
 
-}  // namespace
-
-size_t sweep3ChunkSmemBytes() { return 2 * kRingC * kPlane * 16 * kWarpsPerBlock; }
-
-template <class T>
-cudaError_t launchSweep3Chunk(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s) {
-    const size_t smem = sweep3ChunkSmemBytes();
-    const bool rev = (a.sweep & 1) != 0;
-    if (a.units) launchChunk<T, true>(a, uniform, rev, blocks, smem, s);
-    else launchChunk<T, false>(a, uniform, rev, blocks, smem, s);
-    return cudaGetLastError();
-}
-
-template <class T> int sweep3ChunkBlocksPerSM(bool uniform, bool batch) {
-    // the instantiations of one kind differ only in the sweep direction; take the least
-    void *k[2];
-    if (batch) {
-        k[0] = uniform ? chunkKernel<T, true, false, true>() : chunkKernel<T, false, false, true>();
-        k[1] = uniform ? chunkKernel<T, true, true, true>() : chunkKernel<T, false, true, true>();
+template <class T, bool B, int LY, int LZ> int blocksPerSM(bool uniform) {
+    // the two sweep directions differ only in addressing; take the lower occupancy
+    const void *k[2];
+    if (uniform) {
+        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, false, B, LY, LZ>);
+        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, true, B, LY, LZ>);
     } else {
-        k[0] = uniform ? chunkKernel<T, true, false, false>() : chunkKernel<T, false, false, false>();
-        k[1] = uniform ? chunkKernel<T, true, true, false>() : chunkKernel<T, false, true, false>();
+        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, false, B, LY, LZ>);
+        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, true, B, LY, LZ>);
     }
     int best = 1 << 30;
-    for (void *f : k) {
+    for (const void *f : k) {
         int n = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kThreads, sweep3ChunkSmemBytes());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kThreadsC, smemBytes<LY, LZ>());
         best = n < best ? n : best;
     }
     return best > 0 ? best : 1;
 }
 
-template cudaError_t launchSweep3Chunk<float>(const Sweep3Args<float> &, bool, int, cudaStream_t);
-template cudaError_t launchSweep3Chunk<double>(const Sweep3Args<double> &, bool, int, cudaStream_t);
-template int sweep3ChunkBlocksPerSM<float>(bool, bool);
-template int sweep3ChunkBlocksPerSM<double>(bool, bool);
+}  // namespace chunk
+
+// Launch and occupancy entry points of one warp-block shape (one translation unit each).
+#define EIKX_CHUNK_SHAPE(LY_, LZ_)                                                                    \
+    template <class T>                                                                                \
+    cudaError_t launchSweep3Chunk_##LY_##x##LZ_(const Sweep3Args<T> &a, bool uniform, int blocks,     \
+                                                cudaStream_t s) {                                     \
+        if (a.units) chunk::launchShape<T, true, LY_, LZ_>(a, uniform, blocks, s);                    \
+        else chunk::launchShape<T, false, LY_, LZ_>(a, uniform, blocks, s);                           \
+        return cudaGetLastError();                                                                    \
+    }                                                                                                 \
+    template <class T> int sweep3ChunkBlocksPerSM_##LY_##x##LZ_(bool uniform, bool batch) {           \
+        return batch ? chunk::blocksPerSM<T, true, LY_, LZ_>(uniform)                                 \
+                     : chunk::blocksPerSM<T, false, LY_, LZ_>(uniform);                               \
+    }                                                                                                 \
+    template cudaError_t launchSweep3Chunk_##LY_##x##LZ_<float>(const Sweep3Args<float> &, bool, int, \
+                                                                cudaStream_t);                        \
+    template cudaError_t launchSweep3Chunk_##LY_##x##LZ_<double>(const Sweep3Args<double> &, bool,    \
+                                                                 int, cudaStream_t);                  \
+    template int sweep3ChunkBlocksPerSM_##LY_##x##LZ_<float>(bool, bool);                             \
+    template int sweep3ChunkBlocksPerSM_##LY_##x##LZ_<double>(bool, bool);
 
 }  // namespace eikx

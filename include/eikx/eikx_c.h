@@ -68,10 +68,16 @@ typedef struct {
                               = one field per lane, measured faster on GB300 at every batch
                               size (the paired kernel needs 168 registers per thread, which
                               leaves 12 resident warps per SM).  Both give identical times. */
-    int sweep_kernel;      /* 3D sweep kernel: 0 (default) = chunk-step, 1 = node-step (a
+    int sweep_kernel;      /* 3D sweep kernel: 0 (default) = the tuned kernel of this grid class
+                              if eikx_autotune3d ran, else chunk-step; 1 = node-step (a
                               lane updates one node per wavefront step), 2 = chunk-step (a
                               lane updates one 16-byte chunk, 4 FP32 / 2 FP64 nodes, per
                               step).  All give identical travel times. */
+    int block_shape;       /* 3D chunk-step warp block (pencils along y' x z'): 0 (default) =
+                              the tuned shape of this grid class if eikx_autotune3d ran, else
+                              8x4; 1 = 8x4, 2 = 4x8, 3 = 16x2.  Identical travel times. */
+    int blocks_per_sm;     /* persistent sweep grid: resident blocks per SM; 0 (default) = as
+                              many as fit (or the tuned value) */
     int reserved[2];
 } eikx_options;
 
@@ -135,6 +141,34 @@ eikx_status eikx_solve3d(eikx_ctx *ctx, const eikx_source3d *src, int n_src,
                          const eikx_options *opt, int precision, void *t_out, int where);
 
 /* ---- 2D ---------------------------------------------------------------- */
+/* ---- autotuning ---------------------------------------------------------- */
+
+/* The configuration eikx_autotune3d chose for one grid class. */
+typedef struct {
+    int sweep_kernel;              /* 1 = node-step, 2 = chunk-step */
+    int pair_fields;               /* 1 = two FP32 fields per lane */
+    int block_shape;               /* 1 = 8x4, 2 = 4x8, 3 = 16x2 (chunk-step) */
+    int blocks_per_sm;             /* resident blocks per SM of the persistent grid */
+    double ms_per_sweep;           /* measured mean sweep launch of the choice */
+    double default_ms_per_sweep;   /* the untuned default (chunk-step, 8x4, full grid) */
+    int candidates;                /* configurations timed */
+} eikx_tuning;
+
+/* No counterpart in the reference.  Times the sweep kernels, warp-block shapes and grid
+ * sizes on the context's 3D model with these sources -- one refinement iteration per
+ * candidate, CUDA events around every sweep launch, each candidate run twice and the
+ * second run kept -- and records the fastest for the grid class (precision, uniform
+ * spacing, nx, ny, nz rounded up to multiples of 32, source count rounded up to a power
+ * of two).  Later eikx_solve3d calls of the same class whose options leave sweep_kernel,
+ * block_shape and blocks_per_sm at 0 and pair_fields at 0 use it.  All candidates give
+ * identical travel times. */
+eikx_status eikx_autotune3d(eikx_ctx *ctx, const eikx_source3d *src, int n_src, int precision,
+                            eikx_tuning *out);
+/* Writes the context's tuning table to `path` (one JSON object per line) / merges the
+ * table at `path` into the context. */
+eikx_status eikx_tuning_save(const eikx_ctx *ctx, const char *path);
+eikx_status eikx_tuning_load(eikx_ctx *ctx, const char *path);
+
 /* ---- multi-model batch ------------------------------------------------- */
 
 /* One model of a multi-model batch and the sources to solve on it. */

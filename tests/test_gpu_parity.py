@@ -198,12 +198,13 @@ def test_paired_fields_converge_independently(ctx, oracle, n_src):
         assert np.array_equal(_bits(outs[False][i]), _bits(t_or)), i
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant,block", [(1, 0), (2, 1), (2, 2), (2, 3)])
 @pytest.mark.parametrize("precision", [ex.F32, ex.F64])
 @pytest.mark.parametrize("shape", [(29, 23, 19, 40., 40., 40.), (18, 21, 13, 50., 45., 60.), (5, 4, 3, 10., 10., 10.)])
-def test_sweep_kernel_variants_match_oracle(ctx, oracle, variant, precision, shape):
+def test_sweep_kernel_variants_match_oracle(ctx, oracle, variant, block, precision, shape):
     """Node-step (one node per lane and step) and chunk-step (one 16-byte chunk per lane
-    and step) kernels, uniform and non-uniform grids, near-source nodes included."""
+    and step, warp blocks of 8x4, 4x8 and 16x2 pencils) kernels, uniform and non-uniform
+    grids, near-source nodes included."""
     rng = np.random.default_rng(200 + variant)
     nx, ny, nz = shape[:3]
     dt = np.float32 if precision == ex.F32 else np.float64
@@ -211,7 +212,7 @@ def test_sweep_kernel_variants_match_oracle(ctx, oracle, variant, precision, sha
     ctx.set_grid3d(*shape)
     ctx.set_slowness3d(s)
     srcs = [_src(rng, (nx, ny, nz), shape[3:]) for _ in range(3)]
-    opt = ex.Options(n_sweeps=3, tolerance=-1, factored_radius=2, sweep_kernel=variant)
+    opt = ex.Options(n_sweeps=3, tolerance=-1, factored_radius=2, sweep_kernel=variant, block_shape=block)
     t = ctx.solve3d([p for p, _, _ in srcs], opt, precision)
     for i, (_, cell, off) in enumerate(srcs):
         t_or = oracle.solve3d(s, shape, cell, off, n_sweeps=3, radius=2)
