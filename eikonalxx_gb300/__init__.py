@@ -35,6 +35,7 @@ EXPORTED = [
     "eikx_solve3d", "eikx_set_grid2d", "eikx_set_slowness2d", "eikx_set_nodal_velocity2d",
     "eikx_solve2d", "eikx_graph3d_tables", "eikx_levels2d", "eikx_analytic3d", "eikx_analytic2d",
     "eikx_solve3d_noalloc", "eikx_solve3d_batch", "eikx_autotune3d", "eikx_tuning_save", "eikx_tuning_load",
+    "eikx_gradient3d", "eikx_gradient2d", "eikx_station_times3d", "eikx_station_times2d",
 ]
 CELL_SLOWNESS, NODAL_VELOCITY = 0, 1
 
@@ -135,6 +136,10 @@ def load(path=None):
     lib.eikx_analytic2d.argtypes = [vp, ctypes.POINTER(_Src2), c_double, c_double, vp, c_int]
     lib.eikx_solve3d_batch.argtypes = [vp, ctypes.POINTER(_Model3), c_int, ctypes.POINTER(_Options), c_int]
     lib.eikx_autotune3d.argtypes = [vp, ctypes.POINTER(_Src3), c_int, c_int, ctypes.POINTER(_Tuning)]
+    lib.eikx_gradient3d.argtypes = [vp, c_int, vp, c_int]
+    lib.eikx_gradient2d.argtypes = [vp, c_int, vp, c_int]
+    lib.eikx_station_times3d.argtypes = [vp, c_int, ctypes.POINTER(_Src3), c_int, ctypes.POINTER(c_double)]
+    lib.eikx_station_times2d.argtypes = [vp, c_int, ctypes.POINTER(_Src2), c_int, ctypes.POINTER(c_double)]
     lib.eikx_tuning_save.argtypes = [vp, ctypes.c_char_p]
     lib.eikx_tuning_load.argtypes = [vp, ctypes.c_char_p]
     for name in EXPORTED:
@@ -273,6 +278,44 @@ class Context:
         p, where = _ptr(out)
         o = (options or Options())._c()
         _check(self._lib.eikx_solve3d(self._h, arr, n, ctypes.byref(o), precision, p, where))
+        return out
+
+    def gradient3d(self, field=0, precision=F32, out=None):
+        """Travel-time gradient of field `field` of the last 3D solve: (nz, ny, nx, 3)."""
+        if self.grid3 is None:                       # no solve yet: the library reports it
+            _check(self._lib.eikx_gradient3d(self._h, int(field), None, HOST))
+        nx, ny, nz = self.grid3[:3]
+        if out is None:
+            out = np.empty((nz, ny, nx, 3), dtype=np.float32 if precision == F32 else np.float64)
+        p, where = _ptr(out)
+        _check(self._lib.eikx_gradient3d(self._h, int(field), p, where))
+        return out
+
+    def gradient2d(self, field=0, precision=F64, out=None):
+        """Travel-time gradient of field `field` of the last 2D solve: (nz, nx, 2)."""
+        if self.grid2 is None:
+            _check(self._lib.eikx_gradient2d(self._h, int(field), None, HOST))
+        nx, nz = self.grid2[:2]
+        if out is None:
+            out = np.empty((nz, nx, 2), dtype=np.float32 if precision == F32 else np.float64)
+        p, where = _ptr(out)
+        _check(self._lib.eikx_gradient2d(self._h, int(field), p, where))
+        return out
+
+    def station_times3d(self, stations, field=0):
+        st = np.atleast_2d(np.asarray(stations, dtype=np.float64))
+        arr = (_Src3 * len(st))(*[_Src3(*map(float, q)) for q in st])
+        out = np.empty(len(st), dtype=np.float64)
+        _check(self._lib.eikx_station_times3d(self._h, int(field), arr, len(st),
+                                              out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def station_times2d(self, stations, field=0):
+        st = np.atleast_2d(np.asarray(stations, dtype=np.float64))
+        arr = (_Src2 * len(st))(*[_Src2(float(q[0]), float(q[1])) for q in st])
+        out = np.empty(len(st), dtype=np.float64)
+        _check(self._lib.eikx_station_times2d(self._h, int(field), arr, len(st),
+                                              out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out
 
     def autotune3d(self, sources, precision=F32):

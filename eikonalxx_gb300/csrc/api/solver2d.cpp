@@ -1,5 +1,5 @@
 // Solver2D<T> (reference: src/solver2d.cpp) over the C ABI; station times and the
-// gradient field are computed on the host from the solved field, as the reference does.
+// gradient field are computed on the GPU from the solved field.
 #include <cmath>
 #include <stdexcept>
 #include <string>
@@ -29,33 +29,17 @@ public:
     bool initialized{false}, haveModel{false}, haveSource{false}, haveField{false}, haveGradient{false};
     bool gridOnDevice{false}, modelOnDevice{false};
 
-    // Bilinear interpolation of the field at the stations (src/solver2d.cpp:106-167,
-    // src/ray/bilinear.hpp); a station in the source cell gets the straight-ray time.
+    // Travel times at the stations (src/solver2d.cpp:106-167): bilinear interpolation of
+    // the solved field on the GPU, the straight-ray time in the source cell.
     void interpolate()
     {
         stationTimes.assign(stations.size(), 0);
         if (stations.empty()) return;
-        const double dx = geometry.getGridSpacingInX(), dz = geometry.getGridSpacingInZ();
-        const int nx = geometry.getNumberOfGridPointsInX();
-        const int srcCell = source.getCell();
-        const double s0 = static_cast<double>(model.getSlowness(source.getCellInX(), source.getCellInZ()));
-        for (size_t i = 0; i < stations.size(); ++i) {
-            const auto &st = stations[i];
-            const double xi = st.getOffsetInX(), zi = st.getOffsetInZ();
-            if (st.getCell() == srcCell) {
-                stationTimes[i] = static_cast<T>(std::hypot(xi - source.getOffsetInX(), zi - source.getOffsetInZ()) * s0);
-                continue;
-            }
-            const int cx = st.getCellInX(), cz = st.getCellInZ();
-            const size_t i00 = static_cast<size_t>(cz) * nx + cx;
-            const double x1 = cx * dx, x2 = (cx + 1) * dx, z1 = cz * dz, z2 = (cz + 1) * dz;
-            const double f00 = travelTimes[i00], f10 = travelTimes[i00 + 1];
-            const double f01 = travelTimes[i00 + nx], f11 = travelTimes[i00 + nx + 1];
-            const double dxi = 1. / dx, dzi = 1. / dz;
-            const double fxz1 = dxi * ((x2 - xi) * f00 + (xi - x1) * f10);
-            const double fxz2 = dxi * ((x2 - xi) * f01 + (xi - x1) * f11);
-            stationTimes[i] = static_cast<T>(dzi * ((z2 - zi) * fxz1 + (zi - z1) * fxz2));
-        }
+        std::vector<eikx_source2d> xz(stations.size());
+        for (size_t i = 0; i < stations.size(); ++i) xz[i] = {stations[i].getLocationInX(), stations[i].getLocationInZ()};
+        std::vector<double> t(stations.size());
+        Detail::check(eikx_station_times2d(gpu.get(), 0, xz.data(), static_cast<int>(xz.size()), t.data()));
+        for (size_t i = 0; i < t.size(); ++i) stationTimes[i] = static_cast<T>(t[i]);
     }
 };
 
@@ -194,25 +178,15 @@ template <class T> void Solver2D<T>::solve()
     p.interpolate();
 }
 
-// Central differences of T with 0 standing in for a missing neighbour at the edges,
-// interleaved (dT/dx, dT/dz) per node (src/gradient.hpp:20-131).
+// The gradient of the solved field on the GPU (src/gradient.hpp:20-289): central
+// differences inside, second-order one-sided differences at the edges, the analytic
+// gradient at the source cell's corners; interleaved (dT/dx, dT/dz) per node.
 template <class T> void Solver2D<T>::computeTravelTimeGradientField()
 {
     if (!haveTravelTimeField()) throw std::runtime_error("Travel time field not yet computed");
     auto &p = *pImpl;
-    const size_t nx = p.geometry.getNumberOfGridPointsInX(), nz = p.geometry.getNumberOfGridPointsInZ();
-    const T twodxi = static_cast<T>(1. / (2. * p.geometry.getGridSpacingInX()));
-    const T twodzi = static_cast<T>(1. / (2. * p.geometry.getGridSpacingInZ()));
-    p.gradient.assign(2 * nx * nz, 0);
-    const T *t = p.travelTimes.data();
-    for (size_t iz = 0; iz < nz; ++iz)
-        for (size_t ix = 0; ix < nx; ++ix) {
-            const size_t i = iz * nx + ix;
-            const T uxm1 = ix > 0 ? t[i - 1] : T(0), uxp1 = ix < nx - 1 ? t[i + 1] : T(0);
-            const T uzm1 = iz > 0 ? t[i - nx] : T(0), uzp1 = iz < nz - 1 ? t[i + nx] : T(0);
-            p.gradient[2 * i] = (uxp1 - uxm1) * twodxi;
-            p.gradient[2 * i + 1] = (uzp1 - uzm1) * twodzi;
-        }
+    p.gradient.resize(2 * p.travelTimes.size());
+    Detail::check(eikx_gradient2d(p.gpu.get(), 0, p.gradient.data(), EIKX_HOST));
     p.haveGradient = true;
 }
 

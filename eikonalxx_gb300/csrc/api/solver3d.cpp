@@ -24,9 +24,22 @@ public:
     Model3D<T> model;
     Source3D source;
     std::vector<Station3D> stations;
-    std::vector<T> travelTimes;
-    bool initialized{false}, haveModel{false}, haveSource{false}, haveField{false};
+    std::vector<T> travelTimes, gradient, stationTimes;
+    bool initialized{false}, haveModel{false}, haveSource{false}, haveField{false}, haveGradient{false};
     bool gridOnDevice{false}, modelOnDevice{false};
+
+    // travel times at the stations, interpolated on the GPU from the solved field
+    void interpolate()
+    {
+        stationTimes.assign(stations.size(), 0);
+        if (stations.empty()) return;
+        std::vector<eikx_source3d> xyz(stations.size());
+        for (size_t i = 0; i < stations.size(); ++i)
+            xyz[i] = {stations[i].getLocationInX(), stations[i].getLocationInY(), stations[i].getLocationInZ()};
+        std::vector<double> t(stations.size());
+        Detail::check(eikx_station_times3d(gpu.get(), 0, xyz.data(), static_cast<int>(xyz.size()), t.data()));
+        for (size_t i = 0; i < t.size(); ++i) stationTimes[i] = static_cast<T>(t[i]);
+    }
 };
 
 template <class T> Solver3D<T>::Solver3D() : pImpl(std::make_unique<Solver3DImpl>()) {}
@@ -41,7 +54,9 @@ template <class T> void Solver3D<T>::clear() noexcept
     p.source.clear();
     p.stations.clear();
     p.travelTimes.clear();
-    p.initialized = p.haveModel = p.haveSource = p.haveField = false;
+    p.gradient.clear();
+    p.stationTimes.clear();
+    p.initialized = p.haveModel = p.haveSource = p.haveField = p.haveGradient = false;
     p.gridOnDevice = p.modelOnDevice = false;
 }
 
@@ -138,6 +153,7 @@ template <class T> void Solver3D<T>::setStations(const std::vector<Station3D> &s
         if (std::abs(g.getOriginInZ() - sg.getOriginInZ()) > 1.e-3) throw std::invalid_argument("z0 is inconsistent");
     }
     pImpl->stations = stations;
+    if (pImpl->haveField) pImpl->interpolate();
 }
 template <class T> std::vector<Station3D> Solver3D<T>::getStations() const { return pImpl->stations; }
 template <class T> const std::vector<Station3D> &Solver3D<T>::getStationsReference() const { return pImpl->stations; }
@@ -145,7 +161,7 @@ template <class T> const std::vector<Station3D> &Solver3D<T>::getStationsReferen
 template <class T> void Solver3D<T>::solve()
 {
     auto &p = *pImpl;
-    p.haveField = false;
+    p.haveField = p.haveGradient = false;
     if (!isInitialized()) throw std::runtime_error("Class not initialized");
     if (!haveVelocityModel()) throw std::runtime_error("Velocity model not set");
     if (!haveSource()) throw std::runtime_error("Source location not set");
@@ -167,6 +183,22 @@ template <class T> void Solver3D<T>::solve()
     const eikx_options opt = Detail::toOptions(p.options);
     Detail::check(eikx_solve3d(ctx, &src, 1, &opt, Detail::dtypeOf<T>(), p.travelTimes.data(), EIKX_HOST));
     p.haveField = true;
+    p.interpolate();
+}
+
+template <class T> void Solver3D<T>::computeTravelTimeGradientField()
+{
+    if (!haveTravelTimeField()) throw std::runtime_error("Travel time field not yet computed");
+    auto &p = *pImpl;
+    p.gradient.resize(3 * p.travelTimes.size());
+    Detail::check(eikx_gradient3d(p.gpu.get(), 0, p.gradient.data(), EIKX_HOST));
+    p.haveGradient = true;
+}
+
+template <class T> std::vector<T> Solver3D<T>::getTravelTimesAtStations() const
+{
+    if (!haveTravelTimeField()) throw std::runtime_error("Travel time field not yet computed");
+    return pImpl->stationTimes;
 }
 
 template <class T> std::vector<T> Solver3D<T>::getTravelTimeField() const { return pImpl->travelTimes; }
@@ -176,14 +208,16 @@ template <class T> const T *Solver3D<T>::getTravelTimeFieldPointer() const
     return pImpl->travelTimes.data();
 }
 template <class T> bool Solver3D<T>::haveTravelTimeField() const noexcept { return pImpl->haveField; }
-template <class T> bool Solver3D<T>::haveTravelTimeGradientField() const noexcept { return false; }
+template <class T> bool Solver3D<T>::haveTravelTimeGradientField() const noexcept { return pImpl->haveGradient; }
 template <class T> std::vector<T> Solver3D<T>::getTravelTimeGradientField() const
 {
-    throw std::runtime_error("Travel time gradient field not computed");
+    if (!haveTravelTimeGradientField()) throw std::runtime_error("Travel time gradient field not computed");
+    return pImpl->gradient;
 }
 template <class T> const T *Solver3D<T>::getTravelTimeGradientFieldPointer() const
 {
-    throw std::runtime_error("Travel time gradient field not computed");
+    if (!haveTravelTimeGradientField()) throw std::runtime_error("Travel time gradient field not computed");
+    return pImpl->gradient.data();
 }
 
 template class EikonalXX::Solver3D<double>;

@@ -164,6 +164,15 @@ struct eikx_ctx {
     Workspace ws;
     BatchWorkspace bw;
     std::map<TuneKey, eikx_tuning> tuning;   // eikx_autotune3d results per grid class
+    // the last eikx_solve3d / eikx_solve2d: its fields stay in ws.tt (row pitch Px)
+    struct {
+        bool valid = false;
+        int dim = 0, precision = -1, nSrc = 0, nx = 0, ny = 0, nz = 0, Px = 0;
+        long long fieldStride = 0;
+        double dx = 0, dy = 0, dz = 0, x0 = 0, y0 = 0, z0 = 0;
+        std::vector<eikx::Corner3> corners;      // source cell, offsets, source-cell slowness
+    } last;
+    DevBuf postBuf;                          // gradient / station staging
     DevBuf tuneOut;                          // fields written while tuning
     eikx_stats stats{};
     // cached schedule graph
@@ -616,7 +625,17 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     s.kernel_launches = launches;
     s.device_ms = ms;
     c->stats = s;
+    c->last.valid = false;
     if (aborted) return fail(EIKX_ERR_TIMEOUT, "a bounded inter-tile wait ran out; the fields are not valid");
+    c->last.valid = true;
+    c->last.dim = DIM;
+    c->last.precision = P;
+    c->last.nSrc = nSrc;
+    c->last.nx = nx; c->last.ny = ny; c->last.nz = nz; c->last.Px = Px;
+    c->last.fieldStride = fieldStride;
+    c->last.dx = dx; c->last.dy = dy; c->last.dz = dz;
+    c->last.x0 = x0; c->last.y0 = y0; c->last.z0 = z0;
+    c->last.corners = corners;
     return EIKX_OK;
 }
 
@@ -1361,6 +1380,96 @@ eikx_status eikx_tuning_load(eikx_ctx *c, const char *path) {
     }
     for (const auto &kv : add) c->tuning[kv.first] = kv.second;
     return EIKX_OK;
+}
+
+static eikx_status checkLast(const eikx_ctx *c, int dim, int field) {
+    if (eikx_status r = checkCtx(c); r) return r;
+    if (!c->last.valid || c->last.dim != dim)
+        return fail(EIKX_ERR_STATE, "Travel time field not yet computed");
+    if (field < 0 || field >= c->last.nSrc) return fail(EIKX_ERR_INVALID, "field index out of range");
+    return EIKX_OK;
+}
+
+static eikx_status gradientImpl(eikx_ctx *c, int dim, int field, void *grad, int where) {
+    if (eikx_status r = checkLast(c, dim, field); r) return r;
+    if (!grad) return fail(EIKX_ERR_INVALID, "gradient output is NULL");
+    if (where != EIKX_HOST && where != EIKX_DEVICE) return fail(EIKX_ERR_INVALID, "where must be EIKX_HOST or EIKX_DEVICE");
+    EIKX_CUDA(cudaSetDevice(c->device));
+    const auto &L = c->last;
+    const size_t nodes = static_cast<size_t>(L.nx) * L.ny * L.nz;
+    const size_t elem = L.precision == EIKX_F32 ? 4 : 8;
+    const size_t bytes = nodes * dim * elem;
+    void *dst = grad;
+    if (where == EIKX_HOST) {
+        EIKX_CUDA(c->postBuf.ensure(bytes));
+        dst = c->postBuf.p;
+    }
+    if (L.precision == EIKX_F32)
+        EIKX_CUDA(eikx::launchGradient<float>(c->ws.tt.as<float>() + field * L.fieldStride, dim, L.Px, L.nx, L.ny, L.nz,
+                                              L.dx, L.dy, L.dz, L.corners[field], static_cast<float *>(dst), c->stream));
+    else
+        EIKX_CUDA(eikx::launchGradient<double>(c->ws.tt.as<double>() + field * L.fieldStride, dim, L.Px, L.nx, L.ny,
+                                               L.nz, L.dx, L.dy, L.dz, L.corners[field], static_cast<double *>(dst),
+                                               c->stream));
+    if (where == EIKX_HOST) EIKX_CUDA(cudaMemcpyAsync(grad, dst, bytes, cudaMemcpyDeviceToHost, c->stream));
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));
+    return EIKX_OK;
+}
+
+static eikx_status stationsImpl(eikx_ctx *c, int dim, int field, const double *xyz, int n, double *times) {
+    if (eikx_status r = checkLast(c, dim, field); r) return r;
+    if (n < 0 || (n > 0 && (!xyz || !times))) return fail(EIKX_ERR_INVALID, "stations or output is NULL");
+    if (n == 0) return EIKX_OK;
+    EIKX_CUDA(cudaSetDevice(c->device));
+    const auto &L = c->last;
+    std::vector<int> cells(static_cast<size_t>(n) * dim);
+    std::vector<double> offs(static_cast<size_t>(n) * dim);
+    for (int i = 0; i < n; ++i) {
+        int cx, cy = 0, cz;
+        double ox, oy = 0, oz;
+        const double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        if (!locate(x, L.x0, L.dx, L.nx, &cx, &ox) || (dim == 3 && !locate(y, L.y0, L.dy, L.ny, &cy, &oy)) ||
+            !locate(z, L.z0, L.dz, L.nz, &cz, &oz))
+            return fail(EIKX_ERR_INVALID, "station " + std::to_string(i) + " lies outside the grid");
+        if (dim == 3) {
+            cells[3 * i] = cx; cells[3 * i + 1] = cy; cells[3 * i + 2] = cz;
+            offs[3 * i] = ox; offs[3 * i + 1] = oy; offs[3 * i + 2] = oz;
+        } else {
+            cells[2 * i] = cx; cells[2 * i + 1] = cz;
+            offs[2 * i] = ox; offs[2 * i + 1] = oz;
+        }
+    }
+    const size_t cb = cells.size() * sizeof(int), ob = offs.size() * sizeof(double), tb = static_cast<size_t>(n) * 8;
+    EIKX_CUDA(c->postBuf.ensure(cb + ob + tb + 32));
+    char *base = static_cast<char *>(c->postBuf.p);
+    int *dCells = reinterpret_cast<int *>(base);
+    double *dOffs = reinterpret_cast<double *>(base + (cb + 15) / 16 * 16);
+    double *dOut = dOffs + offs.size();
+    EIKX_CUDA(cudaMemcpyAsync(dCells, cells.data(), cb, cudaMemcpyHostToDevice, c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(dOffs, offs.data(), ob, cudaMemcpyHostToDevice, c->stream));
+    if (L.precision == EIKX_F32)
+        EIKX_CUDA(eikx::launchStations<float>(c->ws.tt.as<float>() + field * L.fieldStride, dim, L.Px, L.ny, L.dx, L.dy,
+                                              L.dz, L.corners[field], n, dCells, dOffs, dOut, c->stream));
+    else
+        EIKX_CUDA(eikx::launchStations<double>(c->ws.tt.as<double>() + field * L.fieldStride, dim, L.Px, L.ny, L.dx,
+                                               L.dy, L.dz, L.corners[field], n, dCells, dOffs, dOut, c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(times, dOut, tb, cudaMemcpyDeviceToHost, c->stream));
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));
+    return EIKX_OK;
+}
+
+eikx_status eikx_gradient3d(eikx_ctx *c, int field, void *grad, int where) { return gradientImpl(c, 3, field, grad, where); }
+eikx_status eikx_gradient2d(eikx_ctx *c, int field, void *grad, int where) { return gradientImpl(c, 2, field, grad, where); }
+
+eikx_status eikx_station_times3d(eikx_ctx *c, int field, const eikx_source3d *st, int n, double *times) {
+    std::vector<double> xyz(3 * static_cast<size_t>(std::max(n, 0)));
+    for (int i = 0; i < n && st; ++i) { xyz[3 * i] = st[i].x; xyz[3 * i + 1] = st[i].y; xyz[3 * i + 2] = st[i].z; }
+    return stationsImpl(c, 3, field, st ? xyz.data() : nullptr, n, times);
+}
+eikx_status eikx_station_times2d(eikx_ctx *c, int field, const eikx_source2d *st, int n, double *times) {
+    std::vector<double> xyz(3 * static_cast<size_t>(std::max(n, 0)));
+    for (int i = 0; i < n && st; ++i) { xyz[3 * i] = st[i].x; xyz[3 * i + 1] = 0; xyz[3 * i + 2] = st[i].z; }
+    return stationsImpl(c, 2, field, st ? xyz.data() : nullptr, n, times);
 }
 
 eikx_status eikx_solve2d(eikx_ctx *c, const eikx_source2d *src, int nSrc, const eikx_options *opt, int precision,

@@ -163,6 +163,14 @@ cudaError_t launchResetState(const SolveState &st, int nFields, int buf, cudaStr
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st);
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,
                                    int iteration, double tol, cudaStream_t s);
+// Products of a solved field (post.cu): the travel-time gradient (3 or 2 values per
+// natural node) and travel times at stations (cells and origin offsets per station).
+template <class T>
+cudaError_t launchGradient(const T *tt, int dim, int Px, int nx, int ny, int nz, double dx, double dy, double dz,
+                           const Corner3 &src, T *grad, cudaStream_t s);
+template <class T>
+cudaError_t launchStations(const T *tt, int dim, int Px, int ny, double dx, double dy, double dz, const Corner3 &src,
+                           int n, const int *cells, const double *offs, double *out, cudaStream_t s);
 cudaError_t launchAnalytic3(double *t, int nx, int ny, int nz, double dx, double dy, double dz,
                             double xs, double ys, double zs, double vTop, double vBottom, cudaStream_t s);
 cudaError_t launchAnalytic2(double *t, int nx, int nz, double dx, double dz, double xs, double zs,

@@ -50,6 +50,14 @@ public:
     [[nodiscard]] std::vector<T> getTravelTimeGradientField() const override;
     [[nodiscard]] const T *getTravelTimeGradientFieldPointer() const override;
     [[nodiscard]] bool haveTravelTimeGradientField() const noexcept override;
+    /// Computes the gradient of the solved field on the GPU: (dT/dx, dT/dy, dT/dz) per node,
+    /// natural order.  Central differences inside, second-order one-sided differences on
+    /// the faces, the analytic gradient at the source cell's corners.  An addition: the
+    /// reference declares the gradient getters but never computes the field.
+    void computeTravelTimeGradientField();
+    /// Travel times at the stations of setStations(): trilinear interpolation of the solved
+    /// field, the straight-ray time in the source cell.  An addition, as for the gradient.
+    [[nodiscard]] std::vector<T> getTravelTimesAtStations() const;
     void clear() noexcept;
 private:
     class Solver3DImpl;

@@ -141,6 +141,28 @@ eikx_status eikx_solve3d(eikx_ctx *ctx, const eikx_source3d *src, int n_src,
                          const eikx_options *opt, int precision, void *t_out, int where);
 
 /* ---- 2D ---------------------------------------------------------------- */
+/* ---- products of the last solve ---------------------------------------- */
+
+/* Travel-time gradient of field `field` (0-based source index) of the last eikx_solve3d /
+ * eikx_solve2d on this context, in that solve's precision, natural node order,
+ * interleaved per node: (dT/dx, dT/dy, dT/dz) in 3D, (dT/dx, dT/dz) in 2D.  Replaces
+ * Solver2D::computeTravelTimeGradientField (src/solver2d.cpp:865-879) with the
+ * reference's central-difference scheme (src/gradient.hpp:20-289): central differences
+ * inside, second-order one-sided differences on the first and last node of each axis,
+ * the analytic constant-slowness gradient at the corners of the source cell; the 3D
+ * gradient, declared but never computed by the reference's Solver3D, applies the same
+ * rule per axis.  grad: 3 (2) * nodes values, host or device (where). */
+eikx_status eikx_gradient3d(eikx_ctx *ctx, int field, void *grad, int where);
+eikx_status eikx_gradient2d(eikx_ctx *ctx, int field, void *grad, int where);
+
+/* Travel times of field `field` of the last solve at stations given by their positions
+ * (m): a station in the source cell gets |x - x_s| * s_src, any other the trilinear (3D:
+ * x, then y, then z) / bilinear (2D) interpolation of its cell's corner times, in FP64.
+ * Replaces Solver2D::interpolateTravelTimes (src/solver2d.cpp:106-167); the reference's
+ * Solver3D stores stations but computes no times.  times: n host doubles. */
+eikx_status eikx_station_times3d(eikx_ctx *ctx, int field, const eikx_source3d *stations, int n, double *times);
+eikx_status eikx_station_times2d(eikx_ctx *ctx, int field, const eikx_source2d *stations, int n, double *times);
+
 /* ---- autotuning ---------------------------------------------------------- */
 
 /* The configuration eikx_autotune3d chose for one grid class. */

@@ -81,6 +81,50 @@ class Oracle:
                                           _d(v_bottom), _P(t))
         return t.reshape(nz, nx)
 
+    def gradient3d(self, tt, grid, src_cell, src_off, slow0):
+        """Central-difference gradient (nz, ny, nx, 3) of a solved field (src/gradient.hpp)."""
+        nx, ny, nz, dx, dy, dz = grid
+        tt = np.ascontiguousarray(tt)
+        g = np.zeros(tt.size * 3, tt.dtype)
+        f = self.lib.oracle_gradient3d_f64 if tt.dtype == np.float64 else self.lib.oracle_gradient3d_f32
+        cv = ctypes.c_double if tt.dtype == np.float64 else ctypes.c_float
+        f(nx, ny, nz, _d(dx), _d(dy), _d(dz), int(src_cell[0]), int(src_cell[1]), int(src_cell[2]),
+          _d(src_off[0]), _d(src_off[1]), _d(src_off[2]), cv(slow0), _P(tt), _P(g))
+        return g.reshape(nz, ny, nx, 3)
+
+    def gradient2d(self, tt, grid, src_cell, src_off, slow0):
+        nx, nz, dx, dz = grid
+        tt = np.ascontiguousarray(tt)
+        g = np.zeros(tt.size * 2, tt.dtype)
+        f = self.lib.oracle_gradient2d_f64 if tt.dtype == np.float64 else self.lib.oracle_gradient2d_f32
+        cv = ctypes.c_double if tt.dtype == np.float64 else ctypes.c_float
+        f(nx, nz, _d(dx), _d(dz), int(src_cell[0]), int(src_cell[1]), _d(src_off[0]), _d(src_off[1]), cv(slow0),
+          _P(tt), _P(g))
+        return g.reshape(nz, nx, 2)
+
+    def stations3d(self, tt, grid, src_cell, src_off, s_src, cells, offs):
+        nx, ny, nz, dx, dy, dz = grid
+        tt = np.ascontiguousarray(tt)
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        offs = np.ascontiguousarray(offs, dtype=np.float64)
+        out = np.zeros(len(cells), np.float64)
+        self.lib.oracle_stations3d(0 if tt.dtype == np.float32 else 1, nx, ny, nz, _d(dx), _d(dy), _d(dz),
+                                   int(src_cell[0]), int(src_cell[1]), int(src_cell[2]), _d(src_off[0]),
+                                   _d(src_off[1]), _d(src_off[2]), _d(s_src), _P(tt), len(cells), _P(cells),
+                                   _P(offs), _P(out))
+        return out
+
+    def stations2d(self, tt, grid, src_cell, src_off, s_src, cells, offs):
+        nx, nz, dx, dz = grid
+        tt = np.ascontiguousarray(tt)
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        offs = np.ascontiguousarray(offs, dtype=np.float64)
+        out = np.zeros(len(cells), np.float64)
+        self.lib.oracle_stations2d(0 if tt.dtype == np.float32 else 1, nx, nz, _d(dx), _d(dz), int(src_cell[0]),
+                                   int(src_cell[1]), _d(src_off[0]), _d(src_off[1]), _d(s_src), _P(tt), len(cells),
+                                   _P(cells), _P(offs), _P(out))
+        return out
+
     def nodal_to_cell3d(self, v, nx, ny, nz, ordering=0):
         v = np.ascontiguousarray(v)
         s = np.zeros((nx - 1) * (ny - 1) * (nz - 1), v.dtype)

@@ -985,6 +985,122 @@ void nodalToCell2(int nx, int nz, const T *v, int ordering, T *slow) {
 //----------------------------------------------------------------------------//
 //                                 C entry points                             //
 //----------------------------------------------------------------------------//
+//----------------------------------------------------------------------------//
+//                 Products of a solved field: gradient, stations             //
+//----------------------------------------------------------------------------//
+
+// Travel-time gradient of a solved field, the reference's 2D finiteDifference with
+// central differences (src/gradient.hpp:20-289): interior nodes (u[i+1] - u[i-1]) / 2h,
+// the first and last node of an axis the second-order one-sided differences
+// (-3 u0 + 4 u1 - u2) / 2h and (u[n-3] - 4 u[n-2] + 3 u[n-1]) / 2h, and -- when the
+// source is off the cell corner by more than 1e-7 m -- the analytic constant-slowness
+// gradient at the corners of the source cell.  The 3D form applies the same rule per
+// axis and at the 8 corners.  Output interleaved per node: (d/dx, d/dz) or (d/dx, d/dy, d/dz).
+template <class T>
+T axisDerivative(const T *t, size_t i, size_t stride, int k, int n, T twodi) {
+    if (k == 0) return (-3 * t[i] + 4 * t[i + stride] - t[i + 2 * stride]) * twodi;
+    if (k == n - 1) return (t[i - 2 * stride] - 4 * t[i - stride] + 3 * t[i]) * twodi;
+    return (t[i + stride] - t[i - stride]) * twodi;
+}
+
+template <class T>
+void gradient3(const Grid3 &g, const Src3 &src, T slow0, const T *t, T *grad) {
+    const T twodxi = static_cast<T>(1. / (2. * g.dx));
+    const T twodyi = static_cast<T>(1. / (2. * g.dy));
+    const T twodzi = static_cast<T>(1. / (2. * g.dz));
+    const size_t sx = 1, sy = g.nx, sz = static_cast<size_t>(g.nx) * g.ny;
+    for (int iz = 0; iz < g.nz; ++iz)
+        for (int iy = 0; iy < g.ny; ++iy)
+            for (int ix = 0; ix < g.nx; ++ix) {
+                const size_t i = iz * sz + iy * sy + ix;
+                grad[3 * i] = axisDerivative(t, i, sx, ix, g.nx, twodxi);
+                grad[3 * i + 1] = axisDerivative(t, i, sy, iy, g.ny, twodyi);
+                grad[3 * i + 2] = axisDerivative(t, i, sz, iz, g.nz, twodzi);
+            }
+    constexpr double tol = 1.e-7;
+    const double d0[3] = {src.isx * g.dx - src.xo, src.isy * g.dy - src.yo, src.isz * g.dz - src.zo};
+    const double d1[3] = {(src.isx + 1) * g.dx - src.xo, (src.isy + 1) * g.dy - src.yo, (src.isz + 1) * g.dz - src.zo};
+    const bool doAxis[3] = {std::abs(d0[0]) > tol, std::abs(d0[1]) > tol, std::abs(d0[2]) > tol};
+    if (!(doAxis[0] || doAxis[1] || doAxis[2])) return;
+    for (int k = 0; k < 2; ++k)
+        for (int j = 0; j < 2; ++j)
+            for (int i = 0; i < 2; ++i) {
+                const double a = i ? d1[0] : d0[0], b = j ? d1[1] : d0[1], c = k ? d1[2] : d0[2];
+                const double r = std::sqrt(a * a + b * b + c * c);
+                const size_t n = (src.isz + k) * sz + (src.isy + j) * sy + (src.isx + i);
+                if (doAxis[0]) grad[3 * n] = static_cast<T>((a / r) * slow0);
+                if (doAxis[1]) grad[3 * n + 1] = static_cast<T>((b / r) * slow0);
+                if (doAxis[2]) grad[3 * n + 2] = static_cast<T>((c / r) * slow0);
+            }
+}
+
+template <class T>
+void gradient2(const Grid2 &g, const Src2 &src, T slow0, const T *t, T *grad) {
+    const T twodxi = static_cast<T>(1. / (2. * g.dx));
+    const T twodzi = static_cast<T>(1. / (2. * g.dz));
+    for (int iz = 0; iz < g.nz; ++iz)
+        for (int ix = 0; ix < g.nx; ++ix) {
+            const size_t i = static_cast<size_t>(iz) * g.nx + ix;
+            grad[2 * i] = axisDerivative(t, i, 1, ix, g.nx, twodxi);
+            grad[2 * i + 1] = axisDerivative(t, i, g.nx, iz, g.nz, twodzi);
+        }
+    constexpr double tol = 1.e-7;
+    const double dx0 = src.isx * g.dx - src.xo, dx1 = (src.isx + 1) * g.dx - src.xo;
+    const double dz0 = src.isz * g.dz - src.zo, dz1 = (src.isz + 1) * g.dz - src.zo;
+    const bool doX = std::abs(dx0) > tol, doZ = std::abs(dz0) > tol;
+    if (!(doX || doZ)) return;
+    for (int k = 0; k < 2; ++k)
+        for (int i = 0; i < 2; ++i) {
+            const double a = i ? dx1 : dx0, c = k ? dz1 : dz0;
+            const double r = std::sqrt(a * a + c * c);
+            const size_t n = static_cast<size_t>(src.isz + k) * g.nx + (src.isx + i);
+            if (doX) grad[2 * n] = static_cast<T>((a / r) * slow0);
+            if (doZ) grad[2 * n + 1] = static_cast<T>((c / r) * slow0);
+        }
+}
+
+// Travel times at stations (Solver2D::interpolateTravelTimes, src/solver2d.cpp:106-167,
+// with bilinear() of src/ray/bilinear.hpp): a station in the source cell gets the
+// straight-ray time |x - x_s| * s_src; any other station the bilinear (2D) / trilinear
+// (3D, x then y then z) interpolation of the 4 / 8 corner times of its cell, in double.
+// Stations are located as sources are: offset = x - x0, cell = min(nCell - 1, offset / d).
+template <class T>
+double station3(const Grid3 &g, const Src3 &src, double sSrc, const T *t, int cx, int cy, int cz, double xi,
+                double yi, double zi) {
+    if (cx == src.isx && cy == src.isy && cz == src.isz) {
+        const double a = xi - src.xo, b = yi - src.yo, c = zi - src.zo;
+        return std::sqrt(a * a + b * b + c * c) * sSrc;
+    }
+    const size_t sy = g.nx, sz = static_cast<size_t>(g.nx) * g.ny;
+    const size_t i0 = cz * sz + cy * sy + cx;
+    auto f = [&](int i, int j, int k) { return static_cast<double>(t[i0 + k * sz + j * sy + i]); };
+    const double dxi = 1. / g.dx, dyi = 1. / g.dy, dzi = 1. / g.dz;
+    const double x1 = cx * g.dx, x2 = (cx + 1) * g.dx, y1 = cy * g.dy, y2 = (cy + 1) * g.dy;
+    const double z1 = cz * g.dz, z2 = (cz + 1) * g.dz;
+    const double x2mx = x2 - xi, xmx1 = xi - x1;
+    const double f11 = dxi * (x2mx * f(0, 0, 0) + xmx1 * f(1, 0, 0));
+    const double f21 = dxi * (x2mx * f(0, 1, 0) + xmx1 * f(1, 1, 0));
+    const double f12 = dxi * (x2mx * f(0, 0, 1) + xmx1 * f(1, 0, 1));
+    const double f22 = dxi * (x2mx * f(0, 1, 1) + xmx1 * f(1, 1, 1));
+    const double y2my = y2 - yi, ymy1 = yi - y1;
+    const double fz1 = dyi * (y2my * f11 + ymy1 * f21);
+    const double fz2 = dyi * (y2my * f12 + ymy1 * f22);
+    return dzi * ((z2 - zi) * fz1 + (zi - z1) * fz2);
+}
+
+template <class T>
+double station2(const Grid2 &g, const Src2 &src, double sSrc, const T *t, int cx, int cz, double xi, double zi) {
+    if (cx == src.isx && cz == src.isz) return eikxHypot(xi - src.xo, zi - src.zo) * sSrc;
+    const size_t i00 = static_cast<size_t>(cz) * g.nx + cx;
+    const double f00 = t[i00], f10 = t[i00 + 1], f01 = t[i00 + g.nx], f11 = t[i00 + g.nx + 1];
+    const double dxi = 1. / g.dx, dzi = 1. / g.dz;
+    const double x1 = cx * g.dx, x2 = (cx + 1) * g.dx, z1 = cz * g.dz, z2 = (cz + 1) * g.dz;
+    const double x2mx = x2 - xi, xmx1 = xi - x1;
+    const double fxz1 = dxi * (x2mx * f00 + xmx1 * f10);
+    const double fxz2 = dxi * (x2mx * f01 + xmx1 * f11);
+    return dzi * ((z2 - zi) * fxz1 + (zi - z1) * fxz2);
+}
+
 extern "C" {
 
 int oracle_solve3d_f64(int nx, int ny, int nz, double dx, double dy, double dz, int isx,
@@ -1071,4 +1187,51 @@ double oracle_hypot(double a, double b) { return eikxHypot(a, b); }
 // 0: the 2D analytic times use std::hypot (as the reference); 1: eikxHypot (as the GPU).
 void oracle_set_hypot_mode(int mode) { gHypotMode = mode; }
 
+
+int oracle_gradient3d_f32(int nx, int ny, int nz, double dx, double dy, double dz, int isx, int isy, int isz,
+                          double xo, double yo, double zo, float slow0, const float *tt, float *grad) {
+    gradient3<float>(Grid3{nx, ny, nz, dx, dy, dz}, Src3{isx, isy, isz, xo, yo, zo}, slow0, tt, grad);
+    return 0;
+}
+int oracle_gradient3d_f64(int nx, int ny, int nz, double dx, double dy, double dz, int isx, int isy, int isz,
+                          double xo, double yo, double zo, double slow0, const double *tt, double *grad) {
+    gradient3<double>(Grid3{nx, ny, nz, dx, dy, dz}, Src3{isx, isy, isz, xo, yo, zo}, slow0, tt, grad);
+    return 0;
+}
+int oracle_gradient2d_f32(int nx, int nz, double dx, double dz, int isx, int isz, double xo, double zo, float slow0,
+                          const float *tt, float *grad) {
+    gradient2<float>(Grid2{nx, nz, dx, dz}, Src2{isx, isz, xo, zo}, slow0, tt, grad);
+    return 0;
+}
+int oracle_gradient2d_f64(int nx, int nz, double dx, double dz, int isx, int isz, double xo, double zo, double slow0,
+                          const double *tt, double *grad) {
+    gradient2<double>(Grid2{nx, nz, dx, dz}, Src2{isx, isz, xo, zo}, slow0, tt, grad);
+    return 0;
+}
+// Station times; stations given as (cell x, cell y, cell z) and offsets from the origin.
+int oracle_stations3d(int precision, int nx, int ny, int nz, double dx, double dy, double dz, int isx, int isy, int isz,
+                      double xo, double yo, double zo, double sSrc, const void *tt, int n, const int *cells,
+                      const double *offs, double *out) {
+    Grid3 g{nx, ny, nz, dx, dy, dz};
+    Src3 s{isx, isy, isz, xo, yo, zo};
+    for (int i = 0; i < n; ++i)
+        out[i] = precision == 0
+            ? station3<float>(g, s, sSrc, static_cast<const float *>(tt), cells[3 * i], cells[3 * i + 1],
+                              cells[3 * i + 2], offs[3 * i], offs[3 * i + 1], offs[3 * i + 2])
+            : station3<double>(g, s, sSrc, static_cast<const double *>(tt), cells[3 * i], cells[3 * i + 1],
+                               cells[3 * i + 2], offs[3 * i], offs[3 * i + 1], offs[3 * i + 2]);
+    return 0;
+}
+int oracle_stations2d(int precision, int nx, int nz, double dx, double dz, int isx, int isz, double xo, double zo,
+                      double sSrc, const void *tt, int n, const int *cells, const double *offs, double *out) {
+    Grid2 g{nx, nz, dx, dz};
+    Src2 s{isx, isz, xo, zo};
+    for (int i = 0; i < n; ++i)
+        out[i] = precision == 0
+            ? station2<float>(g, s, sSrc, static_cast<const float *>(tt), cells[2 * i], cells[2 * i + 1],
+                              offs[2 * i], offs[2 * i + 1])
+            : station2<double>(g, s, sSrc, static_cast<const double *>(tt), cells[2 * i], cells[2 * i + 1],
+                               offs[2 * i], offs[2 * i + 1]);
+    return 0;
+}
 }  // extern "C"
