@@ -34,6 +34,7 @@ NX, NY, NZ, H = 256, 256, 128, 50.0
 MODEL_SEED, SOURCE_SEED = 20240601, 7
 N_SWEEPS_MAX, TOL, RADIUS = 10, 1e-5, 3
 SURFACE = [False]  # sources on the top surface (station tables by reciprocity)
+SLAB = [False]     # layered + GRF model with a dipping high-velocity slab (full-scale workload)
 PAIR = [False]  # pair_fields option of the GPU arm (set from the command line)
 KERNEL = [0]    # sweep_kernel option of the GPU arm: 0 default, 1 node-step, 2 chunk-step
 L2_BYTES = 129 * 2 ** 20
@@ -115,7 +116,8 @@ class ClockSampler:
 
 def make_workload(fields):
     from eikonalxx_gb300 import synthetic
-    v = synthetic.layered_grf_model(NX, NY, NZ, H, MODEL_SEED)
+    v = (synthetic.slab_model(NX, NY, NZ, H, MODEL_SEED) if SLAB[0] else
+         synthetic.layered_grf_model(NX, NY, NZ, H, MODEL_SEED))
     src = synthetic.uniform_sources(fields, NX, NY, NZ, H, SOURCE_SEED, surface=SURFACE[0])
     return v, src
 
@@ -164,6 +166,20 @@ def run_gpu(args):
         d = np.abs(t32 - t64)
         acc = {"max_err_vs_fp64_s": float(d.max()), "rms_err_vs_fp64_s": float(np.sqrt(np.mean(d ** 2))),
                "fp64_iterations": ctx.stats()["iterations_max"]}
+        if not SLAB[0]:
+            # against closed forms on the same grid: constant velocity, and a linear gradient
+            # from the top to the bottom of the grid (nodal model, one source)
+            for name, (vt, vb) in {"constant_velocity_5000": (5000.0, 5000.0),
+                                   "linear_gradient_3000_7000": (3000.0, 7000.0)}.items():
+                vz = vt + (vb - vt) * np.arange(NZ) / (NZ - 1)
+                vm = np.ascontiguousarray(np.broadcast_to(vz[:, None, None], (NZ, NY, NX)), dtype=np.float32)
+                ctx.set_nodal_velocity3d(vm)
+                ta = ctx.analytic3d(src[0], vt, vb)
+                e32 = np.abs(ctx.solve3d(src[:1], opt, ex.F32)[0].astype(np.float64) - ta)
+                e64 = np.abs(ctx.solve3d(src[:1], o64, ex.F64)[0] - ta)
+                acc[name] = {"fp32_max_s": float(e32.max()), "fp32_rms_s": float(np.sqrt(np.mean(e32 ** 2))),
+                             "fp64_max_s": float(e64.max()), "fp64_rms_s": float(np.sqrt(np.mean(e64 ** 2)))}
+            ctx.set_nodal_velocity3d(v_host)
 
     for _ in range(args.warmup):
         step_device()
@@ -226,7 +242,9 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered+GRF model, seeded sources)",
-        "config": {"workload": (f"station tables, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, {fields} sources on the "
+        "config": {"workload": (f"full scale, {NX}x{NY}x{NZ} h={H:g} m layered+GRF with an 8000 m/s slab dipping 30 "
+                                f"degrees, {fields} sources on the top surface per step per GPU" if SLAB[0] else
+                                f"station tables, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, {fields} sources on the "
                                 f"top surface per step per GPU, one persistent launch per sweep" if SURFACE[0] else
                                 f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, "
                                 f"{fields} independent sources per step per GPU"),
@@ -339,6 +357,92 @@ def run_models(args):
                 "d2h_bytes_per_step": int(4 * nodes), "ms_per_step": float(np.mean(e2e_ms))},
         "gpu_launches": int(launches), "clocks": clk.summary(),
         "iterations": {"max": int(max(iters)), "min": int(min(iters))}, "accuracy": acc,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_2d(args):
+    """The reference's plain 2D configuration: FP64, 501 x 251 nodes, dx = dz = 10 m,
+    v(z) = 3000 m/s + 0.5 s^-1 z, source at (2500 m, 500 m), factored radius 3, 2 sweep
+    iterations, tolerance 1e-8 s.  Errors against the analytic linear-gradient times and
+    the CPU oracle (the reference's 2D fast sweeping restated, bit-identical to it)."""
+    import torch
+    import eikonalxx_gb300 as ex
+    from eikonalxx_gb300 import synthetic
+    from oracle import Oracle
+
+    nx, nz, h = 501, 251, 10.0
+    src = (2500.0, 500.0)
+    v = synthetic.linear_gradient_2d(nx, nz, h, 3000.0, 0.5)
+    dev = torch.cuda.current_device()
+    ctx = ex.Context(dev)
+    ctx.set_grid2d(nx, nz, h, h)
+    ctx.set_nodal_velocity2d(v)
+    opt = ex.Options(n_sweeps=2, tolerance=1e-8, factored_radius=3)
+    fields = args.fields
+    srcs = [src] * fields
+    out_dev = torch.empty((fields, nz, nx), dtype=torch.float64, device=f"cuda:{dev}")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    t = ctx.solve2d([src], opt, ex.F64)[0]
+    ta = ctx.analytic2d(src, 3000.0, 3000.0 + 0.5 * (nz - 1) * h)
+    orc = Oracle()
+    s_cells = orc.nodal_to_cell2d(v.ravel(), nx, nz, 0)
+    cell = (min(nx - 2, int(src[0] / h)), min(nz - 2, int(src[1] / h)))
+    t0 = time.perf_counter()
+    t_or = orc.solve2d(s_cells, (nx, nz, h, h), cell, src, n_sweeps=2, radius=3, tol=1e-8)
+    cpu_s = time.perf_counter() - t0
+    e = np.abs(t - ta)
+    acc = {"max_err_vs_analytic_s": float(e.max()), "rms_err_vs_analytic_s": float(np.sqrt(np.mean(e ** 2))),
+           "max_abs_diff_vs_oracle_s": float(np.abs(t - t_or).max()),
+           "bit_identical_to_oracle": bool(np.array_equal(t.view(np.uint64), t_or.view(np.uint64)))}
+
+    for _ in range(args.warmup):
+        ctx.solve2d(srcs, opt, ex.F64, out=out_dev)
+    torch.cuda.synchronize()
+    per, launches, iters = [], 0, []
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            ctx.solve2d(srcs, opt, ex.F64, out=out_dev)
+            st = ctx.stats()
+            per.append(st["device_ms"])
+            launches += st["kernel_launches"]
+            iters.append(st["iterations_max"])
+    ms = float(np.mean(per))
+    prof = ex.Options(n_sweeps=2, tolerance=1e-8, factored_radius=3, profile_sweeps=True)
+    ctx.solve2d(srcs, prof, ex.F64, out=out_dev)
+    pst = ctx.stats()
+    launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
+    bpl = 24 * nx * nz * fields
+    peak, peak_kind = _peaks()
+    e2e_ms = []
+    out_host = torch.empty((fields, nz, nx), dtype=torch.float64).pin_memory()
+    v_host = torch.from_numpy(v).pin_memory()
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        ctx.set_nodal_velocity2d(v_host)
+        ctx.solve2d(srcs, opt, ex.F64, out=out_host)
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    line = {
+        "metric": "2D travel-time grids/s (FP64) at the reference's plain 2D configuration", "value": fields / (ms / 1e3),
+        "unit": "grids/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (analytic linear-gradient model)",
+        "config": {"workload": f"plain 2D solve, {nx}x{nz} h={h:g} m, v(z)=3000+0.5z m/s, source (2500, 500) m, "
+                               f"{fields} field(s) per step", "factored_radius": 3, "n_sweeps": 2, "tolerance_s": 1e-8,
+                   "l2": "flushed (write of 2x L2) between timed steps"},
+        "roofline": {"bound": "hbm", "kernel": "sweep2Kernel<double,uniform>", "achieved": bpl / (launch_ms / 1e3) / 1e9,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": bpl / (launch_ms / 1e3) / 1e9 / peak, "bytes_per_launch": bpl, "launch_ms": launch_ms,
+                     "traffic": None, "note": "one field of 126 k nodes: latency-bound wavefront (751 levels)"},
+        "e2e": {"value": fields / (float(np.mean(e2e_ms)) / 1e3), "unit": "grids/s", "h2d_bytes_per_step": int(v.nbytes),
+                "d2h_bytes_per_step": int(8 * nx * nz * fields), "ms_per_step": float(np.mean(e2e_ms))},
+        "gpu_launches": int(launches), "clocks": clk.summary(), "iterations": {"max": int(max(iters))},
+        "accuracy": acc,
+        "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "grids/s", "cores": 1, "kind": "port",
+                         "sample": "one full FP64 solve of the configuration by the CPU oracle"},
     }
     print(json.dumps(line), flush=True)
 
@@ -470,9 +574,10 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="plain", choices=["plain", "stations", "models"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "stations", "models", "full", "2d"],
                     help="plain: 256x256x128 h=50 m, independent sources; stations: 200x200x100 h=100 m, "
-                         "sources on the top surface; models: uneven models, one source each")
+                         "sources on the top surface; models: uneven models, one source each; full: "
+                         "512x512x256 h=25 m with a dipping slab, surface sources; 2d: 501x251 FP64")
     ap.add_argument("--fields", type=int, default=None,
                     help="sources (plain: 32, stations: 64) or models (models: 32) per step per GPU")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -493,8 +598,14 @@ def main():
     if args.workload == "stations":
         NX, NY, NZ, H = 200, 200, 100, 100.0
         SURFACE[0] = True
+    global N_SWEEPS_MAX
+    if args.workload == "full":
+        NX, NY, NZ, H = 512, 512, 256, 25.0
+        SURFACE[0] = True
+        SLAB[0] = True
+        N_SWEEPS_MAX = 20      # the slab model converges more slowly than 10 iterations
     if args.fields is None:
-        args.fields = 64 if args.workload == "stations" else 32
+        args.fields = {"stations": 64, "full": 256, "2d": 1}.get(args.workload, 32)
     PAIR[0] = args.pair_fields
     KERNEL[0] = args.sweep_kernel
     if args.profile_case:
@@ -506,6 +617,8 @@ def main():
         run_reference(args)
     elif args.workload == "models":
         run_models(args)
+    elif args.workload == "2d":
+        run_2d(args)
     else:
         run_gpu(args)
 

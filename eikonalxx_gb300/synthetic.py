@@ -60,3 +60,28 @@ def uneven_models(n, seed, h=100.0, nxy=(64, 256), nz=(32, 128), dtype=np.float3
         src = uniform_sources(1, gx, gy, gz, h, int(rng.integers(1 << 31)))[0]
         out.append({"grid": (gx, gy, gz, h, h, h), "v": v, "source": tuple(float(c) for c in src)})
     return out
+
+
+def slab_model(nx, ny, nz, h, seed, slab_v=8000.0, dip_deg=30.0, thickness_m=None, dtype=np.float32):
+    """Layered + GRF model with a high-velocity slab: nodes within thickness/2 of a plane
+    dipping `dip_deg` degrees along x (through a seeded point near the top centre) get
+    `slab_v`.  Nodal velocities (nz, ny, nx)."""
+    v = layered_grf_model(nx, ny, nz, h, seed, dtype=np.float64)
+    rng = np.random.default_rng(seed + 1)
+    x0 = rng.uniform(0.3, 0.5) * (nx - 1) * h
+    z0 = rng.uniform(0.05, 0.15) * (nz - 1) * h
+    thick = thickness_m if thickness_m is not None else 0.08 * (nz - 1) * h
+    dip = np.deg2rad(dip_deg)
+    z, _, x = np.meshgrid(np.arange(nz) * h, np.zeros(1), np.arange(nx) * h, indexing="ij", sparse=True)
+    # signed distance to the plane through (x0, z0) dipping along +x
+    d = (z - z0) * np.cos(dip) - (x - x0) * np.sin(dip)
+    mask = np.abs(d) <= thick / 2
+    v = np.where(np.broadcast_to(mask, v.shape), slab_v, v)
+    return np.ascontiguousarray(v, dtype=dtype)
+
+
+def linear_gradient_2d(nx, nz, h, v_top, gradient, dtype=np.float64):
+    """Nodal velocities (nz, nx) of v(z) = v_top + gradient * z, z = iz * h."""
+    z = np.arange(nz) * h
+    v = v_top + gradient * z
+    return np.ascontiguousarray(np.broadcast_to(v[:, None], (nz, nx)), dtype=dtype)

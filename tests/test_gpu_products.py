@@ -69,3 +69,19 @@ def test_products_need_a_solve(ctx):
         c.gradient3d(1)                                       # one field only
     with pytest.raises(ex.InvalidArgument):
         c.station_times3d([(100., 0., 0.)])                   # outside the grid
+
+
+@pytest.mark.parametrize("v_top,v_bottom", [(4000.0, 4000.0), (3000.0, 6000.0)])
+def test_analytic_fields_match_oracle(ctx, oracle, v_top, v_bottom):
+    """Closed-form constant-velocity and linear-gradient times (the accuracy references):
+    CUDA's acosh / sqrt / hypot against the C library's, a few ulps apart at most."""
+    grid3 = (41, 33, 29, 50., 50., 50.)
+    src3 = (812.5, 433.0, 610.0)
+    ctx.set_grid3d(*grid3)
+    g3 = ctx.analytic3d(src3, v_top, v_bottom)
+    assert np.allclose(g3, oracle.linear_gradient3d(grid3, src3, v_top, v_bottom), rtol=1e-13, atol=1e-15)
+    grid2 = (81, 43, 25., 25.)
+    src2 = (1010.0, 320.0)
+    ctx.set_grid2d(*grid2)
+    g2 = ctx.analytic2d(src2, v_top, v_bottom)
+    assert np.allclose(g2, oracle.linear_gradient2d(grid2, src2, v_top, v_bottom), rtol=1e-13, atol=1e-15)
