@@ -447,6 +447,58 @@ def run_2d(args):
     print(json.dumps(line), flush=True)
 
 
+def run_warmstart_study(args):
+    """Does a warm start save sweeps on this discretization?  Cold-start solves of the
+    plain workload, then warm starts (eikx_solve3d_warm) from the best predictions any
+    predictor could make: the cold-start result itself (exactly and inflated), and its
+    factor tau = T / T0 sampled every F nodes and upsampled, inflated.  Reports refinement
+    iterations, device time and the deviation from the cold-start fields, for factored
+    radius 3 (the reference default) and 0."""
+    import torch
+    import eikonalxx_gb300 as ex
+    from eikonalxx_gb300 import synthetic
+    from scipy.ndimage import zoom
+
+    v, src = make_workload(args.fields)
+    ctx = ex.Context(torch.cuda.current_device())
+    ctx.set_grid3d(NX, NY, NZ, H, H, H)
+    ctx.set_nodal_velocity3d(v.ravel())
+    cells = np.empty((NZ - 1) * (NY - 1) * (NX - 1), np.float64)
+    _check = ex._check
+    _check(ctx._lib.eikx_get_slowness3d(ctx._h, cells.ctypes.data, ex.F64))
+    cells = cells.reshape(NZ - 1, NY - 1, NX - 1)
+    z, y, x = np.meshgrid(np.arange(NZ) * H, np.arange(NY) * H, np.arange(NX) * H, indexing="ij", sparse=True)
+    T0 = []
+    for p in src:
+        c = [min(n - 2, int(q / H)) for q, n in zip(p, (NX, NY, NZ))]
+        T0.append(np.sqrt((x - p[0]) ** 2 + (y - p[1]) ** 2 + (z - p[2]) ** 2) * cells[c[2], c[1], c[0]])
+    T0 = np.stack(T0)
+    rows = []
+    for radius in (RADIUS, 0):
+        opt = ex.Options(n_sweeps=20, tolerance=TOL, factored_radius=radius)
+        cold = ctx.solve3d(src, opt, ex.F32)
+        cst = ctx.stats()
+        rows.append({"radius": radius, "start": "cold", "iterations": cst["iterations_max"],
+                     "device_ms": cst["device_ms"]})
+        tau = np.where(T0 > 0, cold / np.maximum(T0, 1e-12), 1.0)
+        starts = {"cold result x1.0": cold, "cold result x1.001": cold * 1.001}
+        for F in (2, 4):
+            tc = tau[:, ::F, ::F, ::F]
+            up = np.stack([zoom(t, (NZ / t.shape[0], NY / t.shape[1], NX / t.shape[2]), order=1) for t in tc])
+            starts[f"tau every {F} nodes, x1.01"] = T0 * up * 1.01
+        for name, init in starts.items():
+            out = ctx.solve3d_warm(src, np.ascontiguousarray(init, dtype=np.float32), opt, ex.F32,
+                                   gate_tol=1e9 if name.startswith("cold") else 1e-6)
+            st = ctx.stats()
+            d = out.astype(np.float64) - cold
+            rows.append({"radius": radius, "start": name, "iterations": st["iterations_max"],
+                         "device_ms": st["device_ms"], "reset_nodes": st["reset_nodes"],
+                         "max_below_cold_s": float(-d.min()), "max_above_cold_s": float(d.max()),
+                         "nodes_off_by_more_than_1e-4": int((np.abs(d) > 1e-4).sum())})
+    print(json.dumps({"study": "warm start on the plain workload", "fields": args.fields,
+                      "grid": [NX, NY, NZ], "rows": rows}), flush=True)
+
+
 def profile_case(fields):
     """The workload's grid and model, `fields` sources, one refinement iteration, without
     the CUDA graph: 8 source-limited sweeps then 8 full sweeps (launches 9-16)."""
@@ -574,7 +626,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="plain", choices=["plain", "stations", "models", "full", "2d"],
+    ap.add_argument("--workload", default="plain",
+                    choices=["plain", "stations", "models", "full", "2d", "warmstart"],
                     help="plain: 256x256x128 h=50 m, independent sources; stations: 200x200x100 h=100 m, "
                          "sources on the top surface; models: uneven models, one source each; full: "
                          "512x512x256 h=25 m with a dipping slab, surface sources; 2d: 501x251 FP64")
@@ -605,7 +658,7 @@ def main():
         SLAB[0] = True
         N_SWEEPS_MAX = 20      # the slab model converges more slowly than 10 iterations
     if args.fields is None:
-        args.fields = {"stations": 64, "full": 256, "2d": 1}.get(args.workload, 32)
+        args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8}.get(args.workload, 32)
     PAIR[0] = args.pair_fields
     KERNEL[0] = args.sweep_kernel
     if args.profile_case:
@@ -619,6 +672,8 @@ def main():
         run_models(args)
     elif args.workload == "2d":
         run_2d(args)
+    elif args.workload == "warmstart":
+        run_warmstart_study(args)
     else:
         run_gpu(args)
 

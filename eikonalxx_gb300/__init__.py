@@ -35,7 +35,7 @@ EXPORTED = [
     "eikx_solve3d", "eikx_set_grid2d", "eikx_set_slowness2d", "eikx_set_nodal_velocity2d",
     "eikx_solve2d", "eikx_graph3d_tables", "eikx_levels2d", "eikx_analytic3d", "eikx_analytic2d",
     "eikx_solve3d_noalloc", "eikx_solve3d_batch", "eikx_autotune3d", "eikx_tuning_save", "eikx_tuning_load",
-    "eikx_gradient3d", "eikx_gradient2d", "eikx_station_times3d", "eikx_station_times2d",
+    "eikx_gradient3d", "eikx_gradient2d", "eikx_station_times3d", "eikx_station_times2d", "eikx_solve3d_warm",
 ]
 CELL_SLOWNESS, NODAL_VELOCITY = 0, 1
 
@@ -74,7 +74,7 @@ class _Stats(ctypes.Structure):
     _fields_ = [("n_fields", ctypes.c_int), ("iterations_max", ctypes.c_int),
                 ("iterations_min", ctypes.c_int), ("sweeps_launched", ctypes.c_int),
                 ("kernel_launches", ctypes.c_int), ("residual_last", ctypes.c_double),
-                ("device_ms", ctypes.c_double), ("sweep_ms", ctypes.c_double)]
+                ("device_ms", ctypes.c_double), ("sweep_ms", ctypes.c_double), ("reset_nodes", ctypes.c_longlong)]
 
 
 class _Src3(ctypes.Structure):
@@ -136,6 +136,8 @@ def load(path=None):
     lib.eikx_analytic2d.argtypes = [vp, ctypes.POINTER(_Src2), c_double, c_double, vp, c_int]
     lib.eikx_solve3d_batch.argtypes = [vp, ctypes.POINTER(_Model3), c_int, ctypes.POINTER(_Options), c_int]
     lib.eikx_autotune3d.argtypes = [vp, ctypes.POINTER(_Src3), c_int, c_int, ctypes.POINTER(_Tuning)]
+    lib.eikx_solve3d_warm.argtypes = [vp, ctypes.POINTER(_Src3), c_int, ctypes.POINTER(_Options), c_int, vp, c_int,
+                                      c_double, vp, c_int]
     lib.eikx_gradient3d.argtypes = [vp, c_int, vp, c_int]
     lib.eikx_gradient2d.argtypes = [vp, c_int, vp, c_int]
     lib.eikx_station_times3d.argtypes = [vp, c_int, ctypes.POINTER(_Src3), c_int, ctypes.POINTER(c_double)]
@@ -278,6 +280,22 @@ class Context:
         p, where = _ptr(out)
         o = (options or Options())._c()
         _check(self._lib.eikx_solve3d(self._h, arr, n, ctypes.byref(o), precision, p, where))
+        return out
+
+    def solve3d_warm(self, sources, t_init, options=None, precision=F32, gate_tol=1e-6, out=None):
+        """Solve from initial fields `t_init` (n_src, nz, ny, nx): underestimated nodes are
+        reset, then sweeps run to the tolerance without the initialisation pass."""
+        src = np.atleast_2d(np.asarray(sources, dtype=np.float64))
+        n = src.shape[0]
+        arr = (_Src3 * n)(*[_Src3(*map(float, q)) for q in src])
+        nx, ny, nz = self.grid3[:3]
+        if out is None:
+            out = np.empty((n, nz, ny, nx), dtype=np.float32 if precision == F32 else np.float64)
+        ip, iwhere = _ptr(t_init)
+        p, where = _ptr(out)
+        o = (options or Options())._c()
+        _check(self._lib.eikx_solve3d_warm(self._h, arr, n, ctypes.byref(o), precision, ip, iwhere, float(gate_tol),
+                                           p, where))
         return out
 
     def gradient3d(self, field=0, precision=F32, out=None):

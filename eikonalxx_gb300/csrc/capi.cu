@@ -91,7 +91,8 @@ bool locate(double x, double x0, double d, int n, int *cell, double *offset) {
 }
 
 struct Workspace {
-    DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, pairs;
+    DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, pairs, init,
+        resetCount;
     PinnedBuf stage;
     std::vector<int> orderKey;   // (tilesY, tilesZ, nFields, dim) of the uploaded order table
 };
@@ -115,8 +116,9 @@ struct BatchWorkspace {
 
 struct ScheduleKey {
     int dim = 0, precision = -1, nFields = 0, nx = 0, ny = 0, nz = 0, nSweeps = -1, radius = 0,
-        initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0, variant = 0, shape = 0;
-    double tol = 0, h = 0, dx = 0, dy = 0, dz = 0;
+        initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0, variant = 0, shape = 0,
+        warm = 0;
+    double tol = 0, h = 0, dx = 0, dy = 0, dz = 0, gate = 0;
     unsigned long long spin = 0;
     const void *tt = nullptr, *sp = nullptr, *srcs = nullptr, *corners = nullptr;
     bool operator==(const ScheduleKey &o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
@@ -262,6 +264,7 @@ eikx_status finishModel2(eikx_ctx *c) {
     return EIKX_OK;
 }
 
+template <class T> eikx::Spacing3<T> spacing3(double dx, double dy, double dz);
 template <class T> int precOf();
 template <> int precOf<float>() { return EIKX_F32; }
 template <> int precOf<double>() { return EIKX_F64; }
@@ -269,7 +272,9 @@ template <> int precOf<double>() { return EIKX_F64; }
 // Shared solve driver for 2D and 3D.
 template <class T, int DIM>
 eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options o, void *tOut,
-                      int where) {
+                      int where, const void *tInit = nullptr, int initWhere = EIKX_HOST, double gateTol = 0) {
+    const bool warm = DIM == 3 && tInit != nullptr;
+    if (warm) o.init_sweeps = 0;   // the initial field replaces the initialisation pass
     const int P = precOf<T>();
     const int nx = DIM == 3 ? c->nx : c->nx2;
     const int ny = DIM == 3 ? c->ny : 1;
@@ -421,6 +426,16 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         EIKX_CUDA(cudaMemcpyAsync(w.pairs.p, pstage, pairBytes, cudaMemcpyHostToDevice, c->stream));
     }
 
+    if (warm) {
+        const size_t initBytes = static_cast<size_t>(nx) * ny * nz * nSrc * sizeof(T);
+        const void *initBefore = w.init.p;
+        EIKX_CUDA(w.init.ensure(initBytes));
+        EIKX_CUDA(w.resetCount.ensure(sizeof(unsigned long long)));
+        if (w.init.p != initBefore) dropGraph(c);
+        EIKX_CUDA(cudaMemcpyAsync(w.init.p, tInit, initBytes,
+                                  initWhere == EIKX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                  c->stream));
+    }
     const int nSweepLaunches = nSweepKinds * ((o.init_sweeps ? 1 : 0) + nSweeps);
     eikx::SolveState st{};
     st.queue[0] = w.queue.as<unsigned>();
@@ -454,6 +469,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     sk.initFp64 = o.init_fp64 ? 1 : 0; sk.uniform = uniform; sk.blocks = blocks; sk.tol = o.tolerance;
     sk.h = dx; sk.dx = dx; sk.dy = dy; sk.dz = dz; sk.spin = st.spinLimit; sk.dropBlocks = drop;
     sk.paired = paired ? 1 : 0;
+    sk.warm = warm ? 1 : 0;
+    sk.gate = gateTol;
     sk.variant = variant;
     sk.shape = shape;
     sk.tt = w.tt.p; sk.sp = spad[0].p; sk.srcs = w.srcs.p; sk.corners = w.corners.p;
@@ -474,7 +491,14 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         int buf = 0;
         EIKX_CUDA(eikx::launchResetState(st, nSrc, buf, c->stream));
         ++launches;
-        if (DIM == 3)
+        if (warm) {
+            EIKX_CUDA(cudaMemsetAsync(w.resetCount.p, 0, sizeof(unsigned long long), c->stream));
+            EIKX_CUDA(eikx::launchWarmInit3<T>(w.tt.as<T>(), w.init.as<T>(), nSrc, fieldStride, Px, nx, ny, nz, dx, dy,
+                                               dz, w.corners.as<eikx::Corner3>(), w.srcs.as<eikx::SourceT<T>>(),
+                                               c->slow3.as<double>(), o.factored_radius, uniform, static_cast<T>(dx),
+                                               spacing3<T>(dx, dy, dz), gateTol, o.init_fp64 ? 1 : 0,
+                                               w.resetCount.as<unsigned long long>(), c->stream));
+        } else if (DIM == 3)
             EIKX_CUDA(eikx::launchInit3<T>(w.tt.as<T>(), nSrc, fieldStride, Px, nx, ny, nz, dx, dy, dz,
                                            w.corners.as<eikx::Corner3>(), o.init_fp64 ? 1 : 0, c->stream));
         else
@@ -583,6 +607,9 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     EIKX_CUDA(cudaEventRecord(c->ev1, c->stream));
     std::vector<int> iters(nSrc);
     int aborted = 0;
+    unsigned long long resets = 0;
+    if (warm)
+        EIKX_CUDA(cudaMemcpyAsync(&resets, w.resetCount.p, sizeof(resets), cudaMemcpyDeviceToHost, c->stream));
     EIKX_CUDA(cudaMemcpyAsync(iters.data(), w.iterations.p, nSrc * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     EIKX_CUDA(cudaMemcpyAsync(&aborted, w.abortFlag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     std::vector<unsigned long long> lastRes;
@@ -624,6 +651,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     }
     s.kernel_launches = launches;
     s.device_ms = ms;
+    s.reset_nodes = static_cast<long long>(resets);
     c->stats = s;
     c->last.valid = false;
     if (aborted) return fail(EIKX_ERR_TIMEOUT, "a bounded inter-tile wait ran out; the fields are not valid");
@@ -1287,6 +1315,27 @@ eikx_status eikx_solve3d(eikx_ctx *c, const eikx_source3d *src, int nSrc, const 
     for (int i = 0; i < nSrc; ++i) { xyz[3 * i] = src[i].x; xyz[3 * i + 1] = src[i].y; xyz[3 * i + 2] = src[i].z; }
     if (precision == EIKX_F32) return solveImpl<float, 3>(c, xyz.data(), nSrc, o, tOut, where);
     if (precision == EIKX_F64) return solveImpl<double, 3>(c, xyz.data(), nSrc, o, tOut, where);
+    return fail(EIKX_ERR_INVALID, "precision must be EIKX_F32 or EIKX_F64");
+}
+
+eikx_status eikx_solve3d_warm(eikx_ctx *c, const eikx_source3d *src, int nSrc, const eikx_options *opt, int precision,
+                              const void *tInit, int initWhere, double gateTol, void *tOut, int where) {
+    if (eikx_status r = checkCtx(c); r) return r;
+    if (!c->haveGrid3) return fail(EIKX_ERR_STATE, "Class not initialized");
+    if (!c->haveSlow3) return fail(EIKX_ERR_STATE, "Velocity model not set");
+    if (!src || nSrc <= 0) return fail(EIKX_ERR_STATE, "Source location not set");
+    if (!tOut || !tInit) return fail(EIKX_ERR_INVALID, "initial field or output is NULL");
+    if (where != EIKX_HOST && where != EIKX_DEVICE) return fail(EIKX_ERR_INVALID, "where must be EIKX_HOST or EIKX_DEVICE");
+    if (initWhere != EIKX_HOST && initWhere != EIKX_DEVICE)
+        return fail(EIKX_ERR_INVALID, "init_where must be EIKX_HOST or EIKX_DEVICE");
+    if (!(gateTol >= 0)) return fail(EIKX_ERR_INVALID, "gate_tol must be >= 0");
+    eikx_options o;
+    if (eikx_status r = fillOptions(opt, &o); r) return r;
+    EIKX_CUDA(cudaSetDevice(c->device));
+    std::vector<double> xyz(3 * static_cast<size_t>(nSrc));
+    for (int i = 0; i < nSrc; ++i) { xyz[3 * i] = src[i].x; xyz[3 * i + 1] = src[i].y; xyz[3 * i + 2] = src[i].z; }
+    if (precision == EIKX_F32) return solveImpl<float, 3>(c, xyz.data(), nSrc, o, tOut, where, tInit, initWhere, gateTol);
+    if (precision == EIKX_F64) return solveImpl<double, 3>(c, xyz.data(), nSrc, o, tOut, where, tInit, initWhere, gateTol);
     return fail(EIKX_ERR_INVALID, "precision must be EIKX_F32 or EIKX_F64");
 }
 

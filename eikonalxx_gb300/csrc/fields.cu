@@ -64,6 +64,96 @@ __global__ void init3Kernel(T *tt, int nFields, long long fieldStride, int pitch
     }
 }
 
+// Warm start of a 3D solve from an initial field (natural order): the field is taken as
+// given except where the local solver shows it underestimates.  For every node the
+// upwind update is evaluated from the initial field in all 8 sweep orderings (the
+// stencils of Solver3DSweep::updateFSM, neighbours clamped to the grid); a node whose
+// initial time lies more than gateTol below the smallest of them is lower than any of
+// its neighbourhoods supports -- sweeps only lower times, so it could never recover --
+// and is reset to HUGE.  The source cell's corners take the analytic initialisation.
+// Only values of the initial field are read, so the pass is order-independent.
+template <class T, bool UNIFORM>
+__global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny,
+                                int nz, double dx, double dy, double dz, const Corner3 *corners,
+                                const SourceT<T> *srcs, const double *slow, int radius, T h, Spacing3<T> g,
+                                double gateTol, int fp64, unsigned long long *nReset) {
+    const long long perField = static_cast<long long>(nx) * ny * nz;
+    const long long n = perField * nFields;
+    const int ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
+    unsigned long long resets = 0;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int f = static_cast<int>(i / perField);
+        const long long r = i - f * perField;
+        const int ix = static_cast<int>(r % nx);
+        const int iy = static_cast<int>((r / nx) % ny);
+        const int iz = static_cast<int>(r / (static_cast<long long>(nx) * ny));
+        const Corner3 cn = corners[f];
+        const T *fi = init + static_cast<long long>(f) * perField;
+        T v;
+        if (ix - cn.isx >= 0 && ix - cn.isx <= 1 && iy - cn.isy >= 0 && iy - cn.isy <= 1 && iz - cn.isz >= 0 &&
+            iz - cn.isz <= 1) {
+            v = fp64 ? static_cast<T>(analyticT3<double>(ix, iy, iz, dx, dy, dz, cn.xo, cn.yo, cn.zo, cn.s))
+                     : analyticT3<T>(ix, iy, iz, static_cast<T>(dx), static_cast<T>(dy), static_cast<T>(dz),
+                                     static_cast<T>(cn.xo), static_cast<T>(cn.yo), static_cast<T>(cn.zo),
+                                     static_cast<T>(cn.s));
+        } else {
+            v = fi[r];
+            const SourceT<T> src = srcs[f];
+            T uMin = static_cast<T>(1.e10);
+            for (int e = 0; e < 8; ++e) {
+                const int fx = e & 1, fy = (e >> 1) & 1, fz = (e >> 2) & 1;
+                SweepSigns sg;
+                sg.ixShift = fx ? 1 : -1; sg.iyShift = fy ? 1 : -1; sg.izShift = fz ? 1 : -1;
+                sg.signX = fx ? -1 : 1; sg.signY = fy ? -1 : 1; sg.signZ = fz ? -1 : 1;
+                auto clampi_ = [](int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); };
+                const int cxu = fx ? clampi_(ix, 0, ncx - 1) : clampi_(ix - 1, 0, ncx - 1);
+                const int cxo = fx ? clampi_(cxu - 1, 0, ncx - 1) : clampi_(cxu + 1, 0, ncx - 1);
+                const int cyu = fy ? clampi_(iy, 0, ncy - 1) : clampi_(iy - 1, 0, ncy - 1);
+                const int cyo = fy ? clampi_(cyu - 1, 0, ncy - 1) : clampi_(cyu + 1, 0, ncy - 1);
+                const int czu = fz ? clampi_(iz, 0, ncz - 1) : clampi_(iz - 1, 0, ncz - 1);
+                const int czo = fz ? clampi_(czu - 1, 0, ncz - 1) : clampi_(czu + 1, 0, ncz - 1);
+                auto cell = [&](int x, int y, int z) {
+                    return static_cast<T>(slow[(static_cast<long long>(z) * ncy + y) * ncx + x]);
+                };
+                const int xs = clampi_(ix + sg.ixShift, 0, nx - 1), ys = clampi_(iy + sg.iyShift, 0, ny - 1);
+                const int zs = clampi_(iz + sg.izShift, 0, nz - 1);
+                auto tv = [&](int x, int y, int z) { return fi[(static_cast<long long>(z) * ny + y) * nx + x]; };
+                Stencil3<T> st;
+                st.s0 = cell(cxu, cyu, czu); st.s1 = cell(cxo, cyu, czu); st.s2 = cell(cxo, cyo, czu);
+                st.s3 = cell(cxu, cyo, czu); st.s4 = cell(cxu, cyu, czo); st.s5 = cell(cxo, cyu, czo);
+                st.s7 = cell(cxu, cyo, czo);
+                st.t1 = tv(xs, iy, iz); st.t2 = tv(xs, ys, iz); st.t3 = tv(ix, ys, iz); st.t4 = tv(ix, iy, zs);
+                st.t5 = tv(xs, iy, zs); st.t6 = tv(xs, ys, zs); st.t7 = tv(ix, ys, zs);
+                const T u = UNIFORM ? fd3Uniform<T>(radius, h, src, sg, ix, iy, iz, st)
+                                    : fd3NonUniform<T>(radius, g, src, sg, ix, iy, iz, st);
+                uMin = u < uMin ? u : uMin;
+            }
+            if (static_cast<double>(v) < static_cast<double>(uMin) - gateTol) {
+                v = static_cast<T>(1.e10);
+                ++resets;
+            }
+        }
+        tt[static_cast<long long>(f) * fieldStride + (static_cast<long long>(iz) * ny + iy) * pitch + ix] = v;
+    }
+    if (resets) atomicAdd(nReset, resets);
+}
+
+// Pads of the pitched rows (x >= nx) stay HUGE in a warm start.
+template <class T>
+__global__ void fillPadKernel(T *tt, int nFields, long long fieldStride, int pitch, int nx, int rows) {
+    const int padW = pitch - nx;
+    const long long n = static_cast<long long>(nFields) * rows * padW;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long q = i / padW;
+        const int x = nx + static_cast<int>(i % padW);
+        const int f = static_cast<int>(q / rows);
+        const long long row = q % rows;
+        tt[f * fieldStride + row * pitch + x] = static_cast<T>(1.e10);
+    }
+}
+
 // 2D (Solver2D::initializeTravelTimes, src/solver2d.cpp:61-105).
 template <class T>
 __global__ void init2Kernel(T *tt, int nFields, long long fieldStride, int pitch, int nx, int nz,
@@ -343,6 +433,35 @@ cudaError_t launchResetState(const SolveState &st, int nFields, int buf, cudaStr
     resetKernel<<<gridFor(static_cast<long long>(nFields) * st.residualStride), kThreads, 0, s>>>(st, nFields, buf);
     return cudaGetLastError();
 }
+template <class T>
+cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
+                            double dx, double dy, double dz, const Corner3 *corners, const SourceT<T> *srcs,
+                            const double *slow, int radius, bool uniform, T h, const Spacing3<T> &g, double gateTol,
+                            int fp64, unsigned long long *nReset, cudaStream_t s) {
+    const long long n = static_cast<long long>(nx) * ny * nz * nFields;
+    if (uniform)
+        warmInit3Kernel<T, true><<<gridFor(n), kThreads, 0, s>>>(tt, init, nFields, fieldStride, pitch, nx, ny, nz, dx,
+                                                                 dy, dz, corners, srcs, slow, radius, h, g, gateTol,
+                                                                 fp64, nReset);
+    else
+        warmInit3Kernel<T, false><<<gridFor(n), kThreads, 0, s>>>(tt, init, nFields, fieldStride, pitch, nx, ny, nz, dx,
+                                                                  dy, dz, corners, srcs, slow, radius, h, g, gateTol,
+                                                                  fp64, nReset);
+    if (pitch > nx) {
+        const long long np = static_cast<long long>(nFields) * ny * nz * (pitch - nx);
+        fillPadKernel<T><<<gridFor(np), kThreads, 0, s>>>(tt, nFields, fieldStride, pitch, nx, ny * nz);
+    }
+    return cudaGetLastError();
+}
+template cudaError_t launchWarmInit3<float>(float *, const float *, int, long long, int, int, int, int, double, double,
+                                            double, const Corner3 *, const SourceT<float> *, const double *, int, bool,
+                                            float, const Spacing3<float> &, double, int, unsigned long long *,
+                                            cudaStream_t);
+template cudaError_t launchWarmInit3<double>(double *, const double *, int, long long, int, int, int, int, double,
+                                             double, double, const Corner3 *, const SourceT<double> *, const double *,
+                                             int, bool, double, const Spacing3<double> &, double, int,
+                                             unsigned long long *, cudaStream_t);
+
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st) {
     positiveKernel<<<gridFor(n), kThreads, 0, st>>>(s, n, flag);
     return cudaGetLastError();

@@ -159,6 +159,14 @@ cudaError_t launchCellsToNatural3(double *slow, const U *c, int nx, int ny, int 
 template <class U>
 cudaError_t launchCellsToNatural2(double *slow, const U *c, int nx, int nz, int ordering, cudaStream_t s);
 cudaError_t launchResetState(const SolveState &st, int nFields, int buf, cudaStream_t s);
+// Warm start of a 3D solve: the initial fields (natural order) into the pitched fields,
+// nodes the local solver shows underestimated reset to HUGE (count added to *nReset),
+// the source cells' corners initialised analytically.
+template <class T>
+cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
+                            double dx, double dy, double dz, const Corner3 *corners, const SourceT<T> *srcs,
+                            const double *slow, int radius, bool uniform, T h, const Spacing3<T> &g, double gateTol,
+                            int fp64, unsigned long long *nReset, cudaStream_t s);
 // Sets *flag (ORs 1) if any of the n slownesses is not positive and finite.
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st);
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,

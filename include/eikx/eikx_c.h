@@ -100,6 +100,7 @@ typedef struct {
     double residual_last;    /* largest decrease of the last iteration over all fields (s) */
     double device_ms;        /* device time of the solve incl. the copy-out (CUDA events) */
     double sweep_ms;         /* summed device time of the sweep kernels (profile_sweeps), else -1 */
+    long long reset_nodes;   /* warm start: initial nodes reset as underestimated (else 0) */
 } eikx_stats;
 
 /* ---- context ----------------------------------------------------------- */
@@ -141,6 +142,22 @@ eikx_status eikx_solve3d(eikx_ctx *ctx, const eikx_source3d *src, int n_src,
                          const eikx_options *opt, int precision, void *t_out, int where);
 
 /* ---- 2D ---------------------------------------------------------------- */
+/* No counterpart in the reference: a 3D solve warm-started from initial fields, one per
+ * source (natural order, the solve precision, host or device by init_where) -- e.g. a
+ * learned prediction inflated to bound the solution from above.  A node whose initial
+ * time lies more than gate_tol seconds below the smallest upwind update its initial
+ * neighbourhood gives, over all 8 sweep orderings, is reset to HUGE (sweeps only lower
+ * times, so it could not recover); the source cells' corners take the analytic
+ * initialisation; then refinement iterations run to the tolerance without the
+ * initialisation pass.  eikx_stats.reset_nodes counts the resets.  Note: the reference's
+ * local solver is not monotone in its neighbours (causality windows of the 2D and 3D
+ * operators, the factored branch), so sweeps started from a different field can settle
+ * on a different fixed point than the cold start, by up to several milliseconds on
+ * layered models even when started from the cold-start result itself. */
+eikx_status eikx_solve3d_warm(eikx_ctx *ctx, const eikx_source3d *src, int n_src, const eikx_options *opt,
+                              int precision, const void *t_init, int init_where, double gate_tol, void *t_out,
+                              int where);
+
 /* ---- products of the last solve ---------------------------------------- */
 
 /* Travel-time gradient of field `field` (0-based source index) of the last eikx_solve3d /
