@@ -378,7 +378,7 @@ def run_2d(args):
     ctx = ex.Context(dev)
     ctx.set_grid2d(nx, nz, h, h)
     ctx.set_nodal_velocity2d(v)
-    opt = ex.Options(n_sweeps=2, tolerance=1e-8, factored_radius=3)
+    opt = ex.Options(n_sweeps=2, tolerance=1e-8, factored_radius=3, sweep_kernel=KERNEL[0])
     fields = args.fields
     srcs = [src] * fields
     out_dev = torch.empty((fields, nz, nx), dtype=torch.float64, device=f"cuda:{dev}")
@@ -410,7 +410,7 @@ def run_2d(args):
             launches += st["kernel_launches"]
             iters.append(st["iterations_max"])
     ms = float(np.mean(per))
-    prof = ex.Options(n_sweeps=2, tolerance=1e-8, factored_radius=3, profile_sweeps=True)
+    prof = ex.Options(n_sweeps=2, tolerance=1e-8, factored_radius=3, profile_sweeps=True, sweep_kernel=KERNEL[0])
     ctx.solve2d(srcs, prof, ex.F64, out=out_dev)
     pst = ctx.stats()
     launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
@@ -433,7 +433,9 @@ def run_2d(args):
         "config": {"workload": f"plain 2D solve, {nx}x{nz} h={h:g} m, v(z)=3000+0.5z m/s, source (2500, 500) m, "
                                f"{fields} field(s) per step", "factored_radius": 3, "n_sweeps": 2, "tolerance_s": 1e-8,
                    "l2": "flushed (write of 2x L2) between timed steps"},
-        "roofline": {"bound": "hbm", "kernel": "sweep2Kernel<double,uniform>", "achieved": bpl / (launch_ms / 1e3) / 1e9,
+        "roofline": {"bound": "hbm", "kernel": ("sweep2BlockKernel<double,uniform>" if KERNEL[0] == 2 and nz <= 512
+                                                else "sweep2Kernel<double,uniform>"),
+                     "achieved": bpl / (launch_ms / 1e3) / 1e9,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": bpl / (launch_ms / 1e3) / 1e9 / peak, "bytes_per_launch": bpl, "launch_ms": launch_ms,
                      "traffic": None, "note": "one field of 126 k nodes: latency-bound wavefront (751 levels)"},

@@ -352,6 +352,9 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     // sweep kernel and warp-block shape
     const int variant = o.sweep_kernel == eikx::kNodeStep ? eikx::kNodeStep : eikx::kChunkStep;
     const bool chunkStep = DIM == 3 && !paired && variant == eikx::kChunkStep;
+    // 2D grids of up to 512 rows can run one CTA per field (sweep_kernel = 2); the warp-block
+    // kernel is the default: measured faster on GB300 for 1 to 512 fields of 501 x 251 nodes
+    const bool block2 = DIM == 2 && nz <= eikx::kMaxBlockRows2 && o.sweep_kernel == eikx::kChunkStep;
     const int shape = chunkStep && o.block_shape > 0 ? o.block_shape - 1 : eikx::kShape8x4;
 
     // workspace
@@ -553,7 +556,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
                 g.cosTheta = static_cast<T>(dx / std::hypot(dx, dz));
                 g.sinTheta = static_cast<T>(dz / std::hypot(dx, dz));
                 a.sp2 = g;
-                EIKX_CUDA(eikx::launchSweep2<T>(a, uniform, blocks, c->stream));
+                if (block2) EIKX_CUDA(eikx::launchSweep2Block<T>(a, uniform, nSrc, c->stream));
+                else EIKX_CUDA(eikx::launchSweep2<T>(a, uniform, blocks, c->stream));
             }
             if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched + 1], c->stream));
             buf ^= 1;

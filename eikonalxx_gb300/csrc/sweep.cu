@@ -405,6 +405,99 @@ __global__ void __launch_bounds__(kThreads) sweep2Kernel(const Sweep2Args<T> a) 
     }
 }
 
+// One CTA per field for 2D grids of up to 512 rows (sweep2BlockKernel): thread z' owns
+// row z' and updates x' = s - z' at step s; the only upwind value from another thread is
+// the row above's result of the step before, passed through shared memory with one
+// __syncthreads() per step.  No mailbox, no inter-CTA waits: fields are independent
+// CTAs, and a single field's sweep is a chain of barrier-separated steps instead of
+// L2 round trips between warp blocks.
+template <class T, bool UNIFORM>
+__global__ void __launch_bounds__(512) sweep2BlockKernel(const Sweep2Args<T> a) {
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    const int nzp = blockDim.x;                         // rows rounded up to a warp multiple
+    T *tUp = reinterpret_cast<T *>(smemRaw);            // [2][nzp + 1]: value of row z'-1 at step s-1
+    T *sUp = tUp + 2 * (nzp + 1);                       // [2][nzp + 1]: its cell slowness
+    const SolveState &st = a.st;
+    const int f = blockIdx.x;
+    if (st.converged[f]) return;
+    const int lz = threadIdx.x;
+    const int fx = a.sweep & 1, fz = (a.sweep >> 1) & 1;
+    SweepSigns sg;
+    sg.ixShift = fx ? 1 : -1; sg.iyShift = 0; sg.izShift = fz ? 1 : -1;
+    sg.signX = fx ? -1 : 1; sg.signY = 1; sg.signZ = fz ? -1 : 1;
+    const int Px = a.pitch;
+    const int nSteps = Px + a.nz - 1;
+    const T *sp = fx ? a.spNeg : a.spPos;
+    const T huge = hugeT<T>();
+    const SourceT<T> src = a.srcs[f];
+    const bool laneValid = lz < a.nz;
+    const int za = laneValid ? reflect(lz, a.nz, fz) : 0;
+    int xlo, xhi, zlo, zhi;
+    axisBounds(a.nx, fx, a.init, src.isx, xlo, xhi);
+    axisBounds(a.nz, fz, a.init, src.isz, zlo, zhi);
+    const bool zUpd = laneValid && za >= zlo && za <= zhi;
+    T *row = a.tt + static_cast<long long>(f) * a.fieldStride + static_cast<long long>(za) * a.pitch;
+    RowStream<T> rs;
+    rs.row = row;
+    rs.srow = sp + static_cast<long long>(za + (fz ? 0 : 1)) * a.spPitch;
+    rs.Px = Px;
+    rs.rev = fx;
+    rs.nChunks = Px / RowStream<T>::V;
+    if (laneValid) rs.start();
+    // both buffers start as "nothing upwind": slot 0 is the virtual row above row 0 and
+    // stays HUGE; the other slots hold HUGE until their row publishes (inactive rows
+    // publish HUGE too, as the lanes of the warp-block kernel do)
+    for (int i = lz; i < 2 * (nzp + 1); i += nzp) {
+        tUp[i] = huge;
+        sUp[i] = huge;
+    }
+    T t1 = huge, t2 = huge, s3 = huge, s0 = huge;      // own previous value / slowness, carries
+    T res = 0;
+    __syncthreads();
+    for (int s = 0; s < nSteps; ++s) {
+        const int cur = (s & 1) * (nzp + 1), prv = ((s - 1) & 1) * (nzp + 1);
+        const int xp = s - lz;
+        const bool active = laneValid && xp >= 0 && xp < Px;
+        T t0 = huge, sOwn = huge;
+        if (active) rs.take(xp, t0, sOwn);
+        const T t3 = tUp[prv + lz];                     // row above, same x', previous step
+        const T s1 = sUp[prv + lz];
+        T v = t0;
+        if (active) {
+            const int xa = reflect(xp, Px, fx);
+            if (zUpd && xa >= xlo && xa <= xhi) {
+                const T tu = UNIFORM ? fd2Uniform<T>(a.radius, a.h, src, sg, xa, za, s0, s1, s3, t1, t2, t3)
+                                     : fd2NonUniform<T>(a.radius, a.sp2, src, sg, xa, za, s0, s1, s3, t1, t2, t3);
+                if (tu < t0) {
+                    v = tu;
+                    row[xa] = tu;
+                    res = dmax(res, t0 - tu);
+                }
+            }
+        }
+        // publish for row z'+1 (slot lz + 1 of the current buffer)
+        tUp[cur + lz + 1] = v;
+        sUp[cur + lz + 1] = sOwn;
+        // carries: t2 = row above at x'-1, s0 = its cell; t1 / s3 = own x'-1
+        t2 = t3;
+        s0 = s1;
+        t1 = v;
+        s3 = sOwn;
+        __syncthreads();
+    }
+    double r = warpMax(static_cast<double>(res));
+    __shared__ double blockMax[32];
+    if ((lz & 31) == 0) blockMax[lz >> 5] = r;
+    __syncthreads();
+    if (lz < 32) {
+        r = lz < (nzp >> 5) ? blockMax[lz] : 0.0;
+        r = warpMax(r);
+        if (lz == 0 && r > 0)
+            atomicMax(st.residual + static_cast<long long>(f) * st.residualStride + a.residualSlot,
+                      static_cast<unsigned long long>(__double_as_longlong(r)));
+    }
+}
+
 }  // namespace
 
 size_t sweep3SmemBytes(size_t elem) { return elem * 2 * kRing * kPlane3 * kWarpsPerBlock; }
@@ -425,6 +518,17 @@ cudaError_t launchSweep2(const Sweep2Args<T> &a, bool uniform, int blocks, cudaS
     else sweep2Kernel<T, false><<<blocks, kThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
+
+template <class T>
+cudaError_t launchSweep2Block(const Sweep2Args<T> &a, bool uniform, int nFields, cudaStream_t s) {
+    const int nzp = (a.nz + 31) / 32 * 32;
+    const size_t smem = 4 * (nzp + 1) * sizeof(T);
+    if (uniform) sweep2BlockKernel<T, true><<<nFields, nzp, smem, s>>>(a);
+    else sweep2BlockKernel<T, false><<<nFields, nzp, smem, s>>>(a);
+    return cudaGetLastError();
+}
+template cudaError_t launchSweep2Block<float>(const Sweep2Args<float> &, bool, int, cudaStream_t);
+template cudaError_t launchSweep2Block<double>(const Sweep2Args<double> &, bool, int, cudaStream_t);
 
 template <class T> int sweep3BlocksPerSM(bool uniform) {
     int n = 0;

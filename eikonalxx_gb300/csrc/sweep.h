@@ -91,6 +91,10 @@ template <class T>
 cudaError_t launchSweep3(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s);
 template <class T>
 cudaError_t launchSweep2(const Sweep2Args<T> &a, bool uniform, int blocks, cudaStream_t s);
+// 2D grids of at most kMaxBlockRows2 rows: one CTA per field, one thread per row.
+constexpr int kMaxBlockRows2 = 512;
+template <class T>
+cudaError_t launchSweep2Block(const Sweep2Args<T> &a, bool uniform, int nFields, cudaStream_t s);
 // Chunk-step 3D kernel (sweep_chunk.cuh): a lane updates one 16-byte chunk of its pencil
 // per wavefront step.  With a.units set, a work item's field index is a unit of a
 // multi-model batch and the grid, slowness, mailbox and spacing come from a.units[unit].

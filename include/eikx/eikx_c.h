@@ -72,7 +72,10 @@ typedef struct {
                               if eikx_autotune3d ran, else chunk-step; 1 = node-step (a
                               lane updates one node per wavefront step), 2 = chunk-step (a
                               lane updates one 16-byte chunk, 4 FP32 / 2 FP64 nodes, per
-                              step).  All give identical travel times. */
+                              step).  2D: 0 and 1 = warp blocks of 32 rows; 2 = one CTA
+                              per field, one thread per row (grids of up to 512 rows; slower
+                              on GB300, whose FP64 units one SM cannot keep fed).  All give
+                              identical travel times. */
     int block_shape;       /* 3D chunk-step warp block (pencils along y' x z'): 0 (default) =
                               the tuned shape of this grid class if eikx_autotune3d ran, else
                               8x4; 1 = 8x4, 2 = 4x8, 3 = 16x2.  Identical travel times. */

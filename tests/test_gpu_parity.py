@@ -126,13 +126,15 @@ def test_nodal_velocity_model_matches_oracle(ctx, oracle):
     assert np.array_equal(ctx.get_slowness3d(), oracle.nodal_to_cell3d(vt, nx, ny, nz, 1))
 
 
-SHAPES2 = [(31, 27, 10., 10.), (25, 33, 10., 12.5), (3, 3, 10., 10.), (70, 45, 5., 5.)]
+SHAPES2 = [(31, 27, 10., 10.), (25, 33, 10., 12.5), (3, 3, 10., 10.), (70, 45, 5., 5.),
+           (12, 530, 10., 10.)]   # more rows than one CTA holds: the warp-block kernel
 
 
+@pytest.mark.parametrize("kernel", [0, 2])        # 0: warp blocks, 2: one CTA per field (<= 512 rows)
 @pytest.mark.parametrize("precision", [ex.F64, ex.F32])
 @pytest.mark.parametrize("radius", [0, 3, 1000])
 @pytest.mark.parametrize("shape", SHAPES2)
-def test_solve2d_bitexact_vs_oracle(ctx, oracle, precision, radius, shape):
+def test_solve2d_bitexact_vs_oracle(ctx, oracle, precision, radius, shape, kernel):
     rng = np.random.default_rng(abs(hash((shape, radius, precision, 2))) % 2**32)
     nx, nz, dx, dz = shape
     dt = np.float32 if precision == ex.F32 else np.float64
@@ -140,7 +142,7 @@ def test_solve2d_bitexact_vs_oracle(ctx, oracle, precision, radius, shape):
     pos, cell, off = _src(rng, (nx, nz), (dx, dz))
     ctx.set_grid2d(nx, nz, dx, dz)
     ctx.set_slowness2d(s)
-    opt = ex.Options(n_sweeps=2, tolerance=-1, factored_radius=radius)
+    opt = ex.Options(n_sweeps=2, tolerance=-1, factored_radius=radius, sweep_kernel=kernel)
     t_gpu = ctx.solve2d([pos], opt, precision)[0]
     t_or = oracle.solve2d(s, shape, cell, off, n_sweeps=2, radius=radius, hypot_mode=1)
     assert np.array_equal(_bits(t_gpu), _bits(t_or)), np.abs(t_gpu - t_or).max()
@@ -217,3 +219,19 @@ def test_sweep_kernel_variants_match_oracle(ctx, oracle, variant, block, precisi
     for i, (_, cell, off) in enumerate(srcs):
         t_or = oracle.solve3d(s, shape, cell, off, n_sweeps=3, radius=2)
         assert np.array_equal(_bits(t[i]), _bits(t_or)), (i, np.abs(t[i] - t_or).max())
+
+
+@pytest.mark.parametrize("kernel", [0, 2])
+def test_solve2d_batch_converges_per_field(ctx, oracle, kernel):
+    rng = np.random.default_rng(71)
+    shape = (57, 41, 20., 20.)
+    nx, nz, dx, dz = shape
+    s = random_slowness(rng, (nz - 1) * (nx - 1), dtype=np.float64)
+    ctx.set_grid2d(nx, nz, dx, dz)
+    ctx.set_slowness2d(s)
+    srcs = [_src(rng, (nx, nz), (dx, dz)) for _ in range(5)]
+    opt = ex.Options(n_sweeps=15, tolerance=1e-7, factored_radius=3, sweep_kernel=kernel)
+    t = ctx.solve2d([p for p, _, _ in srcs], opt, ex.F64)
+    for i, (_, cell, off) in enumerate(srcs):
+        t_or = oracle.solve2d(s, shape, cell, off, n_sweeps=15, radius=3, tol=1e-7, hypot_mode=1)
+        assert np.array_equal(_bits(t[i]), _bits(t_or)), i
