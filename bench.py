@@ -65,6 +65,24 @@ def _traffic():
         return None
 
 
+def refinement_roofline(solve, opts, opts_init, bytes_per_update):
+    """Roofline of the refinement sweeps of one solve.  `solve(options)` runs the solve and
+    returns its statistics.  Time: the CUDA-event time of all sweep launches minus that of
+    the initialisation pass alone (a second solve with no refinement iteration).  Work: the
+    node updates the refinement sweeps performed, from the solve's statistics -- fields
+    that converged are skipped by the later launches, so the count is not fields x
+    launches."""
+    st0 = solve(opts_init)
+    st = solve(opts)
+    refine_ms = st["sweep_ms"] - st0["sweep_ms"]
+    launches = st["sweeps_launched"] - st0["sweeps_launched"]
+    updates = st["refine_node_updates"]
+    algorithmic = bytes_per_update * updates
+    return {"achieved": algorithmic / (refine_ms / 1e3) / 1e9, "algorithmic_bytes": algorithmic,
+            "node_updates": updates, "refine_ms": refine_ms, "refine_launches": launches,
+            "launch_ms": refine_ms / max(1, launches)}
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle-reason sampling during the timed region."""
 
@@ -194,7 +212,7 @@ def run_gpu(args):
             st = step_device()
             wall.append((time.perf_counter() - t0) * 1e3)
             per_step_ms.append(st["device_ms"])
-            iters.append(st["iterations_max"])
+            iters.append((st["iterations_min"], st["iterations_max"]))
             launches += st["kernel_launches"]
     torch.cuda.synchronize()
     sharding.barrier()
@@ -202,13 +220,14 @@ def run_gpu(args):
     value = fields * world / (ms / 1e3)
 
     # roofline of the sweep kernel: per-launch durations from CUDA events around each sweep
-    prof = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True,
-                      pair_fields=PAIR[0], sweep_kernel=KERNEL[0])
-    ctx.solve3d(src, prof, ex.F32, out=out_dev)
-    pst = ctx.stats()
-    sweep_launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
-    bytes_per_launch = BYTES_PER_NODE_SWEEP * n_nodes * fields
-    achieved = bytes_per_launch / (sweep_launch_ms / 1e3) / 1e9
+    def prof_solve(o):
+        ctx.solve3d(src, o, ex.F32, out=out_dev)
+        return ctx.stats()
+    popts = dict(tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0],
+                 sweep_kernel=KERNEL[0])
+    rl = refinement_roofline(prof_solve, ex.Options(n_sweeps=N_SWEEPS_MAX, **popts),
+                             ex.Options(n_sweeps=0, **popts), BYTES_PER_NODE_SWEEP)
+    achieved = rl["achieved"]
     peak, peak_kind = _peaks()
     tr = _traffic()
     shapes = {1: "8x4", 2: "4x8", 3: "16x2"}
@@ -254,14 +273,17 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world} (sources sharded, no collective)"},
         "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "bytes_per_launch": bytes_per_launch, "launch_ms": sweep_launch_ms,
+                     "algorithmic_bytes": rl["algorithmic_bytes"], "node_updates": rl["node_updates"],
+                     "refine_ms": rl["refine_ms"], "launch_ms": rl["launch_ms"],
+                     "note": "refinement sweeps only; 12 B per node update (read T, read slowness, write T)",
                      "traffic": traffic, "traffic_source": traffic_src},
         "e2e": {"value": e2e, "unit": "grids/s", "h2d_bytes_per_step": int(v.nbytes + 24 * fields),
                 "d2h_bytes_per_step": int(4 * n_nodes * fields), "ms_per_step": float(np.mean(e2e_ms))},
         "gpu_launches": int(launches), "clocks": clk.summary(),
-        "iterations": {"max": int(max(iters)), "min": int(min(iters))},
+        "iterations": {"max_over_fields": int(max(i[1] for i in iters)),
+                       "min_over_fields": int(min(i[0] for i in iters))},
         "wall_ms_per_step": float(np.mean(wall)), "accuracy": acc, "tuning": tuning,
-        "cpu_baseline": (cpu_baseline(args.cpu_seconds, 1, _sweeps_per_grid(max(iters)))
+        "cpu_baseline": (cpu_baseline(args.cpu_seconds, 1, _sweeps_per_grid(max(i[1] for i in iters)))
                          if not args.skip_cpu else None),
     }
     print(json.dumps(line), flush=True)
@@ -315,19 +337,21 @@ def run_models(args):
             ctx.solve3d_batch(dev_models, opt, ex.F32)
             st = ctx.stats()
             per_step.append(st["device_ms"])
-            iters.append(st["iterations_max"])
+            iters.append((st["iterations_min"], st["iterations_max"]))
             launches += st["kernel_launches"]
     torch.cuda.synchronize()
     sharding.barrier()
     ms = sharding.max_over_ranks(float(np.mean(per_step)), device=f"cuda:{dev}")
     value = n * world / (ms / 1e3)
 
-    prof = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True)
-    ctx.solve3d_batch(dev_models, prof, ex.F32)
-    pst = ctx.stats()
-    launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
-    bytes_per_launch = BYTES_PER_NODE_SWEEP * nodes
-    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    def prof_solve(o):
+        ctx.solve3d_batch(dev_models, o, ex.F32)
+        return ctx.stats()
+    rl = refinement_roofline(prof_solve,
+                             ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True),
+                             ex.Options(n_sweeps=0, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True),
+                             BYTES_PER_NODE_SWEEP)
+    achieved = rl["achieved"]
     peak, peak_kind = _peaks()
 
     e2e_ms = []
@@ -352,11 +376,14 @@ def run_models(args):
                    "parallelism": f"replicas x{world} (models sharded, no collective)"},
         "roofline": {"bound": "hbm", "kernel": "sweep3ChunkKernel<float,uniform,batch>", "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms, "traffic": None},
+                     "algorithmic_bytes": rl["algorithmic_bytes"], "node_updates": rl["node_updates"],
+                     "refine_ms": rl["refine_ms"], "launch_ms": rl["launch_ms"], "traffic": None,
+                     "note": "refinement sweeps only; 12 B per node update"},
         "e2e": {"value": e2e, "unit": "grids/s", "h2d_bytes_per_step": int(sum(m["v"].nbytes for m in mine)),
                 "d2h_bytes_per_step": int(4 * nodes), "ms_per_step": float(np.mean(e2e_ms))},
         "gpu_launches": int(launches), "clocks": clk.summary(),
-        "iterations": {"max": int(max(iters)), "min": int(min(iters))}, "accuracy": acc,
+        "iterations": {"max_over_fields": int(max(i[1] for i in iters)),
+                       "min_over_fields": int(min(i[0] for i in iters))}, "accuracy": acc,
     }
     print(json.dumps(line), flush=True)
 
@@ -408,13 +435,13 @@ def run_2d(args):
             st = ctx.stats()
             per.append(st["device_ms"])
             launches += st["kernel_launches"]
-            iters.append(st["iterations_max"])
+            iters.append((st["iterations_min"], st["iterations_max"]))
     ms = float(np.mean(per))
-    prof = ex.Options(n_sweeps=2, tolerance=1e-8, factored_radius=3, profile_sweeps=True, sweep_kernel=KERNEL[0])
-    ctx.solve2d(srcs, prof, ex.F64, out=out_dev)
-    pst = ctx.stats()
-    launch_ms = pst["sweep_ms"] / max(1, pst["sweeps_launched"])
-    bpl = 24 * nx * nz * fields
+    def prof_solve(o):
+        ctx.solve2d(srcs, o, ex.F64, out=out_dev)
+        return ctx.stats()
+    popts = dict(tolerance=1e-8, factored_radius=3, profile_sweeps=True, sweep_kernel=KERNEL[0])
+    rl = refinement_roofline(prof_solve, ex.Options(n_sweeps=2, **popts), ex.Options(n_sweeps=0, **popts), 24)
     peak, peak_kind = _peaks()
     e2e_ms = []
     out_host = torch.empty((fields, nz, nx), dtype=torch.float64).pin_memory()
@@ -435,13 +462,14 @@ def run_2d(args):
                    "l2": "flushed (write of 2x L2) between timed steps"},
         "roofline": {"bound": "hbm", "kernel": ("sweep2BlockKernel<double,uniform>" if KERNEL[0] == 2 and nz <= 512
                                                 else "sweep2Kernel<double,uniform>"),
-                     "achieved": bpl / (launch_ms / 1e3) / 1e9,
-                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": bpl / (launch_ms / 1e3) / 1e9 / peak, "bytes_per_launch": bpl, "launch_ms": launch_ms,
+                     "achieved": rl["achieved"], "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": rl["achieved"] / peak, "algorithmic_bytes": rl["algorithmic_bytes"],
+                     "node_updates": rl["node_updates"], "refine_ms": rl["refine_ms"], "launch_ms": rl["launch_ms"],
                      "traffic": None, "note": "one field of 126 k nodes: latency-bound wavefront (751 levels)"},
         "e2e": {"value": fields / (float(np.mean(e2e_ms)) / 1e3), "unit": "grids/s", "h2d_bytes_per_step": int(v.nbytes),
                 "d2h_bytes_per_step": int(8 * nx * nz * fields), "ms_per_step": float(np.mean(e2e_ms))},
-        "gpu_launches": int(launches), "clocks": clk.summary(), "iterations": {"max": int(max(iters))},
+        "gpu_launches": int(launches), "clocks": clk.summary(), "iterations": {"max_over_fields": int(max(i[1] for i in iters)),
+                                                                       "min_over_fields": int(min(i[0] for i in iters))},
         "accuracy": acc,
         "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "grids/s", "cores": 1, "kind": "port",
                          "sample": "one full FP64 solve of the configuration by the CPU oracle"},
@@ -634,7 +662,7 @@ def main():
                          "sources on the top surface; models: uneven models, one source each; full: "
                          "512x512x256 h=25 m with a dipping slab, surface sources; 2d: 501x251 FP64")
     ap.add_argument("--fields", type=int, default=None,
-                    help="sources (plain: 32, stations: 64) or models (models: 32) per step per GPU")
+                    help="sources (plain: 64, stations: 64, full: 256) or models (models: 32) per step per GPU")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -660,7 +688,10 @@ def main():
         SLAB[0] = True
         N_SWEEPS_MAX = 20      # the slab model converges more slowly than 10 iterations
     if args.fields is None:
-        args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8}.get(args.workload, 32)
+        # plain: 64 sources per step, where the sweep kernel's throughput saturates on GB300
+        # (32: 252, 64: 292, 128: 292, 256: 313 grids/s); with fewer, a sweep is bound by one
+        # field's wavefront critical path rather than by work
+        args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8, "models": 32}.get(args.workload, 64)
     PAIR[0] = args.pair_fields
     KERNEL[0] = args.sweep_kernel
     if args.profile_case:

@@ -74,7 +74,8 @@ class _Stats(ctypes.Structure):
     _fields_ = [("n_fields", ctypes.c_int), ("iterations_max", ctypes.c_int),
                 ("iterations_min", ctypes.c_int), ("sweeps_launched", ctypes.c_int),
                 ("kernel_launches", ctypes.c_int), ("residual_last", ctypes.c_double),
-                ("device_ms", ctypes.c_double), ("sweep_ms", ctypes.c_double), ("reset_nodes", ctypes.c_longlong)]
+                ("device_ms", ctypes.c_double), ("sweep_ms", ctypes.c_double), ("reset_nodes", ctypes.c_longlong),
+                ("refine_node_updates", ctypes.c_longlong)]
 
 
 class _Src3(ctypes.Structure):

@@ -629,9 +629,11 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     s.iterations_max = 0;
     s.iterations_min = nSrc ? 1 << 30 : 0;
     double rl = 0;
+    const long long nodes = static_cast<long long>(nx) * ny * nz;
     for (int i = 0; i < nSrc; ++i) {
         s.iterations_max = std::max(s.iterations_max, iters[i]);
         s.iterations_min = std::min(s.iterations_min, iters[i]);
+        s.refine_node_updates += nodes * nSweepKinds * iters[i];
         if (iters[i] > 0) {
             for (int e = 0; e < nSweepKinds; ++e) {
                 unsigned long long bits = lastRes[static_cast<size_t>(i) * resStride + nSweepKinds * iters[i] + e];
@@ -1038,9 +1040,14 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     EIKX_CUDA(cudaStreamSynchronize(c->stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    std::vector<long long> unitNodes(nUnits);
+    for (int i = 0; i < nM; ++i)
+        for (int j = 0; j < L[i].nSrc; ++j)
+            unitNodes[L[i].firstUnit + j] = static_cast<long long>(L[i].nx) * L[i].ny * L[i].nz;
     for (int u = 0; u < nUnits; ++u) {
         agg.iterations_max = std::max(agg.iterations_max, iters[u]);
         agg.iterations_min = std::min(agg.iterations_min, iters[u]);
+        agg.refine_node_updates += unitNodes[u] * nSweepKinds * iters[u];
         if (iters[u] > 0)
             for (int e = 0; e < nSweepKinds; ++e) {
                 double r;

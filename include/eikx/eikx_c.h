@@ -104,6 +104,9 @@ typedef struct {
     double device_ms;        /* device time of the solve incl. the copy-out (CUDA events) */
     double sweep_ms;         /* summed device time of the sweep kernels (profile_sweeps), else -1 */
     long long reset_nodes;   /* warm start: initial nodes reset as underestimated (else 0) */
+    long long refine_node_updates;  /* node updates of the refinement sweeps actually run: nodes
+                                       x sweep orderings x iterations, summed over the fields
+                                       (converged fields are skipped, so fields differ) */
 } eikx_stats;
 
 /* ---- context ----------------------------------------------------------- */

@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libeikx_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libeikx_ref.so")
 FLAGS = ["-O2", "-ffp-contract=off", "-fPIC", "-shared"]
+_REF_SKIP_SAID = False
 
 
 def reference_root():
@@ -45,7 +46,10 @@ def build_oracle():
 def build_ref():
     ref = reference_root()
     if not os.path.isdir(os.path.join(ref, "include", "private")):
-        print(f"oracle/_ref: reference sources not found at {ref}; skipped")
+        global _REF_SKIP_SAID
+        if not _REF_SKIP_SAID:
+            print(f"oracle/_ref: reference sources not found at {ref}; skipped", file=sys.stderr)
+            _REF_SKIP_SAID = True
         return None
     os.makedirs(os.path.dirname(REF_LIB), exist_ok=True)
     srcs = [os.path.join(HERE, "ref_driver.cpp")] + [
