@@ -138,6 +138,53 @@ __device__ __forceinline__ T fd3UniformFar(T h, const Stencil3<T> &n) {
     return tUpd;
 }
 
+// fd3UniformFar for a node whose current time is t0, for callers that keep min(t0, result):
+// it returns t0 as soon as a lower bound shows that no operator goes below t0, and leaves
+// out the 8-point operator when its lower bound shows that it cannot be the one below t0.
+// The bounds hold for the rounded values, since round-to-nearest is monotone:
+//   * the 2D operators return t5 + r, t7 + r, t2 + r with r >= 0: each >= t5, t7, t2;
+//   * the 8-point operator returns third * (S + r3) with S = (Tx + Ty) + Tz, r3 >= 0:
+//     it is >= third * S (or huge when its window is closed);
+//   * if t0 <= min(t1d, t2, t5, t7, third * S), fd3UniformFar's result is >= t0;
+//   * if third * S >= min(t0, t1d, t2d), fd3UniformFar's result is below t0 only when
+//     min(t1d, t2d) is, and then it equals min(t1d, t2d).
+// So min(t0, result) is min(t0, fd3UniformFar(h, n)) bit for bit.
+template <class T>
+__device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t0) {
+    EIKX_FD3_UNIFORM_PREFIX
+    (void)tUpd;
+    const T one = 1;
+    const T third = static_cast<T>(0.33333333333333333333333);
+    const T half = static_cast<T>(0.5);
+    const T Tx = t1 + half * (-t4 + t5 - t3 + t2) - t7 + t6;
+    const T Ty = t3 + half * (-t4 + t7 - t1 + t2) - t5 + t6;
+    const T Tz = t4 + half * (-t1 + t5 - t3 + t7) - t2 + t6;
+    const T S = (Tx + Ty) + Tz;
+    const T lo3 = third * S;
+    if (t0 <= dmin(dmin(t1d, dmin(t2, t5)), dmin(t7, lo3))) return t0;
+    T dXZ = t1 - t4;
+    T detXZ = 2 * (hs03 * hs03) - dXZ * dXZ;
+    const bool cXZ = detXZ > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03;
+    const T rXZ = dsqrt(cXZ ? detXZ : one);
+    T t2d = cXZ ? t5 + rXZ : huge;
+    T dYZ = t3 - t4;
+    T detYZ = 2 * (hs01 * hs01) - dYZ * dYZ;
+    const bool cYZ = detYZ > 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01;
+    const T rYZ = dsqrt(cYZ ? detYZ : one);
+    t2d = dmin(t2d, cYZ ? t7 + rYZ : huge);
+    T dXY = t1 - t3;
+    T detXY = 2 * (hs04 * hs04) - dXY * dXY;
+    const bool cXY = detXY > 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04;
+    const T rXY = dsqrt(cXY ? detXY : one);
+    t2d = dmin(t2d, cXY ? t2 + rXY : huge);
+    if (lo3 >= dmin(t0, dmin(t1d, t2d))) return dmin(t1d, t2d);
+    T det = 27 * (h * s0) * (h * s0) - (Tx - Ty) * (Tx - Ty) - (Tx - Tz) * (Tx - Tz) - (Ty - Tz) * (Ty - Tz);
+    const bool c3 = dmin(t1d, t2d) > dmax(dmax(t1, t4), t3) && det >= 0;
+    const T r3 = dsqrt(c3 ? det : one);
+    const T t3d = c3 ? third * (S + r3) : huge;
+    return dmin(t1d, dmin(t2d, t3d));
+}
+
 template <class T>
 __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const SweepSigns &sg,
                                             int ix, int iy, int iz, const Stencil3<T> &n) {

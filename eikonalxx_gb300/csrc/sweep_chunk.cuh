@@ -343,14 +343,16 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
                     n.s5 = sY.v[e];
                     n.s7 = e ? sOwn.v[e - 1] : cS7;
                     const bool near = yzNear && abs(src.isx - xa) <= a.radius;
+                    const T t0 = out.v[e];
                     T tu;
                     if (UNIFORM) {
-                        tu = near ? nearUniform<T>(h, src, sg, xa, ya, za, n) : fd3UniformFar<T>(h, n);
+                        // the Cartesian operators with lower-bound exits: min(t0, tu) is the
+                        // same bit for bit as with fd3UniformFar
+                        tu = near ? nearUniform<T>(h, src, sg, xa, ya, za, n) : fd3UniformFarBounded<T>(h, n, t0);
                     } else {
                         const Spacing3<T> &g = BATCH ? unit->sp3 : a.sp3;
                         tu = near ? nearNonUniform<T>(g, src, sg, xa, ya, za, n) : fd3NonUniformFar<T>(g, n);
                     }
-                    const T t0 = out.v[e];
                     if (tu < t0) {
                         out.v[e] = tu;
                         changed = true;

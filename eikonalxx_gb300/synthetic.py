@@ -19,7 +19,8 @@ def grf(shape, spacing, corr_m, rng):
     k2 = sum(g ** 2 for g in grids)
     # Gaussian kernel exp(-r^2/corr^2) has spectrum ~ exp(-pi^2 corr^2 k^2)
     filt = np.exp(-(np.pi ** 2) * corr_m ** 2 * k2)
-    field = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=shape)
+    axes = list(range(len(shape)))
+    field = np.fft.irfftn(np.fft.rfftn(noise, axes=axes) * filt, s=shape, axes=axes)
     field -= field.mean()
     m = np.max(np.abs(field))
     return field / m if m > 0 else field
