@@ -177,12 +177,13 @@ __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t
     const bool cXY = detXY > 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04;
     const T rXY = dsqrt(cXY ? detXY : one);
     t2d = dmin(t2d, cXY ? t2 + rXY : huge);
-    if (lo3 >= dmin(t0, dmin(t1d, t2d))) return dmin(t1d, t2d);
+    // the 8-point operator under fd3UniformFar's condition, as a branch (its window is
+    // closed for a whole warp at most nodes): min(t1d, t2d, huge) is min(t1d, t2d)
+    const T t12 = dmin(t1d, t2d);
+    if (lo3 >= dmin(t0, t12) || !(t12 > dmax(dmax(t1, t4), t3))) return t12;
     T det = 27 * (h * s0) * (h * s0) - (Tx - Ty) * (Tx - Ty) - (Tx - Tz) * (Tx - Tz) - (Ty - Tz) * (Ty - Tz);
-    const bool c3 = dmin(t1d, t2d) > dmax(dmax(t1, t4), t3) && det >= 0;
-    const T r3 = dsqrt(c3 ? det : one);
-    const T t3d = c3 ? third * (S + r3) : huge;
-    return dmin(t1d, dmin(t2d, t3d));
+    if (!(det >= 0)) return t12;
+    return dmin(t1d, dmin(t2d, third * (S + dsqrt(det))));
 }
 
 template <class T>
