@@ -378,8 +378,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         EIKX_CUDA(cudaMemsetAsync(w.mbox.p, 0, w.mbox.bytes, c->stream));
     }
     if (!w.epoch.p) {
-        EIKX_CUDA(w.epoch.ensure(sizeof(unsigned)));
-        EIKX_CUDA(cudaMemsetAsync(w.epoch.p, 0, sizeof(unsigned), c->stream));
+        EIKX_CUDA(w.epoch.ensure(2 * sizeof(unsigned)));
+        EIKX_CUDA(cudaMemsetAsync(w.epoch.p, 0, 2 * sizeof(unsigned), c->stream));
     }
     EIKX_CUDA(w.queue.ensure(2 * sizeof(unsigned)));
     EIKX_CUDA(w.residual.ensure(static_cast<size_t>(nSrc) * resStride * 8));
@@ -772,8 +772,8 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
         EIKX_CUDA(cudaMemsetAsync(w.mbox.p, 0, w.mbox.bytes, c->stream));
     }
     if (!w.epoch.p) {
-        EIKX_CUDA(w.epoch.ensure(sizeof(unsigned)));
-        EIKX_CUDA(cudaMemsetAsync(w.epoch.p, 0, sizeof(unsigned), c->stream));
+        EIKX_CUDA(w.epoch.ensure(2 * sizeof(unsigned)));
+        EIKX_CUDA(cudaMemsetAsync(w.epoch.p, 0, 2 * sizeof(unsigned), c->stream));
     }
     EIKX_CUDA(w.queue.ensure(2 * sizeof(unsigned)));
     EIKX_CUDA(w.residual.ensure(static_cast<size_t>(nUnits) * resStride * 8));

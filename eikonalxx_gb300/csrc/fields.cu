@@ -289,8 +289,10 @@ __global__ void cells2Kernel(double *slow, const U *c, int nx, int nz, int order
     }
 }
 
-// Start of a solve: fresh residual slots and flags, and a new range of mailbox tags
-// (words written by earlier solves can never match a tag of this one).
+// Start of a solve: fresh residual slots and flags, and a new range of mailbox tags.  The
+// base moves past every tag the previous solve used (epoch[1] holds how many), so words
+// written by earlier solves can never match a tag of this one, whatever their sweep
+// counts; the first base is 1, so zeroed words (tag 0) never match either.
 __global__ void resetKernel(SolveState st, int nFields, int buf) {
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gthreads = gridDim.x * blockDim.x;
@@ -303,7 +305,8 @@ __global__ void resetKernel(SolveState st, int nFields, int buf) {
     if (gtid == 0) {
         *st.queue[buf] = 0u;
         *st.abortFlag = 0;
-        *st.epoch += static_cast<unsigned>(st.epochStride);
+        st.epoch[0] += st.epoch[1] + 1u;
+        st.epoch[1] = static_cast<unsigned>(st.epochStride);
     }
 }
 

@@ -176,9 +176,11 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     float *tt = cv.take<float>(static_cast<size_t>(Px) * ny * nz);
     float *spPos = cv.take<float>(spElems);
     float *spNeg = cv.take<float>(spElems);
-    unsigned long long *mbox = cv.take<unsigned long long>(static_cast<size_t>(nTiles) * (eikx::LY3 + eikx::LZ3) * Px);
+    const size_t mboxWords = static_cast<size_t>(nTiles) * (eikx::LY3 + eikx::LZ3) * Px;
+    unsigned long long *mbox = cv.take<unsigned long long>(mboxWords);
     unsigned long long *residual = cv.take<unsigned long long>(static_cast<size_t>(resStride));
-    unsigned *small = cv.take<unsigned>(8);   // [0..1] queue heads, [2] epoch, [3] abort, [4] converged, [5] iterations
+    // [0..1] queue heads, [3] abort, [4] converged, [5] iterations, [6..7] mailbox epoch
+    unsigned *small = cv.take<unsigned>(8);
     int4 *order = cv.take<int4>(static_cast<size_t>(nTiles));
     eikx::SourceT<float> *srcDev = cv.take<eikx::SourceT<float>>(1);
     eikx::Corner3 *cornerDev = cv.take<eikx::Corner3>(1);
@@ -195,7 +197,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     eikx::SolveState st{};
     st.queue[0] = small;
     st.queue[1] = small + 1;
-    st.epoch = small + 2;
+    st.epoch = small + 6;
     st.abortFlag = reinterpret_cast<int *>(small + 3);
     st.converged = reinterpret_cast<int *>(small + 4);
     st.iterations = reinterpret_cast<int *>(small + 5);
@@ -210,6 +212,10 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     const int spinLog2 = o.spin_limit_log2 > 0 ? std::min(o.spin_limit_log2, 40) : 22;
     st.spinLimit = 1ull << spinLog2;
 
+    // The scratch array is laid out afresh for each grid, so the mailbox and the control
+    // words may hold another call's data: clear them (tag 0 is never a sweep's tag).
+    NOALLOC_CUDA(cudaMemsetAsync(mbox, 0, mboxWords * sizeof(unsigned long long), stream));
+    NOALLOC_CUDA(cudaMemsetAsync(small, 0, 8 * sizeof(unsigned), stream));
     orderKernel<<<(nTiles + 127) / 128, 128, 0, stream>>>(order, tilesY, tilesZ);
     NOALLOC_CUDA(cudaGetLastError());
     sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, slowness, nx - 1, ny - 1, cx, cy, cz, ox, oy, oz);

@@ -17,8 +17,9 @@ constexpr int kWarpsPerBlock = 4;
 struct SolveState {
     unsigned *queue[2];             // work-queue heads, double-buffered across sweeps
     unsigned long long *mbox;       // per warp block: its downstream faces, tagged words
-    unsigned *epoch;                // sweep-tag base, advanced by the reset of each solve
-    int epochStride;                // tags a solve uses (sweep launches + 1)
+    unsigned *epoch;                // [0] sweep-tag base, advanced by the reset of each solve
+                                    // past the tags of the previous one; [1] tags it used
+    int epochStride;                // tags this solve uses (sweep launches + 1)
     unsigned long long *residual;   // [field][sweep slot] largest decrease (double bits)
     int residualStride;             // slots per field
     int *converged;                 // 1 once a field's iteration decrease fell below tol

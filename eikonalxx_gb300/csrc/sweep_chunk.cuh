@@ -111,6 +111,22 @@ template <class T> struct MailChunk {
         return true;
     }
 };
+// The four tagged words a chunk of values would carry in the mailbox.
+template <class T>
+__device__ __forceinline__ void tagWords(unsigned tag, const Vec<T> &v, unsigned long long (&w)[4]) {
+    const unsigned long long t = static_cast<unsigned long long>(tag) << 32;
+    if constexpr (sizeof(T) == 4) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) w[e] = t | __float_as_uint(v.v[e]);
+    } else {
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v.v[e]));
+            w[2 * e] = t | (b & 0xffffffffull);
+            w[2 * e + 1] = t | (b >> 32);
+        }
+    }
+}
 template <class T>
 __device__ __forceinline__ void putChunk(unsigned long long *p, unsigned tag, const Vec<T> &v) {
     const unsigned long long t = static_cast<unsigned long long>(tag) << 32;
@@ -147,7 +163,9 @@ __device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *st.queue[buf ^ 1] = 0u;
 }
 
-template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ>
+// INIT: the source-limited initialisation pass (a.init = 1), compiled apart so that the
+// refinement sweeps carry none of its block skipping.
+template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT>
 __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<T> a) {
     static_assert(LY * LZ == 32 && LZ + 1 + LY <= 32, "a warp holds 32 pencils and its halo helpers");
     constexpr int HY = LY + 1, HZ = LZ + 1;          // ring plane incl. halo row/column
@@ -209,9 +227,19 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
         const int ya = laneValid ? reflect(yp, ny, fy) : 0;
         const int za = laneValid ? reflect(zp, nz, fz) : 0;
         int xlo, xhi, ylo, yhi, zlo, zhi;
-        axisBounds(nx, REV, a.init, src.isx, xlo, xhi);
-        axisBounds(ny, fy, a.init, src.isy, ylo, yhi);
-        axisBounds(nz, fz, a.init, src.isz, zlo, zhi);
+        axisBounds(nx, REV, INIT, src.isx, xlo, xhi);
+        axisBounds(ny, fy, INIT, src.isy, ylo, yhi);
+        axisBounds(nz, fz, INIT, src.isz, zlo, zhi);
+        // Initialisation pass: the update range starts at y' = yp0, z' = zp0 and runs to the
+        // end of each axis.  Warp blocks wholly before it update nothing: they are left out,
+        // and the blocks after them read those rows from the field, which the sweep does not
+        // change, instead of from the mailbox.
+        int bStart = 0, cStart = 0;
+        if constexpr (INIT) {
+            bStart = (fy ? ny - 1 - yhi : ylo) / LY;
+            cStart = (fz ? nz - 1 - zhi : zlo) / LZ;
+            if (b < bStart || c < cStart) continue;
+        }
         const bool yzUpd = laneValid && ya >= ylo && ya <= yhi && za >= zlo && za <= zhi;
         // the factored branch applies within `radius` cells of the source cell on every axis
         const bool yzNear = abs(src.isy - ya) <= a.radius && abs(src.isz - za) <= a.radius;
@@ -234,11 +262,16 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
         unsigned long long *zFace = box + static_cast<long long>(LZ + ly) * Px * W;    // lz == LZ-1
         const int vyp = y0 + vly, vzp = z0 + vlz;
         const bool vValid = helper && vyp >= 0 && vzp >= 0 && vyp < ny && vzp < nz;
+        // the virtual lane's block was left out: its row is read from the field (vbox then
+        // holds the row's address)
+        const bool vField = INIT && vValid && ((vly < 0 && b - 1 < bStart) || (vlz < 0 && c - 1 < cStart));
         const unsigned long long *vbox = box;
         const T *vsrow = sp;
         if (vValid) {
             const int vya = reflect(vyp, ny, fy), vza = reflect(vzp, nz, fz);
-            if (vly < 0) {
+            if (vField) {
+                vbox = reinterpret_cast<const unsigned long long *>(field + (static_cast<long long>(vza) * ny + vya) * Px);
+            } else if (vly < 0) {
                 // block (b-1, c), or the corner block (b-1, c-1): its y' face row
                 vbox = box - (vlz >= 0 ? faceWords : (tilesY + 1) * faceWords) +
                        static_cast<long long>(vlz >= 0 ? vlz : LZ - 1) * Px * W;
@@ -264,7 +297,12 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
         auto issue = [&](int sv) {
             const int kv = haloChunk(sv);
             if (helper && haloValid(kv)) {
-                mslot.issue(vbox + static_cast<long long>(kv) * V * W);
+                if (INIT && vField) {
+                    T *vrow = const_cast<T *>(reinterpret_cast<const T *>(vbox));
+                    tagWords(tag, walk(ldVec(tChunk(vrow, kv))), mslot.w);
+                } else {
+                    mslot.issue(vbox + static_cast<long long>(kv) * V * W);
+                }
                 sslot = ldVec(sChunk(vsrow, kv));
             }
         };
@@ -381,28 +419,37 @@ template <int LY, int LZ> constexpr size_t smemBytes() {
     return 2 * kRingC * (LY + 1) * (LZ + 1) * 16 * kWarpsPerBlock;
 }
 
+template <class T, bool U, bool R, bool B, int LY, int LZ>
+void launchOne(const Sweep3Args<T> &a, int blocks, cudaStream_t s) {
+    const size_t smem = smemBytes<LY, LZ>();
+    if (a.init) sweep3ChunkKernel<T, U, R, B, LY, LZ, true><<<blocks, kThreadsC, smem, s>>>(a);
+    else sweep3ChunkKernel<T, U, R, B, LY, LZ, false><<<blocks, kThreadsC, smem, s>>>(a);
+}
+
 template <class T, bool B, int LY, int LZ>
 void launchShape(const Sweep3Args<T> &a, bool uniform, int blocks, cudaStream_t s) {
-    const size_t smem = smemBytes<LY, LZ>();
     const bool rev = (a.sweep & 1) != 0;
     if (uniform) {
-        if (rev) sweep3ChunkKernel<T, true, true, B, LY, LZ><<<blocks, kThreadsC, smem, s>>>(a);
-        else sweep3ChunkKernel<T, true, false, B, LY, LZ><<<blocks, kThreadsC, smem, s>>>(a);
+        if (rev) launchOne<T, true, true, B, LY, LZ>(a, blocks, s);
+        else launchOne<T, true, false, B, LY, LZ>(a, blocks, s);
     } else {
-        if (rev) sweep3ChunkKernel<T, false, true, B, LY, LZ><<<blocks, kThreadsC, smem, s>>>(a);
-        else sweep3ChunkKernel<T, false, false, B, LY, LZ><<<blocks, kThreadsC, smem, s>>>(a);
+        if (rev) launchOne<T, false, true, B, LY, LZ>(a, blocks, s);
+        else launchOne<T, false, false, B, LY, LZ>(a, blocks, s);
     }
 }
 
 template <class T, bool B, int LY, int LZ> int blocksPerSM(bool uniform) {
-    // the two sweep directions differ only in addressing; take the lower occupancy
+    // the persistent grid is sized for the refinement sweeps (the two directions differ only
+    // in addressing; take the lower occupancy).  An initialisation sweep whose kernel fits
+    // fewer blocks runs the rest as they free up: a block dequeues work only once resident
+    // and waits only on work dequeued before it, so no wait depends on a block not running.
     const void *k[2];
     if (uniform) {
-        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, false, B, LY, LZ>);
-        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, true, B, LY, LZ>);
+        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, false, B, LY, LZ, false>);
+        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, true, B, LY, LZ, false>);
     } else {
-        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, false, B, LY, LZ>);
-        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, true, B, LY, LZ>);
+        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, false, B, LY, LZ, false>);
+        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, true, B, LY, LZ, false>);
     }
     int best = 1 << 30;
     for (const void *f : k) {

@@ -1,4 +1,9 @@
-"""Many refinement iterations of the chunk-step kernel against the oracle, bit for bit.
+"""Work the chunk-step kernel leaves out, checked against the oracle bit for bit.
+
+The initialisation pass updates only the octant of each sweep that lies downstream of the
+source; warp blocks wholly before it along y' or z' are left out and their rows are read
+from the field by the blocks after them.  Sources in corners, on faces and in the middle
+put the octant boundary in every position relative to the warp blocks.
 
 The kernel evaluates the Cartesian (far-field) operators with lower-bound exits
 (local_solver.cuh, fd3UniformFarBounded): it stops as soon as the rounded lower bounds of
@@ -104,3 +109,87 @@ def test_batch_of_smooth_models_exact(ctx, oracle, precision):
         for j, (pos, cell) in enumerate(srcs):
             ref = oracle.solve3d(cells, g, cell, pos, n_sweeps=6, radius=3)
             assert np.array_equal(_bits(out[j]), _bits(ref)), (g, j)
+
+
+CORNERS = [(0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (1.0, 0.0, 0.5), (0.0, 1.0, 1.0), (0.5, 0.5, 0.0), (0.37, 0.81, 0.66),
+           (0.99, 0.02, 0.51), (0.12, 0.93, 0.97)]
+
+
+@pytest.mark.parametrize("precision", [ex.F32, ex.F64])
+@pytest.mark.parametrize("block_shape", [1, 2, 3])
+def test_initialisation_pass_for_sources_anywhere(ctx, oracle, precision, block_shape):
+    """n_sweeps = 0: the field after the 8 source-limited sweeps alone."""
+    shape = (29, 35, 23, 40., 40., 40.)
+    nx, ny, nz, dx, dy, dz = shape
+    dt = np.float32 if precision == ex.F32 else np.float64
+    cells = _cells(oracle, shape, 14, dt)
+    ctx.set_grid3d(*shape)
+    ctx.set_slowness3d(cells)
+    pos = [(fx * (nx - 1) * dx, fy * (ny - 1) * dy, fz * (nz - 1) * dz) for fx, fy, fz in CORNERS]
+    for n_sweeps in (0, 1):
+        opt = ex.Options(n_sweeps=n_sweeps, tolerance=-1, factored_radius=3, sweep_kernel=2,
+                         block_shape=block_shape)
+        t = ctx.solve3d(pos, opt, precision)
+        for p, a in zip(pos, t):
+            cell = [min(k - 2, int(q / h)) for q, k, h in zip(p, (nx, ny, nz), (dx, dy, dz))]
+            ref = oracle.solve3d(cells, shape, cell, p, n_sweeps=n_sweeps, radius=3)
+            assert np.array_equal(_bits(a), _bits(ref)), (p, n_sweeps, np.abs(a - ref).max())
+
+
+def test_initialisation_pass_of_a_batch(ctx, oracle):
+    grids = [(26, 33, 21, 50., 50., 50.), (40, 17, 30, 50., 50., 50.)]
+    models, refs = [], []
+    for k, g in enumerate(grids):
+        nx, ny, nz, dx, dy, dz = g
+        cells = _cells(oracle, g, 40 + k, np.float32)
+        pos = [(fx * (nx - 1) * dx, fy * (ny - 1) * dy, fz * (nz - 1) * dz) for fx, fy, fz in CORNERS[:4]]
+        models.append({"grid": g + (0., 0., 0.), "model": cells, "sources": pos})
+        refs.append((cells, pos))
+    outs = ctx.solve3d_batch(models, ex.Options(n_sweeps=0, tolerance=-1, factored_radius=3), ex.F32)
+    for g, (cells, pos), out in zip(grids, refs, outs):
+        nx, ny, nz, dx, dy, dz = g
+        for j, p in enumerate(pos):
+            cell = [min(k - 2, int(q / h)) for q, k, h in zip(p, (nx, ny, nz), (dx, dy, dz))]
+            ref = oracle.solve3d(cells, g, cell, p, n_sweeps=0, radius=3)
+            assert np.array_equal(_bits(out[j]), _bits(ref)), (g, j)
+
+
+@pytest.mark.parametrize("block_shape", [1, 2, 3])
+def test_mailbox_tags_after_a_longer_solve(ctx, oracle, block_shape):
+    """A solve with fewer sweeps than the one before it must not meet that solve's mailbox
+    words under its own tags, whatever the layout in between (precision, grid, warp block)."""
+    rng = np.random.default_rng(50 + block_shape)
+    long_shape, short_shape = (31, 27, 25, 40., 40., 40.), (29, 35, 23, 40., 40., 40.)
+    cells = _cells(oracle, long_shape, 51, np.float64)
+    ctx.set_grid3d(*long_shape)
+    ctx.set_slowness3d(cells)
+    ctx.solve3d([p for p, _ in _sources(rng, long_shape, 8)], ex.Options(n_sweeps=9, tolerance=-1), ex.F64)
+    nx, ny, nz, dx, dy, dz = short_shape
+    cells = _cells(oracle, short_shape, 52, np.float32)
+    ctx.set_grid3d(*short_shape)
+    ctx.set_slowness3d(cells)
+    pos = [(fx * (nx - 1) * dx, fy * (ny - 1) * dy, fz * (nz - 1) * dz) for fx, fy, fz in CORNERS]
+    for n_sweeps in (0, 1):
+        t = ctx.solve3d(pos, ex.Options(n_sweeps=n_sweeps, tolerance=-1, sweep_kernel=2, block_shape=block_shape),
+                        ex.F32)
+        for p, a in zip(pos, t):
+            cell = [min(k - 2, int(q / h)) for q, k, h in zip(p, (nx, ny, nz), (dx, dy, dz))]
+            ref = oracle.solve3d(cells, short_shape, cell, p, n_sweeps=n_sweeps, radius=3)
+            assert np.array_equal(_bits(a), _bits(ref)), (p, n_sweeps, np.abs(a - ref).max())
+
+
+def test_batch_mailbox_tags_after_a_longer_batch(ctx, oracle):
+    rng = np.random.default_rng(60)
+    first = [{"grid": (30, 26, 20, 50., 50., 50., 0., 0., 0.), "model": _cells(oracle, (30, 26, 20, 50.), 61, np.float64),
+              "sources": [p for p, _ in _sources(rng, (30, 26, 20, 50., 50., 50.), 3)]}]
+    ctx.solve3d_batch(first, ex.Options(n_sweeps=8, tolerance=-1), ex.F64)
+    g = (26, 33, 21, 50., 50., 50.)
+    nx, ny, nz, dx, dy, dz = g
+    cells = _cells(oracle, g, 62, np.float32)
+    pos = [(fx * (nx - 1) * dx, fy * (ny - 1) * dy, fz * (nz - 1) * dz) for fx, fy, fz in CORNERS]
+    out = ctx.solve3d_batch([{"grid": g + (0., 0., 0.), "model": cells, "sources": pos}],
+                            ex.Options(n_sweeps=0, tolerance=-1), ex.F32)[0]
+    for j, p in enumerate(pos):
+        cell = [min(k - 2, int(q / h)) for q, k, h in zip(p, (nx, ny, nz), (dx, dy, dz))]
+        ref = oracle.solve3d(cells, g, cell, p, n_sweeps=0, radius=3)
+        assert np.array_equal(_bits(out[j]), _bits(ref)), j
