@@ -90,6 +90,17 @@ bool locate(double x, double x0, double d, int n, int *cell, double *offset) {
     return true;
 }
 
+// Convergence test after refinement sweep j (counted over all refinement iterations from 0):
+// a field stops once each of its last nSweepKinds refinement sweeps decreased no node by tol
+// or more.  The window slides sweep by sweep and may span two iterations; the first full
+// window ends with the first iteration.  Slot nSweepKinds + j holds sweep j's residual.
+cudaError_t checkAfterSweep(const eikx::SolveState &st, int nFields, int nSweepKinds, int j, double tol,
+                            cudaStream_t s) {
+    const int lo = std::max(0, j - (nSweepKinds - 1));
+    return eikx::launchCheckConvergence(st, nFields, nSweepKinds + lo, j - lo + 1, j + 1,
+                                        j >= nSweepKinds - 1 ? tol : -1.0, s);
+}
+
 struct Workspace {
     DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, pairs, init,
         resetCount;
@@ -449,7 +460,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     st.residual = w.residual.as<unsigned long long>();
     st.residualStride = resStride;
     st.converged = w.converged.as<int>();
-    st.iterations = w.iterations.as<int>();
+    st.sweepsRun = w.iterations.as<int>();
     st.abortFlag = w.abortFlag.as<int>();
     // test hook: leave the first blocks of the queue out (their dependants time out)
     const int drop = std::min(std::max(o.test_drop_blocks, 0), nProgress);
@@ -569,11 +580,11 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
             for (int e = 0; e < nSweepKinds; ++e)
                 if (eikx_status r = sweep(e, 1, e); r != EIKX_OK) return r;
         for (int k = 0; k < nSweeps; ++k) {
-            for (int e = 0; e < nSweepKinds; ++e)
+            for (int e = 0; e < nSweepKinds; ++e) {
                 if (eikx_status r = sweep(e, 0, nSweepKinds * (1 + k) + e); r != EIKX_OK) return r;
-            EIKX_CUDA(eikx::launchCheckConvergence(st, nSrc, nSweepKinds * (1 + k), nSweepKinds, k, o.tolerance,
-                                                   c->stream));
-            ++launches;
+                EIKX_CUDA(checkAfterSweep(st, nSrc, nSweepKinds, nSweepKinds * k + e, o.tolerance, c->stream));
+                ++launches;
+            }
         }
         return EIKX_OK;
     };
@@ -631,12 +642,15 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     double rl = 0;
     const long long nodes = static_cast<long long>(nx) * ny * nz;
     for (int i = 0; i < nSrc; ++i) {
-        s.iterations_max = std::max(s.iterations_max, iters[i]);
-        s.iterations_min = std::min(s.iterations_min, iters[i]);
-        s.refine_node_updates += nodes * nSweepKinds * iters[i];
-        if (iters[i] > 0) {
-            for (int e = 0; e < nSweepKinds; ++e) {
-                unsigned long long bits = lastRes[static_cast<size_t>(i) * resStride + nSweepKinds * iters[i] + e];
+        // iters[i] holds the refinement sweeps the field ran; report iterations begun
+        const int sweepsRun = iters[i], it = (sweepsRun + nSweepKinds - 1) / nSweepKinds;
+        s.iterations_max = std::max(s.iterations_max, it);
+        s.iterations_min = std::min(s.iterations_min, it);
+        s.refine_node_updates += nodes * sweepsRun;
+        if (sweepsRun > 0) {
+            // the residual window: the last nSweepKinds refinement sweeps the field ran
+            for (int j = std::max(0, sweepsRun - nSweepKinds); j < sweepsRun; ++j) {
+                unsigned long long bits = lastRes[static_cast<size_t>(i) * resStride + nSweepKinds + j];
                 double r;
                 std::memcpy(&r, &bits, sizeof(r));
                 rl = std::max(rl, r);
@@ -920,7 +934,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     st.residual = w.residual.as<unsigned long long>();
     st.residualStride = resStride;
     st.converged = w.converged.as<int>();
-    st.iterations = w.iterations.as<int>();
+    st.sweepsRun = w.iterations.as<int>();
     st.abortFlag = w.abortFlag.as<int>();
     st.order = w.order.as<int4>();
     st.totalItems = static_cast<int>(nItems);
@@ -972,11 +986,11 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
             for (int e = 0; e < nSweepKinds; ++e)
                 if (eikx_status r = sweep(e, 1, e); r != EIKX_OK) return r;
         for (int k = 0; k < nSweeps; ++k) {
-            for (int e = 0; e < nSweepKinds; ++e)
+            for (int e = 0; e < nSweepKinds; ++e) {
                 if (eikx_status r = sweep(e, 0, nSweepKinds * (1 + k) + e); r != EIKX_OK) return r;
-            EIKX_CUDA(eikx::launchCheckConvergence(st, nUnits, nSweepKinds * (1 + k), nSweepKinds, k, o.tolerance,
-                                                   c->stream));
-            ++launches;
+                EIKX_CUDA(checkAfterSweep(st, nUnits, nSweepKinds, nSweepKinds * k + e, o.tolerance, c->stream));
+                ++launches;
+            }
         }
         return EIKX_OK;
     };
@@ -1045,13 +1059,15 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
         for (int j = 0; j < L[i].nSrc; ++j)
             unitNodes[L[i].firstUnit + j] = static_cast<long long>(L[i].nx) * L[i].ny * L[i].nz;
     for (int u = 0; u < nUnits; ++u) {
-        agg.iterations_max = std::max(agg.iterations_max, iters[u]);
-        agg.iterations_min = std::min(agg.iterations_min, iters[u]);
-        agg.refine_node_updates += unitNodes[u] * nSweepKinds * iters[u];
-        if (iters[u] > 0)
-            for (int e = 0; e < nSweepKinds; ++e) {
+        // iters[u] holds the refinement sweeps the unit ran; report iterations begun
+        const int sweepsRun = iters[u], it = (sweepsRun + nSweepKinds - 1) / nSweepKinds;
+        agg.iterations_max = std::max(agg.iterations_max, it);
+        agg.iterations_min = std::min(agg.iterations_min, it);
+        agg.refine_node_updates += unitNodes[u] * sweepsRun;
+        if (sweepsRun > 0)
+            for (int j = std::max(0, sweepsRun - nSweepKinds); j < sweepsRun; ++j) {
                 double r;
-                std::memcpy(&r, &res[static_cast<size_t>(u) * resStride + nSweepKinds * iters[u] + e], sizeof(r));
+                std::memcpy(&r, &res[static_cast<size_t>(u) * resStride + nSweepKinds + j], sizeof(r));
                 agg.residual_last = std::max(agg.residual_last, r);
             }
     }

@@ -300,7 +300,7 @@ __global__ void resetKernel(SolveState st, int nFields, int buf) {
     for (long long i = gtid; i < nres; i += gthreads) st.residual[i] = 0ull;
     for (int i = gtid; i < nFields; i += gthreads) {
         st.converged[i] = 0;
-        st.iterations[i] = 0;
+        st.sweepsRun[i] = 0;
     }
     if (gtid == 0) {
         *st.queue[buf] = 0u;
@@ -310,9 +310,9 @@ __global__ void resetKernel(SolveState st, int nFields, int buf) {
     }
 }
 
-// After refinement iteration `iteration`: a field whose largest decrease over the
-// iteration's sweeps fell below tol is frozen (later sweeps skip it).
-__global__ void checkKernel(SolveState st, int nFields, int firstSlot, int nSlots, int iteration,
+// After a refinement sweep: a field whose largest decrease in each of the last sweeps of the
+// window (slots [firstSlot, firstSlot + nSlots)) fell below tol is frozen; later sweeps skip it.
+__global__ void checkKernel(SolveState st, int nFields, int firstSlot, int nSlots, int sweepsDone,
                             double tol) {
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nFields; f += gridDim.x * blockDim.x) {
         if (st.converged[f]) continue;
@@ -320,7 +320,7 @@ __global__ void checkKernel(SolveState st, int nFields, int firstSlot, int nSlot
         for (int k = 0; k < nSlots; ++k)
             m = fmax(m, __longlong_as_double(static_cast<long long>(
                             st.residual[static_cast<long long>(f) * st.residualStride + firstSlot + k])));
-        st.iterations[f] = iteration + 1;
+        st.sweepsRun[f] = sweepsDone;
         if (m < tol) st.converged[f] = 1;
     }
 }
@@ -470,9 +470,9 @@ cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots, int iteration,
+cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots, int sweepsDone,
                                    double tol, cudaStream_t s) {
-    checkKernel<<<gridFor(nFields, 128), 128, 0, s>>>(st, nFields, firstSlot, nSlots, iteration, tol);
+    checkKernel<<<gridFor(nFields, 128), 128, 0, s>>>(st, nFields, firstSlot, nSlots, sweepsDone, tol);
     return cudaGetLastError();
 }
 cudaError_t launchAnalytic3(double *t, int nx, int ny, int nz, double dx, double dy, double dz, double xs,

@@ -200,7 +200,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     st.epoch = small + 6;
     st.abortFlag = reinterpret_cast<int *>(small + 3);
     st.converged = reinterpret_cast<int *>(small + 4);
-    st.iterations = reinterpret_cast<int *>(small + 5);
+    st.sweepsRun = reinterpret_cast<int *>(small + 5);
     st.mbox = mbox;
     st.epochStride = nSweepLaunches + 1;
     st.residual = residual;
@@ -253,9 +253,13 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
         for (int e = 0; e < 8; ++e)
             if (eikx_status r = sweep(e, 1, e); r != EIKX_OK) return r;
     for (int k = 0; k < nSweeps; ++k) {
-        for (int e = 0; e < 8; ++e)
+        for (int e = 0; e < 8; ++e) {
             if (eikx_status r = sweep(e, 0, 8 * (1 + k) + e); r != EIKX_OK) return r;
-        NOALLOC_CUDA(eikx::launchCheckConvergence(st, 1, 8 * (1 + k), 8, k, o.tolerance, stream));
+            // the window: the last 8 refinement sweeps (fewer in the first iteration: no test)
+            const int j = 8 * k + e, lo = std::max(0, j - 7);
+            NOALLOC_CUDA(eikx::launchCheckConvergence(st, 1, 8 + lo, j - lo + 1, j + 1, j >= 7 ? o.tolerance : -1.0,
+                                                      stream));
+        }
     }
     NOALLOC_CUDA(cudaMemcpy2DAsync(tOut, static_cast<size_t>(nx) * sizeof(float), tt, static_cast<size_t>(Px) * sizeof(float),
                                    static_cast<size_t>(nx) * sizeof(float), static_cast<size_t>(ny) * nz,

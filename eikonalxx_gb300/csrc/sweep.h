@@ -23,7 +23,7 @@ struct SolveState {
     unsigned long long *residual;   // [field][sweep slot] largest decrease (double bits)
     int residualStride;             // slots per field
     int *converged;                 // 1 once a field's iteration decrease fell below tol
-    int *iterations;                // refinement iterations each field ran
+    int *sweepsRun;                 // refinement sweeps each field ran
     int *abortFlag;                 // raised when a bounded wait ran out
     const int4 *order;              // work queue: (field, by, bz, 0) sorted by start step
     int totalItems;                 // fields * warp blocks per field
@@ -174,8 +174,10 @@ cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldSt
                             int fp64, unsigned long long *nReset, cudaStream_t s);
 // Sets *flag (ORs 1) if any of the n slownesses is not positive and finite.
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st);
+// After refinement sweep `sweepsDone - 1`: a field whose residual slots
+// [firstSlot, firstSlot + nSlots) all fell below tol is frozen (later sweeps skip it).
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,
-                                   int iteration, double tol, cudaStream_t s);
+                                   int sweepsDone, double tol, cudaStream_t s);
 // Products of a solved field (post.cu): the travel-time gradient (3 or 2 values per
 // natural node) and travel times at stations (cells and origin offsets per station).
 template <class T>

@@ -5,8 +5,8 @@
 // index in the EIKX_DEVICE environment variable) through the C ABI of
 // include/eikx/eikx_c.h: travel times initialised at the 8 corners of the source cell,
 // one source-limited pass of the 8 sweeps, then up to getNumberOfSweeps() iterations of
-// the 8 sweeps, stopping after an iteration whose largest decrease is below the
-// convergence tolerance.  Solver3D<float> sweeps in FP32, Solver3D<double> in FP64.
+// the 8 sweeps, stopping once each of the last 8 sweeps decreased no travel time by the
+// convergence tolerance or more.  Solver3D<float> sweeps in FP32, Solver3D<double> in FP64.
 // Errors are std::invalid_argument (bad input) and std::runtime_error (wrong order of
 // calls, GPU failure), as the reference throws.  Not thread-safe.
 #ifndef EIKONALXX_SOLVER_3D_HPP

@@ -1,8 +1,8 @@
 // Solver options (drop-in for include/eikonalxx/solverOptions.hpp:11-111 of the
 // reference).  Defaults as src/solverOptions.cpp:5-21: 5 refinement iterations,
 // tolerance 1e-5 s, factored-eikonal radius 3, level-set algorithm, Error verbosity.
-// Unlike the reference, the tolerance is applied: a solve ends after the first
-// iteration whose largest travel-time decrease is below it.
+// Unlike the reference, the tolerance is applied: a solve ends once each of its last
+// 8 (3D) / 4 (2D) refinement sweeps decreased no travel time by the tolerance or more.
 #ifndef EIKONALXX_SOLVER_OPTIONS_HPP
 #define EIKONALXX_SOLVER_OPTIONS_HPP
 #include <cstdint>

@@ -48,9 +48,11 @@ enum { EIKX_HOST = 0, EIKX_DEVICE = 1 };             /* where a pointer lives */
  * (include/eikonalxx/solverOptions.hpp:11-111, defaults src/solverOptions.cpp:5-21). */
 typedef struct {
     int n_sweeps;          /* refinement iterations, each = all 8 (3D) / 4 (2D) sweeps; default 5 */
-    double tolerance;      /* s; an iteration whose largest decrease is below this ends the
-                              solve (the reference stores but never applies it); <= 0 runs
-                              all n_sweeps iterations, as the reference does; default 1e-5 */
+    double tolerance;      /* s; a field stops once each of its last 8 (3D) / 4 (2D)
+                              refinement sweeps decreased no node by this or more (a window
+                              that slides sweep by sweep across iterations; the reference
+                              stores the tolerance but never applies it); <= 0 runs all
+                              n_sweeps iterations, as the reference does; default 1e-5 */
     int factored_radius;   /* factored-eikonal radius in grid points; default 3 */
     int init_sweeps;       /* 1 = run the source-limited initialisation pass first; default 1 */
     int init_fp64;         /* 1 = source-corner times computed in FP64 then rounded to the
@@ -96,17 +98,18 @@ typedef struct { double x, z; } eikx_source2d;
 /* Per-solve statistics of the last eikx_solve3d/2d call on a context. */
 typedef struct {
     int n_fields;            /* fields solved by the call */
-    int iterations_max;      /* largest number of refinement iterations any field ran */
+    int iterations_max;      /* largest number of refinement iterations any field began */
     int iterations_min;
     int sweeps_launched;     /* sweep kernels launched (init pass included) */
     int kernel_launches;     /* all kernels launched by the call (graph nodes included) */
-    double residual_last;    /* largest decrease of the last iteration over all fields (s) */
+    double residual_last;    /* largest decrease over each field's last 8 (3D) / 4 (2D)
+                                refinement sweeps, over all fields (s) */
     double device_ms;        /* device time of the solve incl. the copy-out (CUDA events) */
     double sweep_ms;         /* summed device time of the sweep kernels (profile_sweeps), else -1 */
     long long reset_nodes;   /* warm start: initial nodes reset as underestimated (else 0) */
     long long refine_node_updates;  /* node updates of the refinement sweeps actually run: nodes
-                                       x sweep orderings x iterations, summed over the fields
-                                       (converged fields are skipped, so fields differ) */
+                                       x refinement sweeps, summed over the fields (a field
+                                       that has converged is skipped, so fields differ) */
 } eikx_stats;
 
 /* ---- context ----------------------------------------------------------- */

@@ -18,8 +18,9 @@
 //      (src/solver2d.cpp:61-105, src/solver3d.cpp:21-84);
 //   2. one initialisation pass of all sweeps restricted to the source quadrant/octant
 //      (getLoopLimits with source, solverUtilities3d.hpp:1075-1184);
-//   3. nSweeps refinement iterations of all sweeps over the full grid; new: an
-//      iteration whose largest decrease is below the tolerance ends the solve.
+//   3. nSweeps refinement iterations of all sweeps over the full grid; new: the solve
+//      ends once each of the last 8 (3D) / 4 (2D) refinement sweeps decreased no node by
+//      the tolerance or more.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -499,15 +500,20 @@ int solve3(const Grid3 &g, const Src3 &src, const T *slow, int nSweeps, int radi
     T sSrc = slow[static_cast<size_t>(src.isz) * ncx * ncy + static_cast<size_t>(src.isy) * ncx + src.isx];
     if (doInitSweeps)
         for (int e = 0; e < 8; ++e) sweep3<T>(e, true, g, radius, src, sSrc, slow, tt);
-    int k = 0;
-    for (; k < nSweeps; ++k) {
-        double itMax = 0;
+    // the solve ends once each of the last 8 refinement sweeps (a window that may span two
+    // iterations) decreased no node by tol or more; *nIter = refinement iterations begun
+    int k = 0, quiet = 0;
+    bool done = false;
+    for (; k < nSweeps && !done; ++k) {
         for (int e = 0; e < 8; ++e) {
             double r = sweep3<T>(e, false, g, radius, src, sSrc, slow, tt);
             if (residuals) residuals[k * 8 + e] = r;
-            itMax = std::max(itMax, r);
+            quiet = r < tol ? quiet + 1 : 0;
+            if (quiet >= 8) {
+                done = true;
+                break;
+            }
         }
-        if (itMax < tol) { ++k; break; }
     }
     if (nIter) *nIter = k;
     return 0;
@@ -813,15 +819,19 @@ int solve2(const Grid2 &g, const Src2 &src, const T *slow, int nSweeps, int radi
     T sSrc = slow[static_cast<size_t>(src.isz) * (g.nx - 1) + src.isx];
     if (doInitSweeps)
         for (int e = 0; e < 4; ++e) sweep2<T>(e, true, g, radius, src, sSrc, slow, tt);
-    int k = 0;
-    for (; k < nSweeps; ++k) {
-        double itMax = 0;
+    // as solve3, with a window of the last 4 refinement sweeps
+    int k = 0, quiet = 0;
+    bool done = false;
+    for (; k < nSweeps && !done; ++k) {
         for (int e = 0; e < 4; ++e) {
             double r = sweep2<T>(e, false, g, radius, src, sSrc, slow, tt);
             if (residuals) residuals[k * 4 + e] = r;
-            itMax = std::max(itMax, r);
+            quiet = r < tol ? quiet + 1 : 0;
+            if (quiet >= 4) {
+                done = true;
+                break;
+            }
         }
-        if (itMax < tol) { ++k; break; }
     }
     if (nIter) *nIter = k;
     return 0;

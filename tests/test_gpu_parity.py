@@ -92,7 +92,13 @@ def test_convergence_stops_like_the_oracle(ctx, oracle):
     t_or, res, it = oracle.solve3d(s, shape, cell, off, n_sweeps=20, radius=0, tol=1e-6, residuals=True)
     assert st["iterations_max"] == it < 20
     assert np.array_equal(_bits(t), _bits(t_or))
-    assert st["residual_last"] == pytest.approx(res[-1].max(), rel=0, abs=0)
+    # the field stops after the first run of 8 sweeps with decreases below tol; residual_last
+    # is the largest decrease of that window
+    r = res.ravel()
+    quiet = np.convolve((r < 1e-6).astype(int), np.ones(8, int), "valid")
+    stop = int(np.argmax(quiet == 8)) + 8
+    assert (it - 1) * 8 < stop <= it * 8
+    assert st["residual_last"] == pytest.approx(r[stop - 8:stop].max(), rel=0, abs=0)
 
 
 def test_slowness_orderings_and_device_inputs(ctx, oracle):
