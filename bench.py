@@ -245,6 +245,21 @@ def run_gpu(args):
         traffic = tr["dram_bytes_per_launch"] * fields / tr["fields"]
         traffic_src = f"profiles/sweep3d_traffic.json ({tr['fields']} fields, scaled to {fields})"
 
+    # the configuration's own form, one source per solve: bound by one field's wavefront
+    # latency rather than by throughput (device-resident, CUDA events, not the headline)
+    single = None
+    if rank == 0 and not SURFACE[0] and not SLAB[0]:
+        one = torch.empty((1, NZ, NY, NX), dtype=torch.float32, device=f"cuda:{dev}")
+        for _ in range(3):
+            ctx.solve3d(src[:1], opt, ex.F32, out=one)
+        t1 = []
+        for _ in range(5):
+            flush.fill_(1.0)
+            ctx.solve3d(src[:1], opt, ex.F32, out=one)
+            t1.append(ctx.stats()["device_ms"])
+        single = {"grids_s": 1e3 / float(np.mean(t1)), "ms_per_solve": float(np.mean(t1)),
+                  "iterations": ctx.stats()["iterations_max"]}
+
     # end to end through the public API with host buffers every step
     e2e_ms = []
     for i in range(max(1, args.warmup) + args.steps):
@@ -282,6 +297,7 @@ def run_gpu(args):
         "gpu_launches": int(launches), "clocks": clk.summary(),
         "iterations": {"max_over_fields": int(max(i[1] for i in iters)),
                        "min_over_fields": int(min(i[0] for i in iters))},
+        "single_source": single,
         "wall_ms_per_step": float(np.mean(wall)), "accuracy": acc, "tuning": tuning,
         "cpu_baseline": (cpu_baseline(args.cpu_seconds, 1, _sweeps_per_grid(max(i[1] for i in iters)))
                          if not args.skip_cpu else None),
