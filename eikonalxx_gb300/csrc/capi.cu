@@ -162,7 +162,8 @@ struct eikx_ctx {
     double dx = 0, dy = 0, dz = 0, x0 = 0, y0 = 0, z0 = 0;
     bool haveGrid3 = false, haveSlow3 = false;
     DevBuf slow3;                  // natural-order cell slowness, FP64
-    std::vector<double> hostSlow3; // host mirror (source-cell slowness lookups)
+    mutable std::vector<double> hostSlow3;   // host copy, fetched when first asked for
+    mutable bool hostSlow3Valid = false;
     DevBuf spad3[2][2];            // [precision][0: shifted for +x sweeps, 1: unshifted]
     bool spadValid3[2] = {false, false};
     // 2D model
@@ -170,7 +171,10 @@ struct eikx_ctx {
     double dx2 = 0, dz2 = 0, x02 = 0, z02 = 0;
     bool haveGrid2 = false, haveSlow2 = false;
     DevBuf slow2;
-    std::vector<double> hostSlow2;
+    mutable std::vector<double> hostSlow2;
+    mutable bool hostSlow2Valid = false;
+    DevBuf modelFlag;              // raised by the device checks of a new model
+    PinnedBuf srcSlow;             // source-cell slownesses of a solve, read from the device
     DevBuf spad2[2][2];
     bool spadValid2[2] = {false, false};
     DevBuf scratch;                // staging for host inputs and analytic fields
@@ -245,33 +249,49 @@ eikx_status toDevice(eikx_ctx *c, const U *src, size_t n, int where, const U **d
     return EIKX_OK;
 }
 
-eikx_status finishModel3(eikx_ctx *c) {
-    const size_t nCell = static_cast<size_t>(c->nx - 1) * (c->ny - 1) * (c->nz - 1);
-    c->hostSlow3.resize(nCell);
-    EIKX_CUDA(cudaMemcpyAsync(c->hostSlow3.data(), c->slow3.p, nCell * sizeof(double), cudaMemcpyDeviceToHost,
-                              c->stream));
+// A new model is checked on the device (the input was checked by setCells into the same
+// flag): every cell slowness must be positive and finite.  Only the flag comes back; the
+// host copy of the model is fetched when eikx_get_slowness asks for it.  The cached
+// schedule graph stays valid: it holds buffer addresses, and the padded copies are rebuilt
+// before the next launch.
+eikx_status finishModel(eikx_ctx *c, int dim) {
+    const size_t nCell = dim == 3 ? static_cast<size_t>(c->nx - 1) * (c->ny - 1) * (c->nz - 1)
+                                  : static_cast<size_t>(c->nx2 - 1) * (c->nz2 - 1);
+    const DevBuf &slow = dim == 3 ? c->slow3 : c->slow2;
+    EIKX_CUDA(eikx::launchCheckPositive(slow.as<double>(), static_cast<long long>(nCell), c->modelFlag.as<int>(),
+                                        c->stream));
+    int bad = 0;
+    EIKX_CUDA(cudaMemcpyAsync(&bad, c->modelFlag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     EIKX_CUDA(cudaStreamSynchronize(c->stream));
-    for (double s : c->hostSlow3)
-        if (!(s > 0) || !std::isfinite(s))
-            return fail(EIKX_ERR_INVALID, "Non-positive velocities detected");
-    c->spadValid3[0] = c->spadValid3[1] = false;
-    c->haveSlow3 = true;
-    dropGraph(c);
+    if (dim == 3) {
+        c->haveSlow3 = false;
+        c->hostSlow3Valid = false;
+        c->spadValid3[0] = c->spadValid3[1] = false;
+    } else {
+        c->haveSlow2 = false;
+        c->hostSlow2Valid = false;
+        c->spadValid2[0] = c->spadValid2[1] = false;
+    }
+    if (bad) return fail(EIKX_ERR_INVALID, "Non-positive velocities detected");
+    (dim == 3 ? c->haveSlow3 : c->haveSlow2) = true;
     return EIKX_OK;
 }
 
-eikx_status finishModel2(eikx_ctx *c) {
-    const size_t nCell = static_cast<size_t>(c->nx2 - 1) * (c->nz2 - 1);
-    c->hostSlow2.resize(nCell);
-    EIKX_CUDA(cudaMemcpyAsync(c->hostSlow2.data(), c->slow2.p, nCell * sizeof(double), cudaMemcpyDeviceToHost,
-                              c->stream));
-    EIKX_CUDA(cudaStreamSynchronize(c->stream));
-    for (double s : c->hostSlow2)
-        if (!(s > 0) || !std::isfinite(s))
-            return fail(EIKX_ERR_INVALID, "Non-positive velocities detected");
-    c->spadValid2[0] = c->spadValid2[1] = false;
-    c->haveSlow2 = true;
-    dropGraph(c);
+// The host copy of the cell slowness (natural order, FP64), fetched once per model.
+eikx_status hostSlowness(const eikx_ctx *c, int dim, const std::vector<double> **out) {
+    std::vector<double> &h = dim == 3 ? c->hostSlow3 : c->hostSlow2;
+    bool &valid = dim == 3 ? c->hostSlow3Valid : c->hostSlow2Valid;
+    if (!valid) {
+        const size_t nCell = dim == 3 ? static_cast<size_t>(c->nx - 1) * (c->ny - 1) * (c->nz - 1)
+                                      : static_cast<size_t>(c->nx2 - 1) * (c->nz2 - 1);
+        h.resize(nCell);
+        EIKX_CUDA(cudaSetDevice(c->device));
+        EIKX_CUDA(cudaMemcpyAsync(h.data(), (dim == 3 ? c->slow3 : c->slow2).p, nCell * sizeof(double),
+                                  cudaMemcpyDeviceToHost, c->stream));
+        EIKX_CUDA(cudaStreamSynchronize(c->stream));
+        valid = true;
+    }
+    *out = &h;
     return EIKX_OK;
 }
 
@@ -295,11 +315,12 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     const int Px = roundUp(nx, 4);
     const int spPitch = Px + 8;
     const long long fieldStride = static_cast<long long>(Px) * ny * nz;
-    const std::vector<double> &hs = DIM == 3 ? c->hostSlow3 : c->hostSlow2;
-
-    // sources: cell, offsets, source-cell slowness (reference Source3D / Solver3D::solve)
+    // sources: cell, offsets, source-cell slowness (reference Source3D / Solver3D::solve);
+    // the slownesses are read from the device model, one value per source
     std::vector<eikx::SourceT<T>> srcT(nSrc);
     std::vector<eikx::Corner3> corners(nSrc);
+    std::vector<size_t> srcCells(nSrc);
+    std::vector<std::array<double, 3>> srcOffs(nSrc);
     for (int i = 0; i < nSrc; ++i) {
         const double x = srcXYZ[3 * i], y = srcXYZ[3 * i + 1], z = srcXYZ[3 * i + 2];
         int cx, cy = 0, cz;
@@ -313,14 +334,26 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         if (!locate(z, z0, dz, nz, &cz, &oz))
             return fail(EIKX_ERR_INVALID, "z source position = " + std::to_string(z) + " must be in range [" +
                                               std::to_string(z0) + "," + std::to_string(z0 + (nz - 1) * dz) + "]");
-        const size_t cell = DIM == 3 ? (static_cast<size_t>(cz) * (ny - 1) + cy) * (nx - 1) + cx
-                                     : static_cast<size_t>(cz) * (nx - 1) + cx;
-        const double s = hs[cell];
+        srcCells[i] = DIM == 3 ? (static_cast<size_t>(cz) * (ny - 1) + cy) * (nx - 1) + cx
+                               : static_cast<size_t>(cz) * (nx - 1) + cx;
+        srcOffs[i] = {ox, oy, oz};
         srcT[i].isx = cx; srcT[i].isy = cy; srcT[i].isz = cz;
         srcT[i].xs = static_cast<T>(ox); srcT[i].ys = static_cast<T>(oy); srcT[i].zs = static_cast<T>(oz);
+    }
+    EIKX_CUDA(c->srcSlow.ensure(static_cast<size_t>(nSrc) * sizeof(double)));
+    double *srcSlow = static_cast<double *>(c->srcSlow.p);
+    const double *slowDev = (DIM == 3 ? c->slow3 : c->slow2).as<double>();
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));   // the pinned values of a previous call are free
+    for (int i = 0; i < nSrc; ++i)
+        EIKX_CUDA(cudaMemcpyAsync(srcSlow + i, slowDev + srcCells[i], sizeof(double), cudaMemcpyDeviceToHost,
+                                  c->stream));
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < nSrc; ++i) {
+        const double s = srcSlow[i];
         srcT[i].sSrc = static_cast<T>(s);
         // corner init: slowness as the field type holds it, offsets in FP64
-        corners[i] = eikx::Corner3{cx, cy, cz, ox, oy, oz, static_cast<double>(static_cast<T>(s))};
+        corners[i] = eikx::Corner3{srcT[i].isx, srcT[i].isy, srcT[i].isz, srcOffs[i][0], srcOffs[i][1], srcOffs[i][2],
+                                   static_cast<double>(static_cast<T>(s))};
     }
 
     // edge-replicated slowness in the sweep precision: one copy shifted by V-1 columns
@@ -1258,26 +1291,17 @@ static eikx_status setCells(eikx_ctx *c, int dim, const void *v, int dtype, int 
     const int nx = dim == 3 ? c->nx : c->nx2, ny = dim == 3 ? c->ny : 2, nz = dim == 3 ? c->nz : c->nz2;
     const size_t nIn = nodal ? static_cast<size_t>(nx) * (dim == 3 ? ny : 1) * nz
                              : static_cast<size_t>(nx - 1) * (ny - 1) * (nz - 1);
-    // Model3D/Model2D reject non-positive velocities (src/model3d.cpp:301-305); host
-    // inputs are checked before upload, device inputs through the resulting slowness.
-    if (where == EIKX_HOST) {
-        bool bad = false;
-        if (dtype == EIKX_F32) {
-            const float *p = static_cast<const float *>(v);
-            for (size_t i = 0; i < nIn && !bad; ++i) bad = !(p[i] > 0);
-        } else {
-            const double *p = static_cast<const double *>(v);
-            for (size_t i = 0; i < nIn && !bad; ++i) bad = !(p[i] > 0);
-        }
-        if (bad) return fail(EIKX_ERR_INVALID, nodal ? "Non-positive velocities detected"
-                                                     : "Non-positive slowness detected");
-    }
+    // Model3D/Model2D reject non-positive velocities (src/model3d.cpp:301-305): the input
+    // and the resulting cell slowness are checked on the device, into one flag
+    EIKX_CUDA(c->modelFlag.ensure(sizeof(int)));
+    EIKX_CUDA(cudaMemsetAsync(c->modelFlag.p, 0, sizeof(int), c->stream));
     const size_t nCell = static_cast<size_t>(nx - 1) * (ny - 1) * (nz - 1);
     DevBuf &dst = dim == 3 ? c->slow3 : c->slow2;
     EIKX_CUDA(dst.ensure(nCell * sizeof(double)));
     if (dtype == EIKX_F32) {
         const float *d = nullptr;
         if (eikx_status r = toDevice<float>(c, static_cast<const float *>(v), nIn, where, &d); r) return r;
+        EIKX_CUDA(eikx::launchCheckPositive(d, static_cast<long long>(nIn), c->modelFlag.as<int>(), c->stream));
         if (nodal) {
             if (dim == 3) EIKX_CUDA(eikx::launchNodalToCell3<float>(dst.as<double>(), d, nx, ny, nz, ordering, c->stream));
             else EIKX_CUDA(eikx::launchNodalToCell2<float>(dst.as<double>(), d, nx, nz, ordering, c->stream));
@@ -1288,6 +1312,7 @@ static eikx_status setCells(eikx_ctx *c, int dim, const void *v, int dtype, int 
     } else {
         const double *d = nullptr;
         if (eikx_status r = toDevice<double>(c, static_cast<const double *>(v), nIn, where, &d); r) return r;
+        EIKX_CUDA(eikx::launchCheckPositive(d, static_cast<long long>(nIn), c->modelFlag.as<int>(), c->stream));
         if (nodal) {
             if (dim == 3) EIKX_CUDA(eikx::launchNodalToCell3<double>(dst.as<double>(), d, nx, ny, nz, ordering, c->stream));
             else EIKX_CUDA(eikx::launchNodalToCell2<double>(dst.as<double>(), d, nx, nz, ordering, c->stream));
@@ -1296,7 +1321,7 @@ static eikx_status setCells(eikx_ctx *c, int dim, const void *v, int dtype, int 
             else EIKX_CUDA(eikx::launchCellsToNatural2<double>(dst.as<double>(), d, nx, nz, ordering, c->stream));
         }
     }
-    return dim == 3 ? finishModel3(c) : finishModel2(c);
+    return finishModel(c, dim);
 }
 
 eikx_status eikx_set_slowness3d(eikx_ctx *c, const void *s, int dtype, int ordering, int where) {
@@ -1316,13 +1341,14 @@ eikx_status eikx_get_slowness3d(const eikx_ctx *c, void *out, int dtype) {
     if (eikx_status r = checkCtx(c); r) return r;
     if (!c->haveSlow3) return fail(EIKX_ERR_STATE, "Velocity model not set");
     if (!out) return fail(EIKX_ERR_INVALID, "output is NULL");
+    if (dtype != EIKX_F64 && dtype != EIKX_F32) return fail(EIKX_ERR_INVALID, "dtype must be EIKX_F32 or EIKX_F64");
+    const std::vector<double> *hs = nullptr;
+    if (eikx_status r = hostSlowness(c, 3, &hs); r) return r;
     if (dtype == EIKX_F64) {
-        std::memcpy(out, c->hostSlow3.data(), c->hostSlow3.size() * sizeof(double));
-    } else if (dtype == EIKX_F32) {
-        float *o = static_cast<float *>(out);
-        for (size_t i = 0; i < c->hostSlow3.size(); ++i) o[i] = static_cast<float>(c->hostSlow3[i]);
+        std::memcpy(out, hs->data(), hs->size() * sizeof(double));
     } else {
-        return fail(EIKX_ERR_INVALID, "dtype must be EIKX_F32 or EIKX_F64");
+        float *o = static_cast<float *>(out);
+        for (size_t i = 0; i < hs->size(); ++i) o[i] = static_cast<float>((*hs)[i]);
     }
     return EIKX_OK;
 }

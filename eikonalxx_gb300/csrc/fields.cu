@@ -20,13 +20,14 @@ inline int gridFor(long long n, int threads = kThreads) {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return max(lo, min(hi, v)); }
 
-// Raises *flag when a slowness is not a positive finite number (Model3D rejects
-// non-positive velocities, src/model3d.cpp:301-305).
-__global__ void positiveKernel(const double *s, long long n, int *flag) {
+// Raises *flag when a velocity or slowness is not a positive finite number (Model3D
+// rejects non-positive velocities, src/model3d.cpp:301-305).
+template <class U>
+__global__ void positiveKernel(const U *s, long long n, int *flag) {
     bool bad = false;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const double v = s[i];
+        const U v = s[i];
         bad = bad || !(v > 0) || !isfinite(v);
     }
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
@@ -466,7 +467,11 @@ template cudaError_t launchWarmInit3<double>(double *, const double *, int, long
                                              unsigned long long *, cudaStream_t);
 
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st) {
-    positiveKernel<<<gridFor(n), kThreads, 0, st>>>(s, n, flag);
+    positiveKernel<double><<<gridFor(n), kThreads, 0, st>>>(s, n, flag);
+    return cudaGetLastError();
+}
+cudaError_t launchCheckPositive(const float *s, long long n, int *flag, cudaStream_t st) {
+    positiveKernel<float><<<gridFor(n), kThreads, 0, st>>>(s, n, flag);
     return cudaGetLastError();
 }
 

@@ -174,6 +174,7 @@ cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldSt
                             int fp64, unsigned long long *nReset, cudaStream_t s);
 // Sets *flag (ORs 1) if any of the n slownesses is not positive and finite.
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st);
+cudaError_t launchCheckPositive(const float *s, long long n, int *flag, cudaStream_t st);
 // After refinement sweep `sweepsDone - 1`: a field whose residual slots
 // [firstSlot, firstSlot + nSlots) all fell below tol is frozen (later sweeps skip it).
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,
