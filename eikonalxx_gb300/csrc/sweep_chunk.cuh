@@ -33,6 +33,10 @@ namespace chunk {
 
 constexpr int kRingC = 4;                           // ring depth in steps (reads go back 2)
 constexpr int kThreadsC = 32 * kWarpsPerBlock;
+// Own-pencil prefetch: a lane's travel-time and slowness chunks of step s are copied into
+// shared-memory slot s % kPre, kAhead steps before they are used (cp.async, no registers).
+constexpr int kPre = 4, kAhead = 3;
+static_assert(kAhead < kPre && (kPre & (kPre - 1)) == 0, "a slot is refilled only after its step");
 
 template <class T> struct alignas(16) Vec {
     static constexpr int N = 16 / sizeof(T);
@@ -65,6 +69,15 @@ __device__ __forceinline__ void ldRelaxed2(const unsigned long long *p, unsigned
 }
 __device__ __forceinline__ void stRelaxed2(unsigned long long *p, unsigned long long a, unsigned long long b) {
     asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b));
+}
+// 16-byte asynchronous copy global -> shared (L2 only), its commit and its wait.
+__device__ __forceinline__ void cpAsync16(void *smem, const void *gmem) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cpAsyncWait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // One chunk in the mailbox: four tagged words.  Each 64-bit word is written and read
@@ -177,6 +190,9 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
     const int ly = lane % LY, lz = lane / LY;
     Vec<T> *tring = reinterpret_cast<Vec<T> *>(smemRaw) + warp * (2 * kRingC * kPlane);
     Vec<T> *sring = tring + kRingC * kPlane;
+    // prefetch slots after all rings: [warp][slot][T | S][lane]
+    Vec<T> *pre = reinterpret_cast<Vec<T> *>(smemRaw) + kWarpsPerBlock * (2 * kRingC * kPlane) +
+                  warp * (kPre * 64) + lane;
     const SolveState &st = a.st;
     clearNextQueue(st, a.buf);
     if (ldVolatile(st.abortFlag)) return;
@@ -250,11 +266,18 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
         auto tChunk = [&](T *r, int k) { return REV ? r + Px - (k + 1) * V : r + k * V; };
         auto sChunk = [&](const T *r, int k) { return REV ? r + Px - (k + 1) * V : r + (k + 1) * V; };
         auto walk = [&](const Vec<T> &m) { return REV ? reversed(m) : m; };   // memory <-> walk order
-        Vec<T> tNext = splat(huge), sNext = splat(huge);
-        if (laneValid) {
-            tNext = ldVec(tChunk(row, 0));
-            sNext = ldVec(sChunk(srow, 0));
-        }
+        // the own pencil's chunk of step sv into slot sv % kPre; one commit group per step
+        auto prefetch = [&](int sv) {
+            const int kv = sv - ly - lz;
+            if (laneValid && kv >= 0 && kv < nChunks) {
+                Vec<T> *slot = pre + (sv & (kPre - 1)) * 64;
+                cpAsync16(slot, tChunk(row, kv));
+                cpAsync16(slot + 32, sChunk(srow, kv));
+            }
+            cpAsyncCommit();
+        };
+#pragma unroll
+        for (int sv = 0; sv < kAhead; ++sv) prefetch(sv);
 
         // mailbox: this block's faces, and the upstream face row a helper lane reads
         unsigned long long *box = fieldBox + (static_cast<long long>(c) * tilesY + b) * faceWords;
@@ -338,14 +361,13 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
             issue(s + 1);
             const int k = s - ly - lz;
             const bool active = laneValid && k >= 0 && k < nChunks;
+            prefetch(s + kAhead);
+            cpAsyncWait<kAhead>();   // this step's group has landed
             Vec<T> tOwn = splat(huge), sOwn = splat(huge);
             if (active) {
-                tOwn = walk(tNext);
-                sOwn = walk(sNext);
-                if (k + 1 < nChunks) {
-                    tNext = ldVec(tChunk(row, k + 1));
-                    sNext = ldVec(sChunk(srow, k + 1));
-                }
+                const Vec<T> *slot = pre + (s & (kPre - 1)) * 64;
+                tOwn = walk(slot[0]);
+                sOwn = walk(slot[32]);
             }
             const int cur = (s & (kRingC - 1)) * kPlane;
             const int p1 = ((s - 1) & (kRingC - 1)) * kPlane;
@@ -407,6 +429,7 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
             cT1 = out.v[V - 1]; cT3 = tY.v[V - 1]; cT4 = tZ.v[V - 1]; cT7 = tYZ.v[V - 1];
             cS1 = sYZ.v[V - 1]; cS2 = sZ.v[V - 1]; cS5 = sY.v[V - 1]; cS7 = sOwn.v[V - 1];
         }
+        cpAsyncWait<0>();   // no copy into the slots outlives the work item
         if (!ok) break;
         const double r = warpMax(static_cast<double>(res));
         if (lane == 0 && r > 0)
@@ -416,7 +439,7 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
 }
 
 template <int LY, int LZ> constexpr size_t smemBytes() {
-    return 2 * kRingC * (LY + 1) * (LZ + 1) * 16 * kWarpsPerBlock;
+    return (2 * kRingC * (LY + 1) * (LZ + 1) + kPre * 64) * 16 * kWarpsPerBlock;
 }
 
 template <class T, bool U, bool R, bool B, int LY, int LZ>
