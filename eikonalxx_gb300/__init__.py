@@ -36,6 +36,7 @@ EXPORTED = [
     "eikx_solve2d", "eikx_graph3d_tables", "eikx_levels2d", "eikx_analytic3d", "eikx_analytic2d",
     "eikx_solve3d_noalloc", "eikx_solve3d_batch", "eikx_autotune3d", "eikx_tuning_save", "eikx_tuning_load",
     "eikx_gradient3d", "eikx_gradient2d", "eikx_station_times3d", "eikx_station_times2d", "eikx_solve3d_warm",
+    "eikx_ray_options_default", "eikx_trace_rays2d",
 ]
 CELL_SLOWNESS, NODAL_VELOCITY = 0, 1
 
@@ -76,6 +77,16 @@ class _Stats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int), ("residual_last", ctypes.c_double),
                 ("device_ms", ctypes.c_double), ("sweep_ms", ctypes.c_double), ("reset_nodes", ctypes.c_longlong),
                 ("refine_node_updates", ctypes.c_longlong)]
+
+
+class _RayOptions(ctypes.Structure):
+    _fields_ = [("n_radii", ctypes.c_int), ("radius", ctypes.c_int * 16), ("scale", ctypes.c_double * 16),
+                ("max_steps", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+class _RaySeg(ctypes.Structure):
+    _fields_ = [("x0", ctypes.c_double), ("z0", ctypes.c_double), ("x1", ctypes.c_double), ("z1", ctypes.c_double),
+                ("slowness", ctypes.c_double), ("cell", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 class _Src3(ctypes.Structure):
@@ -146,7 +157,8 @@ def load(path=None):
     lib.eikx_tuning_save.argtypes = [vp, ctypes.c_char_p]
     lib.eikx_tuning_load.argtypes = [vp, ctypes.c_char_p]
     for name in EXPORTED:
-        if name not in ("eikx_options_default", "eikx_last_error", "eikx_levels2d", "eikx_graph3d_tables"):
+        if name not in ("eikx_options_default", "eikx_last_error", "eikx_levels2d", "eikx_graph3d_tables",
+                        "eikx_ray_options_default"):
             getattr(lib, name).restype = c_int
     lib.eikx_graph3d_tables.restype = c_int
     lib.eikx_levels2d.restype = c_int
@@ -336,6 +348,49 @@ class Context:
         _check(self._lib.eikx_station_times2d(self._h, int(field), arr, len(st),
                                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out
+
+    def trace_rays2d(self, gradient, slowness, source, stations, radius_scale=None, max_steps=0, capacity=None,
+                     grid=None):
+        """Ray::GradientTracer2D::trace: rays from the stations to the source down a gradient
+        field (nz, nx, 2) with cell slowness ((nz-1)*(nx-1), FP64).  grid = (nx, nz, dx, dz,
+        x0, z0), default the context's 2D grid; radius_scale = [(radius, scale), ...], default
+        the reference's.  Returns (paths, counts): paths[i] is an (n_i, 6) array of (x0, z0, x1,
+        z1, slowness, cell) or None when counts[i] < 0 (-1 no convergence, -2 capacity, -3 left
+        the grid)."""
+        nx, nz, dx, dz, x0, z0 = grid if grid is not None else self.grid2
+        g = np.ascontiguousarray(gradient)
+        if g.dtype not in (np.float32, np.float64) or g.size != 2 * nx * nz:
+            raise InvalidArgument(-2, "gradient must hold nz * nx * 2 FP32 or FP64 values")
+        s = np.ascontiguousarray(slowness, dtype=np.float64).ravel()
+        st = np.ascontiguousarray(np.atleast_2d(np.asarray(stations, dtype=np.float64)))
+        n = len(st)
+        opt = _RayOptions()
+        self._lib.eikx_ray_options_default(ctypes.byref(opt))
+        if radius_scale is not None:
+            opt.n_radii = len(radius_scale)
+            for k, (r, sc) in enumerate(radius_scale):
+                opt.radius[k] = int(r)
+                opt.scale[k] = float(sc)
+        opt.max_steps = int(max_steps)
+        cap = int(capacity) if capacity else 4 * (nx + nz) + 16
+        segs = (_RaySeg * (n * cap))()
+        counts = np.zeros(n, dtype=np.int32)
+        _check(self._lib.eikx_trace_rays2d(
+            self._h, nx, nz, ctypes.c_double(dx), ctypes.c_double(dz), ctypes.c_double(x0), ctypes.c_double(z0),
+            ctypes.c_void_p(g.ctypes.data), F64 if g.dtype == np.float64 else F32,
+            s.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_double(float(source[0])),
+            ctypes.c_double(float(source[1])), st.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n,
+            ctypes.byref(opt), cap, segs, counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        raw = np.frombuffer(segs, dtype=np.dtype([("x0", "f8"), ("z0", "f8"), ("x1", "f8"), ("z1", "f8"),
+                                                  ("slowness", "f8"), ("cell", "i4"), ("reserved", "i4")]))
+        paths = []
+        for i in range(n):
+            if counts[i] <= 0:
+                paths.append(None)
+                continue
+            r = raw[i * cap:i * cap + counts[i]]
+            paths.append(np.column_stack([r["x0"], r["z0"], r["x1"], r["z1"], r["slowness"], r["cell"]]))
+        return paths, counts
 
     def autotune3d(self, sources, precision=F32):
         """Time the kernel variants, warp-block shapes and grid sizes on this model and these

@@ -174,6 +174,7 @@ struct eikx_ctx {
     mutable std::vector<double> hostSlow2;
     mutable bool hostSlow2Valid = false;
     DevBuf modelFlag;              // raised by the device checks of a new model
+    DevBuf rayGrad, raySlow, raySt, rayPos, raySeg, rayCnt;   // eikx_trace_rays2d buffers
     PinnedBuf srcSlow;             // source-cell slownesses of a solve, read from the device
     DevBuf spad2[2][2];
     bool spadValid2[2] = {false, false};
@@ -1572,6 +1573,108 @@ eikx_status eikx_station_times2d(eikx_ctx *c, int field, const eikx_source2d *st
     std::vector<double> xyz(3 * static_cast<size_t>(std::max(n, 0)));
     for (int i = 0; i < n && st; ++i) { xyz[3 * i] = st[i].x; xyz[3 * i + 1] = 0; xyz[3 * i + 2] = st[i].z; }
     return stationsImpl(c, 2, field, st ? xyz.data() : nullptr, n, times);
+}
+
+void eikx_ray_options_default(eikx_ray_options *opt) {
+    if (!opt) return;
+    std::memset(opt, 0, sizeof(*opt));
+    // GradientTracerOptions defaults, src/ray/gradientTracerOptions.cpp
+    const int r[5] = {1, 2, 3, 5, std::numeric_limits<int>::max()};
+    const double s[5] = {0.05, 0.10, 0.20, 0.30, 0.45};
+    opt->n_radii = 5;
+    for (int k = 0; k < 5; ++k) { opt->radius[k] = r[k]; opt->scale[k] = s[k]; }
+    opt->max_steps = 0;
+}
+
+eikx_status eikx_trace_rays2d(eikx_ctx *c, int nx, int nz, double dx, double dz, double x0, double z0,
+                              const void *gradient, int dtype, const double *slowness, double sourceX,
+                              double sourceZ, const double *stations, int n, const eikx_ray_options *opt,
+                              int capacity, eikx_ray_segment2d *segments, int *counts) {
+    if (eikx_status r = checkCtx(c); r) return r;
+    if (nx < 3 || nz < 3) return fail(EIKX_ERR_INVALID, "grid needs at least 3 points in each direction");
+    if (!(dx > 0) || !(dz > 0)) return fail(EIKX_ERR_INVALID, "grid spacing must be positive");
+    if (!gradient || !slowness) return fail(EIKX_ERR_INVALID, "Travel time gradient field not set");
+    if (dtype != EIKX_F32 && dtype != EIKX_F64) return fail(EIKX_ERR_INVALID, "dtype must be EIKX_F32 or EIKX_F64");
+    if (n <= 0 || !stations) return fail(EIKX_ERR_STATE, "No stations were set");
+    if (capacity < 1 || !segments || !counts) return fail(EIKX_ERR_INVALID, "segment output is NULL or empty");
+    eikx_ray_options o;
+    if (opt) o = *opt; else eikx_ray_options_default(&o);
+    // GradientTracerOptions::setRadiusScaleFactor (src/ray/gradientTracerOptions.cpp): radii
+    // non-negative and distinct, scales in (eps, 1), sorted by radius, extended to INT_MAX
+    if (o.n_radii < 1 || o.n_radii > 16) return fail(EIKX_ERR_INVALID, "Input vector cannot be empty");
+    std::vector<std::pair<int, double>> rsf;
+    for (int k = 0; k < o.n_radii; ++k) {
+        if (o.radius[k] < 0) return fail(EIKX_ERR_INVALID, "All radii must be non-negative");
+        if (o.scale[k] <= std::numeric_limits<double>::epsilon())
+            return fail(EIKX_ERR_INVALID, "All scale factors must be non-negative");
+        if (o.scale[k] >= 1) return fail(EIKX_ERR_INVALID, "All scale factors must be less than 1");
+        rsf.emplace_back(o.radius[k], o.scale[k]);
+    }
+    std::stable_sort(rsf.begin(), rsf.end(), [](const auto &a, const auto &b) { return a.first < b.first; });
+    for (size_t k = 0; k + 1 < rsf.size(); ++k)
+        if (rsf[k].first == rsf[k + 1].first) return fail(EIKX_ERR_INVALID, "Duplicate radii");
+    if (rsf.back().first < std::numeric_limits<int>::max()) {
+        if (rsf.size() == eikx::kMaxRadii) return fail(EIKX_ERR_INVALID, "at most 15 radii below INT_MAX");
+        rsf.emplace_back(std::numeric_limits<int>::max(), rsf.back().second);
+    }
+    eikx::RayTrace2Args a{};
+    a.nx = nx; a.nz = nz; a.dx = dx; a.dz = dz; a.x0 = x0; a.z0 = z0;
+    if (!locate(sourceX, x0, dx, nx, &a.isx, &a.xs) || !locate(sourceZ, z0, dz, nz, &a.isz, &a.zs))
+        return fail(EIKX_ERR_INVALID, "source position outside the grid");
+    for (int i = 0; i < n; ++i) {
+        int cx, cz;
+        double ox, oz;
+        if (!locate(stations[2 * i], x0, dx, nx, &cx, &ox) || !locate(stations[2 * i + 1], z0, dz, nz, &cz, &oz))
+            return fail(EIKX_ERR_INVALID, "station " + std::to_string(i) + " outside the grid");
+    }
+    a.nRsf = static_cast<int>(rsf.size());
+    double minScale = 1;
+    for (int k = 0; k < a.nRsf; ++k) {
+        a.rsfRadius[k] = rsf[k].first;
+        a.rsfScale[k] = rsf[k].second;
+        minScale = std::min(minScale, rsf[k].second);
+    }
+    a.maxSteps = o.max_steps > 0 ? o.max_steps
+                                 : static_cast<int>(std::min(1.e8, std::ceil(4.0 * (nx + nz) / minScale)) + 16);
+    a.capacity = capacity;
+    const size_t nNode = static_cast<size_t>(nx) * nz, nCell = static_cast<size_t>(nx - 1) * (nz - 1);
+    const size_t gradBytes = 2 * nNode * (dtype == EIKX_F64 ? 8 : 4);
+    const size_t posBytes = static_cast<size_t>(n) * (a.maxSteps + 1) * 2 * sizeof(double);
+    const size_t segBytes = static_cast<size_t>(n) * capacity * 6 * sizeof(double);
+    EIKX_CUDA(cudaSetDevice(c->device));
+    EIKX_CUDA(c->rayGrad.ensure(gradBytes));
+    EIKX_CUDA(c->raySlow.ensure(nCell * sizeof(double)));
+    EIKX_CUDA(c->raySt.ensure(2 * static_cast<size_t>(n) * sizeof(double)));
+    EIKX_CUDA(c->rayPos.ensure(posBytes));
+    EIKX_CUDA(c->raySeg.ensure(segBytes));
+    EIKX_CUDA(c->rayCnt.ensure(static_cast<size_t>(n) * sizeof(int)));
+    EIKX_CUDA(cudaMemcpyAsync(c->rayGrad.p, gradient, gradBytes, cudaMemcpyHostToDevice, c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(c->raySlow.p, slowness, nCell * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(c->raySt.p, stations, 2 * static_cast<size_t>(n) * sizeof(double),
+                              cudaMemcpyHostToDevice, c->stream));
+    a.slow = c->raySlow.as<double>();
+    if (dtype == EIKX_F64)
+        EIKX_CUDA(eikx::launchTraceRays2<double>(a, c->rayGrad.as<double>(), n, c->raySt.as<double>(),
+                                                 c->rayPos.as<double>(), c->raySeg.as<double>(), c->rayCnt.as<int>(),
+                                                 c->stream));
+    else
+        EIKX_CUDA(eikx::launchTraceRays2<float>(a, c->rayGrad.as<float>(), n, c->raySt.as<double>(),
+                                                c->rayPos.as<double>(), c->raySeg.as<double>(), c->rayCnt.as<int>(),
+                                                c->stream));
+    std::vector<double> seg(static_cast<size_t>(n) * capacity * 6);
+    EIKX_CUDA(cudaMemcpyAsync(counts, c->rayCnt.p, static_cast<size_t>(n) * sizeof(int), cudaMemcpyDeviceToHost,
+                              c->stream));
+    EIKX_CUDA(cudaMemcpyAsync(seg.data(), c->raySeg.p, segBytes, cudaMemcpyDeviceToHost, c->stream));
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < n; ++i)
+        for (int k = 0; k < std::max(0, counts[i]); ++k) {
+            const double *s = &seg[(static_cast<size_t>(i) * capacity + k) * 6];
+            eikx_ray_segment2d &d = segments[static_cast<size_t>(i) * capacity + k];
+            d.x0 = s[0]; d.z0 = s[1]; d.x1 = s[2]; d.z1 = s[3]; d.slowness = s[4];
+            d.cell = static_cast<int>(s[5]);
+            d.reserved = 0;
+        }
+    return EIKX_OK;
 }
 
 eikx_status eikx_solve2d(eikx_ctx *c, const eikx_source2d *src, int nSrc, const eikx_options *opt, int precision,

@@ -179,6 +179,24 @@ cudaError_t launchCheckPositive(const float *s, long long n, int *flag, cudaStre
 // [firstSlot, firstSlot + nSlots) all fell below tol is frozen (later sweeps skip it).
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,
                                    int sweepsDone, double tol, cudaStream_t s);
+// 2D gradient ray tracing (rays.cu): grid, source, step rules and output capacity.
+constexpr int kMaxRadii = 16;
+struct RayTrace2Args {
+    int nx, nz;
+    double dx, dz, x0, z0;
+    const double *slow;           // cell slowness (nz-1) x (nx-1), FP64, device
+    int isx, isz;                 // source cell
+    double xs, zs;                // source offsets from the origin
+    int nRsf;                     // radius / scale pairs, ascending radius (the last applies beyond)
+    int rsfRadius[kMaxRadii];
+    double rsfScale[kMaxRadii];
+    int maxSteps;                 // bound on the march (march points per station: maxSteps + 1)
+    int capacity;                 // segments per station
+};
+template <class T>
+cudaError_t launchTraceRays2(const RayTrace2Args &a, const T *grad, int n, const double *stations, double *pos,
+                             double *segments, int *counts, cudaStream_t s);
+
 // Products of a solved field (post.cu): the travel-time gradient (3 or 2 values per
 // natural node) and travel times at stations (cells and origin offsets per station).
 template <class T>

@@ -189,6 +189,53 @@ eikx_status eikx_gradient2d(eikx_ctx *ctx, int field, void *grad, int where);
 eikx_status eikx_station_times3d(eikx_ctx *ctx, int field, const eikx_source3d *stations, int n, double *times);
 eikx_status eikx_station_times2d(eikx_ctx *ctx, int field, const eikx_source2d *stations, int n, double *times);
 
+/* ---- 2D gradient ray tracing ---------------------------------------------- */
+/* Step rule of Ray::GradientTracerOptions (include/eikonalxx/ray/gradientTracerOptions.hpp,
+ * src/ray/gradientTracerOptions.cpp): where the ray is within radius[k] cells of the source
+ * cell (the smaller of the x and z cell distances) it steps scale[k] * min(dx, dz).  The
+ * pairs are sorted by radius; when the largest radius is below INT_MAX a pair (INT_MAX,
+ * last scale) is added, as setRadiusScaleFactor does. */
+typedef struct {
+    int n_radii;           /* pairs used, 1..16 */
+    int radius[16];        /* non-negative, distinct */
+    double scale[16];      /* in (machine epsilon, 1) */
+    int max_steps;         /* bound on one ray's march; 0 = ceil(4 (nx + nz) / smallest scale) + 16
+                              (the reference has no bound) */
+    int reserved;
+} eikx_ray_options;
+
+/* Defaults of GradientTracerOptions: (1, 0.05), (2, 0.10), (3, 0.20), (5, 0.30), (INT_MAX, 0.45). */
+void eikx_ray_options_default(eikx_ray_options *opt);
+
+/* One segment of a ray path (Ray::Segment2D, include/eikonalxx/ray/segment2d.hpp). */
+typedef struct {
+    double x0, z0, x1, z1; /* start and end point, absolute (m) */
+    double slowness;       /* s/m of the cell the segment crosses */
+    int cell;              /* velocity-model cell index, or -1 where the reference leaves it unset */
+    int reserved;
+} eikx_ray_segment2d;
+
+/* Replaces Ray::GradientTracer2D::trace (src/ray/gradientTracer2d.cpp:339-600): a ray from
+ * each station to the source, marched down the travel-time gradient (bilinear in the
+ * current cell) until it ends within one cell of the source cell, then healed into
+ * segments that end where the ray leaves a cell, source to station; a station in the
+ * source cell gets the straight segment.  One GPU thread per station, FP64.
+ *   grid: nx x nz nodes, spacing dx, dz, origin x0, z0 (Geometry2D);
+ *   gradient: host array of nz x nx x 2 values (d/dx, d/dz per node, natural order),
+ *     dtype EIKX_F32 or EIKX_F64 (ISolver2D::getTravelTimeGradientFieldPointer);
+ *   slowness: host array of (nz-1) x (nx-1) cell slownesses, FP64;
+ *   source, stations: absolute positions (m), stations as n (x, z) pairs;
+ *   segments: n x capacity entries, station i's path in [i * capacity, ...);
+ *   counts[i]: segments of station i, or -1 when the march did not reach the source within
+ *     max_steps (the reference prints "did not converge"), -2 when the path needs more than
+ *     capacity segments, -3 when the march left the grid (where the reference reads outside
+ *     its arrays).
+ * The call succeeds (EIKX_OK) when some rays fail; counts tell which. */
+eikx_status eikx_trace_rays2d(eikx_ctx *ctx, int nx, int nz, double dx, double dz, double x0, double z0,
+                              const void *gradient, int dtype, const double *slowness, double source_x,
+                              double source_z, const double *stations, int n_stations, const eikx_ray_options *opt,
+                              int capacity, eikx_ray_segment2d *segments, int *counts);
+
 /* ---- autotuning ---------------------------------------------------------- */
 
 /* The configuration eikx_autotune3d chose for one grid class. */

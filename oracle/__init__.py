@@ -114,6 +114,23 @@ class Oracle:
                                    _P(offs), _P(out))
         return out
 
+    def trace_rays2d(self, grad, grid, origin, slow, source, stations, radii, scales, max_steps, capacity):
+        """Ray::GradientTracer2D::trace: (segments [n][capacity][6], counts [n])."""
+        nx, nz, dx, dz = grid
+        grad = np.ascontiguousarray(grad)
+        slow = np.ascontiguousarray(slow, dtype=np.float64)
+        st = np.ascontiguousarray(stations, dtype=np.float64).reshape(-1, 2)
+        n = len(st)
+        seg = np.zeros((n, capacity, 6), np.float64)
+        counts = np.zeros(n, np.int32)
+        radii = np.ascontiguousarray(radii, dtype=np.int32)
+        scales = np.ascontiguousarray(scales, dtype=np.float64)
+        self.lib.oracle_trace_rays2d(0 if grad.dtype == np.float32 else 1, nx, nz, _d(dx), _d(dz), _d(origin[0]),
+                                     _d(origin[1]), _P(grad), _P(slow), _d(source[0]), _d(source[1]), n, _P(st),
+                                     len(radii), _P(radii), _P(scales), int(max_steps), int(capacity), _P(seg),
+                                     _P(counts))
+        return seg, counts
+
     def stations2d(self, tt, grid, src_cell, src_off, s_src, cells, offs):
         nx, nz, dx, dz = grid
         tt = np.ascontiguousarray(tt)

@@ -1111,6 +1111,155 @@ double station2(const Grid2 &g, const Src2 &src, double sSrc, const T *t, int cx
     return dzi * ((z2 - zi) * fxz1 + (zi - z1) * fxz2);
 }
 
+//----------------------------------------------------------------------------//
+//                       2D gradient ray tracer                               //
+//----------------------------------------------------------------------------//
+
+// Ray::GradientTracer2D::trace (src/ray/gradientTracer2d.cpp:339-600) for one station:
+// march from the station down the travel-time gradient (bilinear, src/ray/bilinear.hpp)
+// with the radius-scaled step lengths of GradientTracerOptions
+// (src/ray/gradientTracerOptions.cpp), until the ray ends within one cell of the source
+// cell; then turn the march around and heal it into segments that end on cell walls
+// (intersect, gradientTracer2d.cpp:137-196).  Positions are offsets from the origin;
+// segments are written in absolute coordinates as (x0, z0, x1, z1, slowness, cell), cell
+// -1 where the reference leaves it unset.  Returns the number of segments, -1 when the
+// march did not reach the source within maxSteps, -2 when the path needs more than
+// `capacity` segments, -3 when the march left the grid (the reference reads outside its
+// arrays there).  Gradient nodes past the end of the array read as 0: they are used only
+// with weight 0.  hypot is eikxHypot, as on the GPU (the reference uses std::hypot).
+template <class T>
+int traceRay2(int nx, int nz, double dx, double dz, double x0, double z0, const T *grad, const double *slow,
+              int isx, int isz, double xs, double zs, double xr, double zr, int nRsf, const int *rsfRadius,
+              const double *rsfScale, int maxSteps, double *pos, int capacity, double *seg) {
+    const int ncx = nx - 1, ncz = nz - 1;
+    auto slowAt = [&](int cx, int cz) {
+        cx = clampi(cx, 0, ncx - 1);
+        cz = clampi(cz, 0, ncz - 1);
+        return slow[static_cast<size_t>(cz) * ncx + cx];
+    };
+    const double dxi = 1. / dx, dzi = 1. / dz;
+    const double hmin = std::min(dx, dz);
+    const int scx = std::min(nx - 2, static_cast<int>(xr / dx)), scz = std::min(nz - 2, static_cast<int>(zr / dz));
+    const double sourceSlowness = slowAt(isx, isz), stationSlowness = slowAt(scx, scz);
+    int nSeg = 0;
+    auto put = [&](double ax, double az, double bx, double bz, double s, int cell) {
+        if (nSeg >= capacity) return false;
+        double *o = seg + 6 * static_cast<size_t>(nSeg++);
+        o[0] = ax; o[1] = az; o[2] = bx; o[3] = bz; o[4] = s; o[5] = cell;
+        return true;
+    };
+    if (scz * ncx + scx == isz * ncx + isx) {
+        return put(x0 + xs, z0 + zs, x0 + xr, z0 + zr, stationSlowness, scz * ncx + scx) ? 1 : -2;
+    }
+    const long long nGrad = 2LL * nx * nz;
+    auto g = [&](long long i) { return i >= 0 && i < nGrad ? static_cast<double>(grad[i]) : 0.0; };
+    auto bilinear = [&](double x, double z, double x1, double x2, double z1, double z2, double f00, double f01,
+                        double f10, double f11) {
+        const double x2mx = x2 - x, xmx1 = x - x1;
+        const double fxz1 = dxi * (x2mx * f00 + xmx1 * f10);
+        const double fxz2 = dxi * (x2mx * f01 + xmx1 * f11);
+        const double z2mz = z2 - z, zmz1 = z - z1;
+        return dzi * (z2mz * fxz1 + zmz1 * fxz2);
+    };
+    double xs0 = xr, zs0 = zr;
+    int cx0 = -1, cz0 = -1;
+    double gx000 = 1.e10, gz000 = 1.e10, gx100 = 1.e10, gz100 = 1.e10;
+    double gx010 = 1.e10, gz010 = 1.e10, gx110 = 1.e10, gz110 = 1.e10;
+    double stepLength0 = rsfScale[nRsf - 1] * hmin;
+    int m = 0;   // march points p_0 .. p_m
+    pos[0] = xr; pos[1] = zr;
+    bool converged = false;
+    for (int step = 0; step < maxSteps; ++step) {
+        const int cxs = static_cast<int>(xs0 / dx), czs = static_cast<int>(zs0 / dz);
+        if (cxs < 0 || cxs > nx - 1 || czs < 0 || czs > nz - 1) return -3;
+        double stepLength = stepLength0;
+        double gx00 = gx000, gz00 = gz000, gx10 = gx100, gz10 = gz100;
+        double gx01 = gx010, gz01 = gz010, gx11 = gx110, gz11 = gz110;
+        if (cxs != cx0 || czs != cz0) {
+            const int dist = std::min(std::abs(isx - cxs), std::abs(isz - czs));
+            stepLength = rsfScale[nRsf - 1] * hmin;
+            for (int k = 0; k < nRsf; ++k)
+                if (rsfRadius[k] >= dist) {
+                    stepLength = rsfScale[k] * hmin;
+                    break;
+                }
+            const long long i00 = 2LL * (static_cast<long long>(czs) * nx + cxs);
+            const long long i10 = 2LL * (static_cast<long long>(czs) * nx + cxs + 1);
+            const long long i11 = 2LL * (static_cast<long long>(czs + 1) * nx + cxs + 1);
+            const long long i01 = 2LL * (static_cast<long long>(czs + 1) * nx + cxs);
+            gx00 = g(i00); gz00 = g(i00 + 1);
+            gx10 = g(i10); gz10 = g(i10 + 1);
+            gx01 = g(i01); gz01 = g(i01 + 1);
+            gx11 = g(i11); gz11 = g(i11 + 1);
+        }
+        const double gx = bilinear(xs0, zs0, cxs * dx, (cxs + 1) * dx, czs * dz, (czs + 1) * dz, gx00, gx01, gx10, gx11);
+        const double gz = bilinear(xs0, zs0, cxs * dx, (cxs + 1) * dx, czs * dz, (czs + 1) * dz, gz00, gz01, gz10, gz11);
+        const double gNorm = eikxHypot(gx, gz);
+        const double gStep = stepLength / gNorm;
+        const double xe = xs0 - gx * gStep, ze = zs0 - gz * gStep;
+        ++m;
+        pos[2 * m] = xe; pos[2 * m + 1] = ze;
+        const int cxe = static_cast<int>(xe / dx), cze = static_cast<int>(ze / dz);
+        if (std::abs(cxe - isx) < 2 && std::abs(cze - isz) < 2) {
+            converged = true;
+            break;
+        }
+        stepLength0 = stepLength;
+        xs0 = xe; zs0 = ze;
+        cx0 = cxs; cz0 = czs;
+        gx000 = gx00; gz000 = gz00; gx100 = gx10; gz100 = gz10;
+        gx010 = gx01; gz010 = gz01; gx110 = gx11; gz110 = gz11;
+    }
+    if (!converged) return -1;
+    // reversed march: R_0 = source -> p_m, R_j = p_{m-j+1} -> p_{m-j} (j = 1..m)
+    auto cellOf = [&](int k, int &cx, int &cz) {
+        cx = static_cast<int>(pos[2 * k] / dx);
+        cz = static_cast<int>(pos[2 * k + 1] / dz);
+    };
+    double xa = xs, za = zs;
+    for (int j = 0; j <= m; ++j) {
+        if (j == m) {
+            if (!put(x0 + xa, z0 + za, x0 + xr, z0 + zr, stationSlowness, -1)) return -2;
+            break;
+        }
+        int c0x, c0z, c1x, c1z;
+        double ax, az, bx, bz;
+        if (j == 0) {
+            c0x = isx; c0z = isz;
+            cellOf(m, c1x, c1z);
+            ax = xs; az = zs; bx = pos[2 * m]; bz = pos[2 * m + 1];
+        } else {
+            cellOf(m - j + 1, c0x, c0z);
+            cellOf(m - j, c1x, c1z);
+            ax = pos[2 * (m - j + 1)]; az = pos[2 * (m - j + 1) + 1];
+            bx = pos[2 * (m - j)]; bz = pos[2 * (m - j) + 1];
+        }
+        if (c0x != c1x || c0z != c1z) {
+            double gx = bx - ax, gz = bz - az;
+            const double gnorm = eikxHypot(gx, gz);
+            gx = gx / gnorm;
+            gz = gz / gnorm;
+            // intersect: where the line from (xa, za) along (gx, gz) leaves cell (c0x, c0z)
+            double ti = 1.e10, tj = 1.e10;
+            const double wx0 = c0x * dx, wx1 = (c0x + 1) * dx, wz0 = c0z * dz, wz1 = (c0z + 1) * dz;
+            if (gx > 0) ti = (wx1 - xa) / gx;
+            else if (gx < 0) ti = (wx0 - xa) / gx;
+            if (gz > 0) tj = (wz1 - za) / gz;
+            else if (gz < 0) tj = (wz0 - za) / gz;
+            const double fxi = xa + gx * ti, fzi = za + gz * ti;
+            const double fxj = xa + gx * tj, fzj = za + gz * tj;
+            const double li = (fxi - xa) * (fxi - xa) + (fzi - za) * (fzi - za);
+            const double lj = (fxj - xa) * (fxj - xa) + (fzj - za) * (fzj - za);
+            const double xb = li < lj ? fxi : fxj, zb = li < lj ? fzi : fzj;
+            const double s = j == 0 ? sourceSlowness : slowAt(c0x, c0z);
+            if (!put(x0 + xa, z0 + za, x0 + xb, z0 + zb, s, -1)) return -2;
+            xa = xb;
+            za = zb;
+        }
+    }
+    return nSeg;
+}
+
 extern "C" {
 
 int oracle_solve3d_f64(int nx, int ny, int nz, double dx, double dy, double dz, int isx,
@@ -1193,6 +1342,27 @@ void oracle_nodal_to_cell2d_f64(int nx, int nz, const double *v, int ordering, d
 }
 
 double oracle_hypot(double a, double b) { return eikxHypot(a, b); }
+
+// Rays from n stations (absolute x, z) to a source (absolute x, z) through a gradient
+// field (nz x nx x 2, natural); segments [station][capacity][6]; counts[station].
+int oracle_trace_rays2d(int precision, int nx, int nz, double dx, double dz, double x0, double z0, const void *grad,
+                        const double *slow, double sx, double sz, int n, const double *stations, int nRsf,
+                        const int *rsfRadius, const double *rsfScale, int maxSteps, int capacity, double *segments,
+                        int *counts) {
+    const double xs = sx - x0, zs = sz - z0;
+    const int isx = std::min(nx - 2, static_cast<int>(xs / dx)), isz = std::min(nz - 2, static_cast<int>(zs / dz));
+    std::vector<double> pos(2 * static_cast<size_t>(maxSteps + 2));
+    for (int i = 0; i < n; ++i) {
+        const double xr = stations[2 * i] - x0, zr = stations[2 * i + 1] - z0;
+        double *seg = segments + static_cast<size_t>(i) * capacity * 6;
+        counts[i] = precision == 0
+            ? traceRay2<float>(nx, nz, dx, dz, x0, z0, static_cast<const float *>(grad), slow, isx, isz, xs, zs, xr, zr,
+                               nRsf, rsfRadius, rsfScale, maxSteps, pos.data(), capacity, seg)
+            : traceRay2<double>(nx, nz, dx, dz, x0, z0, static_cast<const double *>(grad), slow, isx, isz, xs, zs, xr,
+                                zr, nRsf, rsfRadius, rsfScale, maxSteps, pos.data(), capacity, seg);
+    }
+    return 0;
+}
 
 // 0: the 2D analytic times use std::hypot (as the reference); 1: eikxHypot (as the GPU).
 void oracle_set_hypot_mode(int mode) { gHypotMode = mode; }
