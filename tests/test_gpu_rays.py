@@ -89,3 +89,12 @@ def test_stations_outside_the_grid(ctx):
     c = homogeneous_case()
     with pytest.raises(ex.InvalidArgument, match="outside the grid"):
         ctx.trace_rays2d(c["grad"], c["slow"], c["source"], [(-50.0, 10.0)], grid=c["grid"] + c["origin"])
+
+
+def test_cpp_gradient_tracer(ctx, tmp_path):
+    """GradientTracer2D of the C++ API on the GPU: the reference's homogeneous case through an
+    analytic gradient, and rays through a solved field whose travel times match the field."""
+    import subprocess
+    from test_ray_api import build_ray_api
+    r = subprocess.run([build_ray_api(tmp_path), "gpu"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "ray_api ok" in r.stdout, r.stdout + r.stderr
