@@ -186,6 +186,25 @@ class Reference:
             raise RuntimeError("reference solve failed")
         return tt.reshape(nz, nx)
 
+    def trace_rays2d(self, grad, grid, origin, slow, source, stations, radii, scales, capacity):
+        """The reference's own Ray::GradientTracer2D::trace: (segments [n][capacity][6], counts);
+        a ray that does not reach the source has count 0 (an empty path)."""
+        nx, nz, dx, dz = grid
+        grad = np.ascontiguousarray(grad)
+        slow = np.ascontiguousarray(slow, dtype=np.float64)
+        st = np.ascontiguousarray(stations, dtype=np.float64).reshape(-1, 2)
+        n = len(st)
+        seg = np.zeros((n, capacity, 6), np.float64)
+        counts = np.zeros(n, np.int32)
+        radii = np.ascontiguousarray(radii, dtype=np.int32)
+        scales = np.ascontiguousarray(scales, dtype=np.float64)
+        rc = self.lib.ref_trace_rays2d(0 if grad.dtype == np.float32 else 1, nx, nz, _d(dx), _d(dz), _d(origin[0]),
+                                       _d(origin[1]), _P(grad), _P(slow), _d(source[0]), _d(source[1]), n, _P(st),
+                                       len(radii), _P(radii), _P(scales), int(capacity), _P(seg), _P(counts))
+        if rc != 0:
+            raise RuntimeError("reference ray tracing failed")
+        return seg, counts
+
     def graph3d(self, sweep, nx, ny, nz):
         n = nx * ny * nz
         ls = np.zeros(nx + ny + nz - 1, np.int32)

@@ -3,9 +3,11 @@
 * oracle/_build/libeikx_oracle.so : the project's CPU restatement (eikx_oracle.cpp).
 * oracle/_ref/libeikx_ref.so      : the reference's OWN hot-path sources, compiled in
   place from the reference checkout (default /root/reference, or $EIKX_REFERENCE) with
-  the host shim in oracle/shim/ and the driver ref_driver.cpp.  Files compiled from the
-  reference: src/graph3d.cpp, src/geometry3d.cpp, src/geometry2d.cpp,
-  src/solverOptions.cpp, plus the headers include/private/solver{2,3}d.hpp and
+  the host shim in oracle/shim/ and the drivers ref_driver.cpp and ref_trace.cpp.  Files
+  compiled from the reference: src/graph3d.cpp, src/geometry3d.cpp, src/geometry2d.cpp,
+  src/solverOptions.cpp, src/station2d.cpp, src/source2d.cpp, the 2D ray tracer
+  src/ray/{gradientTracer2d,gradientTracerOptions,path2d,segment2d,point2d}.cpp and
+  src/io/vtkLines2d.cpp, plus the headers include/private/solver{2,3}d.hpp and
   solverUtilities{2,3}d.hpp (through ref_driver.cpp).  Skipped, with a message, when
   the checkout is absent (it never travels to a GPU host).
 
@@ -52,9 +54,12 @@ def build_ref():
             _REF_SKIP_SAID = True
         return None
     os.makedirs(os.path.dirname(REF_LIB), exist_ok=True)
-    srcs = [os.path.join(HERE, "ref_driver.cpp")] + [
+    srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "ref_trace.cpp")] + [
         os.path.join(ref, "src", f) for f in ("graph3d.cpp", "geometry3d.cpp", "geometry2d.cpp",
-                                              "solverOptions.cpp")]
+                                              "solverOptions.cpp", "station2d.cpp", "source2d.cpp",
+                                              "ray/gradientTracer2d.cpp", "ray/gradientTracerOptions.cpp",
+                                              "ray/path2d.cpp", "ray/segment2d.cpp", "ray/point2d.cpp",
+                                              "io/vtkLines2d.cpp")]
     if os.path.exists(REF_LIB) and all(os.path.getmtime(REF_LIB) > os.path.getmtime(s) for s in srcs):
         return REF_LIB
     cmd = (["g++", "-std=c++20", "-w"] + FLAGS +

@@ -130,3 +130,60 @@ def test_nodal_to_cell_orderings_agree(oracle):
     mean = (v[:-1, :-1, :-1] + v[:-1, :-1, 1:] + v[:-1, 1:, :-1] + v[:-1, 1:, 1:] + v[1:, :-1, :-1] +
             v[1:, :-1, 1:] + v[1:, 1:, :-1] + v[1:, 1:, 1:]) / 8
     assert np.allclose(s_nat, (1 / mean).ravel(), rtol=1e-14)
+
+
+def _ray_cases():
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_oracle_rays import homogeneous_case
+    c = homogeneous_case()
+    cases = [("homogeneous", c)]
+    # a linear gradient v(z) = 3000 + 0.6 z with its analytic travel-time gradient
+    nx, nz, dx, dz = 161, 81, 25.0, 25.0
+    v0, k = 3000.0, 0.6
+    xs, zs = 2012.5, 812.5
+    zz, xx = np.meshgrid(np.arange(nz) * dz, np.arange(nx) * dx, indexing="ij")
+    vs, v = v0 + k * zs, v0 + k * zz
+    r2 = (xx - xs) ** 2 + (zz - zs) ** 2
+    arg = 1 + k * k * r2 / (2 * vs * v)
+    denom = np.sqrt(np.maximum(arg * arg - 1, 1e-30)) * k
+    dadx = k * k * (xx - xs) / (vs * v)
+    dadz = k * k * (zz - zs) / (vs * v) - k * k * r2 / (2 * vs * v * v) * k
+    grad = np.stack([dadx / denom, dadz / denom], axis=-1)
+    grad[r2 == 0] = 0
+    vc = v0 + k * (np.arange(nz - 1) + 0.5) * dz
+    slow = np.repeat(1 / vc, nx - 1)
+    rng = np.random.default_rng(4)
+    stations = [(float(rng.uniform(0, (nx - 1) * dx)), float(rng.uniform(0, (nz - 1) * dz))) for _ in range(24)]
+    cases.append(("linear", dict(grid=(nx, nz, dx, dz), origin=(0.0, 0.0), source=(xs, zs), grad=grad, slow=slow,
+                                 stations=stations)))
+    return cases
+
+
+@pytest.mark.parametrize("precision", [np.float64, np.float32])
+def test_ray_tracer_matches_the_reference(oracle, reference, precision):
+    """The oracle's restatement of GradientTracer2D::trace against the reference's own tracer:
+    the same segments, end points within 1e-6 m (the march uses eikxHypot where the reference
+    uses std::hypot), the same slownesses; rays the reference does not converge (empty paths)
+    are the oracle's count -1."""
+    radii, scales = [1, 2, 3, 5, 2 ** 31 - 1], [0.05, 0.10, 0.20, 0.30, 0.45]
+    for name, c in _ray_cases():
+        nx, nz, dx, dz = c["grid"]
+        cap = 4 * (nx + nz) + 16
+        g = c["grad"].astype(precision)
+        # A ray starting on the last node row makes the reference read past the end of its
+        # gradient array (gradientTracer2d.cpp:452-455): those stations are left out here.
+        zmax = c["origin"][1] + (nz - 1) * dz
+        stations = [p for p in c["stations"] if p[1] < zmax - 1e-9]
+        # a solver in T reports its slowness in T (ISolver2D<T>::getSlowness)
+        slow = c["slow"].astype(precision).astype(np.float64)
+        seg, counts = oracle.trace_rays2d(g, c["grid"], c["origin"], slow, c["source"], stations, radii,
+                                          scales, 200000, cap)
+        rseg, rcounts = reference.trace_rays2d(g, c["grid"], c["origin"], slow, c["source"], stations,
+                                               radii, scales, cap)
+        assert np.array_equal(np.where(counts < 0, 0, counts), rcounts), (name, counts, rcounts)
+        for i in range(len(counts)):
+            n = max(0, counts[i])
+            assert np.allclose(seg[i, :n, :4], rseg[i, :n, :4], rtol=0, atol=1e-6), (name, i)
+            assert np.array_equal(seg[i, :n, 4], rseg[i, :n, 4]), (name, i)
+            assert np.array_equal(seg[i, :n, 5], rseg[i, :n, 5]), (name, i)
