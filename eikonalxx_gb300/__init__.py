@@ -37,6 +37,9 @@ EXPORTED = [
     "eikx_solve3d_noalloc", "eikx_solve3d_batch", "eikx_autotune3d", "eikx_tuning_save", "eikx_tuning_load",
     "eikx_gradient3d", "eikx_gradient2d", "eikx_station_times3d", "eikx_station_times2d", "eikx_solve3d_warm",
     "eikx_ray_options_default", "eikx_trace_rays2d",
+    "eikx_warmnet_create", "eikx_warmnet_destroy", "eikx_warmnet_num_params", "eikx_warmnet_get_params",
+    "eikx_warmnet_set_params", "eikx_warmnet_train_step", "eikx_warmnet_gradients", "eikx_warmnet_predict",
+    "eikx_warmnet_profile_step",
 ]
 CELL_SLOWNESS, NODAL_VELOCITY = 0, 1
 
@@ -87,6 +90,17 @@ class _RayOptions(ctypes.Structure):
 class _RaySeg(ctypes.Structure):
     _fields_ = [("x0", ctypes.c_double), ("z0", ctypes.c_double), ("x1", ctypes.c_double), ("z1", ctypes.c_double),
                 ("slowness", ctypes.c_double), ("cell", ctypes.c_int), ("reserved", ctypes.c_int)]
+
+
+class _NetConfig(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("dx", ctypes.c_double),
+                ("dy", ctypes.c_double), ("dz", ctypes.c_double), ("x0", ctypes.c_double), ("y0", ctypes.c_double),
+                ("z0", ctypes.c_double), ("batch", ctypes.c_int), ("seed", ctypes.c_ulonglong)]
+
+
+class _NetSample(ctypes.Structure):
+    _fields_ = [("velocity", ctypes.c_void_p), ("travel_time", ctypes.c_void_p), ("x", ctypes.c_double),
+                ("y", ctypes.c_double), ("z", ctypes.c_double)]
 
 
 class _Src3(ctypes.Structure):
@@ -154,6 +168,18 @@ def load(path=None):
     lib.eikx_gradient2d.argtypes = [vp, c_int, vp, c_int]
     lib.eikx_station_times3d.argtypes = [vp, c_int, ctypes.POINTER(_Src3), c_int, ctypes.POINTER(c_double)]
     lib.eikx_station_times2d.argtypes = [vp, c_int, ctypes.POINTER(_Src2), c_int, ctypes.POINTER(c_double)]
+    dp = ctypes.POINTER(c_double)
+    fp = ctypes.POINTER(ctypes.c_float)
+    sp = ctypes.POINTER(_NetSample)
+    lib.eikx_warmnet_create.argtypes = [c_int, ctypes.POINTER(_NetConfig), ctypes.POINTER(vp)]
+    lib.eikx_warmnet_destroy.argtypes = [vp]
+    lib.eikx_warmnet_num_params.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    lib.eikx_warmnet_get_params.argtypes = [vp, fp]
+    lib.eikx_warmnet_set_params.argtypes = [vp, fp]
+    lib.eikx_warmnet_train_step.argtypes = [vp, sp, c_int, ctypes.c_float, dp]
+    lib.eikx_warmnet_gradients.argtypes = [vp, sp, c_int, fp, dp]
+    lib.eikx_warmnet_predict.argtypes = [vp, sp, c_int, c_double, vp, c_int, dp]
+    lib.eikx_warmnet_profile_step.argtypes = [vp, sp, c_int, ctypes.c_float, dp, dp]
     lib.eikx_tuning_save.argtypes = [vp, ctypes.c_char_p]
     lib.eikx_tuning_load.argtypes = [vp, ctypes.c_char_p]
     for name in EXPORTED:

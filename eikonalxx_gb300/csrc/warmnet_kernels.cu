@@ -1,0 +1,734 @@
+// Kernels of the learned warm start's 3D U-Net (declared in warmnet.h).
+//
+// The 3x3x3 convolutions are implicit GEMMs on the BF16 tensor cores with FP32
+// accumulation (mma.sync m16n8k16):
+//   * forward and input-gradient: M = output nodes (one 16-node x-row per MMA row block),
+//     N = output channels, K = 27 taps x input channels.  A block stages a haloed
+//     4 x 10 x 18-node tile of 16 input channels and the 27-tap weight slice of its
+//     output channels in shared memory (cp.async, zero fill outside the grid); every
+//     tap's A operand is an ldmatrix from the shifted halo, so each input value is read
+//     from global memory once per block;
+//   * weight gradient: M = output channels, N = 16 input channels, K = nodes; the A
+//     operand (dy transposed) and the B operand (shifted input) come from the same two
+//     tiles through ldmatrix.trans; each block loops over node tiles and adds its partial
+//     sums to the FP32 gradient with one atomic per element at the end.
+// Shared-memory rows are 48 bytes (an odd number of 16-byte segments), so the eight row
+// addresses of every ldmatrix phase fall in distinct banks.
+#include <cuda_bf16.h>
+
+#include "warmnet.h"
+
+namespace eikx {
+namespace net {
+namespace {
+
+__device__ __forceinline__ unsigned smemAddr(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// 16-byte global -> shared copy; zero fill when !valid (src is then not read).
+__device__ __forceinline__ void cpAsync16(void *dst, const void *src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smemAddr(dst)), "l"(src),
+                 "r"(valid ? 16 : 0));
+}
+__device__ __forceinline__ void cpAsyncCommitWaitAll() {
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void ldsm4(unsigned (&r)[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smemAddr(p)));
+}
+__device__ __forceinline__ void ldsm4t(unsigned (&r)[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smemAddr(p)));
+}
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+struct TileCoord {
+    int gx0, gy0, gz0;
+};
+__device__ __forceinline__ TileCoord tileOf(int t, int D, int H, int W) {
+    (void)D;
+    const int tx = (W + kTileX - 1) / kTileX, ty = (H + kTileY - 1) / kTileY;
+    TileCoord c;
+    c.gx0 = (t % tx) * kTileX;
+    t /= tx;
+    c.gy0 = (t % ty) * kTileY;
+    c.gz0 = (t / ty) * kTileZ;
+    return c;
+}
+__host__ __device__ inline int tilesPerSample(int D, int H, int W) {
+    return ((D + kTileZ - 1) / kTileZ) * ((H + kTileY - 1) / kTileY) * ((W + kTileX - 1) / kTileX);
+}
+
+// Stage 16 channels (ci0..ci0+15) of the haloed input tile: node (hz, hy, hx) of the
+// halo at row (hz*kHaloY + hy)*kHaloX + hx, zero outside the grid.
+__device__ __forceinline__ void stageHalo(bf16 *xs, const bf16 *xb, int cin, int ci0, TileCoord c, int D, int H,
+                                          int W, const bf16 *anyValid) {
+    for (int p = threadIdx.x; p < kHaloNodes * 2; p += kThreads) {
+        const int hv = p >> 1, half = p & 1;
+        const int hx = hv % kHaloX, hy = (hv / kHaloX) % kHaloY, hz = hv / (kHaloX * kHaloY);
+        const int gx = c.gx0 - 1 + hx, gy = c.gy0 - 1 + hy, gz = c.gz0 - 1 + hz;
+        const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H && gz >= 0 && gz < D;
+        const bf16 *src = in ? xb + ((static_cast<long long>(gz) * H + gy) * W + gx) * cin + ci0 + 8 * half : anyValid;
+        cpAsync16(xs + hv * kRowHalfs + 8 * half, src, in);
+    }
+}
+
+template <int NB>
+__global__ void __launch_bounds__(kThreads) convKernel(ConvArgs a) {
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    bf16 *xs = reinterpret_cast<bf16 *>(smemRaw);
+    bf16 *wsm = xs + kHaloNodes * kRowHalfs;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const TileCoord c = tileOf(blockIdx.x, a.D, a.H, a.W);
+    const int b = blockIdx.z, co0 = blockIdx.y * NB;
+    const long long V = static_cast<long long>(a.D) * a.H * a.W;
+    const bf16 *xb = a.x + b * V * a.cin;
+
+    float acc[2][NB / 8][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < NB / 8; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+
+    const int li = lane >> 3, lj = lane & 7;
+    for (int ci0 = 0; ci0 < a.cin; ci0 += 16) {
+        stageHalo(xs, xb, a.cin, ci0, c, a.D, a.H, a.W, a.x);
+        for (int p = threadIdx.x; p < 27 * NB * 2; p += kThreads) {
+            const int row = p >> 1, half = p & 1;   // row = tap * NB + co
+            const int tap = row / NB, co = row % NB;
+            cpAsync16(wsm + row * kRowHalfs + 8 * half,
+                      a.w + (static_cast<long long>(tap) * a.cout + co0 + co) * a.cin + ci0 + 8 * half, true);
+        }
+        cpAsyncCommitWaitAll();
+        __syncthreads();
+#pragma unroll 1
+        for (int tap = 0; tap < 27; ++tap) {
+            const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+            // B fragments: matrix li of ldmatrix.x4 = (channels 16p + 8*(li>>1) .. +7, k half li&1)
+            unsigned bfr[NB / 16][4];
+#pragma unroll
+            for (int p = 0; p < NB / 16; ++p)
+                ldsm4(bfr[p], wsm + (tap * NB + 16 * p + lj + 8 * (li >> 1)) * kRowHalfs + 8 * (li & 1));
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                const int r = warp * 2 + mt, tz = r >> 3, ty = r & 7;
+                // A fragment: matrix li = (nodes 8*(li&1) .. +7 of the x-row, k half li>>1)
+                unsigned afr[4];
+                ldsm4(afr, xs + (((tz + dz) * kHaloY + ty + dy) * kHaloX + lj + 8 * (li & 1) + dx) * kRowHalfs +
+                               8 * (li >> 1));
+#pragma unroll
+                for (int nt = 0; nt < NB / 8; ++nt)
+                    mma16816(acc[mt][nt], afr, bfr[nt >> 1][(nt & 1) * 2], bfr[nt >> 1][(nt & 1) * 2 + 1]);
+            }
+        }
+        __syncthreads();
+    }
+
+    // Epilogue: accumulator (row lane/4 [+8], columns 2*(lane%4), +1) of each 16x8 block.
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+        const int r = warp * 2 + mt;
+        const int gz = c.gz0 + (r >> 3), gy = c.gy0 + (r & 7);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int gx = c.gx0 + (lane >> 2) + 8 * h;
+            if (gz >= a.D || gy >= a.H || gx >= a.W) continue;
+            const long long node = b * V + (static_cast<long long>(gz) * a.H + gy) * a.W + gx;
+#pragma unroll
+            for (int nt = 0; nt < NB / 8; ++nt) {
+                const int co = co0 + 8 * nt + 2 * (lane & 3);
+                float y0 = acc[mt][nt][2 * h], y1 = acc[mt][nt][2 * h + 1];
+                if (a.bias) {
+                    y0 += a.bias[co];
+                    y1 += a.bias[co + 1];
+                }
+                if (a.relu) {
+                    y0 = fmaxf(y0, 0.f);
+                    y1 = fmaxf(y1, 0.f);
+                }
+                if (a.mask) {
+                    const __nv_bfloat162 m = *reinterpret_cast<const __nv_bfloat162 *>(a.mask + node * a.cout + co);
+                    if (!(__bfloat162float(m.x) > 0.f)) y0 = 0.f;
+                    if (!(__bfloat162float(m.y) > 0.f)) y1 = 0.f;
+                }
+                *reinterpret_cast<__nv_bfloat162 *>(a.y + node * a.cout + co) = __floats2bfloat162_rn(y0, y1);
+            }
+        }
+    }
+}
+
+// Weight gradient.  Work unit u = (co block cb = u / 27, tap = u % 27): a 16 (co) x 16
+// (ci) block of dw; a warp holds 4 units, a block 32; grid.y walks the units, grid.z the
+// 16-channel input chunks, grid.x strides over the node tiles of all samples.
+constexpr int kUnitsPerWarp = 4;
+__global__ void __launch_bounds__(kThreads) wgradKernel(WGradArgs a) {
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    bf16 *xs = reinterpret_cast<bf16 *>(smemRaw);
+    bf16 *dys = xs + kHaloNodes * kRowHalfs;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int li = lane >> 3, lj = lane & 7;
+    const int ci0 = blockIdx.z * 16;
+    const int nUnits = 27 * (a.cout / 16);
+    const int dyRow = a.cout + 8;   // halfs; an odd number of 16-byte segments
+    const long long V = static_cast<long long>(a.D) * a.H * a.W;
+    const int tps = tilesPerSample(a.D, a.H, a.W);
+    const int nTiles = tps * a.B;
+
+    float acc[kUnitsPerWarp][2][4];
+#pragma unroll
+    for (int i = 0; i < kUnitsPerWarp; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+
+    for (int t = blockIdx.x; t < nTiles; t += gridDim.x) {
+        const int b = t / tps;
+        const TileCoord c = tileOf(t % tps, a.D, a.H, a.W);
+        stageHalo(xs, a.x + b * V * a.cin, a.cin, ci0, c, a.D, a.H, a.W, a.x);
+        const int pieces = a.cout / 8;
+        for (int p = threadIdx.x; p < 256 * pieces; p += kThreads) {
+            const int node = p / pieces, piece = p % pieces;
+            const int r = node >> 4, xx = node & 15;
+            const int gz = c.gz0 + (r >> 3), gy = c.gy0 + (r & 7), gx = c.gx0 + xx;
+            const bool in = gz < a.D && gy < a.H && gx < a.W;
+            const bf16 *src =
+                in ? a.dy + (b * V + (static_cast<long long>(gz) * a.H + gy) * a.W + gx) * a.cout + 8 * piece : a.dy;
+            cpAsync16(dys + node * dyRow + 8 * piece, src, in);
+        }
+        cpAsyncCommitWaitAll();
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kUnitsPerWarp; ++k) {
+            const int u = (blockIdx.y * (kThreads / 32) + warp) * kUnitsPerWarp + k;
+            if (u >= nUnits) continue;
+            const int tap = u % 27, cb = u / 27;
+            const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+#pragma unroll 2
+            for (int r = 0; r < 16; ++r) {
+                const int tz = r >> 3, ty = r & 7;
+                unsigned afr[4], bfr[4];
+                // A = dy^T: matrix li = (co 16cb + 8*(li&1) .., nodes 16r + 8*(li>>1) ..)
+                ldsm4t(afr, dys + (16 * r + lj + 8 * (li >> 1)) * dyRow + 16 * cb + 8 * (li & 1));
+                // B = shifted input: matrix li = (nodes 8*(li&1) .., channels 8*(li>>1) ..)
+                ldsm4t(bfr, xs + (((tz + dz) * kHaloY + ty + dy) * kHaloX + lj + 8 * (li & 1) + dx) * kRowHalfs +
+                                8 * (li >> 1));
+                mma16816(acc[k][0], afr, bfr[0], bfr[1]);
+                mma16816(acc[k][1], afr, bfr[2], bfr[3]);
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < kUnitsPerWarp; ++k) {
+        const int u = (blockIdx.y * (kThreads / 32) + warp) * kUnitsPerWarp + k;
+        if (u >= nUnits) continue;
+        const int tap = u % 27, cb = u / 27;
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+            const int ci = ci0 + 8 * nt + 2 * (lane & 3);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int co = 16 * cb + (lane >> 2) + 8 * h;
+                float *d = a.dw + (static_cast<long long>(tap) * a.cout + co) * a.cin + ci;
+                atomicAdd(d, acc[k][nt][2 * h]);
+                atomicAdd(d + 1, acc[k][nt][2 * h + 1]);
+            }
+        }
+    }
+}
+
+__global__ void biasGradKernel(const bf16 *dy, int C, long long nodes, float *db) {
+    __shared__ float part[kThreads];
+    const int c = threadIdx.x % C, slot = threadIdx.x / C, slots = kThreads / C;
+    float s = 0.f;
+    for (long long v = static_cast<long long>(blockIdx.x) * slots + slot; v < nodes;
+         v += static_cast<long long>(gridDim.x) * slots)
+        s += __bfloat162float(dy[v * C + c]);
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (slot == 0) {
+        for (int k = 1; k < slots; ++k) s += part[k * C + c];
+        atomicAdd(db + c, s);
+    }
+}
+
+struct alignas(16) Vec8 {
+    __nv_bfloat162 h[4];
+};
+__device__ __forceinline__ void load8(float (&f)[8], const bf16 *p) {
+    const Vec8 v = *reinterpret_cast<const Vec8 *>(p);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        f[2 * i] = __bfloat162float(v.h[i].x);
+        f[2 * i + 1] = __bfloat162float(v.h[i].y);
+    }
+}
+__device__ __forceinline__ void store8(bf16 *p, const float (&f)[8]) {
+    Vec8 v;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v.h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+    *reinterpret_cast<Vec8 *>(p) = v;
+}
+
+__global__ void poolKernel(const bf16 *x, int C, int D, int H, int W, int B, bf16 *y) {
+    const int Dl = D / 2, Hl = H / 2, Wl = W / 2, groups = C / 8;
+    const long long total = static_cast<long long>(B) * Dl * Hl * Wl * groups;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int g = i % groups;
+        long long u = i / groups;
+        const int ux = u % Wl, uy = (u / Wl) % Hl, uz = (u / (static_cast<long long>(Wl) * Hl)) % Dl;
+        const long long b = u / (static_cast<long long>(Wl) * Hl * Dl);
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < 8; ++k) {
+            const int z = 2 * uz + (k >> 2), yy = 2 * uy + ((k >> 1) & 1), xx = 2 * ux + (k & 1);
+            float f[8];
+            load8(f, x + ((b * D + z) * H * static_cast<long long>(W) + static_cast<long long>(yy) * W + xx) * C + 8 * g);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s[j] += f[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) s[j] *= 0.125f;
+        store8(y + u * C + 8 * g, s);
+    }
+}
+
+__global__ void upcatKernel(const bf16 *low, int c1, const bf16 *skip, int c2, int D, int H, int W, int B,
+                            bf16 *out) {
+    const int C = c1 + c2, groups = C / 8;
+    const long long total = static_cast<long long>(B) * D * H * W * groups;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int g = i % groups;
+        const long long v = i / groups;
+        const int x = v % W, y = (v / W) % H, z = (v / (static_cast<long long>(W) * H)) % D;
+        const long long b = v / (static_cast<long long>(W) * H * D);
+        const bf16 *src;
+        if (8 * g < c1) {
+            const long long u = ((b * (D / 2) + z / 2) * (H / 2) + y / 2) * (W / 2) + x / 2;
+            src = low + u * c1 + 8 * g;
+        } else {
+            src = skip + v * c2 + 8 * g - c1;
+        }
+        *reinterpret_cast<Vec8 *>(out + v * C + 8 * g) = *reinterpret_cast<const Vec8 *>(src);
+    }
+}
+
+__global__ void upSumMaskKernel(const bf16 *dcat, int ccat, const bf16 *act, int c1, int Dl, int Hl, int Wl, int B,
+                                bf16 *dpre) {
+    const int groups = c1 / 8, D = 2 * Dl, H = 2 * Hl, W = 2 * Wl;
+    const long long total = static_cast<long long>(B) * Dl * Hl * Wl * groups;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int g = i % groups;
+        const long long u = i / groups;
+        const int ux = u % Wl, uy = (u / Wl) % Hl, uz = (u / (static_cast<long long>(Wl) * Hl)) % Dl;
+        const long long b = u / (static_cast<long long>(Wl) * Hl * Dl);
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < 8; ++k) {
+            const int z = 2 * uz + (k >> 2), yy = 2 * uy + ((k >> 1) & 1), xx = 2 * ux + (k & 1);
+            float f[8];
+            load8(f, dcat + ((b * D + z) * H * static_cast<long long>(W) + static_cast<long long>(yy) * W + xx) * ccat +
+                         8 * g);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s[j] += f[j];
+        }
+        float m[8];
+        load8(m, act + u * c1 + 8 * g);
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (!(m[j] > 0.f)) s[j] = 0.f;
+        store8(dpre + u * c1 + 8 * g, s);
+    }
+}
+
+__global__ void combineSkipKernel(const bf16 *dcat, int ccat, int c1, const bf16 *dpool, const bf16 *skip, int c2,
+                                  int D, int H, int W, int B, bf16 *dpre) {
+    const int groups = c2 / 8;
+    const long long total = static_cast<long long>(B) * D * H * W * groups;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int g = i % groups;
+        const long long v = i / groups;
+        const int x = v % W, y = (v / W) % H, z = (v / (static_cast<long long>(W) * H)) % D;
+        const long long b = v / (static_cast<long long>(W) * H * D);
+        const long long u = ((b * (D / 2) + z / 2) * (H / 2) + y / 2) * (W / 2) + x / 2;
+        float a[8], p[8], m[8];
+        load8(a, dcat + v * ccat + c1 + 8 * g);
+        load8(p, dpool + u * c2 + 8 * g);
+        load8(m, skip + v * c2 + 8 * g);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) a[j] = (m[j] > 0.f) ? a[j] + 0.125f * p[j] : 0.f;
+        store8(dpre + v * c2 + 8 * g, a);
+    }
+}
+
+// Source quantities shared by the per-node kernels.
+struct SourceInfo {
+    double sSrc;   // slowness at the node nearest the source
+};
+__device__ __forceinline__ double sourceSlowness(const Sample &s, const Geometry &g) {
+    const int ix = min(g.nx - 1, max(0, __double2int_rn((s.xs - g.x0) / g.dx)));
+    const int iy = min(g.ny - 1, max(0, __double2int_rn((s.ys - g.y0) / g.dy)));
+    const int iz = min(g.nz - 1, max(0, __double2int_rn((s.zs - g.z0) / g.dz)));
+    return 1.0 / static_cast<double>(s.velocity[(static_cast<long long>(iz) * g.ny + iy) * g.nx + ix]);
+}
+struct NodeGeom {
+    double ddx, ddy, ddz, dist;
+};
+__device__ __forceinline__ NodeGeom nodeGeom(long long v, const Sample &s, const Geometry &g) {
+    const int x = v % g.nx, y = (v / g.nx) % g.ny, z = v / (static_cast<long long>(g.nx) * g.ny);
+    NodeGeom n;
+    n.ddx = (g.x0 + x * g.dx) - s.xs;
+    n.ddy = (g.y0 + y * g.dy) - s.ys;
+    n.ddz = (g.z0 + z * g.dz) - s.zs;
+    n.dist = sqrt(n.ddx * n.ddx + n.ddy * n.ddy + n.ddz * n.ddz);
+    return n;
+}
+
+// Straight-ray estimate of tau - 1 at node (x, y, z): the mean of s/s_src - 1 over
+// kRaySamples midpoints of the segment from the source to the node, the slowness
+// trilinear in the nodal 1/v.  FP32, in an operation order the oracle repeats.
+constexpr int kRaySamples = 32;
+__device__ __forceinline__ float nodalSlowness(const float *vel, const Geometry &g, int x, int y, int z) {
+    return 1.f / vel[(static_cast<long long>(z) * g.ny + y) * g.nx + x];
+}
+__device__ float straightRayContrast(const Sample &s, const Geometry &g, float sSrc, int x, int y, int z) {
+    const float sx = static_cast<float>((s.xs - g.x0) / g.dx), sy = static_cast<float>((s.ys - g.y0) / g.dy),
+                sz = static_cast<float>((s.zs - g.z0) / g.dz);
+    const float ex = static_cast<float>(x) - sx, ey = static_cast<float>(y) - sy, ez = static_cast<float>(z) - sz;
+    float acc = 0.f;
+    for (int k = 0; k < kRaySamples; ++k) {
+        const float t = (static_cast<float>(k) + 0.5f) / static_cast<float>(kRaySamples);
+        const float px = fminf(fmaxf(sx + t * ex, 0.f), static_cast<float>(g.nx - 1));
+        const float py = fminf(fmaxf(sy + t * ey, 0.f), static_cast<float>(g.ny - 1));
+        const float pz = fminf(fmaxf(sz + t * ez, 0.f), static_cast<float>(g.nz - 1));
+        const int ix = min(static_cast<int>(floorf(px)), g.nx - 2), iy = min(static_cast<int>(floorf(py)), g.ny - 2),
+                  iz = min(static_cast<int>(floorf(pz)), g.nz - 2);
+        const float fx = px - static_cast<float>(ix), fy = py - static_cast<float>(iy), fz = pz - static_cast<float>(iz);
+        const float s000 = nodalSlowness(s.velocity, g, ix, iy, iz), s100 = nodalSlowness(s.velocity, g, ix + 1, iy, iz);
+        const float s010 = nodalSlowness(s.velocity, g, ix, iy + 1, iz),
+                    s110 = nodalSlowness(s.velocity, g, ix + 1, iy + 1, iz);
+        const float s001 = nodalSlowness(s.velocity, g, ix, iy, iz + 1),
+                    s101 = nodalSlowness(s.velocity, g, ix + 1, iy, iz + 1);
+        const float s011 = nodalSlowness(s.velocity, g, ix, iy + 1, iz + 1),
+                    s111 = nodalSlowness(s.velocity, g, ix + 1, iy + 1, iz + 1);
+        const float c00 = s000 + fx * (s100 - s000), c10 = s010 + fx * (s110 - s010);
+        const float c01 = s001 + fx * (s101 - s001), c11 = s011 + fx * (s111 - s011);
+        const float c0 = c00 + fy * (c10 - c00), c1 = c01 + fy * (c11 - c01);
+        const float c = c0 + fz * (c1 - c0);
+        acc += c / sSrc - 1.f;
+    }
+    return acc / static_cast<float>(kRaySamples);
+}
+
+__global__ void featuresKernel(const Sample *samples, Geometry g, int B, bf16 *feat) {
+    const long long V = static_cast<long long>(g.nx) * g.ny * g.nz;
+    const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    if (i >= B * V) return;
+    const int b = i / V;
+    const long long v = i % V;
+    const Sample s = samples[b];
+    const double sSrc = sourceSlowness(s, g);
+    const NodeGeom n = nodeGeom(v, s, g);
+    float f[8] = {static_cast<float>(1.0 / static_cast<double>(s.velocity[v]) / sSrc - 1.0),
+                  static_cast<float>(n.dist * g.invL),
+                  static_cast<float>(n.ddx * g.invL),
+                  static_cast<float>(n.ddy * g.invL),
+                  static_cast<float>(n.ddz * g.invL),
+                  straightRayContrast(s, g, static_cast<float>(sSrc), static_cast<int>(v % g.nx),
+                                      static_cast<int>((v / g.nx) % g.ny),
+                                      static_cast<int>(v / (static_cast<long long>(g.nx) * g.ny))),
+                  0.f,
+                  0.f};
+    store8(feat + i * 16, f);
+    const float z[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    store8(feat + i * 16 + 8, z);
+}
+
+__device__ __forceinline__ float warpSum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warpSumD(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float headOut(const float (&h)[16], const float *hw) {
+    float o = hw[16];
+    for (int c = 0; c < 16; ++c) o += hw[c] * h[c];
+    return o;
+}
+
+__global__ void __launch_bounds__(kThreads) headLossKernel(const bf16 *h, const float *hw, const Sample *samples,
+                                                           Geometry g, int B, double invN, float *dhw, bf16 *dpre,
+                                                           double *lossSum) {
+    __shared__ float red[kThreads / 32][17];
+    __shared__ double redL[kThreads / 32];
+    const long long V = static_cast<long long>(g.nx) * g.ny * g.nz;
+    const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    float hv[16];
+    float dout = 0.f;
+    double l = 0.0;
+    if (i < B * V) {
+        const int b = i / V;
+        const long long v = i % V;
+        const Sample s = samples[b];
+        float a[8], c[8];
+        load8(a, h + i * 16);
+        load8(c, h + i * 16 + 8);
+        for (int k = 0; k < 8; ++k) {
+            hv[k] = a[k];
+            hv[8 + k] = c[k];
+        }
+        const float o = headOut(hv, hw);
+        const double T0 = sourceSlowness(s, g) * nodeGeom(v, s, g).dist;
+        if (T0 > 0) {
+            const float tgt = static_cast<float>(static_cast<double>(s.travelTime[v]) / T0 - 1.0);
+            const float diff = o - tgt;
+            l = static_cast<double>(diff) * diff;
+            dout = static_cast<float>(2.0 * diff * invN);
+        }
+        float d[8], e[8];
+        for (int k = 0; k < 8; ++k) {
+            d[k] = hv[k] > 0.f ? dout * hw[k] : 0.f;
+            e[k] = hv[8 + k] > 0.f ? dout * hw[8 + k] : 0.f;
+        }
+        store8(dpre + i * 16, d);
+        store8(dpre + i * 16 + 8, e);
+    } else {
+        for (int k = 0; k < 16; ++k) hv[k] = 0.f;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < 16; ++k) {
+        const float t = warpSum(dout * hv[k]);
+        if (lane == 0) red[warp][k] = t;
+    }
+    const float tb = warpSum(dout);
+    const double tl = warpSumD(l);
+    if (lane == 0) {
+        red[warp][16] = tb;
+        redL[warp] = tl;
+    }
+    __syncthreads();
+    if (threadIdx.x < 17) {
+        float s = 0.f;
+        for (int w = 0; w < kThreads / 32; ++w) s += red[w][threadIdx.x];
+        atomicAdd(dhw + threadIdx.x, s);
+    } else if (threadIdx.x == 32) {
+        double s = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) s += redL[w];
+        atomicAdd(lossSum, s);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) predictKernel(const bf16 *h, const float *hw, const Sample *samples,
+                                                          Geometry g, int B, double inflate, float *out,
+                                                          double *lossSum) {
+    __shared__ double redL[kThreads / 32];
+    const long long V = static_cast<long long>(g.nx) * g.ny * g.nz;
+    const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    double l = 0.0;
+    if (i < B * V) {
+        const int b = i / V;
+        const long long v = i % V;
+        const Sample s = samples[b];
+        float a[8], c[8], hv[16];
+        load8(a, h + i * 16);
+        load8(c, h + i * 16 + 8);
+        for (int k = 0; k < 8; ++k) {
+            hv[k] = a[k];
+            hv[8 + k] = c[k];
+        }
+        const float o = headOut(hv, hw);
+        const double T0 = sourceSlowness(s, g) * nodeGeom(v, s, g).dist;
+        out[i] = static_cast<float>(T0 * (1.0 + o) * inflate);
+        if (lossSum && s.travelTime && T0 > 0) {
+            const float diff = o - static_cast<float>(static_cast<double>(s.travelTime[v]) / T0 - 1.0);
+            l = static_cast<double>(diff) * diff;
+        }
+    }
+    if (!lossSum) return;
+    const double t = warpSumD(l);
+    if ((threadIdx.x & 31) == 0) redL[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) s += redL[w];
+        atomicAdd(lossSum, s);
+    }
+}
+
+__global__ void adamKernel(float *p, const float *g, float *m, float *v, bf16 *pb, long long n, float lr, float b1,
+                           float b2, float eps, float bc1, float bc2) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float pi = p[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+        p[i] = pi;
+        pb[i] = __float2bfloat16_rn(pi);
+    }
+}
+
+__global__ void toBF16Kernel(const float *p, bf16 *pb, long long n) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        pb[i] = __float2bfloat16_rn(p[i]);
+}
+
+__global__ void flipTransposeKernel(const bf16 *w, int cout, int cin, bf16 *wt) {
+    const long long n = 27LL * cout * cin;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int co = i % cout;
+        const int ci = (i / cout) % cin;
+        const int tap = i / (static_cast<long long>(cout) * cin);
+        wt[i] = w[(static_cast<long long>(26 - tap) * cout + co) * cin + ci];
+    }
+}
+
+int gridFor(long long n, int cap = 1 << 20) {
+    long long b = (n + kThreads - 1) / kThreads;
+    if (b < 1) b = 1;
+    return static_cast<int>(b < cap ? b : cap);
+}
+
+template <int NB>
+cudaError_t convOne(const ConvArgs &a, cudaStream_t s) {
+    const int smem = (kHaloNodes + 27 * NB) * kRowHalfs * static_cast<int>(sizeof(bf16));
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(convKernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    dim3 grid(tilesPerSample(a.D, a.H, a.W), a.cout / NB, a.B);
+    convKernel<NB><<<grid, kThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launchConv(const ConvArgs &a, cudaStream_t s) {
+    if (a.cin % 16 || a.cout % 16 || a.B < 1) return cudaErrorInvalidValue;
+    return a.cout % 32 == 0 ? convOne<32>(a, s) : convOne<16>(a, s);
+}
+
+cudaError_t launchWGrad(const WGradArgs &a, int numSMs, cudaStream_t s) {
+    if (a.cin % 16 || a.cout % 16 || a.B < 1) return cudaErrorInvalidValue;
+    const int smem = (kHaloNodes * kRowHalfs + 256 * (a.cout + 8)) * static_cast<int>(sizeof(bf16));
+    static int attrBytes = 0;
+    if (smem > attrBytes) {
+        cudaError_t e = cudaFuncSetAttribute(wgradKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attrBytes = smem;
+    }
+    const int unitsPerBlock = (kThreads / 32) * kUnitsPerWarp;
+    const int gy = (27 * (a.cout / 16) + unitsPerBlock - 1) / unitsPerBlock, gz = a.cin / 16;
+    const int nTiles = tilesPerSample(a.D, a.H, a.W) * a.B;
+    int gx = (4 * numSMs + gy * gz - 1) / (gy * gz);
+    gx = gx < 1 ? 1 : (gx > nTiles ? nTiles : gx);
+    wgradKernel<<<dim3(gx, gy, gz), kThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launchBiasGrad(const bf16 *dy, int c, long long nodes, float *db, int numSMs, cudaStream_t s) {
+    if (c < 1 || c > kThreads || kThreads % c) return cudaErrorInvalidValue;
+    const long long slots = kThreads / c;
+    long long blocks = (nodes + slots * 64 - 1) / (slots * 64);
+    if (blocks > 4LL * numSMs) blocks = 4LL * numSMs;
+    if (blocks < 1) blocks = 1;
+    biasGradKernel<<<static_cast<int>(blocks), kThreads, 0, s>>>(dy, c, nodes, db);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPool(const bf16 *x, int C, int D, int H, int W, int B, bf16 *y, cudaStream_t s) {
+    poolKernel<<<gridFor(static_cast<long long>(B) * (D / 2) * (H / 2) * (W / 2) * (C / 8)), kThreads, 0, s>>>(
+        x, C, D, H, W, B, y);
+    return cudaGetLastError();
+}
+
+cudaError_t launchUpcat(const bf16 *low, int c1, const bf16 *skip, int c2, int D, int H, int W, int B, bf16 *out,
+                        cudaStream_t s) {
+    upcatKernel<<<gridFor(static_cast<long long>(B) * D * H * W * ((c1 + c2) / 8)), kThreads, 0, s>>>(
+        low, c1, skip, c2, D, H, W, B, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launchUpSumMask(const bf16 *dcat, int ccat, const bf16 *act, int c1, int Dl, int Hl, int Wl, int B,
+                            bf16 *dpre, cudaStream_t s) {
+    upSumMaskKernel<<<gridFor(static_cast<long long>(B) * Dl * Hl * Wl * (c1 / 8)), kThreads, 0, s>>>(
+        dcat, ccat, act, c1, Dl, Hl, Wl, B, dpre);
+    return cudaGetLastError();
+}
+
+cudaError_t launchCombineSkip(const bf16 *dcat, int ccat, int c1, const bf16 *dpool, const bf16 *skip, int c2,
+                              int D, int H, int W, int B, bf16 *dpre, cudaStream_t s) {
+    combineSkipKernel<<<gridFor(static_cast<long long>(B) * D * H * W * (c2 / 8)), kThreads, 0, s>>>(
+        dcat, ccat, c1, dpool, skip, c2, D, H, W, B, dpre);
+    return cudaGetLastError();
+}
+
+cudaError_t launchFeatures(const Sample *samples, Geometry g, int B, bf16 *feat, cudaStream_t s) {
+    const long long n = static_cast<long long>(B) * g.nx * g.ny * g.nz;
+    featuresKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(samples, g, B, feat);
+    return cudaGetLastError();
+}
+
+cudaError_t launchHeadLoss(const bf16 *h, const float *hw, const Sample *samples, Geometry g, int B, double invN,
+                           float *dhw, bf16 *dpre, double *lossSum, cudaStream_t s) {
+    const long long n = static_cast<long long>(B) * g.nx * g.ny * g.nz;
+    headLossKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(h, hw, samples, g, B, invN,
+                                                                                       dhw, dpre, lossSum);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPredict(const bf16 *h, const float *hw, const Sample *samples, Geometry g, int B, double inflate,
+                          float *out, double *lossSum, cudaStream_t s) {
+    const long long n = static_cast<long long>(B) * g.nx * g.ny * g.nz;
+    predictKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(h, hw, samples, g, B, inflate,
+                                                                                      out, lossSum);
+    return cudaGetLastError();
+}
+
+cudaError_t launchAdam(float *p, const float *g, float *m, float *v, bf16 *pb, long long n, float lr, float b1,
+                       float b2, float eps, float bc1, float bc2, cudaStream_t s) {
+    adamKernel<<<gridFor(n, 4096), kThreads, 0, s>>>(p, g, m, v, pb, n, lr, b1, b2, eps, bc1, bc2);
+    return cudaGetLastError();
+}
+
+cudaError_t launchToBF16(const float *p, bf16 *pb, long long n, cudaStream_t s) {
+    toBF16Kernel<<<gridFor(n, 4096), kThreads, 0, s>>>(p, pb, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launchFlipTranspose(const bf16 *w, int cout, int cin, bf16 *wt, cudaStream_t s) {
+    flipTransposeKernel<<<gridFor(27LL * cout * cin, 4096), kThreads, 0, s>>>(w, cout, cin, wt);
+    return cudaGetLastError();
+}
+
+}  // namespace net
+}  // namespace eikx

@@ -359,6 +359,76 @@ eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, double dy, d
                                  const eikx_source3d *src, const eikx_options *opt,
                                  float *t_out, void *stream);
 
+/* ---- learned warm start: the travel-time predictor -------------------------- */
+/* No counterpart in the reference.  A 3D U-Net predicts the factored correction
+ * tau = T / T0 - 1 of a travel-time field from its velocity model and source, where
+ * T0 = s_src * |x - x_s| and s_src is the slowness (1/v) at the node nearest the source.
+ * Its prediction, inflated, is an initial field for eikx_solve3d_warm.
+ *
+ * Network (channels-last BF16 activations [sample][z][y][x][channel], BF16 weights,
+ * FP32 accumulation on the tensor cores, FP32 master weights and Adam state):
+ *   input features (16 channels, 6 used): s/s_src - 1, |x - x_s| / L, (x - x_s) / L,
+ *     (y - y_s) / L, (z - z_s) / L, with L the length of the grid's diagonal, and the
+ *     straight-ray estimate of tau: the mean of s/s_src - 1 at 32 midpoints of the
+ *     segment from the source to the node (s trilinear in the nodal 1/v, FP32);
+ *   encoder: two 3x3x3 convolutions + ReLU per level, 16, 32, 64 channels, 2x2x2 average
+ *     pooling between levels; bottleneck: two convolutions with 128 channels;
+ *   decoder: nearest 2x upsampling, concatenation with the encoder level, two
+ *     convolutions + ReLU (64, 32, 16 channels); head: 1x1x1 convolution to tau.
+ *   Zero padding at the grid's faces.  1,466,065 parameters.  The loss is the mean of
+ *   (tau_pred - tau)^2 over the nodes with T0 > 0.
+ * Parameters are one FP32 vector: per convolution (in the order above: E0a, E0b, E1a,
+ * E1b, E2a, E2b, Ba, Bb, D2a, D2b, D1a, D1b, D0a, D0b) its weights [27 taps][out][in]
+ * (tap = (dz*3 + dy)*3 + dx, the input node offset (dz-1, dy-1, dx-1)) then its biases
+ * [out]; then the head's 16 weights and its bias.  E0a takes 16 input channels, of
+ * which the last 10 are zero. */
+typedef struct eikx_warmnet eikx_warmnet;
+
+typedef struct {
+    int nx, ny, nz;        /* node grid; each a multiple of 8 */
+    double dx, dy, dz;     /* grid spacing (m) */
+    double x0, y0, z0;     /* origin (m) */
+    int batch;             /* largest number of samples per call */
+    unsigned long long seed;   /* initial weights (He-normal convolutions, zero biases and head) */
+} eikx_warmnet_config;
+
+/* One sample: DEVICE pointers to its nodal velocity model (nx*ny*nz FP32, m/s, natural
+ * order) and, for training, its solved travel-time field (same layout; NULL when only
+ * predicting), and the source position (m). */
+typedef struct {
+    const float *velocity;
+    const float *travel_time;
+    double x, y, z;
+} eikx_warmnet_sample;
+
+eikx_status eikx_warmnet_create(int device, const eikx_warmnet_config *cfg, eikx_warmnet **net);
+eikx_status eikx_warmnet_destroy(eikx_warmnet *net);
+eikx_status eikx_warmnet_num_params(const eikx_warmnet *net, long long *n);
+/* Copy the FP32 parameter vector out of / into the network (host pointers).  Setting it
+ * also resets the Adam state and its step count. */
+eikx_status eikx_warmnet_get_params(eikx_warmnet *net, float *params);
+eikx_status eikx_warmnet_set_params(eikx_warmnet *net, const float *params);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8, learning rate lr) on n samples
+ * (1 <= n <= batch); loss: the loss before the step. */
+eikx_status eikx_warmnet_train_step(eikx_warmnet *net, const eikx_warmnet_sample *s, int n, float lr,
+                                    double *loss);
+/* The loss and its gradient with respect to the parameter vector (host, num_params
+ * floats) on n samples, without updating the network. */
+eikx_status eikx_warmnet_gradients(eikx_warmnet *net, const eikx_warmnet_sample *s, int n, float *grads,
+                                   double *loss);
+/* Predicted travel times T0 * (1 + tau_pred) * inflate for n samples: n*nx*ny*nz FP32,
+ * natural order, host or device (where).  Also the forward pass a loss evaluation uses:
+ * loss (may be NULL) receives the loss when every sample has a travel_time. */
+eikx_status eikx_warmnet_predict(eikx_warmnet *net, const eikx_warmnet_sample *s, int n, double inflate,
+                                 float *t_out, int where, double *loss);
+/* Device time (ms, CUDA events on the network's stream) of one training step on n
+ * samples, split into forward convolutions, input-gradient convolutions, weight-gradient
+ * kernels and everything else, and the algorithmic tensor-core FLOPs of each of the
+ * first three (2 * nodes * 27 * in * out per convolution and sample).  The step updates
+ * the network.  ms and flops: 4 and 3 doubles. */
+eikx_status eikx_warmnet_profile_step(eikx_warmnet *net, const eikx_warmnet_sample *s, int n, float lr,
+                                      double *ms, double *flops);
+
 #ifdef __cplusplus
 }
 #endif
