@@ -545,6 +545,145 @@ def run_warmstart_study(args):
                       "grid": [NX, NY, NZ], "rows": rows}), flush=True)
 
 
+LEARN_GRID = (128, 128, 64, 50.0)
+PREDICT_LAUNCHES = 22   # features, 14 convolutions, 3 poolings, 3 up-and-concats, the head
+
+
+def run_learned(args):
+    """The learned warm start on 128x128x64 nodes, h = 50 m.  Training data: `fields`
+    random smooth models (Gaussian random fields, 1500-8000 m/s, correlation length
+    0.5-3 km) with 8 seeded sources each, solved cold by the library.  The network is
+    trained on them by its own kernels (Adam, batch 8).  Evaluation on 4 held-out models
+    (32 fields): cold-start solves against warm starts (prediction x 1.02, residual gate,
+    sweeps to the tolerance) from the trained network and from T0 alone (the untrained
+    network).  The line's value is the cold-start grids/s of the held-out fields, the
+    path that meets the error bound; the learned path's rate, sweeps and deviation from
+    the cold start are under "learned"."""
+    import torch
+    import eikonalxx_gb300 as ex
+    from eikonalxx_gb300 import warmstart as ws
+
+    nx, ny, nz, h = LEARN_GRID
+    grid = (nx, ny, nz, h, h, h)
+    dev = torch.cuda.current_device()
+    per_model, test_models, batch = 8, 4, 8
+    ctx = ex.Context(dev)
+    opt = ex.Options(n_sweeps=20, tolerance=TOL, factored_radius=RADIUS)
+    t = time.perf_counter()
+    data = ws.generate_fields(ctx, grid, args.fields + test_models, per_model, seed=MODEL_SEED + 4, options=opt)
+    gen_s = time.perf_counter() - t
+    n_train = args.fields * per_model
+    train_idx = np.arange(n_train)
+    test_idx = np.arange(n_train, n_train + test_models * per_model)
+    net = ws.WarmNet(grid, batch=batch, seed=MODEL_SEED)
+    p0 = net.get_params()
+    net.set_params(np.zeros_like(p0))
+    base_loss = ws.evaluate_loss(net, data, test_idx)
+    net.set_params(p0)
+    steps = args.learn_steps
+    t = time.perf_counter()
+    losses = ws.train(net, data, steps=steps, lr=1e-3, seed=MODEL_SEED + 5, fields=train_idx)
+    train_s = time.perf_counter() - t
+    test_loss = ws.evaluate_loss(net, data, test_idx)
+    p_trained = net.get_params()
+    prof = net.profile_step(ws.samples_of(data, train_idx[:batch]), 0.0)   # lr 0: parameters unchanged
+    net.set_params(p_trained)
+
+    nodes = nx * ny * nz
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    rows = {"cold": [], "network": [], "T0": []}
+    dev_cold = torch.empty((per_model, nz, ny, nx), dtype=torch.float32, device=f"cuda:{dev}")
+    dev_warm = torch.empty_like(dev_cold)
+    init = torch.empty_like(dev_cold)
+    max_fp64 = 0.0
+    launches = 0
+    with ClockSampler(dev) as clk:
+        for k in range(test_models):
+            idx = test_idx[k * per_model:(k + 1) * per_model]
+            m = int(data["model"][idx[0]])
+            ctx.set_grid3d(nx, ny, nz, h, h, h)
+            ctx.set_nodal_velocity3d(data["velocity"][m])
+            src = data["sources"][idx]
+            for _ in range(args.warmup):
+                ctx.solve3d(src, opt, ex.F32, out=dev_cold)
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            ctx.solve3d(src, opt, ex.F32, out=dev_cold)
+            st = ctx.stats()
+            launches += st["kernel_launches"]
+            rows["cold"].append({"ms": st["device_ms"], "iterations": st["iterations_max"]})
+            cold = dev_cold.cpu().numpy().astype(np.float64)
+            if not args.skip_accuracy:
+                t64 = ctx.solve3d(src, ex.Options(n_sweeps=20, tolerance=1e-9, factored_radius=RADIUS), ex.F64)
+                max_fp64 = max(max_fp64, float(np.max(np.abs(cold - t64))))
+            for name, params in (("network", p_trained), ("T0", np.zeros_like(p_trained))):
+                net.set_params(params)
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                net.predict(ws.samples_of(data, idx, with_target=False), inflate=1.02, out=init)
+                pred_ms = (time.perf_counter() - t) * 1e3
+                ctx.solve3d_warm(src, init, opt, ex.F32, gate_tol=1e-6, out=dev_warm)
+                st = ctx.stats()
+                launches += st["kernel_launches"] + PREDICT_LAUNCHES
+                d = dev_warm.cpu().numpy().astype(np.float64) - cold
+                rows[name].append({"ms": st["device_ms"] + pred_ms, "predict_ms": pred_ms,
+                                   "iterations": st["iterations_max"], "reset_nodes": st["reset_nodes"],
+                                   "max_dev_s": float(np.max(np.abs(d))), "rms_dev_s": float(np.sqrt(np.mean(d * d)))})
+    net.set_params(p_trained)
+    fields = test_models * per_model
+
+    def rate(r):
+        return fields / (sum(x["ms"] for x in r) / 1e3)
+
+    def summary(r):
+        out = {"grids_per_s": rate(r), "ms_per_field": sum(x["ms"] for x in r) / fields,
+               "iterations_max": max(x["iterations"] for x in r)}
+        if "max_dev_s" in r[0]:
+            out.update({"max_dev_from_cold_s": max(x["max_dev_s"] for x in r),
+                        "rms_dev_from_cold_s": float(np.sqrt(np.mean([x["rms_dev_s"] ** 2 for x in r]))),
+                        "predict_ms_per_field": sum(x["predict_ms"] for x in r) / fields,
+                        "reset_nodes": int(sum(x["reset_nodes"] for x in r))})
+        return out
+
+    conv_ms = sum(prof["ms"][k] for k in ("forward_conv", "input_grad_conv", "weight_grad"))
+    conv_fl = sum(prof["flops"].values())
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            tpeak, tkind = float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        tpeak, tkind = 1900.0, "fallback"
+    achieved = conv_fl / (conv_ms / 1e3) / 1e12
+    cold_rate = rate(rows["cold"])
+    line = {
+        "metric": METRIC, "value": cold_rate, "unit": "grids/s", "n_gpus": 1, "steps": 1,
+        "warmup": args.warmup, "ms_per_step": 1e3 * fields / cold_rate, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 sweeps, bf16 network",
+        "data": "synthetic (seeded random smooth models, seeded sources; fields solved by the library)",
+        "config": {"workload": f"learned warm start, {nx}x{ny}x{nz} h={h:g} m: {args.fields} training models x "
+                               f"{per_model} sources, {test_models} held-out models x {per_model} sources",
+                   "training_fields": int(n_train), "train_steps": steps, "batch": batch,
+                   "precision": "fp32 sweeps, fp64 init; network bf16 with fp32 accumulation",
+                   "factored_radius": RADIUS, "tolerance_s": TOL, "inflate": 1.02, "gate_tol_s": 1e-6,
+                   "l2": "flushed (write of 2x L2) before each timed solve"},
+        "learned": {"network": summary(rows["network"]), "T0_start": summary(rows["T0"]),
+                    "cold": summary(rows["cold"]), "speedup_vs_cold": rate(rows["network"]) / cold_rate,
+                    "meets_1e-4_s_vs_cold": max(x["max_dev_s"] for x in rows["network"]) <= 1e-4,
+                    "test_loss": test_loss, "tau_1_loss": base_loss,
+                    "train_loss_first_last": [float(np.mean(losses[:20])), float(np.mean(losses[-20:]))],
+                    "generate_s": gen_s, "train_s": train_s, "train_steps_per_s": steps / train_s,
+                    "step_profile": prof},
+        "roofline": {"bound": "tensor", "kernel": "convKernel + wgradKernel (BF16 mma.sync, FP32 accumulate)",
+                     "achieved": achieved, "peak": tpeak, "peak_kind": tkind, "unit": "TFLOP/s",
+                     "frac": achieved / tpeak, "traffic": None,
+                     "note": "one training step of batch 8; algorithmic FLOPs 2 x nodes x 27 x in x out per "
+                             "convolution, forward, input-gradient and weight-gradient passes"},
+        "accuracy": {"cold_max_err_vs_fp64_s": max_fp64 if not args.skip_accuracy else None},
+        "gpu_launches": int(launches), "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def profile_case(fields):
     """The workload's grid and model, `fields` sources, one refinement iteration, without
     the CUDA graph: 8 source-limited sweeps then 8 full sweeps (launches 9-16)."""
@@ -673,12 +812,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--workload", default="plain",
-                    choices=["plain", "stations", "models", "full", "2d", "warmstart"],
+                    choices=["plain", "stations", "models", "full", "2d", "warmstart", "learned"],
                     help="plain: 256x256x128 h=50 m, independent sources; stations: 200x200x100 h=100 m, "
                          "sources on the top surface; models: uneven models, one source each; full: "
-                         "512x512x256 h=25 m with a dipping slab, surface sources; 2d: 501x251 FP64")
+                         "512x512x256 h=25 m with a dipping slab, surface sources; 2d: 501x251 FP64; "
+                         "learned: the learned warm start, 128x128x64 h=50 m (training included)")
     ap.add_argument("--fields", type=int, default=None,
                     help="sources (plain: 64, stations: 64, full: 256) or models (models: 32) per step per GPU")
+    ap.add_argument("--learn-steps", type=int, default=1500, help="learned: training steps")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -707,7 +848,8 @@ def main():
         # plain: 64 sources per step, where the sweep kernel's throughput saturates on GB300
         # (32: 252, 64: 292, 128: 292, 256: 313 grids/s); with fewer, a sweep is bound by one
         # field's wavefront critical path rather than by work
-        args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8, "models": 32}.get(args.workload, 64)
+        args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8, "models": 32,
+                       "learned": 256}.get(args.workload, 64)
     PAIR[0] = args.pair_fields
     KERNEL[0] = args.sweep_kernel
     if args.profile_case:
@@ -723,6 +865,8 @@ def main():
         run_2d(args)
     elif args.workload == "warmstart":
         run_warmstart_study(args)
+    elif args.workload == "learned":
+        run_learned(args)
     else:
         run_gpu(args)
 

@@ -71,8 +71,11 @@ __global__ void init3Kernel(T *tt, int nFields, long long fieldStride, int pitch
 // stencils of Solver3DSweep::updateFSM, neighbours clamped to the grid); a node whose
 // initial time lies more than gateTol below the smallest of them is lower than any of
 // its neighbourhoods supports -- sweeps only lower times, so it could never recover --
-// and is reset to HUGE.  The source cell's corners take the analytic initialisation.
-// Only values of the initial field are read, so the pass is order-independent.
+// and is reset to HUGE.  A corner of the source cell keeps the smaller of its initial
+// value and the analytic initialisation (the cold start begins at the analytic value and
+// its sweeps may lower it, so a converged field starts where it ended); one the gate
+// rejects takes the analytic value.  Only values of the initial field are read, so the
+// pass is order-independent.
 template <class T, bool UNIFORM>
 __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny,
                                 int nz, double dx, double dy, double dz, const Corner3 *corners,
@@ -91,15 +94,10 @@ __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fie
         const int iz = static_cast<int>(r / (static_cast<long long>(nx) * ny));
         const Corner3 cn = corners[f];
         const T *fi = init + static_cast<long long>(f) * perField;
-        T v;
-        if (ix - cn.isx >= 0 && ix - cn.isx <= 1 && iy - cn.isy >= 0 && iy - cn.isy <= 1 && iz - cn.isz >= 0 &&
-            iz - cn.isz <= 1) {
-            v = fp64 ? static_cast<T>(analyticT3<double>(ix, iy, iz, dx, dy, dz, cn.xo, cn.yo, cn.zo, cn.s))
-                     : analyticT3<T>(ix, iy, iz, static_cast<T>(dx), static_cast<T>(dy), static_cast<T>(dz),
-                                     static_cast<T>(cn.xo), static_cast<T>(cn.yo), static_cast<T>(cn.zo),
-                                     static_cast<T>(cn.s));
-        } else {
-            v = fi[r];
+        const bool corner = ix - cn.isx >= 0 && ix - cn.isx <= 1 && iy - cn.isy >= 0 && iy - cn.isy <= 1 &&
+                            iz - cn.isz >= 0 && iz - cn.isz <= 1;
+        T v = fi[r];
+        {
             const SourceT<T> src = srcs[f];
             T uMin = static_cast<T>(1.e10);
             for (int e = 0; e < 8; ++e) {
@@ -130,10 +128,17 @@ __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fie
                                     : fd3NonUniform<T>(radius, g, src, sg, ix, iy, iz, st);
                 uMin = u < uMin ? u : uMin;
             }
-            if (static_cast<double>(v) < static_cast<double>(uMin) - gateTol) {
+            const bool under = static_cast<double>(v) < static_cast<double>(uMin) - gateTol;
+            if (corner) {
+                const T an = fp64 ? static_cast<T>(analyticT3<double>(ix, iy, iz, dx, dy, dz, cn.xo, cn.yo, cn.zo, cn.s))
+                                  : analyticT3<T>(ix, iy, iz, static_cast<T>(dx), static_cast<T>(dy),
+                                                  static_cast<T>(dz), static_cast<T>(cn.xo), static_cast<T>(cn.yo),
+                                                  static_cast<T>(cn.zo), static_cast<T>(cn.s));
+                v = under || !(v < an) ? an : v;
+            } else if (under) {
                 v = static_cast<T>(1.e10);
-                ++resets;
             }
+            if (under) ++resets;
         }
         tt[static_cast<long long>(f) * fieldStride + (static_cast<long long>(iz) * ny + iy) * pitch + ix] = v;
     }

@@ -156,13 +156,16 @@ eikx_status eikx_solve3d(eikx_ctx *ctx, const eikx_source3d *src, int n_src,
  * learned prediction inflated to bound the solution from above.  A node whose initial
  * time lies more than gate_tol seconds below the smallest upwind update its initial
  * neighbourhood gives, over all 8 sweep orderings, is reset to HUGE (sweeps only lower
- * times, so it could not recover); the source cells' corners take the analytic
- * initialisation; then refinement iterations run to the tolerance without the
- * initialisation pass.  eikx_stats.reset_nodes counts the resets.  Note: the reference's
- * local solver is not monotone in its neighbours (causality windows of the 2D and 3D
- * operators, the factored branch), so sweeps started from a different field can settle
- * on a different fixed point than the cold start, by up to several milliseconds on
- * layered models even when started from the cold-start result itself. */
+ * times, so it could not recover); a corner of a source cell keeps the smaller of its
+ * initial value and the analytic initialisation (the cold start's sweeps may lower it
+ * below the analytic value, so a converged field is a fixed point of the warm start), or
+ * takes the analytic value when the gate rejects it; then refinement iterations run to
+ * the tolerance without the initialisation pass.  eikx_stats.reset_nodes counts the
+ * resets.  Note: the reference's local solver is not monotone in its neighbours (the
+ * causality windows of the 2D and 3D operators, the factored branch): raising a
+ * neighbour can lower a node.  Sweeps started from any field other than the cold
+ * start's own result -- even that result inflated by 0.1 % -- can settle on a different
+ * fixed point, by milliseconds on layered models. */
 eikx_status eikx_solve3d_warm(eikx_ctx *ctx, const eikx_source3d *src, int n_src, const eikx_options *opt,
                               int precision, const void *t_init, int init_where, double gate_tol, void *t_out,
                               int where);

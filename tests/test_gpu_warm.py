@@ -49,3 +49,23 @@ def test_underestimated_nodes_are_reset_and_recomputed(ctx):
     assert abs(warm[0, 15, 20, 25] - cold[0, 15, 20, 25]) < 1e-5
     assert abs(warm[0, 5, 6, 7] - cold[0, 5, 6, 7]) < 1e-5
     assert np.isfinite(warm).all() and (warm < 1e9).all()
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_a_converged_field_is_a_fixed_point_of_the_warm_start(ctx, seed):
+    """The cold start's sweeps can lower source-cell corners below their analytic start
+    value; a warm start from the converged field keeps them, so it ends where it began."""
+    rng = np.random.default_rng(seed)
+    shape = (33, 29, 25, 50., 50., 50.)
+    s, src, cell = _setup(ctx, rng, shape)
+    opt = ex.Options(n_sweeps=20, tolerance=1e-5, factored_radius=3)
+    cold = ctx.solve3d([src], opt, ex.F32)
+    start = ctx.solve3d([src], ex.Options(n_sweeps=0, tolerance=-1, factored_radius=3, init_sweeps=False), ex.F32)
+    lowered = sum(cold[0, cell[2] + (k >> 2), cell[1] + ((k >> 1) & 1), cell[0] + (k & 1)] <
+                  start[0, cell[2] + (k >> 2), cell[1] + ((k >> 1) & 1), cell[0] + (k & 1)] for k in range(8))
+    assert lowered >= 1          # the case this test is about
+    warm = ctx.solve3d_warm([src], cold, opt, ex.F32, gate_tol=1e9)
+    st = ctx.stats()
+    assert st["reset_nodes"] == 0
+    assert st["iterations_max"] <= 2
+    assert np.max(np.abs(warm.astype(np.float64) - cold)) < 1e-4
