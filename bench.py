@@ -684,6 +684,28 @@ def run_learned(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_learned_case(batch=4):
+    """One training step of the learned warm start's network on 128x128x64 nodes (for ncu
+    captures): synthetic samples, no solver; about 3 GB on the device at batch 4."""
+    import torch
+    from eikonalxx_gb300 import warmstart as ws
+
+    nx, ny, nz, h = LEARN_GRID
+    net = ws.WarmNet((nx, ny, nz, h, h, h), batch=batch, seed=MODEL_SEED)
+    rng = np.random.default_rng(MODEL_SEED)
+    z, y, x = np.meshgrid(np.arange(nz) * h, np.arange(ny) * h, np.arange(nx) * h, indexing="ij")
+    samples = []
+    for _ in range(batch):
+        v = rng.uniform(2000, 6000)
+        src = rng.uniform(0, 1, 3) * np.array([(nx - 1) * h, (ny - 1) * h, (nz - 1) * h])
+        d = np.sqrt((x - src[0]) ** 2 + (y - src[1]) ** 2 + (z - src[2]) ** 2)
+        vel = torch.full((nx * ny * nz,), v, dtype=torch.float32, device="cuda")
+        tt = torch.from_numpy((d / v * (1 + 0.05 * np.sin(x / 700.0))).astype(np.float32).ravel()).cuda()
+        samples.append((vel, tt, tuple(src)))
+    net.train_step(samples, 1e-4)
+    torch.cuda.synchronize()
+
+
 def profile_case(fields):
     """The workload's grid and model, `fields` sources, one refinement iteration, without
     the CUDA graph: 8 source-limited sweeps then 8 full sweeps (launches 9-16)."""
@@ -853,7 +875,10 @@ def main():
     PAIR[0] = args.pair_fields
     KERNEL[0] = args.sweep_kernel
     if args.profile_case:
-        profile_case(args.fields)
+        if args.workload == "learned":
+            profile_learned_case()
+        else:
+            profile_case(args.fields)
         return
     if args.warmup < 3:
         args.warmup = 3
