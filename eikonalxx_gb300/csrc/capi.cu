@@ -101,9 +101,18 @@ cudaError_t checkAfterSweep(const eikx::SolveState &st, int nFields, int nSweepK
                                         j >= nSweepKinds - 1 ? tol : -1.0, s);
 }
 
+// The host's copy of a workspace's sweep-tag base.  The device's reset kernel advances the
+// base by the previous solve's tag count at the start of every solve; the host repeats that
+// step and, before a solve whose 32-bit tags would wrap (and so could meet words an early
+// solve left in the mailbox), clears the mailbox and restarts the base at 1.
+struct EpochMirror {
+    unsigned long long base = 0, last = 0;
+};
+
 struct Workspace {
     DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, pairs, init,
         resetCount;
+    EpochMirror epochMirror;
     PinnedBuf stage;
     std::vector<int> orderKey;   // (tilesY, tilesZ, nFields, dim) of the uploaded order table
 };
@@ -113,6 +122,7 @@ struct Workspace {
 struct BatchWorkspace {
     DevBuf tt, sp, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, units,
         slow64, input, badFlag;
+    EpochMirror epochMirror;
     PinnedBuf stage, srcCells;
     std::vector<double> key;                 // what the cached graph was captured for
     cudaGraphExec_t exec = nullptr;
@@ -201,6 +211,21 @@ struct eikx_ctx {
 };
 
 namespace {
+
+// Before a solve using `stride` tags: the host's mirror of the reset kernel's update of the
+// tag base, clearing the mailbox (and the base) when the tags would pass 2^32.
+eikx_status advanceEpoch(EpochMirror &m, DevBuf &mbox, DevBuf &epoch, int stride, cudaStream_t s) {
+    unsigned long long next = m.base + m.last + 1;
+    if (next + static_cast<unsigned long long>(stride) >= (1ull << 32)) {
+        EIKX_CUDA(cudaMemsetAsync(mbox.p, 0, mbox.bytes, s));
+        EIKX_CUDA(cudaMemsetAsync(epoch.p, 0, 2 * sizeof(unsigned), s));
+        m.base = m.last = 0;
+        next = 1;
+    }
+    m.base = next;
+    m.last = static_cast<unsigned long long>(stride);
+    return EIKX_OK;
+}
 
 void dropGraph(eikx_ctx *c) {
     if (c->graphExec) cudaGraphExecDestroy(c->graphExec);
@@ -623,6 +648,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         return EIKX_OK;
     };
 
+    if (eikx_status r = advanceEpoch(w.epochMirror, w.mbox, w.epoch, st.epochStride, c->stream); r != EIKX_OK)
+        return r;
     EIKX_CUDA(cudaEventRecord(c->ev0, c->stream));
     if (c->useGraphs && !profile) {
         if (!(c->graphExec && c->graphKey == sk)) {
@@ -1043,6 +1070,8 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     }
     for (const void *p : after) key.push_back(static_cast<double>(reinterpret_cast<uintptr_t>(p)));
 
+    if (eikx_status r = advanceEpoch(w.epochMirror, w.mbox, w.epoch, st.epochStride, c->stream); r != EIKX_OK)
+        return r;
     EIKX_CUDA(cudaEventRecord(c->ev0, c->stream));
     if (c->useGraphs && !profile) {
         if (!(w.exec && w.key == key)) {
