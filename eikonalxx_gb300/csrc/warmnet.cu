@@ -65,6 +65,7 @@ struct eikx_warmnet {
     float *tOut = nullptr;
     eikx::net::Sample *dSamples = nullptr, *hSamples = nullptr;
     double *dLoss = nullptr, *hLoss = nullptr;
+    int *dStatus = nullptr, *hStatus = nullptr;   // raised by a bounded wait that ran out
     long long step = 0;
     std::vector<void *> allocs;
     // profiling: an event pair per launch and its category
@@ -91,6 +92,7 @@ void freeAll(eikx_warmnet *n) {
     n->allocs.clear();
     if (n->hSamples) cudaFreeHost(n->hSamples);
     if (n->hLoss) cudaFreeHost(n->hLoss);
+    if (n->hStatus) cudaFreeHost(n->hStatus);
     for (cudaEvent_t e : n->events) cudaEventDestroy(e);
     if (n->stream) cudaStreamDestroy(n->stream);
 }
@@ -162,6 +164,7 @@ cudaError_t conv(eikx_warmnet *n, int L, int B) {
     a.H = n->dim[lv][1];
     a.W = n->dim[lv][2];
     a.B = B;
+    a.status = n->dStatus;
     return timed(n, kFwd, [&] { return eikx::net::launchConv(a, n->stream); });
 }
 
@@ -200,6 +203,7 @@ cudaError_t convBack(eikx_warmnet *n, int L, int B, bf16 *dx, const bf16 *mask) 
     a.H = H;
     a.W = W;
     a.B = B;
+    a.status = n->dStatus;
     return timed(n, kDgrad, [&] { return eikx::net::launchConv(a, n->stream); });
 }
 
@@ -344,7 +348,13 @@ eikx_status stageSamples(eikx_warmnet *n, const eikx_warmnet_sample *s, int coun
 
 eikx_status finishLoss(eikx_warmnet *n, long long nodes, double *loss) {
     NET_CUDA(cudaMemcpyAsync(n->hLoss, n->dLoss, sizeof(double), cudaMemcpyDeviceToHost, n->stream));
+    NET_CUDA(cudaMemcpyAsync(n->hStatus, n->dStatus, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
     NET_CUDA(cudaStreamSynchronize(n->stream));
+    if (*n->hStatus) {
+        NET_CUDA(cudaMemsetAsync(n->dStatus, 0, sizeof(int), n->stream));
+        NET_CUDA(cudaStreamSynchronize(n->stream));
+        return err(EIKX_ERR_TIMEOUT, "a bounded wait of a tensor-core convolution ran out; the results are not valid");
+    }
     if (loss) *loss = nodes > 0 ? *n->hLoss / static_cast<double>(nodes) : 0.0;
     return EIKX_OK;
 }
@@ -438,7 +448,7 @@ eikx_status eikx_warmnet_create(int device, const eikx_warmnet_config *cfg, eikx
               alloc(n, &n->Pb, n->nParams) == cudaSuccess && alloc(n, &n->Wt, n->nWt) == cudaSuccess &&
               alloc(n, &n->feat, B * n->V[0] * kFeatures) == cudaSuccess &&
               alloc(n, &n->tOut, B * n->V[0]) == cudaSuccess && alloc(n, &n->dSamples, B) == cudaSuccess &&
-              alloc(n, &n->dLoss, 1) == cudaSuccess;
+              alloc(n, &n->dLoss, 1) == cudaSuccess && alloc(n, &n->dStatus, 1) == cudaSuccess;
     for (int L = 0; ok && L < kLayers; ++L) {
         const long long c = B * n->V[kSpec[L][2]] * kSpec[L][1];
         ok = alloc(n, &n->act[L], c) == cudaSuccess && alloc(n, &n->gpre[L], c) == cudaSuccess;
@@ -452,6 +462,8 @@ eikx_status eikx_warmnet_create(int device, const eikx_warmnet_config *cfg, eikx
     if (!ok) return fail(cudaErrorMemoryAllocation, "allocating the network's buffers");
     if ((e = cudaMallocHost(&n->hSamples, sizeof(eikx::net::Sample) * B)) != cudaSuccess) return fail(e, "cudaMallocHost");
     if ((e = cudaMallocHost(&n->hLoss, sizeof(double))) != cudaSuccess) return fail(e, "cudaMallocHost");
+    if ((e = cudaMallocHost(&n->hStatus, sizeof(int))) != cudaSuccess) return fail(e, "cudaMallocHost");
+    if ((e = cudaMemsetAsync(n->dStatus, 0, sizeof(int), n->stream)) != cudaSuccess) return fail(e, "cudaMemset");
 
     // He-normal convolution weights (fan-in: 27 x the input channels carrying data), zero
     // biases and head: the untrained network predicts tau = 1, i.e. T = T0.

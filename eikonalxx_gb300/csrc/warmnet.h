@@ -46,7 +46,10 @@ struct ConvArgs {
     const bf16 *mask;
     int relu;
     int D, H, W, B;
+    int *status;        // raised (device) when a bounded wait of the tcgen05 path ran out; may be null
 };
+// Grids with 128 nodes along x (and H % 4 == 0, D % 2 == 0) run on the tcgen05 tensor cores
+// with TMEM accumulators; other shapes on mma.sync.
 cudaError_t launchConv(const ConvArgs &a, cudaStream_t s);
 
 // dw[tap][co][ci] += sum_b sum_v dy[b][v][co] * x[b][v + off(tap)][ci]  (FP32 atomics).

@@ -1,7 +1,8 @@
 // Kernels of the learned warm start's 3D U-Net (declared in warmnet.h).
 //
 // The 3x3x3 convolutions are implicit GEMMs on the BF16 tensor cores with FP32
-// accumulation (mma.sync m16n8k16):
+// accumulation.  Levels whose x-rows hold 128 nodes run on tcgen05 (TMA staging, TMEM
+// accumulators; convTcKernel below); the others on mma.sync m16n8k16:
 //   * forward and input-gradient: M = output nodes (one 16-node x-row per MMA row block),
 //     N = output channels, K = 27 taps x input channels.  A block stages a haloed
 //     4 x 10 x 18-node tile of 16 input channels and the 27-tap weight slice of its
@@ -14,6 +15,7 @@
 //     sums to the FP32 gradient with one atomic per element at the end.
 // Shared-memory rows are 48 bytes (an odd number of 16-byte segments), so the eight row
 // addresses of every ldmatrix phase fall in distinct banks.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include "warmnet.h"
@@ -610,6 +612,255 @@ __global__ void flipTransposeKernel(const bf16 *w, int cout, int cin, bf16 *wt) 
     }
 }
 
+// ---- tcgen05 convolution for x-rows of 128 nodes ------------------------------------------
+// A block computes 8 output x-rows (4 along y, 2 along z), each a full row of 128 nodes, for
+// N output channels.  Each row accumulates in its own TMEM region (128 lanes = the row's
+// nodes, N FP32 columns).  Per 16-channel input chunk, one thread stages with TMA
+// (cp.async.bulk.tensor, zero fill outside the grid):
+//   * the 6 x 4 haloed input rows of 130 nodes, one box per 8-channel group: in shared memory
+//     [group][row][node][8 channels], so a node's 8 channels are one 16-byte row of a core
+//     matrix and node r + dx starts 16 * dx bytes later;
+//   * the 27-tap weight slice, one box per group: [group][tap][channel out][8 channels in].
+// Both are the no-swizzle K-major canonical layout (K-direction core matrices one group
+// apart, 8-row core matrices 128 bytes apart).  The same thread then issues 8 rows x 27 taps
+// MMAs (M = 128 nodes, N channels, K = 16): every tap's A operand is the staged row, shifted.
+// mbarriers (bounded waits) signal the TMA bytes' arrival and the MMAs' completion; the
+// epilogue reads TMEM with tcgen05.ld (warp w: lanes 32w..32w+31).
+namespace tc {
+constexpr int kRY = 4, kRZ = 2, kRows = kRY * kRZ;
+constexpr int kHY = kRY + 2, kHZ = kRZ + 2, kHaloRows = kHY * kHZ;
+constexpr int kXN = 130;                          // a 128-node row with its two halo nodes
+constexpr int kRowB = kXN * 16;                   // one staged row of one 8-channel group (bytes)
+constexpr int kGroupB = kHaloRows * kRowB;        // one group of the halo: 49,920
+constexpr int kHaloB = 2 * kGroupB;               // 99,840
+constexpr long long kSpin = 1ll << 24;
+
+__device__ __forceinline__ unsigned long long sdesc(unsigned addr, unsigned lbo, unsigned sbo) {
+    // start address, leading (K-direction core-matrix) and stride (8-row) byte offsets, all
+    // in 16-byte units; bit 46: descriptor version of tcgen05; no swizzle
+    return static_cast<unsigned long long>((addr >> 4) & 0x3FFF) |
+           (static_cast<unsigned long long>((lbo >> 4) & 0x3FFF) << 16) |
+           (static_cast<unsigned long long>((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ void mma(unsigned d, unsigned long long ad, unsigned long long bd, unsigned idesc,
+                                    unsigned accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ bool waitParity(unsigned mbar, unsigned parity) {
+    unsigned done = 0;
+    for (long long it = 0; it < kSpin && !done; ++it)
+        asm volatile(
+            "{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n selp.u32 %0, 1, 0, q;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ void fenceBefore() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fenceAfter() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tma5(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, int c3, int c4,
+                                     unsigned mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(mbar)
+        : "memory");
+}
+__device__ __forceinline__ void tma3(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, unsigned mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(mbar)
+        : "memory");
+}
+
+template <int N> __host__ __device__ constexpr int colStride() { return N <= 32 ? 32 : 64; }
+template <int N> __host__ __device__ constexpr int weightGroupB() { return 27 * N * 16; }
+template <int N> __host__ __device__ constexpr int smemBytes() { return kHaloB + 2 * weightGroupB<N>() + 32; }
+
+template <int N>
+__global__ void __launch_bounds__(128) convTcKernel(ConvArgs a, const __grid_constant__ CUtensorMap mapX,
+                                                    const __grid_constant__ CUtensorMap mapW) {
+    constexpr int CS = colStride<N>(), NCOL = kRows * CS, WG = weightGroupB<N>();
+    static_assert(N % 16 == 0 && N <= 64 && (NCOL & (NCOL - 1)) == 0 && NCOL <= 512, "TMEM layout");
+    extern __shared__ __align__(1024) unsigned char smemRaw[];
+    unsigned char *halo = smemRaw;                 // [2 groups][24 rows][130 nodes][16 B]
+    unsigned char *wsm = smemRaw + kHaloB;         // [2 groups][27 taps][N][16 B]
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(wsm + 2 * WG);
+    unsigned long long *mmaDone = full + 1;
+    unsigned *tslot = reinterpret_cast<unsigned *>(full + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tilesY = a.H / kRY;
+    const int z0 = (blockIdx.x / tilesY) * kRZ, y0 = (blockIdx.x % tilesY) * kRY;
+    const int b = blockIdx.z, co0 = blockIdx.y * N;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smemAddr(tslot)),
+                     "r"(NCOL)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smemAddr(full)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smemAddr(mmaDone)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fenceBefore();
+    __syncthreads();
+    fenceAfter();
+    const unsigned tmem = *tslot;
+    // kind::f16: D FP32 (bit 4), A and B BF16 (bits 7, 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+    const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<unsigned>(N >> 3) << 17) | ((128u >> 4) << 24);
+    const unsigned hb = smemAddr(halo), wb = smemAddr(wsm);
+    bool ok = true;
+    int chunk = 0;
+    for (int ci0 = 0; ci0 < a.cin; ci0 += 16, ++chunk) {
+        if (tid == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(full)),
+                         "r"(static_cast<unsigned>(kHaloB + 2 * WG))
+                         : "memory");
+            for (int g = 0; g < 2; ++g) {
+                tma5(hb + g * kGroupB, &mapX, ci0 + 8 * g, -1, y0 - 1, z0 - 1, b, smemAddr(full));
+                tma3(wb + g * WG, &mapW, ci0 + 8 * g, co0, 0, smemAddr(full));
+            }
+        }
+        const bool landed = waitParity(smemAddr(full), static_cast<unsigned>(chunk & 1));
+        if (!__syncthreads_and(landed)) {
+            ok = false;
+            break;
+        }
+        if (tid == 0) {
+            for (int rr = 0; rr < kRows; ++rr) {
+                const int oz = rr / kRY, oy = rr % kRY;
+                for (int tap = 0; tap < 27; ++tap) {
+                    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                    const int hr = (oz + dz) * kHY + oy + dy;
+                    mma(tmem + static_cast<unsigned>(rr * CS),
+                        sdesc(hb + static_cast<unsigned>(hr * kRowB + dx * 16), kGroupB, 128),
+                        sdesc(wb + static_cast<unsigned>(tap * N * 16), WG, 128), idesc,
+                        (ci0 > 0 || tap > 0) ? 1u : 0u);
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smemAddr(mmaDone))
+                         : "memory");
+        }
+        // this chunk's MMAs have read the buffers once the barrier's phase completes
+        const bool done = waitParity(smemAddr(mmaDone), static_cast<unsigned>(chunk & 1));
+        ok = __syncthreads_and(done) != 0;
+        fenceAfter();
+        if (!ok) break;
+    }
+    if (ok) {
+        const int x = warp * 32 + lane;
+        for (int rr = 0; rr < kRows; ++rr) {
+            const int gz = z0 + rr / kRY, gy = y0 + rr % kRY;
+            const long long node = ((static_cast<long long>(b) * a.D + gz) * a.H + gy) * 128 + x;
+#pragma unroll
+            for (int c0 = 0; c0 < N; c0 += 16) {
+                unsigned r[16];
+                const unsigned addr = tmem + ((static_cast<unsigned>(warp) * 32u) << 16) + static_cast<unsigned>(rr * CS + c0);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15])
+                    : "r"(addr)
+                    : "memory");
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    v[j] = __uint_as_float(r[j]);
+                    if (a.bias) v[j] += a.bias[co0 + c0 + j];
+                    if (a.relu) v[j] = fmaxf(v[j], 0.f);
+                }
+                bf16 *dst = a.y + node * a.cout + co0 + c0;
+                if (a.mask) {
+                    float m0[8], m1[8];
+                    load8(m0, a.mask + node * a.cout + co0 + c0);
+                    load8(m1, a.mask + node * a.cout + co0 + c0 + 8);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if (!(m0[j] > 0.f)) v[j] = 0.f;
+                        if (!(m1[j] > 0.f)) v[8 + j] = 0.f;
+                    }
+                }
+                float lo[8], hi[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    lo[j] = v[j];
+                    hi[j] = v[8 + j];
+                }
+                store8(dst, lo);
+                store8(dst + 8, hi);
+            }
+        }
+    } else if (tid == 0 && a.status) {
+        atomicExch(a.status, 1);
+    }
+    fenceBefore();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOL) : "memory");
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiled encodeTiled() {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
+}
+
+template <int N>
+cudaError_t launchTc(const ConvArgs &a, cudaStream_t s) {
+    EncodeTiled enc = encodeTiled();
+    if (!enc) return cudaErrorNotSupported;
+    // activations [B][D][H][128][cin] BF16: box of 8 channels x 130 nodes x 6 rows x 4 planes x 1 sample
+    CUtensorMap mapX, mapW;
+    const cuuint64_t dimX[5] = {static_cast<cuuint64_t>(a.cin), 128, static_cast<cuuint64_t>(a.H),
+                                static_cast<cuuint64_t>(a.D), static_cast<cuuint64_t>(a.B)};
+    const cuuint64_t strideX[4] = {static_cast<cuuint64_t>(a.cin) * 2, 128ull * a.cin * 2,
+                                   static_cast<cuuint64_t>(a.H) * 128 * a.cin * 2,
+                                   static_cast<cuuint64_t>(a.D) * a.H * 128 * a.cin * 2};
+    const cuuint32_t boxX[5] = {8, kXN, kHY, kHZ, 1}, ones[5] = {1, 1, 1, 1, 1};
+    if (enc(&mapX, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(a.x), dimX, strideX, boxX, ones,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    // weights [27][cout][cin] BF16: box of 8 channels in x N channels out x 27 taps
+    const cuuint64_t dimW[3] = {static_cast<cuuint64_t>(a.cin), static_cast<cuuint64_t>(a.cout), 27};
+    const cuuint64_t strideW[2] = {static_cast<cuuint64_t>(a.cin) * 2, static_cast<cuuint64_t>(a.cout) * a.cin * 2};
+    const cuuint32_t boxW[3] = {8, static_cast<cuuint32_t>(N), 27};
+    if (enc(&mapW, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(a.w), dimW, strideW, boxW, ones,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(convTcKernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes<N>());
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    dim3 grid((a.D / kRZ) * (a.H / kRY), a.cout / N, a.B);
+    convTcKernel<N><<<grid, 128, smemBytes<N>(), s>>>(a, mapX, mapW);
+    return cudaGetLastError();
+}
+}  // namespace tc
+
 int gridFor(long long n, int cap = 1 << 20) {
     long long b = (n + kThreads - 1) / kThreads;
     if (b < 1) b = 1;
@@ -634,6 +885,17 @@ cudaError_t convOne(const ConvArgs &a, cudaStream_t s) {
 
 cudaError_t launchConv(const ConvArgs &a, cudaStream_t s) {
     if (a.cin % 16 || a.cout % 16 || a.B < 1) return cudaErrorInvalidValue;
+    if (a.W == 128 && a.H % tc::kRY == 0 && a.D % tc::kRZ == 0) {
+        switch (a.cout) {
+            case 16: return tc::launchTc<16>(a, s);
+            case 32: return tc::launchTc<32>(a, s);
+            case 48: return tc::launchTc<48>(a, s);
+            default:
+                if (a.cout % 64 == 0) return tc::launchTc<64>(a, s);
+                if (a.cout % 32 == 0) return tc::launchTc<32>(a, s);
+                return tc::launchTc<16>(a, s);
+        }
+    }
     return a.cout % 32 == 0 ? convOne<32>(a, s) : convOne<16>(a, s);
 }
 

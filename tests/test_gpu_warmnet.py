@@ -13,17 +13,19 @@ from eikonalxx_gb300 import warmstart as ws        # noqa: E402
 from oracle import warmnet_oracle as wo            # noqa: E402
 
 GRID = (16, 16, 8, 50.0, 50.0, 50.0, 0.0, 0.0, 0.0)
+# x extent 128: the first level's convolutions run on the tcgen05 path
+GRID128 = (128, 8, 8, 50.0, 50.0, 50.0, 0.0, 0.0, 0.0)
 
 
-def _host_samples(seed, n=2):
+def _host_samples(seed, n=2, grid=GRID):
     rng = np.random.default_rng(seed)
-    nx, ny, nz = GRID[:3]
+    nx, ny, nz = grid[:3]
     out = []
     for _ in range(n):
         z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
         vel = (3000 + 800 * np.sin(0.3 * x + rng.uniform(0, 6)) * np.cos(0.2 * y) + 40 * z).astype(np.float32)
         src = (rng.uniform(0, (nx - 1) * 50), rng.uniform(0, (ny - 1) * 50), rng.uniform(0, (nz - 1) * 50))
-        t0 = wo.target(np.zeros(vel.size), vel.ravel(), src, GRID)[2]
+        t0 = wo.target(np.zeros(vel.size), vel.ravel(), src, grid)[2]
         tt = (t0 * (1 + 0.2 * np.sin(0.25 * x + 0.1 * z))).astype(np.float32)
         out.append((vel.ravel(), tt.ravel(), src))
     return out
@@ -48,17 +50,17 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("n", [1, 2])
-def test_gradients_match_the_oracle(n):
-    host = _host_samples(11, n)
+@pytest.mark.parametrize("n,grid", [(1, GRID), (2, GRID), (2, GRID128)])
+def test_gradients_match_the_oracle(n, grid):
+    host = _host_samples(11, n, grid)
     p = _params(5)
-    with ws.WarmNet(GRID, batch=2, seed=0) as net:
+    with ws.WarmNet(grid, batch=2, seed=0) as net:
         assert net.num_params == wo.layout()[2]
         net.set_params(p)
         np.testing.assert_array_equal(net.get_params(), p)
         g, loss = net.gradients(_device(host))
-    oloss, og, _ = wo.loss_and_grads(p, host, GRID, emulate=True)
-    f64 = wo.loss_and_grads(p, host, GRID, emulate=False)[1]
+    oloss, og, _ = wo.loss_and_grads(p, host, grid, emulate=True)
+    f64 = wo.loss_and_grads(p, host, grid, emulate=False)[1]
     assert abs(loss - oloss) <= 1e-3 * oloss
     offs, head, _ = wo.layout()
     rows, bad = [], []
@@ -81,18 +83,19 @@ def test_gradients_match_the_oracle(n):
     assert not np.any(g[:27 * 16 * 16].reshape(27, 16, 16)[:, :, 6:])
 
 
-def test_prediction_matches_the_oracle():
-    host = _host_samples(12, 2)
+@pytest.mark.parametrize("grid", [GRID, GRID128])
+def test_prediction_matches_the_oracle(grid):
+    host = _host_samples(12, 2, grid)
     p = _params(8)
-    with ws.WarmNet(GRID, batch=2, seed=0) as net:
+    with ws.WarmNet(grid, batch=2, seed=0) as net:
         net.set_params(p)
         t, loss = net.predict(_device(host), inflate=1.03)
-        td = torch.empty(2 * 16 * 16 * 8, dtype=torch.float32, device="cuda")
+        td = torch.empty(2 * grid[0] * grid[1] * grid[2], dtype=torch.float32, device="cuda")
         net.predict(_device([(v, None, s) for v, _, s in host]), inflate=1.03, out=td)
-    ot = wo.predict(p, host, GRID, inflate=1.03)
+    ot = wo.predict(p, host, grid, inflate=1.03)
     assert np.max(np.abs(t - ot)) <= 2e-3 * np.max(np.abs(ot))
     np.testing.assert_array_equal(td.cpu().numpy().reshape(t.shape), t)
-    oloss = wo.loss_and_grads(p, host, GRID)[0]
+    oloss = wo.loss_and_grads(p, host, grid)[0]
     assert abs(loss - oloss) <= 1e-2 * oloss
 
 
