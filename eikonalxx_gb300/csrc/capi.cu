@@ -138,10 +138,10 @@ struct BatchWorkspace {
 struct ScheduleKey {
     int dim = 0, precision = -1, nFields = 0, nx = 0, ny = 0, nz = 0, nSweeps = -1, radius = 0,
         initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0, variant = 0, shape = 0,
-        warm = 0;
+        warm = 0, early = 0;
     double tol = 0, h = 0, dx = 0, dy = 0, dz = 0, gate = 0;
     unsigned long long spin = 0;
-    const void *tt = nullptr, *sp = nullptr, *srcs = nullptr, *corners = nullptr;
+    const void *tt = nullptr, *sp = nullptr, *srcs = nullptr, *corners = nullptr, *flags = nullptr;
     bool operator==(const ScheduleKey &o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
 };
 
@@ -166,6 +166,12 @@ struct eikx_ctx {
     int numSMs = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // copying fields to the host as they converge: a second stream, one event per refinement
+    // iteration of the schedule, and the converged flags read back after each iteration
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t copyDone = nullptr;
+    std::vector<cudaEvent_t> iterEv;
+    PinnedBuf iterFlags;
     std::vector<cudaEvent_t> sweepEv;   // per-sweep timing (profile_sweeps)
     // 3D model
     int nx = 0, ny = 0, nz = 0;
@@ -536,6 +542,23 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     int blocks = std::min(c->numSMs * perSM, (nProgress + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock);
     blocks = std::max(blocks, 1);
 
+    // Host output: a field that has converged is not written again, so it is copied out on
+    // a second stream at the end of the iteration in which it converged, while the sweeps
+    // go on for the others; the rest are copied after the schedule.
+    const bool early = where == EIKX_HOST && nSrc > 1 && nSweeps > 1 && o.tolerance > 0 && o.profile_sweeps == 0;
+    int *iterFlags = nullptr;
+    if (early) {
+        while (static_cast<int>(c->iterEv.size()) < nSweeps) {
+            cudaEvent_t e;
+            EIKX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            c->iterEv.push_back(e);
+        }
+        const void *fb = c->iterFlags.p;
+        EIKX_CUDA(c->iterFlags.ensure(static_cast<size_t>(nSweeps) * nSrc * sizeof(int)));
+        if (c->iterFlags.p != fb) dropGraph(c);
+        iterFlags = static_cast<int *>(c->iterFlags.p);
+    }
+
     ScheduleKey sk;
     sk.dim = DIM; sk.precision = P; sk.nFields = nSrc; sk.nx = nx; sk.ny = ny; sk.nz = nz;
     sk.nSweeps = nSweeps; sk.radius = o.factored_radius; sk.initSweeps = o.init_sweeps ? 1 : 0;
@@ -547,6 +570,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     sk.variant = variant;
     sk.shape = shape;
     sk.tt = w.tt.p; sk.sp = spad[0].p; sk.srcs = w.srcs.p; sk.corners = w.corners.p;
+    sk.early = early ? 1 : 0;
+    sk.flags = iterFlags;
 
     int launches = 0;
     int sweepsLaunched = 0;
@@ -644,6 +669,12 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
                 EIKX_CUDA(checkAfterSweep(st, nSrc, nSweepKinds, nSweepKinds * k + e, o.tolerance, c->stream));
                 ++launches;
             }
+            if (early) {
+                EIKX_CUDA(cudaMemcpyAsync(iterFlags + static_cast<size_t>(k) * nSrc, w.converged.p, nSrc * sizeof(int),
+                                          cudaMemcpyDeviceToHost, c->stream));
+                // external: captured into the graph as a real record the host can wait on
+                EIKX_CUDA(cudaEventRecordWithFlags(c->iterEv[k], c->stream, cudaEventRecordExternal));
+            }
         }
         return EIKX_OK;
     };
@@ -675,11 +706,52 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     } else {
         if (eikx_status r = enqueue(); r != EIKX_OK) return r;
     }
-    // one pitched copy for all fields: rows of nx values out of rows of Px
+    // pitched copies: rows of nx values out of rows of Px, one per run of consecutive fields
     const cudaMemcpyKind kind = where == EIKX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    EIKX_CUDA(cudaMemcpy2DAsync(tOut, static_cast<size_t>(nx) * sizeof(T), w.tt.p, static_cast<size_t>(Px) * sizeof(T),
-                                static_cast<size_t>(nx) * sizeof(T), static_cast<size_t>(ny) * nz * nSrc, kind,
-                                c->stream));
+    const long long nodesPerField = static_cast<long long>(nx) * ny * nz;
+    auto copyFields = [&](int f0, int f1, cudaStream_t s) -> cudaError_t {
+        return cudaMemcpy2DAsync(static_cast<char *>(tOut) + static_cast<size_t>(f0) * nodesPerField * sizeof(T),
+                                 static_cast<size_t>(nx) * sizeof(T),
+                                 static_cast<char *>(w.tt.p) + static_cast<size_t>(f0) * fieldStride * sizeof(T),
+                                 static_cast<size_t>(Px) * sizeof(T), static_cast<size_t>(nx) * sizeof(T),
+                                 static_cast<size_t>(ny) * nz * (f1 - f0), kind, s);
+    };
+    std::vector<char> copied(nSrc, 0);
+    if (early) {
+        int left = nSrc;
+        for (int k = 0; k < nSweeps && left > 0; ++k) {
+            EIKX_CUDA(cudaEventSynchronize(c->iterEv[k]));
+            const int *fl = iterFlags + static_cast<size_t>(k) * nSrc;
+            bool waited = false;
+            for (int f = 0; f < nSrc;) {
+                if (!fl[f] || copied[f]) {
+                    ++f;
+                    continue;
+                }
+                int g = f;
+                while (g < nSrc && fl[g] && !copied[g]) copied[g++] = 1;
+                if (!waited) EIKX_CUDA(cudaStreamWaitEvent(c->copyStream, c->iterEv[k], 0));
+                waited = true;
+                EIKX_CUDA(copyFields(f, g, c->copyStream));
+                left -= g - f;
+                f = g;
+            }
+        }
+    }
+    for (int f = 0; f < nSrc;) {
+        if (copied[f]) {
+            ++f;
+            continue;
+        }
+        int g = f;
+        while (g < nSrc && !copied[g]) ++g;
+        EIKX_CUDA(copyFields(f, g, c->stream));
+        f = g;
+    }
+    if (early) {
+        EIKX_CUDA(cudaEventRecord(c->copyDone, c->copyStream));
+        EIKX_CUDA(cudaStreamWaitEvent(c->stream, c->copyDone, 0));
+    }
     EIKX_CUDA(cudaEventRecord(c->ev1, c->stream));
     std::vector<int> iters(nSrc);
     int aborted = 0;
@@ -1247,6 +1319,8 @@ eikx_status eikx_create(eikx_ctx **ctx, int device) {
     EIKX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     EIKX_CUDA(cudaEventCreate(&c->ev0));
     EIKX_CUDA(cudaEventCreate(&c->ev1));
+    EIKX_CUDA(cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking));
+    EIKX_CUDA(cudaEventCreateWithFlags(&c->copyDone, cudaEventDisableTiming));
     if (const char *g = std::getenv("EIKX_GRAPHS")) c->useGraphs = std::atoi(g) != 0;
     *ctx = c.release();
     return EIKX_OK;
@@ -1259,6 +1333,12 @@ eikx_status eikx_destroy(eikx_ctx *c) {
     dropGraph(c);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->copyStream) {
+        cudaStreamSynchronize(c->copyStream);
+        cudaStreamDestroy(c->copyStream);
+    }
+    if (c->copyDone) cudaEventDestroy(c->copyDone);
+    for (cudaEvent_t e : c->iterEv) cudaEventDestroy(e);
     for (cudaEvent_t e : c->sweepEv) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
