@@ -123,7 +123,7 @@ struct BatchWorkspace {
     DevBuf tt, sp, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, units,
         slow64, input, badFlag;
     EpochMirror epochMirror;
-    PinnedBuf stage, srcCells;
+    PinnedBuf stage, srcCells, iterFlags;
     std::vector<double> key;                 // what the cached graph was captured for
     cudaGraphExec_t exec = nullptr;
     int launches = 0;
@@ -1088,6 +1088,21 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
             c->sweepEv.push_back(e);
         }
     }
+    // models with host output are copied out, on a second stream, at the end of the iteration
+    // in which all their fields have converged (see solveImpl)
+    bool anyHost = false;
+    for (int i = 0; i < nM; ++i) anyHost = anyHost || models[sel[i]].t_where == EIKX_HOST;
+    const bool early = anyHost && nSweeps > 1 && o.tolerance > 0 && o.profile_sweeps == 0;
+    int *iterFlags = nullptr;
+    if (early) {
+        while (static_cast<int>(c->iterEv.size()) < nSweeps) {
+            cudaEvent_t e;
+            EIKX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            c->iterEv.push_back(e);
+        }
+        EIKX_CUDA(w.iterFlags.ensure(static_cast<size_t>(nSweeps) * nUnits * sizeof(int)));
+        iterFlags = static_cast<int *>(w.iterFlags.p);
+    }
     auto enqueue = [&]() -> eikx_status {
         launches = 0;
         sweepsLaunched = 0;
@@ -1124,6 +1139,11 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
                 EIKX_CUDA(checkAfterSweep(st, nUnits, nSweepKinds, nSweepKinds * k + e, o.tolerance, c->stream));
                 ++launches;
             }
+            if (early) {
+                EIKX_CUDA(cudaMemcpyAsync(iterFlags + static_cast<size_t>(k) * nUnits, w.converged.p,
+                                          nUnits * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+                EIKX_CUDA(cudaEventRecordWithFlags(c->iterEv[k], c->stream, cudaEventRecordExternal));
+            }
         }
         return EIKX_OK;
     };
@@ -1141,6 +1161,8 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
             key.push_back(v);
     }
     for (const void *p : after) key.push_back(static_cast<double>(reinterpret_cast<uintptr_t>(p)));
+    key.push_back(early ? 1.0 : 0.0);
+    key.push_back(static_cast<double>(reinterpret_cast<uintptr_t>(iterFlags)));
 
     if (eikx_status r = advanceEpoch(w.epochMirror, w.mbox, w.epoch, st.epochStride, c->stream); r != EIKX_OK)
         return r;
@@ -1169,12 +1191,39 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     } else {
         if (eikx_status r = enqueue(); r != EIKX_OK) return r;
     }
-    for (int i = 0; i < nM; ++i) {
+    auto copyModel = [&](int i, cudaStream_t s) -> cudaError_t {
         const eikx_model3d &m = models[sel[i]];
         const cudaMemcpyKind kind = m.t_where == EIKX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-        EIKX_CUDA(cudaMemcpy2DAsync(m.t_out, static_cast<size_t>(m.nx) * sizeof(T), ttBase + L[i].ttOff,
-                                    static_cast<size_t>(L[i].Px) * sizeof(T), static_cast<size_t>(m.nx) * sizeof(T),
-                                    static_cast<size_t>(m.ny) * m.nz * m.n_src, kind, c->stream));
+        return cudaMemcpy2DAsync(m.t_out, static_cast<size_t>(m.nx) * sizeof(T), ttBase + L[i].ttOff,
+                                 static_cast<size_t>(L[i].Px) * sizeof(T), static_cast<size_t>(m.nx) * sizeof(T),
+                                 static_cast<size_t>(m.ny) * m.nz * m.n_src, kind, s);
+    };
+    std::vector<char> copied(nM, 0);
+    if (early) {
+        int left = 0;
+        for (int i = 0; i < nM; ++i) left += models[sel[i]].t_where == EIKX_HOST;
+        for (int k = 0; k < nSweeps && left > 0; ++k) {
+            EIKX_CUDA(cudaEventSynchronize(c->iterEv[k]));
+            const int *fl = iterFlags + static_cast<size_t>(k) * nUnits;
+            bool waited = false;
+            for (int i = 0; i < nM; ++i) {
+                if (copied[i] || models[sel[i]].t_where != EIKX_HOST) continue;
+                bool all = true;
+                for (int j = 0; j < L[i].nSrc && all; ++j) all = fl[L[i].firstUnit + j] != 0;
+                if (!all) continue;
+                if (!waited) EIKX_CUDA(cudaStreamWaitEvent(c->copyStream, c->iterEv[k], 0));
+                waited = true;
+                EIKX_CUDA(copyModel(i, c->copyStream));
+                copied[i] = 1;
+                --left;
+            }
+        }
+    }
+    for (int i = 0; i < nM; ++i)
+        if (!copied[i]) EIKX_CUDA(copyModel(i, c->stream));
+    if (early) {
+        EIKX_CUDA(cudaEventRecord(c->copyDone, c->copyStream));
+        EIKX_CUDA(cudaStreamWaitEvent(c->stream, c->copyDone, 0));
     }
     EIKX_CUDA(cudaEventRecord(c->ev1, c->stream));
     std::vector<int> iters(nUnits);
