@@ -849,12 +849,9 @@ cudaError_t launchTc(const ConvArgs &a, cudaStream_t s) {
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(convTcKernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes<N>());
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // the shared-memory limit is a per-device attribute: set it for the current device
+    cudaError_t e = cudaFuncSetAttribute(convTcKernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes<N>());
+    if (e != cudaSuccess) return e;
     dim3 grid((a.D / kRZ) * (a.H / kRY), a.cout / N, a.B);
     convTcKernel<N><<<grid, 128, smemBytes<N>(), s>>>(a, mapX, mapW);
     return cudaGetLastError();
@@ -870,12 +867,9 @@ int gridFor(long long n, int cap = 1 << 20) {
 template <int NB>
 cudaError_t convOne(const ConvArgs &a, cudaStream_t s) {
     const int smem = (kHaloNodes + 27 * NB) * kRowHalfs * static_cast<int>(sizeof(bf16));
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(convKernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // the shared-memory limit is a per-device attribute: set it for the current device
+    cudaError_t e = cudaFuncSetAttribute(convKernel<NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
     dim3 grid(tilesPerSample(a.D, a.H, a.W), a.cout / NB, a.B);
     convKernel<NB><<<grid, kThreads, smem, s>>>(a);
     return cudaGetLastError();
@@ -902,12 +896,9 @@ cudaError_t launchConv(const ConvArgs &a, cudaStream_t s) {
 cudaError_t launchWGrad(const WGradArgs &a, int numSMs, cudaStream_t s) {
     if (a.cin % 16 || a.cout % 16 || a.B < 1) return cudaErrorInvalidValue;
     const int smem = (kHaloNodes * kRowHalfs + 256 * (a.cout + 8)) * static_cast<int>(sizeof(bf16));
-    static int attrBytes = 0;
-    if (smem > attrBytes) {
-        cudaError_t e = cudaFuncSetAttribute(wgradKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        attrBytes = smem;
-    }
+    // the shared-memory limit is a per-device attribute: set it for the current device
+    cudaError_t e = cudaFuncSetAttribute(wgradKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
     const int unitsPerBlock = (kThreads / 32) * kUnitsPerWarp;
     const int gy = (27 * (a.cout / 16) + unitsPerBlock - 1) / unitsPerBlock, gz = a.cin / 16;
     const int nTiles = tilesPerSample(a.D, a.H, a.W) * a.B;

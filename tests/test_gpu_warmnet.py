@@ -99,9 +99,10 @@ def test_prediction_matches_the_oracle(grid):
     assert abs(loss - oloss) <= 1e-2 * oloss
 
 
-def test_a_step_moves_against_the_gradient():
-    host = _device(_host_samples(13, 2))
-    with ws.WarmNet(GRID, batch=2, seed=3) as net:
+@pytest.mark.parametrize("grid", [GRID, GRID128])
+def test_a_step_moves_against_the_gradient(grid):
+    host = _device(_host_samples(13, 2, grid))
+    with ws.WarmNet(grid, batch=2, seed=3) as net:
         net.set_params(_params(9))
         l0 = net.train_step(host, 1e-4)
         l1 = net.train_step(host, 1e-4)
