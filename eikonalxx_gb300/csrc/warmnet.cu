@@ -63,6 +63,7 @@ struct eikx_warmnet {
     bf16 *act[kLayers] = {}, *gpre[kLayers] = {};
     bf16 *pool[3] = {}, *cat[3] = {}, *gcat[3] = {}, *gpool[3] = {};
     float *tOut = nullptr;
+    float *slow = nullptr;          // [batch][V] nodal slowness of the current samples
     eikx::net::Sample *dSamples = nullptr, *hSamples = nullptr;
     double *dLoss = nullptr, *hLoss = nullptr;
     int *dStatus = nullptr, *hStatus = nullptr;   // raised by a bounded wait that ran out
@@ -215,7 +216,9 @@ cudaError_t convBack(eikx_warmnet *n, int L, int B, bf16 *dx, const bf16 *mask) 
 
 cudaError_t forward(eikx_warmnet *n, int B) {
     auto lvl = [&](int l, int k) { return n->dim[l][k]; };
-    NET_STEP(timed(n, kOther, [&] { return eikx::net::launchFeatures(n->dSamples, n->g, B, n->feat, n->stream); }));
+    NET_STEP(timed(n, kOther, [&] { return eikx::net::launchSlowness(n->dSamples, n->g, B, n->slow, n->stream); }));
+    NET_STEP(timed(n, kOther,
+                   [&] { return eikx::net::launchFeatures(n->dSamples, n->slow, n->g, B, n->feat, n->stream); }));
     NET_STEP(conv(n, E0a, B));
     NET_STEP(conv(n, E0b, B));
     NET_STEP(timed(n, kOther, [&] {
@@ -258,7 +261,7 @@ cudaError_t backward(eikx_warmnet *n, int B, double invN) {
     auto lvl = [&](int l, int k) { return n->dim[l][k]; };
     NET_STEP(cudaMemsetAsync(n->G, 0, sizeof(float) * n->nParams, n->stream));
     NET_STEP(timed(n, kOther, [&] {
-        return eikx::net::launchHeadLoss(n->act[D0b], n->P + n->headOff, n->dSamples, n->g, B, invN,
+        return eikx::net::launchHeadLoss(n->act[D0b], n->P + n->headOff, n->dSamples, n->slow, n->g, B, invN,
                                          n->G + n->headOff, n->gpre[D0b], n->dLoss, n->stream);
     }));
     NET_STEP(convBack(n, D0b, B, n->gpre[D0a], n->act[D0a]));
@@ -447,7 +450,8 @@ eikx_status eikx_warmnet_create(int device, const eikx_warmnet_config *cfg, eikx
               alloc(n, &n->M, n->nParams) == cudaSuccess && alloc(n, &n->Vm, n->nParams) == cudaSuccess &&
               alloc(n, &n->Pb, n->nParams) == cudaSuccess && alloc(n, &n->Wt, n->nWt) == cudaSuccess &&
               alloc(n, &n->feat, B * n->V[0] * kFeatures) == cudaSuccess &&
-              alloc(n, &n->tOut, B * n->V[0]) == cudaSuccess && alloc(n, &n->dSamples, B) == cudaSuccess &&
+              alloc(n, &n->tOut, B * n->V[0]) == cudaSuccess && alloc(n, &n->slow, B * n->V[0]) == cudaSuccess &&
+              alloc(n, &n->dSamples, B) == cudaSuccess &&
               alloc(n, &n->dLoss, 1) == cudaSuccess && alloc(n, &n->dStatus, 1) == cudaSuccess;
     for (int L = 0; ok && L < kLayers; ++L) {
         const long long c = B * n->V[kSpec[L][2]] * kSpec[L][1];
@@ -561,7 +565,7 @@ eikx_status eikx_warmnet_predict(eikx_warmnet *n, const eikx_warmnet_sample *s, 
     NET_CUDA(cudaMemsetAsync(n->dLoss, 0, sizeof(double), n->stream));
     NET_CUDA(forward(n, count));
     float *dst = where == EIKX_DEVICE ? t_out : n->tOut;
-    NET_CUDA(eikx::net::launchPredict(n->act[D0b], n->P + n->headOff, n->dSamples, n->g, count, inflate, dst,
+    NET_CUDA(eikx::net::launchPredict(n->act[D0b], n->P + n->headOff, n->dSamples, n->slow, n->g, count, inflate, dst,
                                       haveTargets && loss ? n->dLoss : nullptr, n->stream));
     if (where == EIKX_HOST)
         NET_CUDA(cudaMemcpyAsync(t_out, n->tOut, sizeof(float) * count * n->V[0], cudaMemcpyDeviceToHost, n->stream));

@@ -85,20 +85,25 @@ cudaError_t launchUpSumMask(const bf16 *dcat, int ccat, const bf16 *act, int c1,
 cudaError_t launchCombineSkip(const bf16 *dcat, int ccat, int c1, const bf16 *dpool, const bf16 *skip, int c2,
                               int D, int H, int W, int B, bf16 *dpre, cudaStream_t s);
 
-// Input features [B][V][16] of the samples.
-cudaError_t launchFeatures(const Sample *samples, Geometry g, int B, bf16 *feat, cudaStream_t s);
+// Nodal slowness 1/v (FP32) of each sample: slow[b][v].  The per-node kernels below read it
+// (and s_src = slow at the node nearest the source) instead of dividing again.
+cudaError_t launchSlowness(const Sample *samples, Geometry g, int B, float *slow, cudaStream_t s);
 
-// Head (1x1x1 convolution of 16 channels) and loss: out = hb + hw . h; target tau - 1
-// from the sample's travel times; accumulates the loss sum (double), the head's
+// Input features [B][V][16] of the samples.
+cudaError_t launchFeatures(const Sample *samples, const float *slow, Geometry g, int B, bf16 *feat, cudaStream_t s);
+
+// Head (1x1x1 convolution of 16 channels) and loss: out = hb + hw . h; target
+// tau - 1 = T / T0 - 1 from the sample's travel times, T0 = s_src |x - x_s| (FP32: the
+// offsets from the source are FP64 differences rounded to FP32); accumulates the loss sum (double), the head's
 // gradients (dhw: 16 weights then the bias) and writes dpre = dout * hw gated by h > 0.
 // invN: 1 / the number of nodes with T0 > 0 over the samples.
-cudaError_t launchHeadLoss(const bf16 *h, const float *hw, const Sample *samples, Geometry g, int B, double invN,
-                           float *dhw, bf16 *dpre, double *lossSum, cudaStream_t s);
+cudaError_t launchHeadLoss(const bf16 *h, const float *hw, const Sample *samples, const float *slow, Geometry g,
+                           int B, double invN, float *dhw, bf16 *dpre, double *lossSum, cudaStream_t s);
 
 // Predicted travel times out[b][v] = T0 (1 + hb + hw . h) * inflate; also the loss sum
 // when the samples carry travel times.
-cudaError_t launchPredict(const bf16 *h, const float *hw, const Sample *samples, Geometry g, int B, double inflate,
-                          float *out, double *lossSum, cudaStream_t s);
+cudaError_t launchPredict(const bf16 *h, const float *hw, const Sample *samples, const float *slow, Geometry g, int B,
+                          double inflate, float *out, double *lossSum, cudaStream_t s);
 
 // Adam on n parameters; writes the BF16 copy pb.
 cudaError_t launchAdam(float *p, const float *g, float *m, float *v, bf16 *pb, long long n, float lr, float b1,

@@ -38,6 +38,7 @@ __device__ __forceinline__ void cpAsyncCommitWaitAll() {
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
+
 __device__ __forceinline__ void ldsm4(unsigned (&r)[4], const void *p) {
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
@@ -174,10 +175,13 @@ __global__ void __launch_bounds__(kThreads) convKernel(ConvArgs a) {
     }
 }
 
-// Weight gradient.  Work unit u = (co block cb = u / 27, tap = u % 27): a 16 (co) x 16
-// (ci) block of dw; a warp holds 4 units, a block 32; grid.y walks the units, grid.z the
-// 16-channel input chunks, grid.x strides over the node tiles of all samples.
+// Weight gradient.  A warp owns one 16-channel block cb of dy and 4 consecutive taps:
+// its 4 accumulators are 16 (co) x 16 (ci) blocks of dw that share the dy^T operand, so
+// each 16-node row loads it once for 4 taps.  Warp w of block y is warp group
+// g = y * 8 + w: cb = g / kTapGroups, taps 4 * (g % kTapGroups) + 0..3 (< 27).  grid.z
+// walks the 16-channel input chunks, grid.x strides over the node tiles of all samples.
 constexpr int kUnitsPerWarp = 4;
+constexpr int kTapGroups = (27 + kUnitsPerWarp - 1) / kUnitsPerWarp;   // 7
 __global__ void __launch_bounds__(kThreads) wgradKernel(WGradArgs a) {
     extern __shared__ __align__(16) unsigned char smemRaw[];
     bf16 *xs = reinterpret_cast<bf16 *>(smemRaw);
@@ -185,7 +189,9 @@ __global__ void __launch_bounds__(kThreads) wgradKernel(WGradArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int li = lane >> 3, lj = lane & 7;
     const int ci0 = blockIdx.z * 16;
-    const int nUnits = 27 * (a.cout / 16);
+    const int group = blockIdx.y * (kThreads / 32) + warp;
+    const int cb = group / kTapGroups, tap0 = kUnitsPerWarp * (group % kTapGroups);
+    const bool warpActive = cb < a.cout / 16;
     const int dyRow = a.cout + 8;   // halfs; an odd number of 16-byte segments
     const long long V = static_cast<long long>(a.D) * a.H * a.W;
     const int tps = tilesPerSample(a.D, a.H, a.W);
@@ -215,32 +221,34 @@ __global__ void __launch_bounds__(kThreads) wgradKernel(WGradArgs a) {
         }
         cpAsyncCommitWaitAll();
         __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kUnitsPerWarp; ++k) {
-            const int u = (blockIdx.y * (kThreads / 32) + warp) * kUnitsPerWarp + k;
-            if (u >= nUnits) continue;
-            const int tap = u % 27, cb = u / 27;
-            const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+        if (warpActive) {
 #pragma unroll 2
             for (int r = 0; r < 16; ++r) {
                 const int tz = r >> 3, ty = r & 7;
-                unsigned afr[4], bfr[4];
                 // A = dy^T: matrix li = (co 16cb + 8*(li&1) .., nodes 16r + 8*(li>>1) ..)
+                unsigned afr[4];
                 ldsm4t(afr, dys + (16 * r + lj + 8 * (li >> 1)) * dyRow + 16 * cb + 8 * (li & 1));
-                // B = shifted input: matrix li = (nodes 8*(li&1) .., channels 8*(li>>1) ..)
-                ldsm4t(bfr, xs + (((tz + dz) * kHaloY + ty + dy) * kHaloX + lj + 8 * (li & 1) + dx) * kRowHalfs +
-                                8 * (li >> 1));
-                mma16816(acc[k][0], afr, bfr[0], bfr[1]);
-                mma16816(acc[k][1], afr, bfr[2], bfr[3]);
+#pragma unroll
+                for (int kk = 0; kk < kUnitsPerWarp; ++kk) {
+                    const int tap = tap0 + kk;
+                    if (tap >= 27) continue;
+                    const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+                    // B = shifted input: matrix li = (nodes 8*(li&1) .., channels 8*(li>>1) ..)
+                    unsigned bfr[4];
+                    ldsm4t(bfr, xs + (((tz + dz) * kHaloY + ty + dy) * kHaloX + lj + 8 * (li & 1) + dx) * kRowHalfs +
+                                    8 * (li >> 1));
+                    mma16816(acc[kk][0], afr, bfr[0], bfr[1]);
+                    mma16816(acc[kk][1], afr, bfr[2], bfr[3]);
+                }
             }
         }
         __syncthreads();
     }
+    if (!warpActive) return;
 #pragma unroll
-    for (int k = 0; k < kUnitsPerWarp; ++k) {
-        const int u = (blockIdx.y * (kThreads / 32) + warp) * kUnitsPerWarp + k;
-        if (u >= nUnits) continue;
-        const int tap = u % 27, cb = u / 27;
+    for (int kk = 0; kk < kUnitsPerWarp; ++kk) {
+        const int tap = tap0 + kk;
+        if (tap >= 27) continue;
 #pragma unroll
         for (int nt = 0; nt < 2; ++nt) {
             const int ci = ci0 + 8 * nt + 2 * (lane & 3);
@@ -248,8 +256,8 @@ __global__ void __launch_bounds__(kThreads) wgradKernel(WGradArgs a) {
             for (int h = 0; h < 2; ++h) {
                 const int co = 16 * cb + (lane >> 2) + 8 * h;
                 float *d = a.dw + (static_cast<long long>(tap) * a.cout + co) * a.cin + ci;
-                atomicAdd(d, acc[k][nt][2 * h]);
-                atomicAdd(d + 1, acc[k][nt][2 * h + 1]);
+                atomicAdd(d, acc[kk][nt][2 * h]);
+                atomicAdd(d + 1, acc[kk][nt][2 * h + 1]);
             }
         }
     }
@@ -381,37 +389,42 @@ __global__ void combineSkipKernel(const bf16 *dcat, int ccat, int c1, const bf16
     }
 }
 
-// Source quantities shared by the per-node kernels.
-struct SourceInfo {
-    double sSrc;   // slowness at the node nearest the source
-};
-__device__ __forceinline__ double sourceSlowness(const Sample &s, const Geometry &g) {
+// Per-node geometry, FP32: the offsets from the source are FP64 differences rounded to
+// FP32, the distance an FP32 square root; s_src is the slowness at the node nearest the
+// source.
+__device__ __forceinline__ long long nearestNode(const Sample &s, const Geometry &g) {
     const int ix = min(g.nx - 1, max(0, __double2int_rn((s.xs - g.x0) / g.dx)));
     const int iy = min(g.ny - 1, max(0, __double2int_rn((s.ys - g.y0) / g.dy)));
     const int iz = min(g.nz - 1, max(0, __double2int_rn((s.zs - g.z0) / g.dz)));
-    return 1.0 / static_cast<double>(s.velocity[(static_cast<long long>(iz) * g.ny + iy) * g.nx + ix]);
+    return (static_cast<long long>(iz) * g.ny + iy) * g.nx + ix;
 }
 struct NodeGeom {
-    double ddx, ddy, ddz, dist;
+    float ddx, ddy, ddz, dist;
 };
 __device__ __forceinline__ NodeGeom nodeGeom(long long v, const Sample &s, const Geometry &g) {
     const int x = v % g.nx, y = (v / g.nx) % g.ny, z = v / (static_cast<long long>(g.nx) * g.ny);
     NodeGeom n;
-    n.ddx = (g.x0 + x * g.dx) - s.xs;
-    n.ddy = (g.y0 + y * g.dy) - s.ys;
-    n.ddz = (g.z0 + z * g.dz) - s.zs;
-    n.dist = sqrt(n.ddx * n.ddx + n.ddy * n.ddy + n.ddz * n.ddz);
+    n.ddx = static_cast<float>((g.x0 + x * g.dx) - s.xs);
+    n.ddy = static_cast<float>((g.y0 + y * g.dy) - s.ys);
+    n.ddz = static_cast<float>((g.z0 + z * g.dz) - s.zs);
+    n.dist = sqrtf(n.ddx * n.ddx + n.ddy * n.ddy + n.ddz * n.ddz);
     return n;
+}
+
+__global__ void slownessKernel(const Sample *samples, Geometry g, int B, float *slow) {
+    const long long V = static_cast<long long>(g.nx) * g.ny * g.nz;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < B * V;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        slow[i] = 1.f / samples[i / V].velocity[i % V];
 }
 
 // Straight-ray estimate of tau - 1 at node (x, y, z): the mean of s/s_src - 1 over
 // kRaySamples midpoints of the segment from the source to the node, the slowness
 // trilinear in the nodal 1/v.  FP32, in an operation order the oracle repeats.
 constexpr int kRaySamples = 32;
-__device__ __forceinline__ float nodalSlowness(const float *vel, const Geometry &g, int x, int y, int z) {
-    return 1.f / vel[(static_cast<long long>(z) * g.ny + y) * g.nx + x];
-}
-__device__ float straightRayContrast(const Sample &s, const Geometry &g, float sSrc, int x, int y, int z) {
+__device__ float straightRayContrast(const Sample &s, const float *sl, const Geometry &g, float sSrc, int x, int y,
+                                     int z) {
+    auto at = [&](int ix, int iy, int iz) { return sl[(static_cast<long long>(iz) * g.ny + iy) * g.nx + ix]; };
     const float sx = static_cast<float>((s.xs - g.x0) / g.dx), sy = static_cast<float>((s.ys - g.y0) / g.dy),
                 sz = static_cast<float>((s.zs - g.z0) / g.dz);
     const float ex = static_cast<float>(x) - sx, ey = static_cast<float>(y) - sy, ez = static_cast<float>(z) - sz;
@@ -424,13 +437,10 @@ __device__ float straightRayContrast(const Sample &s, const Geometry &g, float s
         const int ix = min(static_cast<int>(floorf(px)), g.nx - 2), iy = min(static_cast<int>(floorf(py)), g.ny - 2),
                   iz = min(static_cast<int>(floorf(pz)), g.nz - 2);
         const float fx = px - static_cast<float>(ix), fy = py - static_cast<float>(iy), fz = pz - static_cast<float>(iz);
-        const float s000 = nodalSlowness(s.velocity, g, ix, iy, iz), s100 = nodalSlowness(s.velocity, g, ix + 1, iy, iz);
-        const float s010 = nodalSlowness(s.velocity, g, ix, iy + 1, iz),
-                    s110 = nodalSlowness(s.velocity, g, ix + 1, iy + 1, iz);
-        const float s001 = nodalSlowness(s.velocity, g, ix, iy, iz + 1),
-                    s101 = nodalSlowness(s.velocity, g, ix + 1, iy, iz + 1);
-        const float s011 = nodalSlowness(s.velocity, g, ix, iy + 1, iz + 1),
-                    s111 = nodalSlowness(s.velocity, g, ix + 1, iy + 1, iz + 1);
+        const float s000 = at(ix, iy, iz), s100 = at(ix + 1, iy, iz);
+        const float s010 = at(ix, iy + 1, iz), s110 = at(ix + 1, iy + 1, iz);
+        const float s001 = at(ix, iy, iz + 1), s101 = at(ix + 1, iy, iz + 1);
+        const float s011 = at(ix, iy + 1, iz + 1), s111 = at(ix + 1, iy + 1, iz + 1);
         const float c00 = s000 + fx * (s100 - s000), c10 = s010 + fx * (s110 - s010);
         const float c01 = s001 + fx * (s101 - s001), c11 = s011 + fx * (s111 - s011);
         const float c0 = c00 + fy * (c10 - c00), c1 = c01 + fy * (c11 - c01);
@@ -440,22 +450,23 @@ __device__ float straightRayContrast(const Sample &s, const Geometry &g, float s
     return acc / static_cast<float>(kRaySamples);
 }
 
-__global__ void featuresKernel(const Sample *samples, Geometry g, int B, bf16 *feat) {
+__global__ void featuresKernel(const Sample *samples, const float *slow, Geometry g, int B, bf16 *feat) {
     const long long V = static_cast<long long>(g.nx) * g.ny * g.nz;
     const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (i >= B * V) return;
     const int b = i / V;
     const long long v = i % V;
     const Sample s = samples[b];
-    const double sSrc = sourceSlowness(s, g);
+    const float *sl = slow + b * V;
+    const float sSrc = sl[nearestNode(s, g)];
     const NodeGeom n = nodeGeom(v, s, g);
-    float f[8] = {static_cast<float>(1.0 / static_cast<double>(s.velocity[v]) / sSrc - 1.0),
-                  static_cast<float>(n.dist * g.invL),
-                  static_cast<float>(n.ddx * g.invL),
-                  static_cast<float>(n.ddy * g.invL),
-                  static_cast<float>(n.ddz * g.invL),
-                  straightRayContrast(s, g, static_cast<float>(sSrc), static_cast<int>(v % g.nx),
-                                      static_cast<int>((v / g.nx) % g.ny),
+    const float invL = static_cast<float>(g.invL);
+    float f[8] = {sl[v] / sSrc - 1.f,
+                  n.dist * invL,
+                  n.ddx * invL,
+                  n.ddy * invL,
+                  n.ddz * invL,
+                  straightRayContrast(s, sl, g, sSrc, static_cast<int>(v % g.nx), static_cast<int>((v / g.nx) % g.ny),
                                       static_cast<int>(v / (static_cast<long long>(g.nx) * g.ny))),
                   0.f,
                   0.f};
@@ -482,8 +493,8 @@ __device__ __forceinline__ float headOut(const float (&h)[16], const float *hw) 
 }
 
 __global__ void __launch_bounds__(kThreads) headLossKernel(const bf16 *h, const float *hw, const Sample *samples,
-                                                           Geometry g, int B, double invN, float *dhw, bf16 *dpre,
-                                                           double *lossSum) {
+                                                           const float *slow, Geometry g, int B, double invN,
+                                                           float *dhw, bf16 *dpre, double *lossSum) {
     __shared__ float red[kThreads / 32][17];
     __shared__ double redL[kThreads / 32];
     const long long V = static_cast<long long>(g.nx) * g.ny * g.nz;
@@ -503,9 +514,9 @@ __global__ void __launch_bounds__(kThreads) headLossKernel(const bf16 *h, const 
             hv[8 + k] = c[k];
         }
         const float o = headOut(hv, hw);
-        const double T0 = sourceSlowness(s, g) * nodeGeom(v, s, g).dist;
-        if (T0 > 0) {
-            const float tgt = static_cast<float>(static_cast<double>(s.travelTime[v]) / T0 - 1.0);
+        const float T0 = slow[b * V + nearestNode(s, g)] * nodeGeom(v, s, g).dist;
+        if (T0 > 0.f) {
+            const float tgt = s.travelTime[v] / T0 - 1.f;
             const float diff = o - tgt;
             l = static_cast<double>(diff) * diff;
             dout = static_cast<float>(2.0 * diff * invN);
@@ -544,8 +555,8 @@ __global__ void __launch_bounds__(kThreads) headLossKernel(const bf16 *h, const 
 }
 
 __global__ void __launch_bounds__(kThreads) predictKernel(const bf16 *h, const float *hw, const Sample *samples,
-                                                          Geometry g, int B, double inflate, float *out,
-                                                          double *lossSum) {
+                                                          const float *slow, Geometry g, int B, float inflate,
+                                                          float *out, double *lossSum) {
     __shared__ double redL[kThreads / 32];
     const long long V = static_cast<long long>(g.nx) * g.ny * g.nz;
     const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
@@ -562,10 +573,10 @@ __global__ void __launch_bounds__(kThreads) predictKernel(const bf16 *h, const f
             hv[8 + k] = c[k];
         }
         const float o = headOut(hv, hw);
-        const double T0 = sourceSlowness(s, g) * nodeGeom(v, s, g).dist;
-        out[i] = static_cast<float>(T0 * (1.0 + o) * inflate);
-        if (lossSum && s.travelTime && T0 > 0) {
-            const float diff = o - static_cast<float>(static_cast<double>(s.travelTime[v]) / T0 - 1.0);
+        const float T0 = slow[b * V + nearestNode(s, g)] * nodeGeom(v, s, g).dist;
+        out[i] = T0 * (1.f + o) * inflate;
+        if (lossSum && s.travelTime && T0 > 0.f) {
+            const float diff = o - (s.travelTime[v] / T0 - 1.f);
             l = static_cast<double>(diff) * diff;
         }
     }
@@ -899,8 +910,8 @@ cudaError_t launchWGrad(const WGradArgs &a, int numSMs, cudaStream_t s) {
     // the shared-memory limit is a per-device attribute: set it for the current device
     cudaError_t e = cudaFuncSetAttribute(wgradKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    const int unitsPerBlock = (kThreads / 32) * kUnitsPerWarp;
-    const int gy = (27 * (a.cout / 16) + unitsPerBlock - 1) / unitsPerBlock, gz = a.cin / 16;
+    const int warpsPerBlock = kThreads / 32;
+    const int gy = (kTapGroups * (a.cout / 16) + warpsPerBlock - 1) / warpsPerBlock, gz = a.cin / 16;
     const int nTiles = tilesPerSample(a.D, a.H, a.W) * a.B;
     int gx = (4 * numSMs + gy * gz - 1) / (gy * gz);
     gx = gx < 1 ? 1 : (gx > nTiles ? nTiles : gx);
@@ -945,25 +956,30 @@ cudaError_t launchCombineSkip(const bf16 *dcat, int ccat, int c1, const bf16 *dp
     return cudaGetLastError();
 }
 
-cudaError_t launchFeatures(const Sample *samples, Geometry g, int B, bf16 *feat, cudaStream_t s) {
-    const long long n = static_cast<long long>(B) * g.nx * g.ny * g.nz;
-    featuresKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(samples, g, B, feat);
+cudaError_t launchSlowness(const Sample *samples, Geometry g, int B, float *slow, cudaStream_t s) {
+    slownessKernel<<<gridFor(static_cast<long long>(B) * g.nx * g.ny * g.nz), kThreads, 0, s>>>(samples, g, B, slow);
     return cudaGetLastError();
 }
 
-cudaError_t launchHeadLoss(const bf16 *h, const float *hw, const Sample *samples, Geometry g, int B, double invN,
-                           float *dhw, bf16 *dpre, double *lossSum, cudaStream_t s) {
+cudaError_t launchFeatures(const Sample *samples, const float *slow, Geometry g, int B, bf16 *feat, cudaStream_t s) {
     const long long n = static_cast<long long>(B) * g.nx * g.ny * g.nz;
-    headLossKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(h, hw, samples, g, B, invN,
-                                                                                       dhw, dpre, lossSum);
+    featuresKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(samples, slow, g, B, feat);
     return cudaGetLastError();
 }
 
-cudaError_t launchPredict(const bf16 *h, const float *hw, const Sample *samples, Geometry g, int B, double inflate,
-                          float *out, double *lossSum, cudaStream_t s) {
+cudaError_t launchHeadLoss(const bf16 *h, const float *hw, const Sample *samples, const float *slow, Geometry g,
+                           int B, double invN, float *dhw, bf16 *dpre, double *lossSum, cudaStream_t s) {
     const long long n = static_cast<long long>(B) * g.nx * g.ny * g.nz;
-    predictKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(h, hw, samples, g, B, inflate,
-                                                                                      out, lossSum);
+    headLossKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(h, hw, samples, slow, g, B,
+                                                                                       invN, dhw, dpre, lossSum);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPredict(const bf16 *h, const float *hw, const Sample *samples, const float *slow, Geometry g, int B,
+                          double inflate, float *out, double *lossSum, cudaStream_t s) {
+    const long long n = static_cast<long long>(B) * g.nx * g.ny * g.nz;
+    predictKernel<<<static_cast<int>((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+        h, hw, samples, slow, g, B, static_cast<float>(inflate), out, lossSum);
     return cudaGetLastError();
 }
 

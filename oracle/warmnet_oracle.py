@@ -56,20 +56,22 @@ def unpack(params, emulate):
 
 
 def source_slowness(vel, src, g):
+    """1/v (FP32) at the node nearest the source."""
     nx, ny, nz, dx, dy, dz, x0, y0, z0 = g
     ix = int(min(nx - 1, max(0, np.rint((src[0] - x0) / dx))))
     iy = int(min(ny - 1, max(0, np.rint((src[1] - y0) / dy))))
     iz = int(min(nz - 1, max(0, np.rint((src[2] - z0) / dz))))
-    return 1.0 / float(np.float32(vel.reshape(nz, ny, nx)[iz, iy, ix]))
+    return np.float32(1) / np.float32(vel.reshape(nz, ny, nx)[iz, iy, ix])
 
 
 def geometry_terms(src, g):
-    """Per node (nz, ny, nx): dx, dy, dz offsets from the source and the distance."""
+    """Per node (nz, ny, nx), FP32: the offsets from the source (FP64 differences rounded to
+    FP32) and the distance."""
     nx, ny, nz, dx, dy, dz, x0, y0, z0 = g
     z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
-    ddx = (x0 + x * dx) - src[0]
-    ddy = (y0 + y * dy) - src[1]
-    ddz = (z0 + z * dz) - src[2]
+    ddx = ((x0 + x * dx) - src[0]).astype(np.float32)
+    ddy = ((y0 + y * dy) - src[1]).astype(np.float32)
+    ddz = ((z0 + z * dz) - src[2]).astype(np.float32)
     return ddx, ddy, ddz, np.sqrt(ddx * ddx + ddy * ddy + ddz * ddz)
 
 
@@ -114,23 +116,26 @@ def features(vel, src, g, emulate=True):
     inv_l = 1.0 / np.sqrt(lx * lx + ly * ly + lz * lz)
     s_src = source_slowness(vel, src, g)
     ddx, ddy, ddz, dist = geometry_terms(src, g)
-    v = np.asarray(vel, dtype=np.float32).reshape(nz, ny, nx).astype(np.float64)
+    f32 = np.float32
+    sl = f32(1) / np.asarray(vel, dtype=f32).reshape(nz, ny, nx)
+    il = f32(inv_l)
+    cols = [sl / s_src - f32(1), dist * il, ddx * il, ddy * il, ddz * il,
+            straight_ray_contrast(vel, src, g, s_src)]
     f = np.zeros((nz, ny, nx, 16))
-    cols = [1.0 / v / s_src - 1.0, dist * inv_l, ddx * inv_l, ddy * inv_l, ddz * inv_l]
     for k, c in enumerate(cols):
-        f[..., k] = bf16(c.astype(np.float32)) if emulate else c
-    ray = straight_ray_contrast(vel, src, g, np.float32(s_src)).astype(np.float64)
-    f[..., 5] = bf16(ray) if emulate else ray
+        f[..., k] = bf16(c) if emulate else c.astype(np.float64)
     return f
 
 
 def target(tt, vel, src, g):
-    """(tau - 1, weight): the regression target and 1 where T0 > 0."""
+    """(tau - 1, weight, T0): the regression target, 1 where T0 > 0, and T0, all FP32
+    (returned as float64)."""
     nx, ny, nz = g[:3]
     t0 = source_slowness(vel, src, g) * geometry_terms(src, g)[3]
-    t = np.asarray(tt, dtype=np.float32).reshape(nz, ny, nx).astype(np.float64)
-    w = (t0 > 0).astype(np.float64)
-    return np.where(t0 > 0, t / np.where(t0 > 0, t0, 1.0) - 1.0, 0.0), w, t0
+    t = np.asarray(tt, dtype=np.float32).reshape(nz, ny, nx)
+    pos = t0 > 0
+    tau = np.where(pos, t / np.where(pos, t0, np.float32(1)) - np.float32(1), np.float32(0))
+    return tau.astype(np.float64), pos.astype(np.float64), t0.astype(np.float64)
 
 
 def conv(x, w, b):
