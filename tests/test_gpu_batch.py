@@ -95,3 +95,38 @@ def test_batch_rejects_bad_models(ctx):
         ctx.solve3d_batch([dict(good, model=np.full(64, -1.0, np.float32))])   # non-positive slowness
     out = ctx.solve3d_batch([good])[0]                                       # context still usable
     assert np.isfinite(out).all()
+
+
+def test_fields_copied_out_as_they_converge_equal_the_device_result(ctx):
+    """Host output copies each field (each model, in a batch) at the end of the iteration in
+    which it converged, while the others sweep on; the result must equal the device output."""
+    import torch
+    rng = np.random.default_rng(77)
+    shape = (41, 37, 29, 50.0, 50.0, 50.0)
+    nx, ny, nz = shape[:3]
+    s = random_slowness(rng, (nz - 1) * (ny - 1) * (nx - 1), dtype=np.float32)
+    ctx.set_grid3d(*shape)
+    ctx.set_slowness3d(s)
+    src = np.column_stack([rng.uniform(0, (nx - 1) * 50, 6), rng.uniform(0, (ny - 1) * 50, 6),
+                           rng.uniform(0, (nz - 1) * 50, 6)])
+    opt = ex.Options(n_sweeps=12, tolerance=1e-5)
+    host = ctx.solve3d(src, opt, ex.F32)
+    st = ctx.stats()
+    assert st["iterations_min"] < st["iterations_max"]      # fields converge at different iterations
+    dev = torch.empty((6, nz, ny, nx), dtype=torch.float32, device="cuda")
+    ctx.solve3d(src, opt, ex.F32, out=dev)
+    assert np.array_equal(host.view(np.uint32), dev.cpu().numpy().view(np.uint32))
+    # the same per model in a batch: one model with host output, one with device output
+    models = []
+    for k in range(3):
+        g = (33 + 8 * k, 29, 25, 50.0, 50.0, 50.0)
+        v = (3000 + 2000 * rng.random((g[2], g[1], g[0]))).astype(np.float32)
+        p = [(rng.uniform(0, (g[0] - 1) * 50), rng.uniform(0, (g[1] - 1) * 50), rng.uniform(0, (g[2] - 1) * 50))
+             for _ in range(2)]
+        models.append({"grid": g, "model": v, "nodal": True, "sources": p})
+    outs_host = ctx.solve3d_batch(models, opt, ex.F32)
+    dev_models = [dict(m, out=torch.empty((2, m["grid"][2], m["grid"][1], m["grid"][0]), dtype=torch.float32,
+                                          device="cuda")) for m in models]
+    outs_dev = ctx.solve3d_batch(dev_models, opt, ex.F32)
+    for a, b in zip(outs_host, outs_dev):
+        assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32))
