@@ -71,7 +71,7 @@ class _Options(ctypes.Structure):
                 ("test_drop_blocks", ctypes.c_int), ("profile_sweeps", ctypes.c_int),
                 ("pair_fields", ctypes.c_int), ("sweep_kernel", ctypes.c_int),
                 ("block_shape", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-                ("reserved", ctypes.c_int * 2)]
+                ("test_tag_margin", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 class _Stats(ctypes.Structure):
@@ -220,6 +220,7 @@ class Options:
     sweep_kernel: int = 0         # 3D: 0 = tuned or chunk-step, 1 = node-step, 2 = chunk-step
     block_shape: int = 0          # 3D chunk-step warp block: 0 = tuned or 8x4, 1 = 8x4, 2 = 4x8, 3 = 16x2
     blocks_per_sm: int = 0        # persistent grid: 0 = as many as fit (or tuned)
+    test_tag_margin: int = 0      # test hook only (see eikx_options.test_tag_margin)
 
     def _c(self):
         o = _Options()
@@ -235,6 +236,7 @@ class Options:
         o.sweep_kernel = int(self.sweep_kernel)
         o.block_shape = int(self.block_shape)
         o.blocks_per_sm = int(self.blocks_per_sm)
+        o.test_tag_margin = int(self.test_tag_margin)
         return o
 
 

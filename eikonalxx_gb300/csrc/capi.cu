@@ -679,6 +679,14 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         return EIKX_OK;
     };
 
+    if (o.test_tag_margin > 0 && w.epochMirror.base == 0 && w.epochMirror.last == 0) {
+        // test hook: put the tag base just below the 32-bit wrap-around
+        const unsigned start[2] = {static_cast<unsigned>((1ull << 32) - static_cast<unsigned long long>(o.test_tag_margin)), 0u};
+        EIKX_CUDA(cudaMemcpyAsync(w.epoch.p, start, sizeof(start), cudaMemcpyHostToDevice, c->stream));
+        EIKX_CUDA(cudaStreamSynchronize(c->stream));
+        w.epochMirror.base = start[0];
+        w.epochMirror.last = 0;
+    }
     if (eikx_status r = advanceEpoch(w.epochMirror, w.mbox, w.epoch, st.epochStride, c->stream); r != EIKX_OK)
         return r;
     EIKX_CUDA(cudaEventRecord(c->ev0, c->stream));
@@ -1334,6 +1342,7 @@ eikx_status fillOptions(const eikx_options *in, eikx_options *out) {
         return fail(EIKX_ERR_INVALID, "block_shape must be 0..3");
     if (out->sweep_kernel < 0 || out->sweep_kernel > 2) return fail(EIKX_ERR_INVALID, "sweep_kernel must be 0..2");
     if (out->blocks_per_sm < 0) return fail(EIKX_ERR_INVALID, "blocks_per_sm must be >= 0");
+    if (out->test_tag_margin < 0) return fail(EIKX_ERR_INVALID, "test_tag_margin must be >= 0");
     return EIKX_OK;
 }
 

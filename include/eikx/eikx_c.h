@@ -83,7 +83,11 @@ typedef struct {
                               8x4; 1 = 8x4, 2 = 4x8, 3 = 16x2.  Identical travel times. */
     int blocks_per_sm;     /* persistent sweep grid: resident blocks per SM; 0 (default) = as
                               many as fit (or the tuned value) */
-    int reserved[2];
+    int test_tag_margin;   /* test hook, 0 in production: before the first solve of a context,
+                              start the 32-bit sweep-tag base this many tags below 2^32, so
+                              that the next few solves cross the wrap-around (the host then
+                              clears the mailbox and restarts the base at 1) */
+    int reserved[1];
 } eikx_options;
 
 /* Fills *opt with the defaults above. */

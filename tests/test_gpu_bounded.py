@@ -193,3 +193,27 @@ def test_batch_mailbox_tags_after_a_longer_batch(ctx, oracle):
         cell = [min(k - 2, int(q / h)) for q, k, h in zip(p, (nx, ny, nz), (dx, dy, dz))]
         ref = oracle.solve3d(cells, g, cell, p, n_sweeps=0, radius=3)
         assert np.array_equal(_bits(out[j]), _bits(ref)), j
+
+
+def test_sweep_tags_across_the_32_bit_wrap_around(oracle):
+    """Before a solve whose 32-bit sweep tags would wrap, the host clears the mailbox and
+    restarts the tag base; solves on either side of the wrap stay exact."""
+    c = ex.Context(0)
+    try:
+        shape = (29, 27, 23, 40., 40., 40.)
+        nx, ny, nz, dx, dy, dz = shape
+        cells = _cells(oracle, shape, 71, np.float32)
+        c.set_grid3d(*shape)
+        c.set_slowness3d(cells)
+        pos = [(fx * (nx - 1) * dx, fy * (ny - 1) * dy, fz * (nz - 1) * dz) for fx, fy, fz in CORNERS]
+        stride = 8 * (1 + 1) + 1               # tags one solve of one refinement iteration uses
+        # the third solve would pass 2^32: it runs after the clear, with tags from 1
+        opt = ex.Options(n_sweeps=1, tolerance=-1, test_tag_margin=2 * stride + 5)
+        for rep in range(4):
+            t = c.solve3d(pos, opt, ex.F32)
+            for p, a in zip(pos, t):
+                cell = [min(k - 2, int(q / h)) for q, k, h in zip(p, (nx, ny, nz), (dx, dy, dz))]
+                ref = oracle.solve3d(cells, shape, cell, p, n_sweeps=1, radius=3)
+                assert np.array_equal(_bits(a), _bits(ref)), (rep, p)
+    finally:
+        c.close()
