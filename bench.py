@@ -841,7 +841,7 @@ def main():
                          "learned: the learned warm start, 128x128x64 h=50 m (training included)")
     ap.add_argument("--fields", type=int, default=None,
                     help="sources (plain: 64, stations: 64, full: 256) or models (models: 32) per step per GPU")
-    ap.add_argument("--learn-steps", type=int, default=1500, help="learned: training steps")
+    ap.add_argument("--learn-steps", type=int, default=2000, help="learned: training steps")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -870,8 +870,9 @@ def main():
         # plain: 64 sources per step, where the sweep kernel's throughput saturates on GB300
         # (32: 252, 64: 292, 128: 292, 256: 313 grids/s); with fewer, a sweep is bound by one
         # field's wavefront critical path rather than by work
+        # learned: 2,500 training models x 8 sources = the configuration's 20,000 fields
         args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8, "models": 32,
-                       "learned": 256}.get(args.workload, 64)
+                       "learned": 2500}.get(args.workload, 64)
     PAIR[0] = args.pair_fields
     KERNEL[0] = args.sweep_kernel
     if args.profile_case:
