@@ -369,8 +369,11 @@ eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, double dy, d
 /* ---- learned warm start: the travel-time predictor -------------------------- */
 /* No counterpart in the reference.  A 3D U-Net predicts the factored correction
  * tau = T / T0 - 1 of a travel-time field from its velocity model and source, where
- * T0 = s_src * |x - x_s| and s_src is the slowness (1/v) at the node nearest the source.
- * Its prediction, inflated, is an initial field for eikx_solve3d_warm.
+ * T0 = s_src * |x - x_s| and s_src is the slowness (1/v) at the node nearest the source,
+ * in FP32 (the offsets from the source are FP64 differences rounded to FP32).  Its
+ * prediction, inflated, is an initial field for eikx_solve3d_warm.  Grids with 128 nodes
+ * along x run the first level's convolutions on tcgen05 (TMA staging, TMEM accumulators),
+ * the rest on mma.sync.
  *
  * Network (channels-last BF16 activations [sample][z][y][x][channel], BF16 weights,
  * FP32 accumulation on the tensor cores, FP32 master weights and Adam state):
