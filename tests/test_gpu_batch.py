@@ -130,3 +130,18 @@ def test_fields_copied_out_as_they_converge_equal_the_device_result(ctx):
     outs_dev = ctx.solve3d_batch(dev_models, opt, ex.F32)
     for a, b in zip(outs_host, outs_dev):
         assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32))
+
+
+def test_2d_fields_copied_out_as_they_converge_equal_the_device_result(ctx):
+    import torch
+    rng = np.random.default_rng(78)
+    nx, nz, h = 61, 47, 25.0
+    s = random_slowness(rng, (nz - 1) * (nx - 1), dtype=np.float64)
+    ctx.set_grid2d(nx, nz, h, h)
+    ctx.set_slowness2d(s)
+    src = np.column_stack([rng.uniform(0, (nx - 1) * h, 5), rng.uniform(0, (nz - 1) * h, 5)])
+    opt = ex.Options(n_sweeps=15, tolerance=1e-9)
+    host = ctx.solve2d(src, opt, ex.F64)
+    dev = torch.empty((5, nz, nx), dtype=torch.float64, device="cuda")
+    ctx.solve2d(src, opt, ex.F64, out=dev)
+    assert np.array_equal(host.view(np.uint64), dev.cpu().numpy().view(np.uint64))
