@@ -395,7 +395,11 @@ eikx_status eikx_warmnet_create(int device, const eikx_warmnet_config *cfg, eikx
         if (ext[k] < 8 || ext[k] % 8)
             return err(EIKX_ERR_INVALID, std::string("Number of grid points in ") + axis[k] + " = " +
                                              std::to_string(ext[k]) + " must be a positive multiple of 8");
-    if (!(cfg->dx > 0) || !(cfg->dy > 0) || !(cfg->dz > 0)) return err(EIKX_ERR_INVALID, "grid spacing must be positive");
+    if (!(cfg->dx > 0) || !(cfg->dy > 0) || !(cfg->dz > 0) || !std::isfinite(cfg->dx) || !std::isfinite(cfg->dy) ||
+        !std::isfinite(cfg->dz))
+        return err(EIKX_ERR_INVALID, "grid spacing must be positive and finite");
+    if (!std::isfinite(cfg->x0) || !std::isfinite(cfg->y0) || !std::isfinite(cfg->z0))
+        return err(EIKX_ERR_INVALID, "grid origin must be finite");
     if (cfg->batch < 1) return err(EIKX_ERR_INVALID, "batch must be at least 1");
     int nDev = 0;
     if (cudaGetDeviceCount(&nDev) != cudaSuccess || nDev == 0) return err(EIKX_ERR_CUDA, "no CUDA device");

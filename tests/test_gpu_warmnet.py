@@ -115,6 +115,10 @@ def test_invalid_arguments():
         ws.WarmNet((20, 16, 8, 50.0, 50.0, 50.0), batch=1)
     with pytest.raises(ex.InvalidArgument):
         ws.WarmNet(GRID, batch=0)
+    with pytest.raises(ex.InvalidArgument):
+        ws.WarmNet(tuple(GRID[:3]) + (float("inf"), 50.0, 50.0), batch=1)
+    with pytest.raises(ex.InvalidArgument):
+        ws.WarmNet(tuple(GRID[:6]) + (0.0, float("nan"), 0.0), batch=1)
     host = _device(_host_samples(14, 2))
     with ws.WarmNet(GRID, batch=1) as net:
         with pytest.raises(ex.InvalidArgument):
