@@ -396,9 +396,9 @@ typedef struct eikx_warmnet eikx_warmnet;
 
 typedef struct {
     int nx, ny, nz;        /* node grid; each a multiple of 8 */
-    double dx, dy, dz;     /* grid spacing (m) */
-    double x0, y0, z0;     /* origin (m) */
-    int batch;             /* largest number of samples per call */
+    double dx, dy, dz;     /* grid spacing (m); positive and finite */
+    double x0, y0, z0;     /* origin (m); finite */
+    int batch;             /* largest number of samples per call; at least 1 */
     unsigned long long seed;   /* initial weights (He-normal convolutions, zero biases and head) */
 } eikx_warmnet_config;
 
