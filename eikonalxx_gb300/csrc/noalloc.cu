@@ -9,24 +9,29 @@
 // that they grow with cudaMalloc; this one keeps every intermediate buffer of the
 // solve in one fixed array compiled into the library.
 //
-// The scratch: a file-scope `static __device__` array of kScratchBytes (64 MiB).  Every
-// GPU that loads the library holds it until the process exits, whether or not this
-// entry point is ever called.  A grid needs about 15 bytes per node of it (padded
+// The scratch: a file-scope `static __device__` array of kScratchBytes (64 MiB).  It
+// belongs to this translation unit's module.  Under CUDA's default lazy module loading
+// the driver loads that module -- and reserves the array and loads the sweep kernels --
+// on a device the first time this entry point runs there, so that first call is not
+// free of allocation; with CUDA_MODULE_LOADING=EAGER it happens when the library is
+// loaded.  From then on the device holds the array until the process exits.  A caller
+// that cannot allocate at all makes one warm-up call per device at start-up, before
+// its own pool takes the memory and before any stream capture; every later call makes
+// no allocating call.  A grid needs about 15 bytes per node of the array (padded
 // travel times 4 B, two edge-replicated slowness copies 8 B, block-face mailbox 3 B,
-// plus a few kB); grids whose need exceeds the array are rejected with
-// EIKX_ERR_INVALID before anything runs -- about 4 million nodes (e.g. 160^3).
+// plus a few kB); grids whose need exceeds it are rejected with EIKX_ERR_INVALID before
+// anything runs -- about 4 million nodes (e.g. 160^3).
 //
 // Sharing: all calls on a device share the array and it keeps the previous call's
 // contents.  Whatever a solve requires to start at zero (queue heads, residual slots,
-// convergence flags, the abort flag) is cleared by the solve itself; mailbox words
-// carry a tag that only the current solve uses.  Two calls whose work overlaps on the
-// GPU (different streams, or different host threads) race on the array and corrupt
-// each other's fields: serialise them.
+// convergence flags, the abort flag, the model check) is cleared by the solve itself;
+// mailbox words carry a tag that only the current solve uses.  Two calls whose work
+// overlaps on the GPU (different streams, or different host threads) race on the array
+// and corrupt each other's fields: serialise them.
 //
 // Set-up: the first call on a device, with that device current, looks up the device
 // address of the array (cudaGetSymbolAddress; in host code the array's name is only a
-// host-side stand-in) and clears the array once.  That first call should therefore be
-// made before any stream capture.
+// host-side stand-in) and clears the array once.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -86,17 +91,18 @@ struct Carve {
     }
 };
 
-// Work order of one field's warp blocks, sorted by start step (by*LY + bz*LZ, then by):
-// each thread ranks its block by counting the blocks that come before it.
-__global__ void orderKernel(int4 *order, int tilesY, int tilesZ) {
+// Work order of one field's warp blocks of ly x lz pencils, sorted by start step
+// (by*ly + bz*lz, then by): each thread ranks its block by counting the blocks that come
+// before it.
+__global__ void orderKernel(int4 *order, int tilesY, int tilesZ, int ly, int lz) {
     const int n = tilesY * tilesZ;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const int b = t % tilesY, c = t / tilesY;
-        const int key = b * eikx::LY3 + c * eikx::LZ3;
+        const int key = b * ly + c * lz;
         int rank = 0;
         for (int u = 0; u < n; ++u) {
             const int b2 = u % tilesY, c2 = u / tilesY;
-            const int k2 = b2 * eikx::LY3 + c2 * eikx::LZ3;
+            const int k2 = b2 * ly + c2 * lz;
             rank += (k2 < key || (k2 == key && b2 < b)) ? 1 : 0;
         }
         order[rank] = make_int4(0, b, c, 0);
@@ -135,17 +141,26 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     if (!slowness || !src || !tOut) return err(EIKX_ERR_INVALID, "slowness, source and output must not be NULL");
     eikx_options o;
     if (opt) o = *opt; else eikx_options_default(&o);
+    // the option checks of eikx_solve3d
     if (o.n_sweeps < 0) return err(EIKX_ERR_INVALID, "n_sweeps must be non-negative");
+    if (o.factored_radius < 0) o.factored_radius = 0;
+    if (o.block_shape < 0 || o.block_shape > eikx::kNumShapes) return err(EIKX_ERR_INVALID, "block_shape must be 0..3");
+    if (o.sweep_kernel < 0 || o.sweep_kernel > 2) return err(EIKX_ERR_INVALID, "sweep_kernel must be 0..2");
+    if (o.blocks_per_sm < 0) return err(EIKX_ERR_INVALID, "blocks_per_sm must be >= 0");
     int cx, cy, cz;
     double ox, oy, oz;
     if (!locate(src->x, x0, dx, nx, &cx, &ox) || !locate(src->y, y0, dy, ny, &cy, &oy) ||
         !locate(src->z, z0, dz, nz, &cz, &oz))
         return err(EIKX_ERR_INVALID, "source position outside the grid");
 
-    // layout and scratch need (same shapes as eikx_solve3d)
+    // layout and scratch need (same shapes as eikx_solve3d): the chunk-step kernel takes
+    // the requested warp-block shape, the node-step kernel is 8x4
+    const bool chunk = o.sweep_kernel != eikx::kNodeStep;
+    const int shape = chunk && o.block_shape > 0 ? o.block_shape - 1 : eikx::kShape8x4;
+    const int ly = eikx::shapeLY(shape), lz = eikx::shapeLZ(shape);
     const int Px = (nx + 3) / 4 * 4;
     const int spPitch = Px + 8;
-    const int tilesY = (ny + eikx::LY3 - 1) / eikx::LY3, tilesZ = (nz + eikx::LZ3 - 1) / eikx::LZ3;
+    const int tilesY = (ny + ly - 1) / ly, tilesZ = (nz + lz - 1) / lz;
     const int nTiles = tilesY * tilesZ;
     const int nSweeps = o.n_sweeps;
     const int nSweepLaunches = 8 * ((o.init_sweeps ? 1 : 0) + nSweeps);
@@ -155,7 +170,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     plan.take<float>(static_cast<size_t>(Px) * ny * nz);                       // travel times
     plan.take<float>(spElems);                                                  // slowness, +x sweeps
     plan.take<float>(spElems);                                                  // slowness, -x sweeps
-    plan.take<unsigned long long>(static_cast<size_t>(nTiles) * (eikx::LY3 + eikx::LZ3) * Px);  // mailbox
+    plan.take<unsigned long long>(static_cast<size_t>(nTiles) * (ly + lz) * Px);  // mailbox
     plan.take<unsigned long long>(static_cast<size_t>(resStride));             // residual slots
     plan.take<unsigned>(8);                                                     // queue heads, epoch, flags
     plan.take<int4>(static_cast<size_t>(nTiles));                               // work order
@@ -176,10 +191,11 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     float *tt = cv.take<float>(static_cast<size_t>(Px) * ny * nz);
     float *spPos = cv.take<float>(spElems);
     float *spNeg = cv.take<float>(spElems);
-    const size_t mboxWords = static_cast<size_t>(nTiles) * (eikx::LY3 + eikx::LZ3) * Px;
+    const size_t mboxWords = static_cast<size_t>(nTiles) * (ly + lz) * Px;
     unsigned long long *mbox = cv.take<unsigned long long>(mboxWords);
     unsigned long long *residual = cv.take<unsigned long long>(static_cast<size_t>(resStride));
-    // [0..1] queue heads, [3] abort, [4] converged, [5] iterations, [6..7] mailbox epoch
+    // [0..1] queue heads, [2] model check, [3] abort, [4] converged, [5] iterations,
+    // [6..7] mailbox epoch
     unsigned *small = cv.take<unsigned>(8);
     int4 *order = cv.take<int4>(static_cast<size_t>(nTiles));
     eikx::SourceT<float> *srcDev = cv.take<eikx::SourceT<float>>(1);
@@ -189,9 +205,9 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     NOALLOC_CUDA(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device));
     const double eps = std::numeric_limits<float>::epsilon() * 100;
     const bool uniform = std::abs(dx - dy) < eps && std::abs(dx - dz) < eps;
-    const bool chunk = o.sweep_kernel != eikx::kNodeStep;
-    const int perSM = chunk ? eikx::sweep3ChunkBlocksPerSM<float>(uniform, false, eikx::kShape8x4)
-                            : eikx::sweep3BlocksPerSM<float>(uniform);
+    int perSM = chunk ? eikx::sweep3ChunkBlocksPerSM<float>(uniform, false, shape)
+                      : eikx::sweep3BlocksPerSM<float>(uniform);
+    if (o.blocks_per_sm > 0) perSM = std::min(perSM, o.blocks_per_sm);
     const int blocks = std::max(1, std::min(numSMs * perSM, (nTiles + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock));
 
     eikx::SolveState st{};
@@ -216,7 +232,14 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     // words may hold another call's data: clear them (tag 0 is never a sweep's tag).
     NOALLOC_CUDA(cudaMemsetAsync(mbox, 0, mboxWords * sizeof(unsigned long long), stream));
     NOALLOC_CUDA(cudaMemsetAsync(small, 0, 8 * sizeof(unsigned), stream));
-    orderKernel<<<(nTiles + 127) / 128, 128, 0, stream>>>(order, tilesY, tilesZ);
+    // the model check of eikx_set_slowness3d: every slowness positive and finite
+    int bad = 0;
+    NOALLOC_CUDA(eikx::launchCheckPositive(slowness, static_cast<long long>(nx - 1) * (ny - 1) * (nz - 1),
+                                           reinterpret_cast<int *>(small + 2), stream));
+    NOALLOC_CUDA(cudaMemcpyAsync(&bad, small + 2, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NOALLOC_CUDA(cudaStreamSynchronize(stream));
+    if (bad) return err(EIKX_ERR_INVALID, "Non-positive velocities detected");
+    orderKernel<<<(nTiles + 127) / 128, 128, 0, stream>>>(order, tilesY, tilesZ, ly, lz);
     NOALLOC_CUDA(cudaGetLastError());
     sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, slowness, nx - 1, ny - 1, cx, cy, cz, ox, oy, oz);
     NOALLOC_CUDA(cudaGetLastError());
@@ -243,7 +266,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
         a.nx = nx; a.ny = ny; a.nz = nz; a.tilesY = tilesY; a.tilesZ = tilesZ;
         a.srcs = srcDev; a.st = st; a.buf = buf; a.sweepIndex = launched; a.residualSlot = slot;
         a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = fdx; a.sp3 = g;
-        if (chunk) NOALLOC_CUDA(eikx::launchSweep3Chunk<float>(a, uniform, eikx::kShape8x4, blocks, stream));
+        if (chunk) NOALLOC_CUDA(eikx::launchSweep3Chunk<float>(a, uniform, shape, blocks, stream));
         else NOALLOC_CUDA(eikx::launchSweep3<float>(a, uniform, blocks, stream));
         buf ^= 1;
         ++launched;

@@ -345,22 +345,33 @@ eikx_status eikx_analytic2d(eikx_ctx *ctx, const eikx_source2d *src, double v_to
  * not allocate GPU memory while they run -- hosts whose framework owns every device
  * allocation through its own pool, real-time pipelines that forbid allocation after
  * start-up, code running where cudaMalloc would synchronise or is not allowed.
- * One FP32 3D field (FP64 corner initialisation) is solved with the schedule of
+ * One FP32 3D field (FP64 corner initialisation) is solved with the sweep schedule of
  * eikx_solve3d; every intermediate buffer lives in a fixed 64 MiB array compiled into
- * the library (each GPU that loads the library holds it until exit), so the call makes
- * no cudaMalloc, cudaFree or other allocating call.
- *   slowness: device pointer, (nx-1)(ny-1)(nz-1) cell slownesses (s/m), natural order.
- *   src, opt: host pointers (opt may be NULL for the defaults).
+ * the library, so once the array is resident the call makes no cudaMalloc, cudaFree or
+ * other allocating call.
+ *   slowness: device pointer, (nx-1)(ny-1)(nz-1) cell slownesses (s/m), natural order;
+ *             checked on the device like eikx_set_slowness3d (a non-positive or
+ *             non-finite value returns EIKX_ERR_INVALID before any sweep runs).
+ *   src, opt: host pointers (opt may be NULL for the defaults).  The options are checked
+ *             as eikx_solve3d checks them; sweep_kernel, block_shape and blocks_per_sm
+ *             are honoured, and the value 0 means the untuned default (chunk-step
+ *             kernel, 8x4 warp blocks, full occupancy): there is no context, so no
+ *             autotuned choice applies.
  *   t_out:    device pointer, nx*ny*nz travel times, natural order.
  *   stream:   a cudaStream_t (NULL = the legacy default stream); the call returns when
  *             the field is written.
+ * Residency: under CUDA's default lazy module loading the driver reserves the array (and
+ * loads the sweep kernels) on a device the first time this function runs there; with
+ * CUDA_MODULE_LOADING=EAGER it does so when the library is loaded.  That device then
+ * holds the array until the process exits.  A caller that cannot allocate makes one
+ * warm-up call per device at start-up, before its own memory pool takes the device's
+ * memory and before any stream capture; that first call also looks up the array's
+ * device address and clears it.
  * Limit: a grid needs about 15 bytes of the array per node (padded fields, two slowness
  * copies, block-face mailbox); larger grids -- beyond about 4 million nodes -- return
  * EIKX_ERR_INVALID without running.  All calls on a device share the array and it keeps
  * the last call's contents (each solve clears what must start at zero); calls that
- * overlap on the GPU race and must be serialised by the caller.  The first call on a
- * device looks up the array's device address and clears it, so make that first call
- * before any stream capture. */
+ * overlap on the GPU race and must be serialised by the caller. */
 eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, double dy, double dz,
                                  double x0, double y0, double z0, const float *slowness,
                                  const eikx_source3d *src, const eikx_options *opt,

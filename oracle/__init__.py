@@ -156,6 +156,40 @@ class Oracle:
         return s
 
 
+class ColdSolve3:
+    """A cold-start FP32 3D solve run a bounded number of sweeps at a time, for the
+    benchmark's CPU baselines: ``advance(n)`` runs up to n more sweeps of the schedule
+    (initialisation, 8 source-limited sweeps, then refinement sweeps to the convergence
+    rule) and returns True once the solve has ended.  ``sweeps`` counts the schedule sweeps
+    run.  Run to the end, the field equals Oracle.solve3d's bit for bit."""
+
+    def __init__(self, oracle, slow, grid, src_pos, n_sweeps, radius, tol, init_fp64=True):
+        nx, ny, nz, dx, dy, dz = grid
+        self._lib = oracle.lib
+        self._slow = np.ascontiguousarray(slow, dtype=np.float32)
+        self._grid = grid
+        self._cell = [min(n - 2, int(p / d)) for p, n, d in zip(src_pos, (nx, ny, nz), (dx, dy, dz))]
+        self._off = [float(p) for p in src_pos]
+        self._args = (int(n_sweeps), int(radius), _d(tol), int(init_fp64))
+        self.tt = np.empty(nx * ny * nz, np.float32)
+        self._pos, self._quiet = ctypes.c_int(0), ctypes.c_int(0)
+        self.done = False
+
+    @property
+    def sweeps(self):
+        return self._pos.value
+
+    def advance(self, n):
+        nx, ny, nz, dx, dy, dz = self._grid
+        c, o = self._cell, self._off
+        n_sweeps, radius, tol, init_fp64 = self._args
+        rc = self._lib.oracle_advance3d_f32(nx, ny, nz, _d(dx), _d(dy), _d(dz), c[0], c[1], c[2], _d(o[0]),
+                                            _d(o[1]), _d(o[2]), _P(self._slow), n_sweeps, radius, tol, init_fp64,
+                                            _P(self.tt), ctypes.byref(self._pos), ctypes.byref(self._quiet), int(n))
+        self.done = bool(rc)
+        return self.done
+
+
 class Reference:
     """The reference's own sweep code (oracle/_ref); None-valued if not built."""
 

@@ -26,6 +26,9 @@ _REF_SKIP_SAID = False
 
 
 def reference_root():
+    """Where the reference checkout is read from: $EIKX_REFERENCE, else the read-only
+    checkout this recipe was written against.  The tests and the golden-vector script
+    ask this function, so the location is named in this recipe alone."""
     return os.environ.get("EIKX_REFERENCE", "/root/reference")
 
 

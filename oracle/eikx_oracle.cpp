@@ -519,6 +519,36 @@ int solve3(const Grid3 &g, const Src3 &src, const T *slow, int nSweeps, int radi
     return 0;
 }
 
+// solve3 in pieces, for the CPU baselines, which time real cold-start solves a bounded
+// number of sweeps at a time.  *pos counts the schedule sweeps done (0 = not started:
+// the field is initialised first; then the 8 initialisation sweeps, then refinement
+// sweeps), *quiet the current run of refinement sweeps that decreased no node by tol or
+// more.  Runs at most maxSweeps more sweeps of the schedule; returns 1 once the solve has
+// ended (the convergence rule of solve3, or nSweeps iterations), else 0.  Run to the end,
+// the field is solve3's, bit for bit.
+template <class T>
+int advance3(const Grid3 &g, const Src3 &src, const T *slow, int nSweeps, int radius, double tol, int initFp64,
+             T *tt, int *pos, int *quiet, int maxSweeps) {
+    const int ncx = g.nx - 1, ncy = g.ny - 1;
+    const T sSrc = slow[static_cast<size_t>(src.isz) * ncx * ncy + static_cast<size_t>(src.isy) * ncx + src.isx];
+    if (*pos == 0) {
+        init3<T>(g, src, slow, initFp64 != 0, tt);
+        *quiet = 0;
+    }
+    const int total = 8 * (1 + nSweeps);
+    for (int n = 0; n < maxSweeps && *pos < total && *quiet < 8; ++n) {
+        const int e = *pos % 8;
+        if (*pos < 8) {
+            sweep3<T>(e, true, g, radius, src, sSrc, slow, tt);
+        } else {
+            const double r = sweep3<T>(e, false, g, radius, src, sSrc, slow, tt);
+            *quiet = r < tol ? *quiet + 1 : 0;
+        }
+        ++*pos;
+    }
+    return (*pos >= total || *quiet >= 8) ? 1 : 0;
+}
+
 //----------------------------------------------------------------------------//
 //                                   2D                                       //
 //----------------------------------------------------------------------------//
@@ -1278,6 +1308,14 @@ int oracle_solve3d_f32(int nx, int ny, int nz, double dx, double dy, double dz, 
     Grid3 g{nx, ny, nz, dx, dy, dz};
     Src3 s{isx, isy, isz, xo, yo, zo};
     return solve3<float>(g, s, slow, nSweeps, radius, tol, initFp64, doInitSweeps, tt, residuals, nIter);
+}
+
+int oracle_advance3d_f32(int nx, int ny, int nz, double dx, double dy, double dz, int isx, int isy, int isz,
+                        double xo, double yo, double zo, const float *slow, int nSweeps, int radius, double tol,
+                        int initFp64, float *tt, int *pos, int *quiet, int maxSweeps) {
+    Grid3 g{nx, ny, nz, dx, dy, dz};
+    Src3 s{isx, isy, isz, xo, yo, zo};
+    return advance3<float>(g, s, slow, nSweeps, radius, tol, initFp64, tt, pos, quiet, maxSweeps);
 }
 
 // One sweep (e = 0..7) on an existing field; returns the largest decrease.

@@ -95,7 +95,9 @@ def levels2d_golden(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle.build import reference_root
+    ref = sys.argv[1] if len(sys.argv) > 1 else reference_root()
     with open(os.path.join(HERE, "graph3d_4x3x5.json"), "w") as f:
         json.dump(graph_golden(ref), f, indent=1)
     with open(os.path.join(HERE, "levels2d.json"), "w") as f:

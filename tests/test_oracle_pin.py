@@ -100,6 +100,27 @@ def test_residual_and_convergence_rule(oracle):
             assert np.array_equal(t, t_full)
 
 
+def test_stepped_cold_solve_equals_one_call(oracle):
+    """The benchmark's CPU baselines run real cold-start solves a few sweeps at a time
+    (oracle.ColdSolve3): stepped to the end, the field and the stopping sweep are those
+    of the one-call solve."""
+    from oracle import ColdSolve3
+    rng = np.random.default_rng(4)
+    s, g, cell, off = _case3(rng, 19, 16, 14, 100., 100., 100., np.float32)
+    for tol, step in ((1e-6, 3), (1e-4, 8), (-1.0, 5)):
+        t, res, it = oracle.solve3d(s, g, cell, off, n_sweeps=9, radius=3, tol=tol, residuals=True)
+        cs = ColdSolve3(oracle, s, g, off, n_sweeps=9, radius=3, tol=tol)
+        n = 0
+        while not cs.advance(step):
+            n += 1
+            assert n < 100
+        assert np.array_equal(cs.tt.reshape(t.shape).view(np.uint32), t.view(np.uint32))
+        r = res.ravel()
+        assert 8 + 8 * (it - 1) < cs.sweeps <= 8 + 8 * it
+        if tol < 0:
+            assert cs.sweeps == 8 * (1 + 9)
+
+
 def test_analytic_homogeneous_matches_closed_form(oracle):
     g = (21, 19, 17, 10., 11., 12.)
     t = oracle.linear_gradient3d(g, (53.0, 41.0, 77.0), 3000.0, 3000.0)

@@ -10,7 +10,9 @@ import pytest
 
 from eikonalxx_gb300 import pyEikonalXX, vtk
 
-REFERENCE = os.environ.get("EIKX_REFERENCE", "/root/reference")
+from oracle.build import reference_root
+
+REFERENCE = reference_root()
 
 
 def test_reference_python_unit_tests_pass():

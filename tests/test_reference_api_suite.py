@@ -13,7 +13,9 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("EIKX_REFERENCE", "/root/reference")
+from oracle.build import reference_root  # noqa: E402
+
+REF = reference_root()
 SUITES = ["geometry", "source", "station", "solverOptions", "graph", "model"]
 
 
