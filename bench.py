@@ -771,7 +771,7 @@ class CpuColdSolves:
         self.per_step = per_step
         v, src = make_workload(64 * self.threads)
         self.src = src
-        self.slow = self.orc.nodal_to_cell3d(v.astype(np.float64).ravel(), NX, NY, NZ, 0).astype(np.float32)
+        self.slow = self.orc.nodal_to_cell3d(v.ravel(), NX, NY, NZ, 0)   # FP32, as the GPU forms it
         self.next_src = list(range(self.threads))    # thread t takes sources t, t + T, t + 2T, ...
         self.cur = [self._start(t) for t in range(self.threads)]
         self.timed = {}          # source index -> sweeps run inside timed steps

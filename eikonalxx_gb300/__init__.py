@@ -71,7 +71,8 @@ class _Options(ctypes.Structure):
                 ("test_drop_blocks", ctypes.c_int), ("profile_sweeps", ctypes.c_int),
                 ("pair_fields", ctypes.c_int), ("sweep_kernel", ctypes.c_int),
                 ("block_shape", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-                ("test_tag_margin", ctypes.c_int), ("reserved", ctypes.c_int)]
+                ("test_tag_margin", ctypes.c_int), ("near_fp64", ctypes.c_int), ("warm_gate", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class _Stats(ctypes.Structure):
@@ -221,6 +222,8 @@ class Options:
     block_shape: int = 0          # 3D chunk-step warp block: 0 = tuned or 8x4, 1 = 8x4, 2 = 4x8, 3 = 16x2
     blocks_per_sm: int = 0        # persistent grid: 0 = as many as fit (or tuned)
     test_tag_margin: int = 0      # test hook only (see eikx_options.test_tag_margin)
+    near_fp64: bool = False       # 3D FP32: factored (near-source) updates in FP64
+    warm_gate: int = 0            # solve3d_warm residual gate: 0 one-sided, 1 two-sided
 
     def _c(self):
         o = _Options()
@@ -237,6 +240,8 @@ class Options:
         o.block_shape = int(self.block_shape)
         o.blocks_per_sm = int(self.blocks_per_sm)
         o.test_tag_margin = int(self.test_tag_margin)
+        o.near_fp64 = int(bool(self.near_fp64))
+        o.warm_gate = int(self.warm_gate)
         return o
 
 

@@ -138,7 +138,7 @@ struct BatchWorkspace {
 struct ScheduleKey {
     int dim = 0, precision = -1, nFields = 0, nx = 0, ny = 0, nz = 0, nSweeps = -1, radius = 0,
         initSweeps = 0, initFp64 = 0, uniform = 0, blocks = 0, dropBlocks = 0, paired = 0, variant = 0, shape = 0,
-        warm = 0, early = 0;
+        warm = 0, early = 0, nearFp64 = 0, warmGate = 0;
     double tol = 0, h = 0, dx = 0, dy = 0, dz = 0, gate = 0;
     unsigned long long spin = 0;
     const void *tt = nullptr, *sp = nullptr, *srcs = nullptr, *corners = nullptr, *flags = nullptr;
@@ -333,6 +333,18 @@ template <> int precOf<float>() { return EIKX_F32; }
 template <> int precOf<double>() { return EIKX_F64; }
 
 // Shared solve driver for 2D and 3D.
+// FP64 factored branch of an FP32 sweep (eikx_options.near_fp64): the source offsets,
+// the source-cell slowness as the sweep holds it, and the grid spacing, in FP64.
+template <class T>
+void setNearFp64(eikx::SourceT<T> &src, const std::array<double, 3> &off, double s, double dx, double dy, double dz) {
+    if constexpr (sizeof(T) == 4) {
+        src.nearFp64 = 1;
+        src.xd = off[0]; src.yd = off[1]; src.zd = off[2];
+        src.sd = static_cast<double>(static_cast<T>(s));
+        src.dxd = dx; src.dyd = dy; src.dzd = dz;
+    }
+}
+
 template <class T, int DIM>
 eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options o, void *tOut,
                       int where, const void *tInit = nullptr, int initWhere = EIKX_HOST, double gateTol = 0) {
@@ -383,6 +395,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     for (int i = 0; i < nSrc; ++i) {
         const double s = srcSlow[i];
         srcT[i].sSrc = static_cast<T>(s);
+        if (DIM == 3 && o.near_fp64) setNearFp64(srcT[i], srcOffs[i], s, dx, dy, dz);
         // corner init: slowness as the field type holds it, offsets in FP64
         corners[i] = eikx::Corner3{srcT[i].isx, srcT[i].isy, srcT[i].isz, srcOffs[i][0], srcOffs[i][1], srcOffs[i][2],
                                    static_cast<double>(static_cast<T>(s))};
@@ -420,6 +433,11 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
             o.block_shape = it->second.block_shape;
             o.blocks_per_sm = it->second.blocks_per_sm;
         }
+    }
+    // the FP64 factored branch runs in the chunk-step kernel (its own instances)
+    if (DIM == 3 && P == EIKX_F32 && o.near_fp64) {
+        o.sweep_kernel = eikx::kChunkStep;
+        o.pair_fields = 0;
     }
     // FP32 uniform 3D batches run two fields per lane (the paired kernel)
     const bool paired = DIM == 3 && P == EIKX_F32 && uniform && nSrc >= 2 && o.pair_fields;
@@ -567,6 +585,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     sk.paired = paired ? 1 : 0;
     sk.warm = warm ? 1 : 0;
     sk.gate = gateTol;
+    sk.nearFp64 = DIM == 3 && P == EIKX_F32 && o.near_fp64 ? 1 : 0;
+    sk.warmGate = warm ? o.warm_gate : 0;
     sk.variant = variant;
     sk.shape = shape;
     sk.tt = w.tt.p; sk.sp = spad[0].p; sk.srcs = w.srcs.p; sk.corners = w.corners.p;
@@ -594,7 +614,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
             EIKX_CUDA(eikx::launchWarmInit3<T>(w.tt.as<T>(), w.init.as<T>(), nSrc, fieldStride, Px, nx, ny, nz, dx, dy,
                                                dz, w.corners.as<eikx::Corner3>(), w.srcs.as<eikx::SourceT<T>>(),
                                                c->slow3.as<double>(), o.factored_radius, uniform, static_cast<T>(dx),
-                                               spacing3<T>(dx, dy, dz), gateTol, o.init_fp64 ? 1 : 0,
+                                               spacing3<T>(dx, dy, dz), gateTol, o.warm_gate == 1 ? 1 : 0,
+                                               o.init_fp64 ? 1 : 0,
                                                w.resetCount.as<unsigned long long>(), c->stream));
         } else if (DIM == 3)
             EIKX_CUDA(eikx::launchInit3<T>(w.tt.as<T>(), nSrc, fieldStride, Px, nx, ny, nz, dx, dy, dz,
@@ -614,6 +635,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
                 a.srcs = w.srcs.as<eikx::SourceT<T>>(); a.st = st; a.buf = buf; a.residualSlot = slot;
                 a.sweepIndex = sweepsLaunched;
                 a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = static_cast<T>(dx);
+                a.nearFp64 = P == EIKX_F32 && o.near_fp64 ? 1 : 0;
                 const T tdx = static_cast<T>(dx), tdy = static_cast<T>(dy), tdz = static_cast<T>(dz);
                 eikx::Spacing3<T> g;
                 g.dx = tdx; g.dy = tdy; g.dz = tdz;
@@ -954,7 +976,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     std::vector<eikx::SourceT<T>> srcT(nUnits);
     std::vector<eikx::Corner3> corners(nUnits);
     std::vector<eikx::Grid3Unit<T>> units(nUnits);
-    std::vector<std::array<double, 3>> offs(nUnits);
+    std::vector<std::array<double, 3>> offs(nUnits), unitSpacing(nUnits);
     T *ttBase = w.tt.as<T>();
     T *spBase = w.sp.as<T>();
     unsigned long long *mbBase = w.mbox.as<unsigned long long>();
@@ -975,6 +997,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
                                                   " lies outside the grid");
             srcT[u].isx = cx; srcT[u].isy = cy; srcT[u].isz = cz;
             offs[u] = {ox, oy, oz};
+            unitSpacing[u] = {m.dx, m.dy, m.dz};
         }
         const bool nodal = m.model_kind == EIKX_NODAL_VELOCITY;
         const size_t nCell = static_cast<size_t>(m.nx - 1) * (m.ny - 1) * (m.nz - 1);
@@ -1030,6 +1053,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
         srcT[u].ys = static_cast<T>(offs[u][1]);
         srcT[u].zs = static_cast<T>(offs[u][2]);
         srcT[u].sSrc = static_cast<T>(sc);
+        if (o.near_fp64) setNearFp64(srcT[u], offs[u], sc, unitSpacing[u][0], unitSpacing[u][1], unitSpacing[u][2]);
         corners[u] = eikx::Corner3{srcT[u].isx, srcT[u].isy, srcT[u].isz, offs[u][0], offs[u][1], offs[u][2],
                                    static_cast<double>(static_cast<T>(sc))};
     }
@@ -1131,6 +1155,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
             a.sweepIndex = sweepsLaunched;
             a.sweep = e; a.init = init; a.radius = o.factored_radius;
             a.units = w.units.as<eikx::Grid3Unit<T>>();
+            a.nearFp64 = sizeof(T) == 4 && o.near_fp64 ? 1 : 0;
             EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, shape, blocks, c->stream));
             if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched + 1], c->stream));
             buf ^= 1;
@@ -1161,7 +1186,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
                                static_cast<double>(o.n_sweeps), static_cast<double>(o.factored_radius),
                                static_cast<double>(o.init_sweeps), static_cast<double>(o.init_fp64), o.tolerance,
                                static_cast<double>(st.spinLimit), static_cast<double>(blocks),
-                               static_cast<double>(shape)};
+                               static_cast<double>(shape), static_cast<double>(o.near_fp64 ? 1 : 0)};
     for (int i = 0; i < nM; ++i) {
         const eikx_model3d &m = models[sel[i]];
         for (double v : {static_cast<double>(m.nx), static_cast<double>(m.ny), static_cast<double>(m.nz), m.dx, m.dy,
@@ -1343,6 +1368,8 @@ eikx_status fillOptions(const eikx_options *in, eikx_options *out) {
     if (out->sweep_kernel < 0 || out->sweep_kernel > 2) return fail(EIKX_ERR_INVALID, "sweep_kernel must be 0..2");
     if (out->blocks_per_sm < 0) return fail(EIKX_ERR_INVALID, "blocks_per_sm must be >= 0");
     if (out->test_tag_margin < 0) return fail(EIKX_ERR_INVALID, "test_tag_margin must be >= 0");
+    if (out->near_fp64 < 0 || out->near_fp64 > 1) return fail(EIKX_ERR_INVALID, "near_fp64 must be 0 or 1");
+    if (out->warm_gate < 0 || out->warm_gate > 1) return fail(EIKX_ERR_INVALID, "warm_gate must be 0 or 1");
     return EIKX_OK;
 }
 

@@ -80,7 +80,7 @@ template <class T, bool UNIFORM>
 __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny,
                                 int nz, double dx, double dy, double dz, const Corner3 *corners,
                                 const SourceT<T> *srcs, const double *slow, int radius, T h, Spacing3<T> g,
-                                double gateTol, int fp64, unsigned long long *nReset) {
+                                double gateTol, int twoSided, int fp64, unsigned long long *nReset) {
     const long long perField = static_cast<long long>(nx) * ny * nz;
     const long long n = perField * nFields;
     const int ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
@@ -124,11 +124,15 @@ __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fie
                 st.s7 = cell(cxu, cyo, czo);
                 st.t1 = tv(xs, iy, iz); st.t2 = tv(xs, ys, iz); st.t3 = tv(ix, ys, iz); st.t4 = tv(ix, iy, zs);
                 st.t5 = tv(xs, iy, zs); st.t6 = tv(xs, ys, zs); st.t7 = tv(ix, ys, zs);
-                const T u = UNIFORM ? fd3Uniform<T>(radius, h, src, sg, ix, iy, iz, st)
-                                    : fd3NonUniform<T>(radius, g, src, sg, ix, iy, iz, st);
+                // a near_fp64 solve gates with the FP64 factored branch its sweeps use
+                const T u = UNIFORM ? fd3Uniform<T, true>(radius, h, src, sg, ix, iy, iz, st)
+                                    : fd3NonUniform<T, true>(radius, g, src, sg, ix, iy, iz, st);
                 uMin = u < uMin ? u : uMin;
             }
-            const bool under = static_cast<double>(v) < static_cast<double>(uMin) - gateTol;
+            // one-sided: reset what sweeps could not raise; two-sided: also what lies above
+            // the update its neighbourhood gives
+            const bool under = static_cast<double>(v) < static_cast<double>(uMin) - gateTol ||
+                               (twoSided && static_cast<double>(v) > static_cast<double>(uMin) + gateTol);
             if (corner) {
                 const T an = fp64 ? static_cast<T>(analyticT3<double>(ix, iy, iz, dx, dy, dz, cn.xo, cn.yo, cn.zo, cn.s))
                                   : analyticT3<T>(ix, iy, iz, static_cast<T>(dx), static_cast<T>(dy),
@@ -446,16 +450,16 @@ template <class T>
 cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
                             double dx, double dy, double dz, const Corner3 *corners, const SourceT<T> *srcs,
                             const double *slow, int radius, bool uniform, T h, const Spacing3<T> &g, double gateTol,
-                            int fp64, unsigned long long *nReset, cudaStream_t s) {
+                            int twoSided, int fp64, unsigned long long *nReset, cudaStream_t s) {
     const long long n = static_cast<long long>(nx) * ny * nz * nFields;
     if (uniform)
         warmInit3Kernel<T, true><<<gridFor(n), kThreads, 0, s>>>(tt, init, nFields, fieldStride, pitch, nx, ny, nz, dx,
                                                                  dy, dz, corners, srcs, slow, radius, h, g, gateTol,
-                                                                 fp64, nReset);
+                                                                 twoSided, fp64, nReset);
     else
         warmInit3Kernel<T, false><<<gridFor(n), kThreads, 0, s>>>(tt, init, nFields, fieldStride, pitch, nx, ny, nz, dx,
                                                                   dy, dz, corners, srcs, slow, radius, h, g, gateTol,
-                                                                  fp64, nReset);
+                                                                  twoSided, fp64, nReset);
     if (pitch > nx) {
         const long long np = static_cast<long long>(nFields) * ny * nz * (pitch - nx);
         fillPadKernel<T><<<gridFor(np), kThreads, 0, s>>>(tt, nFields, fieldStride, pitch, nx, ny * nz);
@@ -464,11 +468,11 @@ cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldSt
 }
 template cudaError_t launchWarmInit3<float>(float *, const float *, int, long long, int, int, int, int, double, double,
                                             double, const Corner3 *, const SourceT<float> *, const double *, int, bool,
-                                            float, const Spacing3<float> &, double, int, unsigned long long *,
+                                            float, const Spacing3<float> &, double, int, int, unsigned long long *,
                                             cudaStream_t);
 template cudaError_t launchWarmInit3<double>(double *, const double *, int, long long, int, int, int, int, double,
                                              double, double, const Corner3 *, const SourceT<double> *, const double *,
-                                             int, bool, double, const Spacing3<double> &, double, int,
+                                             int, bool, double, const Spacing3<double> &, double, int, int,
                                              unsigned long long *, cudaStream_t);
 
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st) {

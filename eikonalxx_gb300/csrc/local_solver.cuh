@@ -39,6 +39,13 @@ template <class T> struct SourceT {
     int isx, isy, isz;
     T xs, ys, zs;
     T sSrc;
+    // FP64 factored branch of an FP32 sweep (eikx_options.near_fp64): when set, a node
+    // within the factored radius is updated by the double-precision operator -- the
+    // reference's Solver3D<double> arithmetic -- on its FP32 neighbours widened to double,
+    // with the analytic factor T0 and its gradient from these FP64 source offsets,
+    // source-cell slowness and grid spacing; the result is rounded to FP32.
+    int nearFp64;
+    double xd, yd, zd, sd, dxd, dyd, dzd;
 };
 
 // Analytic homogeneous time and gradient (computeAnalyticalTravelTime,
@@ -186,9 +193,23 @@ __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t
     return dmin(t1d, dmin(t2d, third * (S + dsqrt(det))));
 }
 
-template <class T>
+template <class T> struct Spacing3;
+template <int D>
+__device__ __noinline__ float fd3UniformNearFp64(const SourceT<float> src, const SweepSigns sg, int ix, int iy,
+                                                 int iz, const Stencil3<float> n);
+template <int D>
+__device__ __noinline__ float fd3NonUniformNearFp64(const SourceT<float> src, const SweepSigns sg, int ix, int iy,
+                                                    int iz, const Stencil3<float> n);
+
+// FP64NEAR: compile the FP64 factored branch of FP32 sweeps in (taken when src.nearFp64
+// is set).  Only the kernel instances that run near_fp64 solves carry it: its double-
+// precision operator needs more registers than the rest of a sweep kernel.
+template <class T, bool FP64NEAR = false>
 __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const SweepSigns &sg,
                                             int ix, int iy, int iz, const Stencil3<T> &n) {
+    if constexpr (FP64NEAR && sizeof(T) == 4) {
+        if (src.nearFp64) return fd3UniformNearFp64<0>(src, sg, ix, iy, iz, n);
+    }
     EIKX_FD3_UNIFORM_PREFIX
     {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
@@ -267,12 +288,12 @@ __device__ __forceinline__ bool nearSource(int radius, int isx, int isy, int isz
     return !(abs(isx - ix) > radius || abs(isy - iy) > radius || abs(isz - iz) > radius);
 }
 
-template <class T>
+template <class T, bool FP64NEAR = false>
 __device__ __forceinline__ T fd3Uniform(int radius, T h, const SourceT<T> &src,
                                         const SweepSigns &sg, int ix, int iy, int iz,
                                         const Stencil3<T> &n) {
     if (!nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) return fd3UniformFar(h, n);
-    return fd3UniformNear(h, src, sg, ix, iy, iz, n);
+    return fd3UniformNear<T, FP64NEAR>(h, src, sg, ix, iy, iz, n);
 }
 
 // Grid constants of the non-uniform 3D solver (include/private/solver3d.hpp:247-261),
@@ -351,10 +372,13 @@ __device__ __forceinline__ T fd3NonUniformFar(const Spacing3<T> &g, const Stenci
     return tUpd;
 }
 
-template <class T>
+template <class T, bool FP64NEAR = false>
 __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const SourceT<T> &src,
                                                const SweepSigns &sg, int ix, int iy, int iz,
                                                const Stencil3<T> &n) {
+    if constexpr (FP64NEAR && sizeof(T) == 4) {
+        if (src.nearFp64) return fd3NonUniformNearFp64<0>(src, sg, ix, iy, iz, n);
+    }
     EIKX_FD3_NONUNIFORM_PREFIX
     {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
@@ -433,12 +457,51 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
 }
 #undef EIKX_FD3_NONUNIFORM_PREFIX
 
-template <class T>
+// The FP64 factored branch of an FP32 sweep (SourceT::nearFp64): the operands widened to
+// double, the double-precision operator of the reference (Solver3D is instantiated for
+// double only, src/solver3d.cpp:626-627), the result rounded to FP32.  Out of line: only
+// the few hundred nodes per field within the factored radius take it.
+__device__ __forceinline__ Stencil3<double> widen(const Stencil3<float> &n) {
+    Stencil3<double> m;
+    m.s0 = n.s0; m.s1 = n.s1; m.s2 = n.s2; m.s3 = n.s3; m.s4 = n.s4; m.s5 = n.s5; m.s7 = n.s7;
+    m.t1 = n.t1; m.t2 = n.t2; m.t3 = n.t3; m.t4 = n.t4; m.t5 = n.t5; m.t6 = n.t6; m.t7 = n.t7;
+    return m;
+}
+__device__ __forceinline__ SourceT<double> sourceFp64(const SourceT<float> &src) {
+    SourceT<double> d{};
+    d.isx = src.isx; d.isy = src.isy; d.isz = src.isz;
+    d.xs = src.xd; d.ys = src.yd; d.zs = src.zd; d.sSrc = src.sd;
+    return d;
+}
+template <int D>
+__device__ __noinline__ float fd3UniformNearFp64(const SourceT<float> src, const SweepSigns sg, int ix, int iy,
+                                                 int iz, const Stencil3<float> n) {
+    return static_cast<float>(fd3UniformNear<double>(src.dxd, sourceFp64(src), sg, ix, iy, iz, widen(n)));
+}
+template <int D>
+__device__ __noinline__ float fd3NonUniformNearFp64(const SourceT<float> src, const SweepSigns sg, int ix, int iy,
+                                                    int iz, const Stencil3<float> n) {
+    // the non-uniform constants in double, as the host forms them for an FP64 solve
+    // (include/private/solver3d.hpp:247-261)
+    const double dx = src.dxd, dy = src.dyd, dz = src.dzd;
+    Spacing3<double> g;
+    g.dx = dx; g.dy = dy; g.dz = dz;
+    g.dxInv = 1 / dx; g.dyInv = 1 / dy; g.dzInv = 1 / dz;
+    g.dx2Inv = 1 / (dx * dx); g.dy2Inv = 1 / (dy * dy); g.dz2Inv = 1 / (dz * dz);
+    g.dx_dz = dx / dz; g.dz_dx = dz / dx; g.dy_dz = dy / dz; g.dz_dy = dz / dy;
+    g.dx_dy = dx / dy; g.dy_dx = dy / dx;
+    g.dx2_p_dz2_inv = 1 / (dx * dx + dz * dz);
+    g.dy2_p_dz2_inv = 1 / (dy * dy + dz * dz);
+    g.dx2_p_dy2_inv = 1 / (dx * dx + dy * dy);
+    return static_cast<float>(fd3NonUniformNear<double>(g, sourceFp64(src), sg, ix, iy, iz, widen(n)));
+}
+
+template <class T, bool FP64NEAR = false>
 __device__ __forceinline__ T fd3NonUniform(int radius, const Spacing3<T> &g, const SourceT<T> &src,
                                            const SweepSigns &sg, int ix, int iy, int iz,
                                            const Stencil3<T> &n) {
     if (!nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) return fd3NonUniformFar(g, n);
-    return fd3NonUniformNear(g, src, sg, ix, iy, iz, n);
+    return fd3NonUniformNear<T, FP64NEAR>(g, src, sg, ix, iy, iz, n);
 }
 
 // ---------------------------------------------------------------------------- 2D

@@ -110,13 +110,21 @@ __global__ void orderKernel(int4 *order, int tilesY, int tilesZ, int ly, int lz)
 }
 
 // Source table of the field: the source-cell slowness is read from the caller's model.
+// With nearFp64 the factored branch runs in FP64 (eikx_options.near_fp64).
 __global__ void sourceKernel(eikx::SourceT<float> *src, eikx::Corner3 *corner, const float *slowness, int ncx,
-                             int ncy, int cx, int cy, int cz, double ox, double oy, double oz) {
+                             int ncy, int cx, int cy, int cz, double ox, double oy, double oz, int nearFp64,
+                             double dx, double dy, double dz) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const float s = slowness[(static_cast<long long>(cz) * ncy + cy) * ncx + cx];
+    *src = eikx::SourceT<float>{};
     src->isx = cx; src->isy = cy; src->isz = cz;
     src->xs = static_cast<float>(ox); src->ys = static_cast<float>(oy); src->zs = static_cast<float>(oz);
     src->sSrc = s;
+    if (nearFp64) {
+        src->nearFp64 = 1;
+        src->xd = ox; src->yd = oy; src->zd = oz; src->sd = static_cast<double>(s);
+        src->dxd = dx; src->dyd = dy; src->dzd = dz;
+    }
     corner->isx = cx; corner->isy = cy; corner->isz = cz;
     corner->xo = ox; corner->yo = oy; corner->zo = oz;
     corner->s = static_cast<double>(s);
@@ -147,6 +155,8 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     if (o.block_shape < 0 || o.block_shape > eikx::kNumShapes) return err(EIKX_ERR_INVALID, "block_shape must be 0..3");
     if (o.sweep_kernel < 0 || o.sweep_kernel > 2) return err(EIKX_ERR_INVALID, "sweep_kernel must be 0..2");
     if (o.blocks_per_sm < 0) return err(EIKX_ERR_INVALID, "blocks_per_sm must be >= 0");
+    if (o.near_fp64 < 0 || o.near_fp64 > 1) return err(EIKX_ERR_INVALID, "near_fp64 must be 0 or 1");
+    if (o.near_fp64) o.sweep_kernel = eikx::kChunkStep;   // the FP64 factored branch's kernel
     int cx, cy, cz;
     double ox, oy, oz;
     if (!locate(src->x, x0, dx, nx, &cx, &ox) || !locate(src->y, y0, dy, ny, &cy, &oy) ||
@@ -241,7 +251,8 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     if (bad) return err(EIKX_ERR_INVALID, "Non-positive velocities detected");
     orderKernel<<<(nTiles + 127) / 128, 128, 0, stream>>>(order, tilesY, tilesZ, ly, lz);
     NOALLOC_CUDA(cudaGetLastError());
-    sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, slowness, nx - 1, ny - 1, cx, cy, cz, ox, oy, oz);
+    sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, slowness, nx - 1, ny - 1, cx, cy, cz, ox, oy, oz,
+                                       o.near_fp64 ? 1 : 0, dx, dy, dz);
     NOALLOC_CUDA(cudaGetLastError());
     NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spPos, spPitch, 3, slowness, nx, ny, nz, stream)));
     NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spNeg, spPitch, 0, slowness, nx, ny, nz, stream)));
@@ -266,6 +277,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
         a.nx = nx; a.ny = ny; a.nz = nz; a.tilesY = tilesY; a.tilesZ = tilesZ;
         a.srcs = srcDev; a.st = st; a.buf = buf; a.sweepIndex = launched; a.residualSlot = slot;
         a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = fdx; a.sp3 = g;
+        a.nearFp64 = o.near_fp64;
         if (chunk) NOALLOC_CUDA(eikx::launchSweep3Chunk<float>(a, uniform, shape, blocks, stream));
         else NOALLOC_CUDA(eikx::launchSweep3<float>(a, uniform, blocks, stream));
         buf ^= 1;

@@ -87,7 +87,18 @@ typedef struct {
                               start the 32-bit sweep-tag base this many tags below 2^32, so
                               that the next few solves cross the wrap-around (the host then
                               clears the mailbox and restarts the base at 1) */
-    int reserved[1];
+    int near_fp64;         /* 3D FP32 solves: 1 = nodes within the factored radius are updated
+                              in FP64 -- the analytic factor T0 = distance x source slowness,
+                              its gradient, the factored differences tau and the quadratic
+                              solves, i.e. the reference's double-precision operator
+                              (Solver3D<double>) on the FP32 neighbours -- and rounded to
+                              FP32; 0 (default) = in FP32 like the rest of the sweep.
+                              Ignored by FP64 solves and 2D. */
+    int warm_gate;         /* eikx_solve3d_warm's residual gate: 0 (default) = reset nodes
+                              whose initial time lies more than gate_tol below the smallest
+                              upwind update of their initial neighbourhood (one-sided);
+                              1 = also reset nodes more than gate_tol above it (two-sided) */
+    int reserved[2];
 } eikx_options;
 
 /* Fills *opt with the defaults above. */

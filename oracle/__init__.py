@@ -30,16 +30,20 @@ class Oracle:
         self.lib.oracle_hypot.restype = ctypes.c_double
 
     def solve3d(self, slow, grid, src_cell, src_off, n_sweeps=2, radius=3, tol=-1.0, init_fp64=True,
-                init_sweeps=True, residuals=False):
+                init_sweeps=True, residuals=False, near_fp64=False):
         nx, ny, nz, dx, dy, dz = grid
         dt = slow.dtype
         tt = np.zeros(nx * ny * nz, dt)
         res = np.zeros(max(1, 8 * n_sweeps), np.float64)
         it = ctypes.c_int(0)
         f = self.lib.oracle_solve3d_f64 if dt == np.float64 else self.lib.oracle_solve3d_f32
-        f(nx, ny, nz, _d(dx), _d(dy), _d(dz), int(src_cell[0]), int(src_cell[1]), int(src_cell[2]),
-          _d(src_off[0]), _d(src_off[1]), _d(src_off[2]), _P(np.ascontiguousarray(slow)), n_sweeps, radius,
-          _d(tol), int(init_fp64), int(init_sweeps), _P(tt), _P(res), ctypes.byref(it))
+        self.lib.oracle_set_near_fp64(int(bool(near_fp64)))
+        try:
+            f(nx, ny, nz, _d(dx), _d(dy), _d(dz), int(src_cell[0]), int(src_cell[1]), int(src_cell[2]),
+              _d(src_off[0]), _d(src_off[1]), _d(src_off[2]), _P(np.ascontiguousarray(slow)), n_sweeps, radius,
+              _d(tol), int(init_fp64), int(init_sweeps), _P(tt), _P(res), ctypes.byref(it))
+        finally:
+            self.lib.oracle_set_near_fp64(0)
         tt = tt.reshape(nz, ny, nx)
         return (tt, res[:8 * it.value].reshape(-1, 8), it.value) if residuals else tt
 

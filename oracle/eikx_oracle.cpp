@@ -398,6 +398,10 @@ void loopLimits3(const Grid3 &g, const Sweep3 &sw, bool init, const Src3 &src,
 // Solver3DSweep<T,E>::updateFSM, include/private/solver3d.hpp:150-326, with the
 // stencil addressing of gridToSurroundingSlownessIndices (:1300-1442) and
 // gridToSurroundingTravelTimeIndices (:1460-1586).  Returns the largest decrease.
+// near_fp64 (FP32 solves): nodes within the factored radius take the double-precision
+// operator on their FP32 neighbours, rounded to FP32 -- the GPU's eikx_options.near_fp64.
+int gNearFp64 = 0;
+
 template <class T>
 double sweep3(int e, bool init, const Grid3 &g, int radius, const Src3 &src, T sSrc,
               const T *slow, T *tt) {
@@ -412,6 +416,7 @@ double sweep3(int e, bool init, const Grid3 &g, int radius, const Src3 &src, T s
     const bool uniform = std::abs(g.dx - g.dy) < eps && std::abs(g.dx - g.dz) < eps;
     const T h = static_cast<T>(g.dx);
     NonUniform3<T> nu(static_cast<T>(g.dx), static_cast<T>(g.dy), static_cast<T>(g.dz));
+    const NonUniform3<double> nu64(g.dx, g.dy, g.dz);
     double diffMax = 0;
     auto cidx = [&](int cx, int cy, int cz) {
         return static_cast<size_t>(cz) * ncx * ncy + static_cast<size_t>(cy) * ncx + cx;
@@ -449,11 +454,24 @@ double sweep3(int e, bool init, const Grid3 &g, int radius, const Src3 &src, T s
                 T t5 = tt[gidx(xsft, iy, zsft)];
                 T t6 = tt[gidx(xsft, ysft, zsft)];
                 T t7 = tt[gidx(ix, ysft, zsft)];
-                T tUpd = uniform
-                    ? fd3Uniform<T>(radius, huge, h, sSrc, ix, iy, iz, sw, src, xs, ys, zs,
-                                    s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7)
-                    : fd3NonUniform<T>(radius, huge, nu, sSrc, ix, iy, iz, sw, src, xs, ys, zs,
-                                       s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7);
+                const bool near = std::abs(src.isx - ix) <= radius && std::abs(src.isy - iy) <= radius &&
+                                  std::abs(src.isz - iz) <= radius;
+                T tUpd;
+                if (gNearFp64 && sizeof(T) == 4 && near) {
+                    // near_fp64: the double-precision operator (the reference's Solver3D<double>)
+                    // on the FP32 neighbours, with FP64 source offsets and spacing, rounded to T
+                    tUpd = static_cast<T>(uniform
+                        ? fd3Uniform<double>(radius, kHuge, g.dx, sSrc, ix, iy, iz, sw, src, src.xo, src.yo, src.zo,
+                                             s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7)
+                        : fd3NonUniform<double>(radius, kHuge, nu64, sSrc, ix, iy, iz, sw, src, src.xo, src.yo,
+                                                src.zo, s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7));
+                } else {
+                    tUpd = uniform
+                        ? fd3Uniform<T>(radius, huge, h, sSrc, ix, iy, iz, sw, src, xs, ys, zs,
+                                        s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7)
+                        : fd3NonUniform<T>(radius, huge, nu, sSrc, ix, iy, iz, sw, src, xs, ys, zs,
+                                           s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7);
+                }
                 if (tUpd < t0) {
                     tt[i0] = tUpd;
                     // decrease formed in T (exact by Sterbenz whenever it is below t0/2),
@@ -1380,6 +1398,7 @@ void oracle_nodal_to_cell2d_f64(int nx, int nz, const double *v, int ordering, d
 }
 
 double oracle_hypot(double a, double b) { return eikxHypot(a, b); }
+void oracle_set_near_fp64(int on) { gNearFp64 = on; }
 
 // Rays from n stations (absolute x, z) to a source (absolute x, z) through a gradient
 // field (nz x nx x 2, natural); segments [station][capacity][6]; counts[station].

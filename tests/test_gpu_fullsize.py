@@ -42,9 +42,12 @@ def _cell(pos, n, d):
 
 @pytest.fixture(scope="module")
 def model3(oracle):
+    """The benchmark's FP32 nodal velocities and their cell slowness (the reference's
+    8 / sum of the 8 corner velocities, formed in the input's precision, FP32)."""
     v = synthetic.layered_grf_model(NX3, NY3, NZ3, H3, MODEL_SEED)
-    s64 = oracle.nodal_to_cell3d(v.astype(np.float64).ravel(), NX3, NY3, NZ3, 0)
-    return v, s64
+    s32 = oracle.nodal_to_cell3d(v.ravel(), NX3, NY3, NZ3, 0)
+    assert s32.dtype == np.float32
+    return v, s32
 
 
 def _pool():
@@ -74,21 +77,21 @@ def test_plain_2d_configuration(ctx, oracle):
 
 
 def test_plain_3d_configuration_one_source(ctx, oracle, model3):
-    v, s64 = model3
+    v, s32 = model3
     ctx.set_grid3d(NX3, NY3, NZ3, H3, H3, H3)
     ctx.set_nodal_velocity3d(v)
     # the device's nodal -> cell slowness at full size
-    assert np.array_equal(ctx.get_slowness3d(), s64)
+    assert np.array_equal(ctx.get_slowness3d(), s32.astype(np.float64))
     src = synthetic.uniform_sources(1, NX3, NY3, NZ3, H3, SOURCE_SEED + 1)[0]
     opt = ex.Options(n_sweeps=1, tolerance=-1, factored_radius=3)
     t = ctx.solve3d([src], opt, ex.F32)[0]
-    t_or = oracle.solve3d(s64.astype(np.float32), (NX3, NY3, NZ3, H3, H3, H3), _cell(src, (NX3, NY3, NZ3), (H3,) * 3),
+    t_or = oracle.solve3d(s32, (NX3, NY3, NZ3, H3, H3, H3), _cell(src, (NX3, NY3, NZ3), (H3,) * 3),
                           src, n_sweeps=1, radius=3)
     assert np.array_equal(_bits(t), _bits(t_or)), np.abs(t - t_or).max()
 
 
 def test_benchmark_batch_fields_match_oracle(ctx, oracle, model3):
-    v, s64 = model3
+    v, s32 = model3
     ctx.set_grid3d(NX3, NY3, NZ3, H3, H3, H3)
     ctx.set_nodal_velocity3d(v)
     srcs = synthetic.uniform_sources(64, NX3, NY3, NZ3, H3, SOURCE_SEED)
@@ -97,7 +100,6 @@ def test_benchmark_batch_fields_match_oracle(ctx, oracle, model3):
     st = ctx.stats()
     assert st["iterations_min"] < st["iterations_max"] <= 10     # fields stop at different iterations
     pick = sorted(np.random.default_rng(3).choice(64, 8, replace=False))
-    s32 = s64.astype(np.float32)
     grid = (NX3, NY3, NZ3, H3, H3, H3)
 
     def one(i):

@@ -241,3 +241,44 @@ def test_solve2d_batch_converges_per_field(ctx, oracle, kernel):
     for i, (_, cell, off) in enumerate(srcs):
         t_or = oracle.solve2d(s, shape, cell, off, n_sweeps=15, radius=3, tol=1e-7, hypot_mode=1)
         assert np.array_equal(_bits(t[i]), _bits(t_or)), i
+
+
+@pytest.mark.parametrize("block", [0, 2, 3])
+@pytest.mark.parametrize("radius", [3, 1000])
+@pytest.mark.parametrize("shape", [(29, 23, 19, 40., 40., 40.), (18, 21, 13, 50., 45., 60.)])
+def test_near_fp64_matches_oracle(ctx, oracle, block, radius, shape):
+    """near_fp64: FP32 sweeps whose nodes within the factored radius take the FP64
+    operator (T0, its gradient, tau and the quadratic solves in double), uniform and
+    non-uniform grids, every warp-block shape, the whole grid factored (radius 1000)."""
+    rng = np.random.default_rng(300 + radius + block)
+    nx, ny, nz = shape[:3]
+    s = random_slowness(rng, (nz - 1) * (ny - 1) * (nx - 1), dtype=np.float32)
+    ctx.set_grid3d(*shape)
+    ctx.set_slowness3d(s)
+    srcs = [_src(rng, (nx, ny, nz), shape[3:]) for _ in range(3)]
+    opt = ex.Options(n_sweeps=4, tolerance=1e-6, factored_radius=radius, near_fp64=True, block_shape=block)
+    t = ctx.solve3d([p for p, _, _ in srcs], opt, ex.F32)
+    for i, (_, cell, off) in enumerate(srcs):
+        t_or = oracle.solve3d(s, shape, cell, off, n_sweeps=4, radius=radius, tol=1e-6, near_fp64=True)
+        assert np.array_equal(_bits(t[i]), _bits(t_or)), (i, np.abs(t[i] - t_or).max())
+        t_32 = oracle.solve3d(s, shape, cell, off, n_sweeps=4, radius=radius, tol=1e-6)
+        assert not np.array_equal(_bits(t_or), _bits(t_32))     # the mode changes the near field
+
+
+def test_near_fp64_batch_and_pair_request(ctx, oracle):
+    """near_fp64 in a multi-model batch, and with pair_fields requested (the FP64 branch
+    runs on the chunk-step kernel, so the request falls back to one field per lane)."""
+    rng = np.random.default_rng(17)
+    shape = (24, 19, 14, 50., 50., 50.)
+    nx, ny, nz = shape[:3]
+    s = random_slowness(rng, (nz - 1) * (ny - 1) * (nx - 1), dtype=np.float32)
+    srcs = [_src(rng, (nx, ny, nz), shape[3:]) for _ in range(4)]
+    opt = ex.Options(n_sweeps=3, tolerance=-1, factored_radius=3, near_fp64=True, pair_fields=True)
+    ctx.set_grid3d(*shape)
+    ctx.set_slowness3d(s)
+    t = ctx.solve3d([p for p, _, _ in srcs], opt, ex.F32)
+    tb = ctx.solve3d_batch([{"grid": shape, "model": s, "sources": [p for p, _, _ in srcs]}], opt, ex.F32)[0]
+    for i, (_, cell, off) in enumerate(srcs):
+        t_or = oracle.solve3d(s, shape, cell, off, n_sweeps=3, radius=3, near_fp64=True)
+        assert np.array_equal(_bits(t[i]), _bits(t_or)), i
+        assert np.array_equal(_bits(tb[i]), _bits(t_or)), i

@@ -121,6 +121,18 @@ def test_stepped_cold_solve_equals_one_call(oracle):
             assert cs.sweeps == 8 * (1 + 9)
 
 
+def test_near_fp64_mode_moves_fp32_towards_fp64(oracle):
+    """The oracle's near_fp64 mode (FP32 sweeps, factored updates in FP64): with the whole
+    grid factored, its field lies closer to the FP64 solve than plain FP32 does."""
+    rng = np.random.default_rng(8)
+    s, g, cell, off = _case3(rng, 21, 18, 16, 50., 50., 50., np.float32)
+    kw = dict(n_sweeps=3, radius=1000)
+    t64 = oracle.solve3d(s.astype(np.float64), g, cell, off, **kw)
+    e32 = np.abs(oracle.solve3d(s, g, cell, off, **kw) - t64).max()
+    e_near = np.abs(oracle.solve3d(s, g, cell, off, near_fp64=True, **kw) - t64).max()
+    assert e_near < e32
+
+
 def test_analytic_homogeneous_matches_closed_form(oracle):
     g = (21, 19, 17, 10., 11., 12.)
     t = oracle.linear_gradient3d(g, (53.0, 41.0, 77.0), 3000.0, 3000.0)
