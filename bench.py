@@ -36,6 +36,9 @@ N_SWEEPS_MAX, TOL, RADIUS = 10, 1e-5, 3
 SURFACE = [False]  # sources on the top surface (station tables by reciprocity)
 SLAB = [False]     # layered + GRF model with a dipping high-velocity slab (full-scale workload)
 PAIR = [False]  # pair_fields option of the GPU arm (set from the command line)
+# FP32 sweeps whose factored (near-source) updates run in FP64: the analytic factor
+# T0 = distance x source slowness, its gradient and tau in double (eikx_options.near_fp64)
+NEAR64 = [True]
 KERNEL = [0]    # sweep_kernel option of the GPU arm: 0 default, 1 node-step, 2 chunk-step
 L2_BYTES = 129 * 2 ** 20
 BYTES_PER_NODE_SWEEP = 12          # FP32: read T, read slowness, write T
@@ -148,7 +151,9 @@ def workload_config(fields, world):
                          f"top surface per step per GPU, one persistent launch per sweep" if SURFACE[0] else
                          f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, "
                          f"{fields} independent sources per step per GPU"),
-            "grid": [NX, NY, NZ], "h_m": H, "fields_per_step": fields, "precision": "fp32 sweeps, fp64 init",
+            "grid": [NX, NY, NZ], "h_m": H, "fields_per_step": fields,
+            "precision": ("fp32 sweeps; fp64 source init and factored (near-source) branch" if NEAR64[0] else
+                          "fp32 sweeps, fp64 source init"),
             "factored_radius": RADIUS, "tolerance_s": TOL, "max_iterations": N_SWEEPS_MAX,
             "l2": "flushed (write of 2x L2) between timed steps; per-step fields exceed L2",
             "parallelism": f"replicas x{world} (sources sharded, no collective)"}
@@ -200,7 +205,8 @@ def run_gpu(args):
     ctx.set_grid3d(NX, NY, NZ, H, H, H)
     v_host = torch.from_numpy(v.ravel()).pin_memory()
     ctx.set_nodal_velocity3d(v_host)
-    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, pair_fields=PAIR[0], sweep_kernel=KERNEL[0])
+    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, pair_fields=PAIR[0],
+                     sweep_kernel=KERNEL[0], near_fp64=NEAR64[0])
     out_dev = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device=f"cuda:{dev}")
     out_host = torch.empty((fields, NZ, NY, NX), dtype=torch.float32).pin_memory()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -260,7 +266,7 @@ def run_gpu(args):
     def prof_solve(o):
         ctx.solve3d(src, o, ex.F32, out=out_dev)
         return ctx.stats()
-    popts = dict(tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0],
+    popts = dict(tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0], near_fp64=NEAR64[0],
                  sweep_kernel=KERNEL[0])
     rl = refinement_roofline(prof_solve, ex.Options(n_sweeps=N_SWEEPS_MAX, **popts),
                              ex.Options(n_sweeps=0, **popts), BYTES_PER_NODE_SWEEP)
@@ -309,6 +315,12 @@ def run_gpu(args):
 
     if rank != 0:
         return
+    # the metric's own comparison: the learned warm start against the plain cold start
+    # (its training budget is bounded so that the default run ends within minutes)
+    learned = None
+    if not args.skip_learned and not SURFACE[0] and not SLAB[0]:
+        learned = learned_record(args.learn_models, args.learn_steps_default, accuracy=not args.skip_accuracy)
+        learned.pop("_conv")
     line = {
         "metric": METRIC, "value": value, "unit": "grids/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -327,6 +339,7 @@ def run_gpu(args):
                        "min_over_fields": int(min(i[0] for i in iters))},
         "single_source": single,
         "wall_ms_per_step": float(np.mean(wall)), "accuracy": acc, "tuning": tuning,
+        "learned": learned,
         "cpu_baseline": cpu_baseline(args.cpu_seconds, 1) if not args.skip_cpu else None,
     }
     print(json.dumps(line), flush=True)
@@ -356,17 +369,21 @@ def run_models(args):
     host_models = [{"grid": m["grid"], "model": torch.from_numpy(m["v"]).pin_memory(), "nodal": True,
                     "sources": [m["source"]],
                     "out": torch.empty((1,) + m["v"].shape, dtype=torch.float32).pin_memory()} for m in mine]
-    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS)
+    opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, near_fp64=NEAR64[0])
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
 
     acc = {}
     if rank == 0 and not args.skip_accuracy:
         t32 = ctx.solve3d_batch(dev_models, opt, ex.F32)
         t32 = [t.cpu().numpy().astype(np.float64) for t in t32]
-        o64 = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=1e-9, factored_radius=RADIUS)
+        o64 = ex.Options(n_sweeps=FP64_MAX_ITERATIONS, tolerance=FP64_TOL, factored_radius=RADIUS)
         t64 = ctx.solve3d_batch([dict(m, out=None) for m in dev_models], o64, ex.F64)
+        it64 = ctx.stats()["iterations_max"]
+        per = [float(np.abs(a - b).max()) for a, b in zip(t32, t64)]
         d = np.concatenate([np.abs(a - b).ravel() for a, b in zip(t32, t64)])
-        acc = {"max_err_vs_fp64_s": float(d.max()), "rms_err_vs_fp64_s": float(np.sqrt(np.mean(d ** 2)))}
+        acc = {"max_err_vs_fp64_s": float(d.max()), "rms_err_vs_fp64_s": float(np.sqrt(np.mean(d ** 2))),
+               "meets_1e-4": bool(d.max() <= 1e-4), "models_over_1e-4": int(sum(e > 1e-4 for e in per)),
+               "fp64_iterations_max": it64, "fp64_converged": bool(it64 < FP64_MAX_ITERATIONS)}
 
     for _ in range(args.warmup):
         ctx.solve3d_batch(dev_models, opt, ex.F32)
@@ -391,7 +408,8 @@ def run_models(args):
         ctx.solve3d_batch(dev_models, o, ex.F32)
         return ctx.stats()
     rl = refinement_roofline(prof_solve,
-                             ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True),
+                             ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True,
+                                        near_fp64=NEAR64[0]),
                              ex.Options(n_sweeps=0, tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True),
                              BYTES_PER_NODE_SWEEP)
     achieved = rl["achieved"]
@@ -414,7 +432,8 @@ def run_models(args):
         "config": {"workload": f"{n} models of uneven size (nx, ny in [64, 256], nz in [32, 128], h=100 m) "
                                f"per step per GPU, one source each, one schedule",
                    "nodes_per_step": nodes, "grids_min": min(grids), "grids_max": max(grids),
-                   "precision": "fp32 sweeps, fp64 init", "factored_radius": RADIUS, "tolerance_s": TOL,
+                   "precision": ("fp32 sweeps; fp64 source init and factored (near-source) branch" if NEAR64[0]
+                                 else "fp32 sweeps, fp64 source init"), "factored_radius": RADIUS, "tolerance_s": TOL,
                    "max_iterations": N_SWEEPS_MAX, "l2": "flushed (write of 2x L2) between timed steps",
                    "parallelism": f"replicas x{world} (models sharded, no collective)"},
         "roofline": {"bound": "hbm", "kernel": "sweep3ChunkKernel<float,uniform,batch>", "achieved": achieved,
@@ -576,16 +595,17 @@ LEARN_GRID = (128, 128, 64, 50.0)
 PREDICT_LAUNCHES = 22   # features, 14 convolutions, 3 poolings, 3 up-and-concats, the head
 
 
-def run_learned(args):
-    """The learned warm start on 128x128x64 nodes, h = 50 m.  Training data: `fields`
-    random smooth models (Gaussian random fields, 1500-8000 m/s, correlation length
-    0.5-3 km) with 8 seeded sources each, solved cold by the library.  The network is
-    trained on them by its own kernels (Adam, batch 8).  Evaluation on 4 held-out models
-    (32 fields): cold-start solves against warm starts (prediction x 1.02, residual gate,
-    sweeps to the tolerance) from the trained network and from T0 alone (the untrained
-    network).  The line's value is the cold-start grids/s of the held-out fields, the
-    path that meets the error bound; the learned path's rate, sweeps and deviation from
-    the cold start are under "learned"."""
+def learned_record(train_models, learn_steps, warmup=1, accuracy=True, per_model=8, test_models=4):
+    """The learned warm start against the plain cold start on 128x128x64 nodes, h = 50 m.
+
+    Training data: `train_models` random smooth models (Gaussian random fields, 1500-8000
+    m/s, correlation length 0.5-3 km) with `per_model` seeded sources each, solved cold by
+    the library; the network is trained on them by its own kernels (Adam, batch 8,
+    `learn_steps` steps).  Evaluation on `test_models` held-out models: cold-start solves
+    against warm starts from the network's prediction (prediction time included), with the
+    one-sided residual gate (prediction x 1.02), the two-sided gate (prediction x 1.0 and
+    x 1.02), and from T0 alone (the untrained network, x 1.02).  Errors are against FP64
+    solves of the same sources run to convergence."""
     import torch
     import eikonalxx_gb300 as ex
     from eikonalxx_gb300 import warmstart as ws
@@ -593,13 +613,13 @@ def run_learned(args):
     nx, ny, nz, h = LEARN_GRID
     grid = (nx, ny, nz, h, h, h)
     dev = torch.cuda.current_device()
-    per_model, test_models, batch = 8, 4, 8
+    batch = 8
     ctx = ex.Context(dev)
-    opt = ex.Options(n_sweeps=20, tolerance=TOL, factored_radius=RADIUS)
+    opt = ex.Options(n_sweeps=20, tolerance=TOL, factored_radius=RADIUS, near_fp64=NEAR64[0])
     t = time.perf_counter()
-    data = ws.generate_fields(ctx, grid, args.fields + test_models, per_model, seed=MODEL_SEED + 4, options=opt)
+    data = ws.generate_fields(ctx, grid, train_models + test_models, per_model, seed=MODEL_SEED + 4, options=opt)
     gen_s = time.perf_counter() - t
-    n_train = args.fields * per_model
+    n_train = train_models * per_model
     train_idx = np.arange(n_train)
     test_idx = np.arange(n_train, n_train + test_models * per_model)
     net = ws.WarmNet(grid, batch=batch, seed=MODEL_SEED)
@@ -607,56 +627,70 @@ def run_learned(args):
     net.set_params(np.zeros_like(p0))
     base_loss = ws.evaluate_loss(net, data, test_idx)
     net.set_params(p0)
-    steps = args.learn_steps
     t = time.perf_counter()
-    losses = ws.train(net, data, steps=steps, lr=1e-3, seed=MODEL_SEED + 5, fields=train_idx)
+    losses = ws.train(net, data, steps=learn_steps, lr=1e-3, seed=MODEL_SEED + 5, fields=train_idx)
     train_s = time.perf_counter() - t
     test_loss = ws.evaluate_loss(net, data, test_idx)
     p_trained = net.get_params()
     prof = net.profile_step(ws.samples_of(data, train_idx[:batch]), 0.0)   # lr 0: parameters unchanged
     net.set_params(p_trained)
 
-    nodes = nx * ny * nz
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
-    rows = {"cold": [], "network": [], "T0": []}
+    variants = {"network x1.02, one-sided gate": (p_trained, 1.02, 0),
+                "network x1.0, two-sided gate": (p_trained, 1.0, 1),
+                "network x1.02, two-sided gate": (p_trained, 1.02, 1),
+                "T0 x1.02 (untrained), one-sided gate": (np.zeros_like(p_trained), 1.02, 0)}
+    rows = {"cold": []}
+    rows.update({k: [] for k in variants})
     dev_cold = torch.empty((per_model, nz, ny, nx), dtype=torch.float32, device=f"cuda:{dev}")
     dev_warm = torch.empty_like(dev_cold)
     init = torch.empty_like(dev_cold)
-    max_fp64 = 0.0
     launches = 0
-    with ClockSampler(dev) as clk:
-        for k in range(test_models):
-            idx = test_idx[k * per_model:(k + 1) * per_model]
-            m = int(data["model"][idx[0]])
-            ctx.set_grid3d(nx, ny, nz, h, h, h)
-            ctx.set_nodal_velocity3d(data["velocity"][m])
-            src = data["sources"][idx]
-            for _ in range(args.warmup):
-                ctx.solve3d(src, opt, ex.F32, out=dev_cold)
+    o64 = ex.Options(n_sweeps=FP64_MAX_ITERATIONS, tolerance=FP64_TOL, factored_radius=RADIUS)
+    fp64_iters = 0
+    for k in range(test_models):
+        idx = test_idx[k * per_model:(k + 1) * per_model]
+        m = int(data["model"][idx[0]])
+        ctx.set_grid3d(nx, ny, nz, h, h, h)
+        ctx.set_nodal_velocity3d(data["velocity"][m])
+        src = data["sources"][idx]
+        t64 = None
+        if accuracy:
+            t64 = ctx.solve3d(src, o64, ex.F64)
+            fp64_iters = max(fp64_iters, ctx.stats()["iterations_max"])
+        for _ in range(warmup):
+            ctx.solve3d(src, opt, ex.F32, out=dev_cold)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ctx.solve3d(src, opt, ex.F32, out=dev_cold)
+        st = ctx.stats()
+        launches += st["kernel_launches"]
+        cold = dev_cold.cpu().numpy().astype(np.float64)
+        row = {"ms": st["device_ms"], "iterations": st["iterations_max"]}
+        if t64 is not None:
+            row["max_err_fp64_s"] = float(np.max(np.abs(cold - t64)))
+        rows["cold"].append(row)
+        for name, (params, inflate, gate) in variants.items():
+            net.set_params(params)
+            wopt = ex.Options(n_sweeps=20, tolerance=TOL, factored_radius=RADIUS, warm_gate=gate,
+                              near_fp64=NEAR64[0])
             flush.fill_(1.0)
             torch.cuda.synchronize()
-            ctx.solve3d(src, opt, ex.F32, out=dev_cold)
+            t = time.perf_counter()
+            net.predict(ws.samples_of(data, idx, with_target=False), inflate=inflate, out=init)
+            torch.cuda.synchronize()
+            pred_ms = (time.perf_counter() - t) * 1e3
+            ctx.solve3d_warm(src, init, wopt, ex.F32, gate_tol=1e-6, out=dev_warm)
             st = ctx.stats()
-            launches += st["kernel_launches"]
-            rows["cold"].append({"ms": st["device_ms"], "iterations": st["iterations_max"]})
-            cold = dev_cold.cpu().numpy().astype(np.float64)
-            if not args.skip_accuracy:
-                t64 = ctx.solve3d(src, ex.Options(n_sweeps=20, tolerance=1e-9, factored_radius=RADIUS), ex.F64)
-                max_fp64 = max(max_fp64, float(np.max(np.abs(cold - t64))))
-            for name, params in (("network", p_trained), ("T0", np.zeros_like(p_trained))):
-                net.set_params(params)
-                flush.fill_(1.0)
-                torch.cuda.synchronize()
-                t = time.perf_counter()
-                net.predict(ws.samples_of(data, idx, with_target=False), inflate=1.02, out=init)
-                pred_ms = (time.perf_counter() - t) * 1e3
-                ctx.solve3d_warm(src, init, opt, ex.F32, gate_tol=1e-6, out=dev_warm)
-                st = ctx.stats()
-                launches += st["kernel_launches"] + PREDICT_LAUNCHES
-                d = dev_warm.cpu().numpy().astype(np.float64) - cold
-                rows[name].append({"ms": st["device_ms"] + pred_ms, "predict_ms": pred_ms,
-                                   "iterations": st["iterations_max"], "reset_nodes": st["reset_nodes"],
-                                   "max_dev_s": float(np.max(np.abs(d))), "rms_dev_s": float(np.sqrt(np.mean(d * d)))})
+            launches += st["kernel_launches"] + PREDICT_LAUNCHES
+            warm = dev_warm.cpu().numpy().astype(np.float64)
+            d = warm - cold
+            row = {"ms": st["device_ms"] + pred_ms, "predict_ms": pred_ms, "iterations": st["iterations_max"],
+                   "reset_nodes": st["reset_nodes"], "max_dev_s": float(np.max(np.abs(d))),
+                   "rms_dev_s": float(np.sqrt(np.mean(d * d)))}
+            if t64 is not None:
+                row["max_err_fp64_s"] = float(np.max(np.abs(warm - t64)))
+            rows[name].append(row)
     net.set_params(p_trained)
     fields = test_models * per_model
 
@@ -666,6 +700,9 @@ def run_learned(args):
     def summary(r):
         out = {"grids_per_s": rate(r), "ms_per_field": sum(x["ms"] for x in r) / fields,
                "iterations_max": max(x["iterations"] for x in r)}
+        if "max_err_fp64_s" in r[0]:
+            out["max_err_vs_fp64_s"] = max(x["max_err_fp64_s"] for x in r)
+            out["meets_1e-4"] = bool(out["max_err_vs_fp64_s"] <= 1e-4)
         if "max_dev_s" in r[0]:
             out.update({"max_dev_from_cold_s": max(x["max_dev_s"] for x in r),
                         "rms_dev_from_cold_s": float(np.sqrt(np.mean([x["rms_dev_s"] ** 2 for x in r]))),
@@ -673,40 +710,60 @@ def run_learned(args):
                         "reset_nodes": int(sum(x["reset_nodes"] for x in r))})
         return out
 
+    cold_rate = rate(rows["cold"])
+    var = {k: dict(summary(rows[k]), speedup_vs_cold=rate(rows[k]) / cold_rate) for k in variants}
+    ok = [v["speedup_vs_cold"] for v in var.values() if v.get("meets_1e-4")]
     conv_ms = sum(prof["ms"][k] for k in ("forward_conv", "input_grad_conv", "weight_grad"))
     conv_fl = sum(prof["flops"].values())
+    return {
+        "workload": f"learned warm start, {nx}x{ny}x{nz} h={h:g} m: {train_models} training models x {per_model} "
+                    f"sources ({n_train} solver-generated fields), {learn_steps} Adam steps of batch {batch}; "
+                    f"{test_models} held-out models x {per_model} sources, warm starts vs cold starts",
+        "cold": summary(rows["cold"]), "variants": var,
+        "learned_vs_plain": var["network x1.02, one-sided gate"]["speedup_vs_cold"],
+        "best_speedup_meeting_1e-4": max(ok) if ok else None,
+        "fp64_iterations_max": fp64_iters if accuracy else None,
+        "test_loss": test_loss, "tau_1_loss": base_loss,
+        "train_loss_first_last": [float(np.mean(losses[:20])), float(np.mean(losses[-20:]))],
+        "generate_s": gen_s, "train_s": train_s, "train_steps_per_s": learn_steps / train_s,
+        "conv_tflops": conv_fl / (conv_ms / 1e3) / 1e12, "step_profile": prof, "gpu_launches": int(launches),
+        "_conv": (conv_fl, conv_ms),
+    }
+
+
+def run_learned(args):
+    """The learned workload's own line: value = the cold-start grids/s of the held-out
+    fields (the path that meets the error bound); the learned variants under "learned";
+    the roofline is the network's convolutions (tensor-bound) over one training step."""
+    import torch
+
+    dev = torch.cuda.current_device()
+    with ClockSampler(dev) as clk:
+        rec = learned_record(args.fields, args.learn_steps, warmup=args.warmup, accuracy=not args.skip_accuracy)
+    conv_fl, conv_ms = rec.pop("_conv")
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             tpeak, tkind = float(json.load(f)["bf16_tflops"]), "measured"
     except Exception:
         tpeak, tkind = 1900.0, "fallback"
     achieved = conv_fl / (conv_ms / 1e3) / 1e12
-    cold_rate = rate(rows["cold"])
+    cold_rate = rec["cold"]["grids_per_s"]
+    nx, ny, nz, h = LEARN_GRID
     line = {
         "metric": METRIC, "value": cold_rate, "unit": "grids/s", "n_gpus": 1, "steps": 1,
-        "warmup": args.warmup, "ms_per_step": 1e3 * fields / cold_rate, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": rec["cold"]["ms_per_field"] * 32, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 sweeps, bf16 network",
         "data": "synthetic (seeded random smooth models, seeded sources; fields solved by the library)",
-        "config": {"workload": f"learned warm start, {nx}x{ny}x{nz} h={h:g} m: {args.fields} training models x "
-                               f"{per_model} sources, {test_models} held-out models x {per_model} sources",
-                   "training_fields": int(n_train), "train_steps": steps, "batch": batch,
-                   "precision": "fp32 sweeps, fp64 init; network bf16 with fp32 accumulation",
-                   "factored_radius": RADIUS, "tolerance_s": TOL, "inflate": 1.02, "gate_tol_s": 1e-6,
-                   "l2": "flushed (write of 2x L2) before each timed solve"},
-        "learned": {"network": summary(rows["network"]), "T0_start": summary(rows["T0"]),
-                    "cold": summary(rows["cold"]), "speedup_vs_cold": rate(rows["network"]) / cold_rate,
-                    "meets_1e-4_s_vs_cold": max(x["max_dev_s"] for x in rows["network"]) <= 1e-4,
-                    "test_loss": test_loss, "tau_1_loss": base_loss,
-                    "train_loss_first_last": [float(np.mean(losses[:20])), float(np.mean(losses[-20:]))],
-                    "generate_s": gen_s, "train_s": train_s, "train_steps_per_s": steps / train_s,
-                    "step_profile": prof},
-        "roofline": {"bound": "tensor", "kernel": "convKernel + wgradKernel (BF16 mma.sync, FP32 accumulate)",
+        "config": {"workload": rec["workload"], "precision": "fp32 sweeps, fp64 init; network bf16 with fp32 "
+                                                            "accumulation", "factored_radius": RADIUS,
+                   "tolerance_s": TOL, "gate_tol_s": 1e-6, "l2": "flushed (write of 2x L2) before each timed solve"},
+        "learned": rec,
+        "roofline": {"bound": "tensor", "kernel": "convTcKernel + convKernel + wgradKernel (BF16, FP32 accumulate)",
                      "achieved": achieved, "peak": tpeak, "peak_kind": tkind, "unit": "TFLOP/s",
                      "frac": achieved / tpeak, "traffic": None,
                      "note": "one training step of batch 8; algorithmic FLOPs 2 x nodes x 27 x in x out per "
                              "convolution, forward, input-gradient and weight-gradient passes"},
-        "accuracy": {"cold_max_err_vs_fp64_s": max_fp64 if not args.skip_accuracy else None},
-        "gpu_launches": int(launches), "clocks": clk.summary(),
+        "gpu_launches": rec["gpu_launches"], "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
 
@@ -772,6 +829,7 @@ class CpuColdSolves:
         v, src = make_workload(64 * self.threads)
         self.src = src
         self.slow = self.orc.nodal_to_cell3d(v.ravel(), NX, NY, NZ, 0)   # FP32, as the GPU forms it
+        self.orc.lib.oracle_set_near_fp64(int(NEAR64[0]))                 # the GPU arm's precision
         self.next_src = list(range(self.threads))    # thread t takes sources t, t + T, t + 2T, ...
         self.cur = [self._start(t) for t in range(self.threads)]
         self.timed = {}          # source index -> sweeps run inside timed steps
@@ -887,6 +945,11 @@ def main():
     ap.add_argument("--fields", type=int, default=None,
                     help="sources (plain: 64, stations: 64, full: 256) or models (models: 32) per step per GPU")
     ap.add_argument("--learn-steps", type=int, default=2000, help="learned: training steps")
+    ap.add_argument("--learn-models", type=int, default=256,
+                    help="plain: training models of the learned sub-record (8 fields each)")
+    ap.add_argument("--learn-steps-default", type=int, default=1500,
+                    help="plain: training steps of the learned sub-record")
+    ap.add_argument("--skip-learned", action="store_true", help="plain: leave out the learned sub-record")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -896,6 +959,8 @@ def main():
                     help="3D sweep kernel: 0 default (chunk-step), 1 node-step, 2 chunk-step")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip eikx_autotune3d before timing (default chunk-step 8x4 configuration)")
+    ap.add_argument("--fp32-near", action="store_true",
+                    help="3D: factored (near-source) updates in FP32 too, instead of FP64")
     ap.add_argument("--pair-fields", action="store_true",
                     help="sweep two fields per lane (the paired FP32 kernel) instead of one")
     ap.add_argument("--profile-case", action="store_true",
@@ -919,6 +984,7 @@ def main():
         args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8, "models": 32,
                        "learned": 2500}.get(args.workload, 64)
     PAIR[0] = args.pair_fields
+    NEAR64[0] = not args.fp32_near
     KERNEL[0] = args.sweep_kernel
     if args.profile_case:
         if args.workload == "learned":

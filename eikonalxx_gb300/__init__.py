@@ -39,7 +39,7 @@ EXPORTED = [
     "eikx_ray_options_default", "eikx_trace_rays2d",
     "eikx_warmnet_create", "eikx_warmnet_destroy", "eikx_warmnet_num_params", "eikx_warmnet_get_params",
     "eikx_warmnet_set_params", "eikx_warmnet_train_step", "eikx_warmnet_gradients", "eikx_warmnet_predict",
-    "eikx_warmnet_profile_step",
+    "eikx_warmnet_profile_step", "eikx_warmnet_set_test_hooks",
 ]
 CELL_SLOWNESS, NODAL_VELOCITY = 0, 1
 
@@ -181,6 +181,7 @@ def load(path=None):
     lib.eikx_warmnet_gradients.argtypes = [vp, sp, c_int, fp, dp]
     lib.eikx_warmnet_predict.argtypes = [vp, sp, c_int, c_double, vp, c_int, dp]
     lib.eikx_warmnet_profile_step.argtypes = [vp, sp, c_int, ctypes.c_float, dp, dp]
+    lib.eikx_warmnet_set_test_hooks.argtypes = [vp, c_int, c_int]
     lib.eikx_tuning_save.argtypes = [vp, ctypes.c_char_p]
     lib.eikx_tuning_load.argtypes = [vp, ctypes.c_char_p]
     for name in EXPORTED:

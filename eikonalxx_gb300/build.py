@@ -35,7 +35,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
 CUDA_SOURCES = ["sweep.cu", "sweep_pair.cu", "sweep_chunk_8x4.cu", "sweep_chunk_4x8.cu", "sweep_chunk_16x2.cu", "fields.cu", "post.cu", "rays.cu", "capi.cu", "noalloc.cu",
                 "warmnet_kernels.cu", "warmnet.cu"]
 CXX_SOURCES = ["levels.cpp", "api/options.cpp", "api/geometry.cpp", "api/source.cpp", "api/model.cpp",
-               "api/graph3d.cpp", "api/solver3d.cpp", "api/solver2d.cpp", "api/ray.cpp"]
+               "api/graph3d.cpp", "api/solver3d.cpp", "api/solver2d.cpp", "api/ray.cpp", "api/vtk.cpp"]
 
 
 def _nvcc():

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 #include "eikonalxx/geometry2d.hpp"
+#include "eikonalxx/io/vtkRectilinearGrid2d.hpp"
+#include "eikonalxx/io/vtkRectilinearGrid3d.hpp"
 #include "eikonalxx/geometry3d.hpp"
 #include "eikonalxx/model2d.hpp"
 #include "eikonalxx/model3d.hpp"
@@ -163,9 +165,14 @@ template <class T> T Model3D<T>::getSlowness(const int ix, const int iy, const i
         throw std::invalid_argument("iCellZ = " + std::to_string(iz) + " must be in range [0," + std::to_string(ncz) + ")");
     return pImpl->slowness[(static_cast<size_t>(iz) * ncy + iy) * ncx + ix];
 }
-template <class T> void Model3D<T>::writeVTK(const std::string &, const std::string &) const
+// src/model3d.cpp:470-480: the cell velocities, binary.
+template <class T> void Model3D<T>::writeVTK(const std::string &fileName, const std::string &title) const
 {
-    throw std::runtime_error("VTK output is not part of eikonalxx_gb300");
+    const auto v = getVelocities();   // throws
+    IO::VTKRectilinearGrid3D vtk;
+    vtk.open(fileName, pImpl->geometry, title, true);
+    vtk.writeCellularDataset(title, v.data(), Ordering3D::Natural);
+    vtk.close();
 }
 
 //------------------------------------------------------------------------------ 2D
@@ -291,9 +298,14 @@ template <class T> T Model2D<T>::getSlowness(const int ix, const int iz) const
         throw std::invalid_argument("iCellZ = " + std::to_string(iz) + " must be in range [0," + std::to_string(ncz) + ")");
     return pImpl->slowness[static_cast<size_t>(iz) * ncx + ix];
 }
-template <class T> void Model2D<T>::writeVTK(const std::string &, const std::string &) const
+// src/model2d.cpp:435-445: the cell velocities, binary.
+template <class T> void Model2D<T>::writeVTK(const std::string &fileName, const std::string &title) const
 {
-    throw std::runtime_error("VTK output is not part of eikonalxx_gb300");
+    const auto v = getVelocities();   // throws
+    IO::VTKRectilinearGrid2D vtk;
+    vtk.open(fileName, pImpl->geometry, title, true);
+    vtk.writeCellularDataset(title, v.data(), Ordering2D::Natural);
+    vtk.close();
 }
 
 template class EikonalXX::Model3D<double>;

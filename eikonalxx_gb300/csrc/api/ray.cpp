@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 #include "eikonalxx/geometry2d.hpp"
+#include "eikonalxx/io/vtkLines2d.hpp"
 #include "eikonalxx/ray/gradientTracer2d.hpp"
 #include "eikonalxx/ray/gradientTracerOptions.hpp"
 #include "eikonalxx/ray/path2d.hpp"
@@ -482,10 +483,30 @@ std::vector<Path2D> GradientTracer2D::getRayPaths() const
     if (!haveRayPaths()) throw std::runtime_error("Ray paths not computed");
     return pImpl->paths;
 }
-void GradientTracer2D::writeVTK(const std::string &, const std::string &)
+// src/ray/gradientTracer2d.cpp:617-655: each path as a polyline through its segments'
+// start points and the last segment's end point.
+void GradientTracer2D::writeVTK(const std::string &fileName, const std::string &title)
 {
     if (!haveRayPaths()) throw std::runtime_error("Ray paths not computed");
-    throw std::runtime_error("VTK output is not part of eikonalxx_gb300");
+    IO::VTKLines2D vtk;
+    vtk.open(fileName, pImpl->geometry, title);
+    if (!pImpl->paths.empty()) {
+        std::vector<std::vector<std::pair<double, double>>> lines;
+        lines.reserve(pImpl->paths.size());
+        for (const auto &path : pImpl->paths) {
+            std::vector<std::pair<double, double>> line;
+            const size_t n = path.size();
+            line.reserve(n + 1);
+            for (size_t i = 0; i < n; ++i) {
+                const auto &seg = path.at(i);
+                line.emplace_back(seg.getStartPoint().getPositionInX(), seg.getStartPoint().getPositionInZ());
+                if (i == n - 1) line.emplace_back(seg.getEndPoint().getPositionInX(), seg.getEndPoint().getPositionInZ());
+            }
+            lines.push_back(std::move(line));
+        }
+        vtk.write(lines);
+    }
+    vtk.close();
 }
 
 template void GradientTracer2D::trace(const EikonalXX::AbstractBaseClass::ISolver2D<double> &);

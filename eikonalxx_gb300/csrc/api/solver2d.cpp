@@ -6,6 +6,7 @@
 #include <utility>
 #include <vector>
 #include "eikonalxx/geometry2d.hpp"
+#include "eikonalxx/io/vtkRectilinearGrid2d.hpp"
 #include "eikonalxx/model2d.hpp"
 #include "eikonalxx/solver2d.hpp"
 #include "eikonalxx/solverOptions.hpp"
@@ -213,9 +214,17 @@ template <class T> const T *Solver2D<T>::getTravelTimeGradientFieldPointer() con
     if (!haveTravelTimeGradientField()) throw std::runtime_error("Travel time gradient field not computed");
     return pImpl->gradient.data();
 }
-template <class T> void Solver2D<T>::writeVTK(const std::string &, const std::string &, bool) const
+// src/solver2d.cpp:946-964: the travel times (and the gradient as vectors), binary.
+template <class T> void Solver2D<T>::writeVTK(const std::string &fileName, const std::string &title,
+                                              const bool writeGradient) const
 {
-    throw std::runtime_error("VTK output is not part of eikonalxx_gb300");
+    const T *t = getTravelTimeFieldPointer();                                  // throws
+    const T *g = writeGradient ? getTravelTimeGradientFieldPointer() : nullptr;  // throws
+    IO::VTKRectilinearGrid2D vtk;
+    vtk.open(fileName, pImpl->geometry, title, true);
+    vtk.writeNodalDataset(title, t, Ordering2D::Natural);
+    if (writeGradient) vtk.writeNodalVectorDataset(title + "_gradient", g, Ordering2D::Natural);
+    vtk.close();
 }
 
 template class EikonalXX::Solver2D<double>;

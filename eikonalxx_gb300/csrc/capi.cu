@@ -111,7 +111,7 @@ struct EpochMirror {
 
 struct Workspace {
     DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, pairs, init,
-        resetCount;
+        resetCount, srcs64;
     EpochMirror epochMirror;
     PinnedBuf stage;
     std::vector<int> orderKey;   // (tilesY, tilesZ, nFields, dim) of the uploaded order table
@@ -121,7 +121,7 @@ struct Workspace {
 // slowness and mailbox packed into one allocation each, plus the cached schedule graph.
 struct BatchWorkspace {
     DevBuf tt, sp, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, units,
-        slow64, input, badFlag;
+        slow64, input, badFlag, srcs64;
     EpochMirror epochMirror;
     PinnedBuf stage, srcCells, iterFlags;
     std::vector<double> key;                 // what the cached graph was captured for
@@ -332,18 +332,14 @@ template <class T> int precOf();
 template <> int precOf<float>() { return EIKX_F32; }
 template <> int precOf<double>() { return EIKX_F64; }
 
-// Shared solve driver for 2D and 3D.
 // FP64 factored branch of an FP32 sweep (eikx_options.near_fp64): the source offsets,
 // the source-cell slowness as the sweep holds it, and the grid spacing, in FP64.
 template <class T>
-void setNearFp64(eikx::SourceT<T> &src, const std::array<double, 3> &off, double s, double dx, double dy, double dz) {
-    if constexpr (sizeof(T) == 4) {
-        src.nearFp64 = 1;
-        src.xd = off[0]; src.yd = off[1]; src.zd = off[2];
-        src.sd = static_cast<double>(static_cast<T>(s));
-        src.dxd = dx; src.dyd = dy; src.dzd = dz;
-    }
+eikx::SourceFp64 sourceFp64(const std::array<double, 3> &off, double s, double dx, double dy, double dz) {
+    return eikx::SourceFp64{off[0], off[1], off[2], static_cast<double>(static_cast<T>(s)), dx, dy, dz};
 }
+
+// Shared solve driver for 2D and 3D.
 
 template <class T, int DIM>
 eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options o, void *tOut,
@@ -362,6 +358,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     // sources: cell, offsets, source-cell slowness (reference Source3D / Solver3D::solve);
     // the slownesses are read from the device model, one value per source
     std::vector<eikx::SourceT<T>> srcT(nSrc);
+    std::vector<eikx::SourceFp64> srcT64;
     std::vector<eikx::Corner3> corners(nSrc);
     std::vector<size_t> srcCells(nSrc);
     std::vector<std::array<double, 3>> srcOffs(nSrc);
@@ -395,7 +392,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     for (int i = 0; i < nSrc; ++i) {
         const double s = srcSlow[i];
         srcT[i].sSrc = static_cast<T>(s);
-        if (DIM == 3 && o.near_fp64) setNearFp64(srcT[i], srcOffs[i], s, dx, dy, dz);
+        if (DIM == 3 && P == EIKX_F32 && o.near_fp64) srcT64.push_back(sourceFp64<T>(srcOffs[i], s, dx, dy, dz));
         // corner init: slowness as the field type holds it, offsets in FP64
         corners[i] = eikx::Corner3{srcT[i].isx, srcT[i].isy, srcT[i].isz, srcOffs[i][0], srcOffs[i][1], srcOffs[i][2],
                                    static_cast<double>(static_cast<T>(s))};
@@ -464,7 +461,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     const int mailWords = paired ? 2 : static_cast<int>(sizeof(T) / 4);   // tagged 64-bit words per unit
     const size_t mboxBytes = static_cast<size_t>(nProgress) * (DIM == 3 ? ly + lz : 1) * Px * mailWords * 8;
     const void *before[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
-                            w.iterations.p, w.order.p, w.srcs.p, w.corners.p};
+                            w.iterations.p, w.order.p, w.srcs.p, w.corners.p, w.srcs64.p};
     EIKX_CUDA(w.tt.ensure(ttBytes));
     if (w.mbox.bytes < mboxBytes || !w.mbox.p) {
         // fresh words carry tag 0, which no sweep uses
@@ -484,8 +481,9 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     EIKX_CUDA(w.srcs.ensure(static_cast<size_t>(nSrc) * sizeof(eikx::SourceT<T>)));
     EIKX_CUDA(w.corners.ensure(static_cast<size_t>(nSrc) * sizeof(eikx::Corner3)));
     EIKX_CUDA(w.pairs.ensure(static_cast<size_t>(nUnits) * sizeof(int2)));
+    if (!srcT64.empty()) EIKX_CUDA(w.srcs64.ensure(srcT64.size() * sizeof(eikx::SourceFp64)));
     const void *after[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
-                           w.iterations.p, w.order.p, w.srcs.p, w.corners.p};
+                           w.iterations.p, w.order.p, w.srcs.p, w.corners.p, w.srcs64.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) dropGraph(c);
 
     // small uploads through pinned staging
@@ -504,8 +502,9 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     const size_t srcBytes = srcT.size() * sizeof(eikx::SourceT<T>);
     const size_t cornerBytes = corners.size() * sizeof(eikx::Corner3);
     const size_t orderBytes = order.size() * sizeof(int);
+    const size_t src64Bytes = srcT64.size() * sizeof(eikx::SourceFp64);
     EIKX_CUDA(cudaStreamSynchronize(c->stream));  // staging buffer reuse
-    EIKX_CUDA(w.stage.ensure(srcBytes + cornerBytes + orderBytes + pairBytes + 64));
+    EIKX_CUDA(w.stage.ensure(srcBytes + cornerBytes + orderBytes + pairBytes + src64Bytes + 64));
     char *stage = static_cast<char *>(w.stage.p);
     std::memcpy(stage, srcT.data(), srcBytes);
     std::memcpy(stage + srcBytes, corners.data(), cornerBytes);
@@ -521,6 +520,13 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         char *pstage = stage + srcBytes + cornerBytes + orderBytes;
         std::memcpy(pstage, pairs.data(), pairBytes);
         EIKX_CUDA(cudaMemcpyAsync(w.pairs.p, pstage, pairBytes, cudaMemcpyHostToDevice, c->stream));
+    }
+    const eikx::SourceFp64 *srcs64 = nullptr;
+    if (!srcT64.empty()) {
+        char *qstage = stage + srcBytes + cornerBytes + orderBytes + pairBytes;
+        std::memcpy(qstage, srcT64.data(), src64Bytes);
+        EIKX_CUDA(cudaMemcpyAsync(w.srcs64.p, qstage, src64Bytes, cudaMemcpyHostToDevice, c->stream));
+        srcs64 = w.srcs64.as<eikx::SourceFp64>();
     }
 
     if (warm) {
@@ -615,7 +621,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
                                                dz, w.corners.as<eikx::Corner3>(), w.srcs.as<eikx::SourceT<T>>(),
                                                c->slow3.as<double>(), o.factored_radius, uniform, static_cast<T>(dx),
                                                spacing3<T>(dx, dy, dz), gateTol, o.warm_gate == 1 ? 1 : 0,
-                                               o.init_fp64 ? 1 : 0,
+                                               o.init_fp64 ? 1 : 0, srcs64,
                                                w.resetCount.as<unsigned long long>(), c->stream));
         } else if (DIM == 3)
             EIKX_CUDA(eikx::launchInit3<T>(w.tt.as<T>(), nSrc, fieldStride, Px, nx, ny, nz, dx, dy, dz,
@@ -635,7 +641,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
                 a.srcs = w.srcs.as<eikx::SourceT<T>>(); a.st = st; a.buf = buf; a.residualSlot = slot;
                 a.sweepIndex = sweepsLaunched;
                 a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = static_cast<T>(dx);
-                a.nearFp64 = P == EIKX_F32 && o.near_fp64 ? 1 : 0;
+                a.srcs64 = srcs64;
                 const T tdx = static_cast<T>(dx), tdy = static_cast<T>(dy), tdz = static_cast<T>(dz);
                 eikx::Spacing3<T> g;
                 g.dx = tdx; g.dy = tdy; g.dz = tdz;
@@ -939,8 +945,9 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     const int nSweeps = std::max(0, o.n_sweeps);
     const int resStride = nSweepKinds * (1 + nSweeps);
 
+    const bool near64 = sizeof(T) == 4 && o.near_fp64;
     const void *before[] = {w.tt.p, w.sp.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p, w.iterations.p,
-                            w.order.p, w.srcs.p, w.corners.p, w.units.p};
+                            w.order.p, w.srcs.p, w.corners.p, w.units.p, w.srcs64.p};
     EIKX_CUDA(w.tt.ensure(ttElems * sizeof(T)));
     EIKX_CUDA(w.sp.ensure(spElems * sizeof(T)));
     if (w.mbox.bytes < mboxWords * 8 || !w.mbox.p) {
@@ -965,8 +972,9 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     EIKX_CUDA(w.input.ensure(maxInBytes));
     EIKX_CUDA(w.badFlag.ensure(sizeof(int)));
     EIKX_CUDA(w.srcCells.ensure(static_cast<size_t>(nUnits) * sizeof(double) + sizeof(int)));
+    if (near64) EIKX_CUDA(w.srcs64.ensure(static_cast<size_t>(nUnits) * sizeof(eikx::SourceFp64)));
     const void *after[] = {w.tt.p, w.sp.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p, w.iterations.p,
-                           w.order.p, w.srcs.p, w.corners.p, w.units.p};
+                           w.order.p, w.srcs.p, w.corners.p, w.units.p, w.srcs64.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) w.dropGraph();
 
     // models -> cell slowness (FP64, natural) -> two padded copies in the sweep precision;
@@ -1047,13 +1055,15 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     EIKX_CUDA(cudaMemcpyAsync(bad, w.badFlag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     EIKX_CUDA(cudaStreamSynchronize(c->stream));
     if (*bad) return fail(EIKX_ERR_INVALID, "Non-positive velocities detected");
+    std::vector<eikx::SourceFp64> srcT64;
     for (int u = 0; u < nUnits; ++u) {
         const double sc = srcCell[u];
         srcT[u].xs = static_cast<T>(offs[u][0]);
         srcT[u].ys = static_cast<T>(offs[u][1]);
         srcT[u].zs = static_cast<T>(offs[u][2]);
         srcT[u].sSrc = static_cast<T>(sc);
-        if (o.near_fp64) setNearFp64(srcT[u], offs[u], sc, unitSpacing[u][0], unitSpacing[u][1], unitSpacing[u][2]);
+        if (near64)
+            srcT64.push_back(sourceFp64<T>(offs[u], sc, unitSpacing[u][0], unitSpacing[u][1], unitSpacing[u][2]));
         corners[u] = eikx::Corner3{srcT[u].isx, srcT[u].isy, srcT[u].isz, offs[u][0], offs[u][1], offs[u][2],
                                    static_cast<double>(static_cast<T>(sc))};
     }
@@ -1075,7 +1085,8 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     const size_t cornerBytes = corners.size() * sizeof(eikx::Corner3);
     const size_t unitBytes = units.size() * sizeof(eikx::Grid3Unit<T>);
     const size_t orderBytes = items.size() * 16;
-    EIKX_CUDA(w.stage.ensure(srcBytes + cornerBytes + unitBytes + orderBytes + 64));
+    const size_t src64Bytes = srcT64.size() * sizeof(eikx::SourceFp64);
+    EIKX_CUDA(w.stage.ensure(srcBytes + cornerBytes + unitBytes + orderBytes + src64Bytes + 64));
     char *stage = static_cast<char *>(w.stage.p);
     std::memcpy(stage, srcT.data(), srcBytes);
     std::memcpy(stage + srcBytes, corners.data(), cornerBytes);
@@ -1088,6 +1099,11 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     EIKX_CUDA(cudaMemcpyAsync(w.corners.p, stage + srcBytes, cornerBytes, cudaMemcpyHostToDevice, c->stream));
     EIKX_CUDA(cudaMemcpyAsync(w.units.p, stage + srcBytes + cornerBytes, unitBytes, cudaMemcpyHostToDevice, c->stream));
     EIKX_CUDA(cudaMemcpyAsync(w.order.p, ord, orderBytes, cudaMemcpyHostToDevice, c->stream));
+    if (near64) {
+        char *qstage = stage + srcBytes + cornerBytes + unitBytes + orderBytes;
+        std::memcpy(qstage, srcT64.data(), src64Bytes);
+        EIKX_CUDA(cudaMemcpyAsync(w.srcs64.p, qstage, src64Bytes, cudaMemcpyHostToDevice, c->stream));
+    }
 
     const int nSweepLaunches = nSweepKinds * ((o.init_sweeps ? 1 : 0) + nSweeps);
     eikx::SolveState st{};
@@ -1155,7 +1171,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
             a.sweepIndex = sweepsLaunched;
             a.sweep = e; a.init = init; a.radius = o.factored_radius;
             a.units = w.units.as<eikx::Grid3Unit<T>>();
-            a.nearFp64 = sizeof(T) == 4 && o.near_fp64 ? 1 : 0;
+            a.srcs64 = near64 ? w.srcs64.as<eikx::SourceFp64>() : nullptr;
             EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, shape, blocks, c->stream));
             if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched + 1], c->stream));
             buf ^= 1;

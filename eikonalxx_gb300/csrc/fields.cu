@@ -80,7 +80,8 @@ template <class T, bool UNIFORM>
 __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny,
                                 int nz, double dx, double dy, double dz, const Corner3 *corners,
                                 const SourceT<T> *srcs, const double *slow, int radius, T h, Spacing3<T> g,
-                                double gateTol, int twoSided, int fp64, unsigned long long *nReset) {
+                                double gateTol, int twoSided, int fp64, const SourceFp64 *srcs64,
+                                unsigned long long *nReset) {
     const long long perField = static_cast<long long>(nx) * ny * nz;
     const long long n = perField * nFields;
     const int ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
@@ -125,8 +126,20 @@ __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fie
                 st.t1 = tv(xs, iy, iz); st.t2 = tv(xs, ys, iz); st.t3 = tv(ix, ys, iz); st.t4 = tv(ix, iy, zs);
                 st.t5 = tv(xs, iy, zs); st.t6 = tv(xs, ys, zs); st.t7 = tv(ix, ys, zs);
                 // a near_fp64 solve gates with the FP64 factored branch its sweeps use
-                const T u = UNIFORM ? fd3Uniform<T, true>(radius, h, src, sg, ix, iy, iz, st)
-                                    : fd3NonUniform<T, true>(radius, g, src, sg, ix, iy, iz, st);
+                T u;
+                if constexpr (sizeof(T) == 4) {
+                    if (srcs64 && nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) {
+                        u = UNIFORM ? fd3UniformNearFp64<0>(src.isx, src.isy, src.isz, srcs64 + f, sg, ix, iy, iz, st)
+                                    : fd3NonUniformNearFp64<0>(src.isx, src.isy, src.isz, srcs64 + f, sg, ix, iy,
+                                                                iz, st);
+                    } else {
+                        u = UNIFORM ? fd3Uniform<T>(radius, h, src, sg, ix, iy, iz, st)
+                                    : fd3NonUniform<T>(radius, g, src, sg, ix, iy, iz, st);
+                    }
+                } else {
+                    u = UNIFORM ? fd3Uniform<T>(radius, h, src, sg, ix, iy, iz, st)
+                                : fd3NonUniform<T>(radius, g, src, sg, ix, iy, iz, st);
+                }
                 uMin = u < uMin ? u : uMin;
             }
             // one-sided: reset what sweeps could not raise; two-sided: also what lies above
@@ -450,16 +463,17 @@ template <class T>
 cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
                             double dx, double dy, double dz, const Corner3 *corners, const SourceT<T> *srcs,
                             const double *slow, int radius, bool uniform, T h, const Spacing3<T> &g, double gateTol,
-                            int twoSided, int fp64, unsigned long long *nReset, cudaStream_t s) {
+                            int twoSided, int fp64, const SourceFp64 *srcs64, unsigned long long *nReset,
+                            cudaStream_t s) {
     const long long n = static_cast<long long>(nx) * ny * nz * nFields;
     if (uniform)
         warmInit3Kernel<T, true><<<gridFor(n), kThreads, 0, s>>>(tt, init, nFields, fieldStride, pitch, nx, ny, nz, dx,
                                                                  dy, dz, corners, srcs, slow, radius, h, g, gateTol,
-                                                                 twoSided, fp64, nReset);
+                                                                 twoSided, fp64, srcs64, nReset);
     else
         warmInit3Kernel<T, false><<<gridFor(n), kThreads, 0, s>>>(tt, init, nFields, fieldStride, pitch, nx, ny, nz, dx,
                                                                   dy, dz, corners, srcs, slow, radius, h, g, gateTol,
-                                                                  twoSided, fp64, nReset);
+                                                                  twoSided, fp64, srcs64, nReset);
     if (pitch > nx) {
         const long long np = static_cast<long long>(nFields) * ny * nz * (pitch - nx);
         fillPadKernel<T><<<gridFor(np), kThreads, 0, s>>>(tt, nFields, fieldStride, pitch, nx, ny * nz);
@@ -468,12 +482,12 @@ cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldSt
 }
 template cudaError_t launchWarmInit3<float>(float *, const float *, int, long long, int, int, int, int, double, double,
                                             double, const Corner3 *, const SourceT<float> *, const double *, int, bool,
-                                            float, const Spacing3<float> &, double, int, int, unsigned long long *,
-                                            cudaStream_t);
+                                            float, const Spacing3<float> &, double, int, int, const SourceFp64 *,
+                                            unsigned long long *, cudaStream_t);
 template cudaError_t launchWarmInit3<double>(double *, const double *, int, long long, int, int, int, int, double,
                                              double, double, const Corner3 *, const SourceT<double> *, const double *,
                                              int, bool, double, const Spacing3<double> &, double, int, int,
-                                             unsigned long long *, cudaStream_t);
+                                             const SourceFp64 *, unsigned long long *, cudaStream_t);
 
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st) {
     positiveKernel<double><<<gridFor(n), kThreads, 0, st>>>(s, n, flag);

@@ -39,13 +39,16 @@ template <class T> struct SourceT {
     int isx, isy, isz;
     T xs, ys, zs;
     T sSrc;
-    // FP64 factored branch of an FP32 sweep (eikx_options.near_fp64): when set, a node
-    // within the factored radius is updated by the double-precision operator -- the
-    // reference's Solver3D<double> arithmetic -- on its FP32 neighbours widened to double,
-    // with the analytic factor T0 and its gradient from these FP64 source offsets,
-    // source-cell slowness and grid spacing; the result is rounded to FP32.
-    int nearFp64;
-    double xd, yd, zd, sd, dxd, dyd, dzd;
+};
+
+// The FP64 factored branch of an FP32 sweep (eikx_options.near_fp64): a node within the
+// factored radius is updated by the double-precision operator -- the reference's
+// Solver3D<double> arithmetic -- on its FP32 neighbours widened to double, with the
+// analytic factor T0 and its gradient from these FP64 source offsets, source-cell
+// slowness (as the sweep holds it) and grid spacing; the result is rounded to FP32.
+// Kept apart from SourceT, so the kernels without this branch carry none of it.
+struct SourceFp64 {
+    double xs, ys, zs, s, dx, dy, dz;
 };
 
 // Analytic homogeneous time and gradient (computeAnalyticalTravelTime,
@@ -193,23 +196,9 @@ __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t
     return dmin(t1d, dmin(t2d, third * (S + dsqrt(det))));
 }
 
-template <class T> struct Spacing3;
-template <int D>
-__device__ __noinline__ float fd3UniformNearFp64(const SourceT<float> src, const SweepSigns sg, int ix, int iy,
-                                                 int iz, const Stencil3<float> n);
-template <int D>
-__device__ __noinline__ float fd3NonUniformNearFp64(const SourceT<float> src, const SweepSigns sg, int ix, int iy,
-                                                    int iz, const Stencil3<float> n);
-
-// FP64NEAR: compile the FP64 factored branch of FP32 sweeps in (taken when src.nearFp64
-// is set).  Only the kernel instances that run near_fp64 solves carry it: its double-
-// precision operator needs more registers than the rest of a sweep kernel.
-template <class T, bool FP64NEAR = false>
+template <class T>
 __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const SweepSigns &sg,
                                             int ix, int iy, int iz, const Stencil3<T> &n) {
-    if constexpr (FP64NEAR && sizeof(T) == 4) {
-        if (src.nearFp64) return fd3UniformNearFp64<0>(src, sg, ix, iy, iz, n);
-    }
     EIKX_FD3_UNIFORM_PREFIX
     {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
@@ -288,12 +277,12 @@ __device__ __forceinline__ bool nearSource(int radius, int isx, int isy, int isz
     return !(abs(isx - ix) > radius || abs(isy - iy) > radius || abs(isz - iz) > radius);
 }
 
-template <class T, bool FP64NEAR = false>
+template <class T>
 __device__ __forceinline__ T fd3Uniform(int radius, T h, const SourceT<T> &src,
                                         const SweepSigns &sg, int ix, int iy, int iz,
                                         const Stencil3<T> &n) {
     if (!nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) return fd3UniformFar(h, n);
-    return fd3UniformNear<T, FP64NEAR>(h, src, sg, ix, iy, iz, n);
+    return fd3UniformNear(h, src, sg, ix, iy, iz, n);
 }
 
 // Grid constants of the non-uniform 3D solver (include/private/solver3d.hpp:247-261),
@@ -372,13 +361,10 @@ __device__ __forceinline__ T fd3NonUniformFar(const Spacing3<T> &g, const Stenci
     return tUpd;
 }
 
-template <class T, bool FP64NEAR = false>
+template <class T>
 __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const SourceT<T> &src,
                                                const SweepSigns &sg, int ix, int iy, int iz,
                                                const Stencil3<T> &n) {
-    if constexpr (FP64NEAR && sizeof(T) == 4) {
-        if (src.nearFp64) return fd3NonUniformNearFp64<0>(src, sg, ix, iy, iz, n);
-    }
     EIKX_FD3_NONUNIFORM_PREFIX
     {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
@@ -457,7 +443,7 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
 }
 #undef EIKX_FD3_NONUNIFORM_PREFIX
 
-// The FP64 factored branch of an FP32 sweep (SourceT::nearFp64): the operands widened to
+// The FP64 factored branch of an FP32 sweep (SourceFp64): the operands widened to
 // double, the double-precision operator of the reference (Solver3D is instantiated for
 // double only, src/solver3d.cpp:626-627), the result rounded to FP32.  Out of line: only
 // the few hundred nodes per field within the factored radius take it.
@@ -467,41 +453,43 @@ __device__ __forceinline__ Stencil3<double> widen(const Stencil3<float> &n) {
     m.t1 = n.t1; m.t2 = n.t2; m.t3 = n.t3; m.t4 = n.t4; m.t5 = n.t5; m.t6 = n.t6; m.t7 = n.t7;
     return m;
 }
-__device__ __forceinline__ SourceT<double> sourceFp64(const SourceT<float> &src) {
-    SourceT<double> d{};
-    d.isx = src.isx; d.isy = src.isy; d.isz = src.isz;
-    d.xs = src.xd; d.ys = src.yd; d.zs = src.zd; d.sSrc = src.sd;
-    return d;
+__device__ __forceinline__ SourceT<double> sourceFp64(int isx, int isy, int isz, const SourceFp64 &d) {
+    SourceT<double> r;
+    r.isx = isx; r.isy = isy; r.isz = isz;
+    r.xs = d.xs; r.ys = d.ys; r.zs = d.zs; r.sSrc = d.s;
+    return r;
 }
 template <int D>
-__device__ __noinline__ float fd3UniformNearFp64(const SourceT<float> src, const SweepSigns sg, int ix, int iy,
-                                                 int iz, const Stencil3<float> n) {
-    return static_cast<float>(fd3UniformNear<double>(src.dxd, sourceFp64(src), sg, ix, iy, iz, widen(n)));
+__device__ __noinline__ float fd3UniformNearFp64(int isx, int isy, int isz, const SourceFp64 *dp, const SweepSigns sg,
+                                                 int ix, int iy, int iz, const Stencil3<float> n) {
+    const SourceFp64 d = *dp;
+    return static_cast<float>(fd3UniformNear<double>(d.dx, sourceFp64(isx, isy, isz, d), sg, ix, iy, iz, widen(n)));
 }
 template <int D>
-__device__ __noinline__ float fd3NonUniformNearFp64(const SourceT<float> src, const SweepSigns sg, int ix, int iy,
-                                                    int iz, const Stencil3<float> n) {
+__device__ __noinline__ float fd3NonUniformNearFp64(int isx, int isy, int isz, const SourceFp64 *dp,
+                                                    const SweepSigns sg, int ix, int iy, int iz,
+                                                    const Stencil3<float> n) {
+    const SourceFp64 d = *dp;
     // the non-uniform constants in double, as the host forms them for an FP64 solve
     // (include/private/solver3d.hpp:247-261)
-    const double dx = src.dxd, dy = src.dyd, dz = src.dzd;
     Spacing3<double> g;
-    g.dx = dx; g.dy = dy; g.dz = dz;
-    g.dxInv = 1 / dx; g.dyInv = 1 / dy; g.dzInv = 1 / dz;
-    g.dx2Inv = 1 / (dx * dx); g.dy2Inv = 1 / (dy * dy); g.dz2Inv = 1 / (dz * dz);
-    g.dx_dz = dx / dz; g.dz_dx = dz / dx; g.dy_dz = dy / dz; g.dz_dy = dz / dy;
-    g.dx_dy = dx / dy; g.dy_dx = dy / dx;
-    g.dx2_p_dz2_inv = 1 / (dx * dx + dz * dz);
-    g.dy2_p_dz2_inv = 1 / (dy * dy + dz * dz);
-    g.dx2_p_dy2_inv = 1 / (dx * dx + dy * dy);
-    return static_cast<float>(fd3NonUniformNear<double>(g, sourceFp64(src), sg, ix, iy, iz, widen(n)));
+    g.dx = d.dx; g.dy = d.dy; g.dz = d.dz;
+    g.dxInv = 1 / d.dx; g.dyInv = 1 / d.dy; g.dzInv = 1 / d.dz;
+    g.dx2Inv = 1 / (d.dx * d.dx); g.dy2Inv = 1 / (d.dy * d.dy); g.dz2Inv = 1 / (d.dz * d.dz);
+    g.dx_dz = d.dx / d.dz; g.dz_dx = d.dz / d.dx; g.dy_dz = d.dy / d.dz; g.dz_dy = d.dz / d.dy;
+    g.dx_dy = d.dx / d.dy; g.dy_dx = d.dy / d.dx;
+    g.dx2_p_dz2_inv = 1 / (d.dx * d.dx + d.dz * d.dz);
+    g.dy2_p_dz2_inv = 1 / (d.dy * d.dy + d.dz * d.dz);
+    g.dx2_p_dy2_inv = 1 / (d.dx * d.dx + d.dy * d.dy);
+    return static_cast<float>(fd3NonUniformNear<double>(g, sourceFp64(isx, isy, isz, d), sg, ix, iy, iz, widen(n)));
 }
 
-template <class T, bool FP64NEAR = false>
+template <class T>
 __device__ __forceinline__ T fd3NonUniform(int radius, const Spacing3<T> &g, const SourceT<T> &src,
                                            const SweepSigns &sg, int ix, int iy, int iz,
                                            const Stencil3<T> &n) {
     if (!nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) return fd3NonUniformFar(g, n);
-    return fd3NonUniformNear<T, FP64NEAR>(g, src, sg, ix, iy, iz, n);
+    return fd3NonUniformNear(g, src, sg, ix, iy, iz, n);
 }
 
 // ---------------------------------------------------------------------------- 2D

@@ -109,22 +109,17 @@ __global__ void orderKernel(int4 *order, int tilesY, int tilesZ, int ly, int lz)
     }
 }
 
-// Source table of the field: the source-cell slowness is read from the caller's model.
-// With nearFp64 the factored branch runs in FP64 (eikx_options.near_fp64).
-__global__ void sourceKernel(eikx::SourceT<float> *src, eikx::Corner3 *corner, const float *slowness, int ncx,
-                             int ncy, int cx, int cy, int cz, double ox, double oy, double oz, int nearFp64,
-                             double dx, double dy, double dz) {
+// Source table of the field: the source-cell slowness is read from the caller's model;
+// src64 (FP64 factored branch, eikx_options.near_fp64) is filled when not null.
+__global__ void sourceKernel(eikx::SourceT<float> *src, eikx::Corner3 *corner, eikx::SourceFp64 *src64,
+                             const float *slowness, int ncx, int ncy, int cx, int cy, int cz, double ox, double oy,
+                             double oz, double dx, double dy, double dz) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const float s = slowness[(static_cast<long long>(cz) * ncy + cy) * ncx + cx];
-    *src = eikx::SourceT<float>{};
     src->isx = cx; src->isy = cy; src->isz = cz;
     src->xs = static_cast<float>(ox); src->ys = static_cast<float>(oy); src->zs = static_cast<float>(oz);
     src->sSrc = s;
-    if (nearFp64) {
-        src->nearFp64 = 1;
-        src->xd = ox; src->yd = oy; src->zd = oz; src->sd = static_cast<double>(s);
-        src->dxd = dx; src->dyd = dy; src->dzd = dz;
-    }
+    if (src64) *src64 = eikx::SourceFp64{ox, oy, oz, static_cast<double>(s), dx, dy, dz};
     corner->isx = cx; corner->isy = cy; corner->isz = cz;
     corner->xo = ox; corner->yo = oy; corner->zo = oz;
     corner->s = static_cast<double>(s);
@@ -186,6 +181,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     plan.take<int4>(static_cast<size_t>(nTiles));                               // work order
     plan.take<eikx::SourceT<float>>(1);
     plan.take<eikx::Corner3>(1);
+    plan.take<eikx::SourceFp64>(1);
     if (plan.used > kScratchBytes)
         return err(EIKX_ERR_INVALID, "grid " + std::to_string(nx) + "x" + std::to_string(ny) + "x" +
                                          std::to_string(nz) + " needs " + std::to_string(plan.used) +
@@ -210,6 +206,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     int4 *order = cv.take<int4>(static_cast<size_t>(nTiles));
     eikx::SourceT<float> *srcDev = cv.take<eikx::SourceT<float>>(1);
     eikx::Corner3 *cornerDev = cv.take<eikx::Corner3>(1);
+    eikx::SourceFp64 *src64Dev = cv.take<eikx::SourceFp64>(1);
 
     int numSMs = 0;
     NOALLOC_CUDA(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device));
@@ -251,8 +248,8 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     if (bad) return err(EIKX_ERR_INVALID, "Non-positive velocities detected");
     orderKernel<<<(nTiles + 127) / 128, 128, 0, stream>>>(order, tilesY, tilesZ, ly, lz);
     NOALLOC_CUDA(cudaGetLastError());
-    sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, slowness, nx - 1, ny - 1, cx, cy, cz, ox, oy, oz,
-                                       o.near_fp64 ? 1 : 0, dx, dy, dz);
+    sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, o.near_fp64 ? src64Dev : nullptr, slowness, nx - 1, ny - 1,
+                                       cx, cy, cz, ox, oy, oz, dx, dy, dz);
     NOALLOC_CUDA(cudaGetLastError());
     NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spPos, spPitch, 3, slowness, nx, ny, nz, stream)));
     NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spNeg, spPitch, 0, slowness, nx, ny, nz, stream)));
@@ -277,7 +274,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
         a.nx = nx; a.ny = ny; a.nz = nz; a.tilesY = tilesY; a.tilesZ = tilesZ;
         a.srcs = srcDev; a.st = st; a.buf = buf; a.sweepIndex = launched; a.residualSlot = slot;
         a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = fdx; a.sp3 = g;
-        a.nearFp64 = o.near_fp64;
+        a.srcs64 = o.near_fp64 ? src64Dev : nullptr;
         if (chunk) NOALLOC_CUDA(eikx::launchSweep3Chunk<float>(a, uniform, shape, blocks, stream));
         else NOALLOC_CUDA(eikx::launchSweep3<float>(a, uniform, blocks, stream));
         buf ^= 1;

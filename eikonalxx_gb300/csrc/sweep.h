@@ -64,7 +64,8 @@ template <class T> struct Sweep3Args {
     Spacing3<T> sp3;          // non-uniform constants
     const int2 *pairs;        // field pairs of the paired kernel (work items index pairs)
     const Grid3Unit<T> *units;  // multi-model batch: per-unit geometry (chunk-step kernel only)
-    int nearFp64;             // FP32 chunk-step: run the kernel instance with the FP64 factored branch
+    const SourceFp64 *srcs64; // per field, FP32 chunk-step only: set = the FP64 factored branch
+                              // (eikx_options.near_fp64), its own kernel instances
 };
 
 template <class T> struct Sweep2Args {
@@ -172,7 +173,8 @@ template <class T>
 cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
                             double dx, double dy, double dz, const Corner3 *corners, const SourceT<T> *srcs,
                             const double *slow, int radius, bool uniform, T h, const Spacing3<T> &g, double gateTol,
-                            int twoSided, int fp64, unsigned long long *nReset, cudaStream_t s);
+                            int twoSided, int fp64, const SourceFp64 *srcs64, unsigned long long *nReset,
+                            cudaStream_t s);
 // Sets *flag (ORs 1) if any of the n slownesses is not positive and finite.
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st);
 cudaError_t launchCheckPositive(const float *s, long long n, int *flag, cudaStream_t st);

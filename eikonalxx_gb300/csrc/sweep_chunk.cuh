@@ -160,17 +160,27 @@ __device__ __forceinline__ void putChunk(unsigned long long *p, unsigned tag, co
 }
 
 // Factored (near-source) updates, out of line: taken by a few hundred nodes per field,
-// so the V inlined copies of the update hold only the Cartesian operators.  The source
-// record is read here, so the sweep loop keeps only the source cell in registers.
-template <class T, bool NEAR64>
+// so the V inlined copies of the update hold only the Cartesian operators.
+template <class T>
 __device__ __noinline__ T nearUniform(T h, const SourceT<T> src, const SweepSigns sg, int ix, int iy, int iz,
                                       const Stencil3<T> n) {
-    return fd3UniformNear<T, NEAR64>(h, src, sg, ix, iy, iz, n);
+    return fd3UniformNear(h, src, sg, ix, iy, iz, n);
 }
-template <class T, bool NEAR64>
+template <class T>
 __device__ __noinline__ T nearNonUniform(const Spacing3<T> g, const SourceT<T> src, const SweepSigns sg, int ix,
                                          int iy, int iz, const Stencil3<T> n) {
-    return fd3NonUniformNear<T, NEAR64>(g, src, sg, ix, iy, iz, n);
+    return fd3NonUniformNear(g, src, sg, ix, iy, iz, n);
+}
+// The FP64 factored branch of FP32 sweeps (eikx_options.near_fp64).
+template <class T>
+__device__ __forceinline__ T nearFp64(bool uniform, const SourceT<T> &src, const SourceFp64 *d, const SweepSigns &sg,
+                                      int ix, int iy, int iz, const Stencil3<T> &n) {
+    if constexpr (sizeof(T) == 4) {
+        return uniform ? fd3UniformNearFp64<0>(src.isx, src.isy, src.isz, d, sg, ix, iy, iz, n)
+                       : fd3NonUniformNearFp64<0>(src.isx, src.isy, src.isz, d, sg, ix, iy, iz, n);
+    } else {
+        return T(0);   // never instantiated for FP64 sweeps
+    }
 }
 
 __device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
@@ -179,9 +189,8 @@ __device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
 
 // INIT: the source-limited initialisation pass (a.init = 1), compiled apart so that the
 // refinement sweeps carry none of its block skipping.  NEAR64: the FP64 factored branch
-// of FP32 sweeps (eikx_options.near_fp64), compiled apart so that the other instances do
-// not reserve its registers; these instances are held to the default's 128 registers
-// (4 blocks per SM), the out-of-line FP64 branch spilling what it needs beyond them.
+// of FP32 sweeps (eikx_options.near_fp64), compiled into its own kernels
+// (sweep3ChunkNear64Kernel) so that the others do not reserve its registers.
 template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT, bool NEAR64>
 __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
     static_assert(LY * LZ == 32 && LZ + 1 + LY <= 32, "a warp holds 32 pencils and its halo helpers");
@@ -224,7 +233,6 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         const int f = item.x, b = item.y, c = item.z;
         if (st.converged[f]) continue;
         const SourceT<T> src = a.srcs[f];
-        const int4 srcCell = make_int4(src.isx, src.isy, src.isz, 0);
 
         // grid of this work item: the launch's (one model) or the unit's (batch)
         const Grid3Unit<T> *unit = BATCH ? a.units + f : nullptr;
@@ -248,9 +256,9 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         const int ya = laneValid ? reflect(yp, ny, fy) : 0;
         const int za = laneValid ? reflect(zp, nz, fz) : 0;
         int xlo, xhi, ylo, yhi, zlo, zhi;
-        axisBounds(nx, REV, INIT, srcCell.x, xlo, xhi);
-        axisBounds(ny, fy, INIT, srcCell.y, ylo, yhi);
-        axisBounds(nz, fz, INIT, srcCell.z, zlo, zhi);
+        axisBounds(nx, REV, INIT, src.isx, xlo, xhi);
+        axisBounds(ny, fy, INIT, src.isy, ylo, yhi);
+        axisBounds(nz, fz, INIT, src.isz, zlo, zhi);
         // Initialisation pass: the update range starts at y' = yp0, z' = zp0 and runs to the
         // end of each axis.  Warp blocks wholly before it update nothing: they are left out,
         // and the blocks after them read those rows from the field, which the sweep does not
@@ -263,7 +271,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         }
         const bool yzUpd = laneValid && ya >= ylo && ya <= yhi && za >= zlo && za <= zhi;
         // the factored branch applies within `radius` cells of the source cell on every axis
-        const bool yzNear = abs(srcCell.y - ya) <= a.radius && abs(srcCell.z - za) <= a.radius;
+        const bool yzNear = abs(src.isy - ya) <= a.radius && abs(src.isz - za) <= a.radius;
         T *row = field + (static_cast<long long>(za) * ny + ya) * Px;
         const T *srow = sp + static_cast<long long>(za + (fz ? 0 : 1)) * spPlane +
                         static_cast<long long>(ya + (fy ? 0 : 1)) * spPitch;
@@ -407,16 +415,18 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
                     n.s4 = e ? sY.v[e - 1] : cS5;
                     n.s5 = sY.v[e];
                     n.s7 = e ? sOwn.v[e - 1] : cS7;
-                    const bool near = yzNear && abs(srcCell.x - xa) <= a.radius;
+                    const bool near = yzNear && abs(src.isx - xa) <= a.radius;
                     const T t0 = out.v[e];
                     T tu;
-                    if (UNIFORM) {
+                    if (NEAR64 && near) {
+                        tu = nearFp64<T>(UNIFORM, src, a.srcs64 + f, sg, xa, ya, za, n);
+                    } else if (UNIFORM) {
                         // the Cartesian operators with lower-bound exits: min(t0, tu) is the
                         // same bit for bit as with fd3UniformFar
-                        tu = near ? nearUniform<T, NEAR64>(h, src, sg, xa, ya, za, n) : fd3UniformFarBounded<T>(h, n, t0);
+                        tu = near ? nearUniform<T>(h, src, sg, xa, ya, za, n) : fd3UniformFarBounded<T>(h, n, t0);
                     } else {
                         const Spacing3<T> &g = BATCH ? unit->sp3 : a.sp3;
-                        tu = near ? nearNonUniform<T, NEAR64>(g, src, sg, xa, ya, za, n) : fd3NonUniformFar<T>(g, n);
+                        tu = near ? nearNonUniform<T>(g, src, sg, xa, ya, za, n) : fd3NonUniformFar<T>(g, n);
                     }
                     if (tu < t0) {
                         out.v[e] = tu;
@@ -443,12 +453,13 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
     }
 }
 
-template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT, bool NEAR64>
+template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT>
 __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<T> a) {
-    static_assert(!NEAR64, "the FP64 factored branch runs in sweep3ChunkNear64Kernel");
     sweep3ChunkBody<T, UNIFORM, REV, BATCH, LY, LZ, INIT, false>(a);
 }
-template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT, bool NEAR64>
+// Held to 128 registers (the default kernels' 4 blocks per SM); the out-of-line FP64
+// branch spills what it needs beyond them.
+template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT>
 __global__ void __launch_bounds__(kThreadsC, 4) sweep3ChunkNear64Kernel(const Sweep3Args<T> a) {
     sweep3ChunkBody<T, UNIFORM, REV, BATCH, LY, LZ, INIT, true>(a);
 }
@@ -461,14 +472,14 @@ template <class T, bool U, bool R, bool B, int LY, int LZ>
 void launchOne(const Sweep3Args<T> &a, int blocks, cudaStream_t s) {
     const size_t smem = smemBytes<LY, LZ>();
     if constexpr (sizeof(T) == 4) {
-        if (a.nearFp64) {
-            if (a.init) sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, true, true><<<blocks, kThreadsC, smem, s>>>(a);
-            else sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, false, true><<<blocks, kThreadsC, smem, s>>>(a);
+        if (a.srcs64) {
+            if (a.init) sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, true><<<blocks, kThreadsC, smem, s>>>(a);
+            else sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, false><<<blocks, kThreadsC, smem, s>>>(a);
             return;
         }
     }
-    if (a.init) sweep3ChunkKernel<T, U, R, B, LY, LZ, true, false><<<blocks, kThreadsC, smem, s>>>(a);
-    else sweep3ChunkKernel<T, U, R, B, LY, LZ, false, false><<<blocks, kThreadsC, smem, s>>>(a);
+    if (a.init) sweep3ChunkKernel<T, U, R, B, LY, LZ, true><<<blocks, kThreadsC, smem, s>>>(a);
+    else sweep3ChunkKernel<T, U, R, B, LY, LZ, false><<<blocks, kThreadsC, smem, s>>>(a);
 }
 
 template <class T, bool B, int LY, int LZ>
@@ -490,11 +501,11 @@ template <class T, bool B, int LY, int LZ> int blocksPerSM(bool uniform) {
     // and waits only on work dequeued before it, so no wait depends on a block not running.
     const void *k[2];
     if (uniform) {
-        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, false, B, LY, LZ, false, false>);
-        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, true, B, LY, LZ, false, false>);
+        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, false, B, LY, LZ, false>);
+        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, true, B, LY, LZ, false>);
     } else {
-        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, false, B, LY, LZ, false, false>);
-        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, true, B, LY, LZ, false, false>);
+        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, false, B, LY, LZ, false>);
+        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, true, B, LY, LZ, false>);
     }
     int best = 1 << 30;
     for (const void *f : k) {

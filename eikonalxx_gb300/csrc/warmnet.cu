@@ -67,6 +67,8 @@ struct eikx_warmnet {
     eikx::net::Sample *dSamples = nullptr, *hSamples = nullptr;
     double *dLoss = nullptr, *hLoss = nullptr;
     int *dStatus = nullptr, *hStatus = nullptr;   // raised by a bounded wait that ran out
+    long long spin = 0;             // tcgen05 waits: polls before giving up (0: the kernel's default)
+    int testLate = 0;               // test hook of the tcgen05 waits (eikx_warmnet_set_test_hooks)
     long long step = 0;
     std::vector<void *> allocs;
     // profiling: an event pair per launch and its category
@@ -166,6 +168,8 @@ cudaError_t conv(eikx_warmnet *n, int L, int B) {
     a.W = n->dim[lv][2];
     a.B = B;
     a.status = n->dStatus;
+    a.spin = n->spin;
+    a.testLate = n->testLate;
     return timed(n, kFwd, [&] { return eikx::net::launchConv(a, n->stream); });
 }
 
@@ -205,6 +209,8 @@ cudaError_t convBack(eikx_warmnet *n, int L, int B, bf16 *dx, const bf16 *mask) 
     a.W = W;
     a.B = B;
     a.status = n->dStatus;
+    a.spin = n->spin;
+    a.testLate = n->testLate;
     return timed(n, kDgrad, [&] { return eikx::net::launchConv(a, n->stream); });
 }
 
@@ -490,6 +496,15 @@ eikx_status eikx_warmnet_create(int device, const eikx_warmnet_config *cfg, eikx
         return r;
     }
     *out = n;
+    return EIKX_OK;
+}
+
+eikx_status eikx_warmnet_set_test_hooks(eikx_warmnet *n, int spin_limit_log2, int late) {
+    if (eikx_status r = checkNet(n); r != EIKX_OK) return r;
+    if (spin_limit_log2 < 0 || spin_limit_log2 > 40) return err(EIKX_ERR_INVALID, "spin_limit_log2 must be 0..40");
+    if (late < 0 || late > 2) return err(EIKX_ERR_INVALID, "late must be 0, 1 or 2");
+    n->spin = spin_limit_log2 > 0 ? (1ll << spin_limit_log2) : 0;
+    n->testLate = late;
     return EIKX_OK;
 }
 

@@ -47,6 +47,12 @@ struct ConvArgs {
     int relu;
     int D, H, W, B;
     int *status;        // raised (device) when a bounded wait of the tcgen05 path ran out; may be null
+    long long spin;     // tcgen05 path: polls of an mbarrier before a wait gives up (<= 0: 2^24)
+    int testLate;       // test hook, 0 in production (tcgen05 path, first input chunk): 1 = the
+                        // operand barrier expects 16 bytes more than the copies bring, and those
+                        // bytes are declared complete only after the wait ran out; 2 = the MMAs'
+                        // completion is committed only after the wait ran out.  Either way the
+                        // wait runs out while nothing is lost, and the recovery path runs.
 };
 // Grids with 128 nodes along x (and H % 4 == 0, D % 2 == 0) run on the tcgen05 tensor cores
 // with TMEM accumulators; other shapes on mma.sync.

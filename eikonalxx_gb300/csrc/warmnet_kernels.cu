@@ -661,9 +661,9 @@ __device__ __forceinline__ void mma(unsigned d, unsigned long long ad, unsigned 
         "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
         : "memory");
 }
-__device__ __forceinline__ bool waitParity(unsigned mbar, unsigned parity) {
+__device__ __forceinline__ bool waitParity(unsigned mbar, unsigned parity, long long spin) {
     unsigned done = 0;
-    for (long long it = 0; it < kSpin && !done; ++it)
+    for (long long it = 0; it < spin && !done; ++it)
         asm volatile(
             "{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n selp.u32 %0, 1, 0, q;\n}\n"
             : "=r"(done)
@@ -727,20 +727,33 @@ __global__ void __launch_bounds__(128) convTcKernel(ConvArgs a, const __grid_con
     // kind::f16: D FP32 (bit 4), A and B BF16 (bits 7, 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
     const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | (static_cast<unsigned>(N >> 3) << 17) | ((128u >> 4) << 24);
     const unsigned hb = smemAddr(halo), wb = smemAddr(wsm);
+    const long long spin = a.spin > 0 ? a.spin : kSpin;
+    // A wait that runs out must not leave the CTA while its copies or MMAs may still write
+    // its shared memory or TMEM: before it leaves, the CTA drains -- it waits again on the
+    // same barrier phase with a bound kDrain times as long -- and only then frees TMEM.
+    constexpr long long kDrain = 64;
     bool ok = true;
     int chunk = 0;
     for (int ci0 = 0; ci0 < a.cin; ci0 += 16, ++chunk) {
+        const bool lateTx = a.testLate == 1 && chunk == 0, lateCommit = a.testLate == 2 && chunk == 0;
         if (tid == 0) {
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(full)),
-                         "r"(static_cast<unsigned>(kHaloB + 2 * WG))
+                         "r"(static_cast<unsigned>(kHaloB + 2 * WG + (lateTx ? 16 : 0)))
                          : "memory");
             for (int g = 0; g < 2; ++g) {
                 tma5(hb + g * kGroupB, &mapX, ci0 + 8 * g, -1, y0 - 1, z0 - 1, b, smemAddr(full));
                 tma3(wb + g * WG, &mapW, ci0 + 8 * g, co0, 0, smemAddr(full));
             }
         }
-        const bool landed = waitParity(smemAddr(full), static_cast<unsigned>(chunk & 1));
+        const bool landed = waitParity(smemAddr(full), static_cast<unsigned>(chunk & 1), spin);
         if (!__syncthreads_and(landed)) {
+            // drain: the copies of this chunk land before the CTA leaves (the test hook's
+            // extra bytes are declared complete here, as late bytes would arrive)
+            if (tid == 0 && lateTx)
+                asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(full)), "r"(16u)
+                             : "memory");
+            waitParity(smemAddr(full), static_cast<unsigned>(chunk & 1), kDrain * spin);
+            __syncthreads();
             ok = false;
             break;
         }
@@ -756,13 +769,24 @@ __global__ void __launch_bounds__(128) convTcKernel(ConvArgs a, const __grid_con
                         (ci0 > 0 || tap > 0) ? 1u : 0u);
                 }
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smemAddr(mmaDone))
-                         : "memory");
+            if (!lateCommit)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smemAddr(mmaDone))
+                             : "memory");
         }
         // this chunk's MMAs have read the buffers once the barrier's phase completes
-        const bool done = waitParity(smemAddr(mmaDone), static_cast<unsigned>(chunk & 1));
+        const bool done = waitParity(smemAddr(mmaDone), static_cast<unsigned>(chunk & 1), spin);
         ok = __syncthreads_and(done) != 0;
+        if (!ok) {
+            // drain: the MMAs issued for this chunk complete before TMEM is freed (the test
+            // hook commits their completion only now, as a late completion would arrive)
+            if (tid == 0 && lateCommit)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smemAddr(mmaDone))
+                             : "memory");
+            waitParity(smemAddr(mmaDone), static_cast<unsigned>(chunk & 1), kDrain * spin);
+            __syncthreads();
+        }
         fenceAfter();
         if (!ok) break;
     }

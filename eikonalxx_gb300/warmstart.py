@@ -114,6 +114,11 @@ class WarmNet:
         _check(self._lib.eikx_warmnet_predict(self._h, arr, n, float(inflate), p, where, ctypes.byref(loss)))
         return out, (loss.value if loss.value >= 0 else None)
 
+    def set_test_hooks(self, spin_limit_log2=0, late=0):
+        """Test hook of the tensor-core convolutions' bounded waits (see
+        eikx_warmnet_set_test_hooks); (0, 0) restores production behaviour."""
+        _check(self._lib.eikx_warmnet_set_test_hooks(self._h, int(spin_limit_log2), int(late)))
+
     def profile_step(self, samples, lr):
         """One training step timed per kernel class: dict of ms and algorithmic FLOPs."""
         arr, n = self._samples(samples)

@@ -33,7 +33,8 @@ public:
     [[nodiscard]] const T* getSlownessPointer() const;
     [[nodiscard]] std::vector<T> getVelocities() const;
     [[nodiscard]] T getSlowness(int iCellX, int iCellY, int iCellZ) const;
-    /// Legacy-VTK output is not part of this library: throws std::runtime_error.
+    /// Writes the cell velocities to a binary legacy-VTK rectilinear-grid file
+    /// (IO::VTKRectilinearGrid3D).  Throws std::runtime_error if no model is set.
     void writeVTK(const std::string &fileName, const std::string &title = "velocity_m/s") const;
     void clear() noexcept;
 private:

@@ -34,7 +34,8 @@ public:
     template <typename T> void trace(const EikonalXX::AbstractBaseClass::ISolver2D<T> &solver);
     [[nodiscard]] bool haveRayPaths() const noexcept;
     [[nodiscard]] std::vector<Path2D> getRayPaths() const;
-    /// Not part of this build: throws std::runtime_error (Python writes VTK instead).
+    /// Writes the ray paths as ASCII legacy-VTK polylines (IO::VTKLines2D).  Throws
+    /// std::runtime_error if no paths have been traced.
     void writeVTK(const std::string &fileName, const std::string &title = "ray_paths");
 private:
     class GradientTracer2DImpl;

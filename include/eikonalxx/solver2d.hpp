@@ -3,8 +3,8 @@
 // Same workflow as Solver3D with the 4 sweeps of 2D; after a solve the travel times at
 // the stations are interpolated bilinearly (src/solver2d.cpp:106-167).  Solver2D<double>
 // sweeps in FP64 and Solver2D<float> in FP32, on the GPU.  The gradient field is central
-// differences of the travel times (src/gradient.hpp).  writeVTK is not part of this
-// library.  Not copyable, not thread-safe.
+// differences of the travel times (src/gradient.hpp).  writeVTK writes legacy-VTK files
+// (IO::VTKRectilinearGrid2D).  Not copyable, not thread-safe.
 #ifndef EIKONALXX_SOLVER_2D_HPP
 #define EIKONALXX_SOLVER_2D_HPP
 #include <memory>
@@ -53,7 +53,9 @@ public:
     [[nodiscard]] std::vector<T> getTravelTimeGradientField() const override;
     [[nodiscard]] const T *getTravelTimeGradientFieldPointer() const override;
     [[nodiscard]] bool haveTravelTimeGradientField() const noexcept override;
-    /// Legacy-VTK output is not part of this library: throws std::runtime_error.
+    /// Writes the travel-time field (and, with writeGradient, its gradient as vectors named
+    /// title + "_gradient") to a binary legacy-VTK file (IO::VTKRectilinearGrid2D).
+    /// Throws std::runtime_error if the field (or gradient) has not been computed.
     void writeVTK(const std::string &fileName, const std::string &title = "travel_time_field_s",
                   bool writeGradient = false) const;
     void clear() noexcept;

@@ -460,6 +460,16 @@ eikx_status eikx_warmnet_predict(eikx_warmnet *net, const eikx_warmnet_sample *s
  * the network.  ms and flops: 4 and 3 doubles. */
 eikx_status eikx_warmnet_profile_step(eikx_warmnet *net, const eikx_warmnet_sample *s, int n, float lr,
                                       double *ms, double *flops);
+/* Test hook of the tcgen05 convolutions' bounded mbarrier waits (0, 0 in production).
+ * spin_limit_log2: a wait gives up after 2^n polls (0 = the default, 2^24).  late = 1:
+ * the first input chunk's operand barrier expects 16 bytes more than its copies bring,
+ * and the kernel declares them complete only after the wait ran out; late = 2: the
+ * first chunk's MMA completion is committed only after the wait ran out.  Either way
+ * the wait runs out while every copy and MMA still completes: the kernel then drains
+ * them (a second wait, 64 times as long) before it frees TMEM and leaves, and the call
+ * returns EIKX_ERR_TIMEOUT; the next call on the network is correct.  Exercises failure
+ * detection without a GPU fault. */
+eikx_status eikx_warmnet_set_test_hooks(eikx_warmnet *net, int spin_limit_log2, int late);
 
 #ifdef __cplusplus
 }

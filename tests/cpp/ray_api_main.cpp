@@ -6,6 +6,7 @@
 // Prints "ray_api ok" and exits 0 when every check holds.
 #include <cmath>
 #include <cstdlib>
+#include <fstream>
 #include <iostream>
 #include <limits>
 #include <stdexcept>
@@ -201,6 +202,26 @@ static void gpuChecks()
     tracer.trace(solver);
     const auto rays = tracer.getRayPaths();
     CHECK(rays.size() == stations.size());
+    // the paths as legacy-VTK polylines (src/ray/gradientTracer2d.cpp:617-655): one point per
+    // segment start plus the last end point, z written as -z
+    {
+        const std::string vtk = std::string(std::getenv("RAY_VTK_DIR") ? std::getenv("RAY_VTK_DIR") : ".") +
+                                "/rays.vtk";
+        tracer.writeVTK(vtk, "ray paths");
+        std::ifstream in(vtk);
+        std::string l;
+        std::getline(in, l); CHECK(l == "# vtk DataFile Version 3.0");
+        std::getline(in, l); CHECK(l == "ray_paths");
+        std::getline(in, l); CHECK(l == "ASCII");
+        std::getline(in, l); CHECK(l == "DATASET POLYDATA");
+        size_t nPoints = 0;
+        for (const auto &r : rays) nPoints += r.empty() ? 0 : r.size() + 1;
+        std::getline(in, l); CHECK(l == "POINTS " + std::to_string(nPoints) + " float");
+        double px, py, pz;
+        in >> px >> py >> pz;
+        const auto p0 = rays[0].at(0).getStartPoint();
+        CHECK(std::abs(px - p0.getPositionInX()) < 1e-9 && py == 0 && std::abs(pz + p0.getPositionInZ()) < 1e-9);
+    }
     for (size_t i = 0; i < rays.size(); ++i) {
         const double d = std::hypot(stations[i].getLocationInX() - xs, stations[i].getLocationInZ() - zs);
         CHECK(!rays[i].empty());

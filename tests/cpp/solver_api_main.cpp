@@ -91,6 +91,7 @@ int run2(const std::string &out)
     dump(out + "/t2.bin", s.getTravelTimeField());
     dump(out + "/st2.bin", s.getTravelTimesAtStations());
     dump(out + "/g2.bin", s.getTravelTimeGradientField());
+    s.writeVTK(out + "/t2.vtk", "travel time", true);   // src/solver2d.cpp:946-964
     return 0;
 }
 

@@ -45,3 +45,14 @@ def test_cpp_solver_api_matches_oracle(ctx, oracle, tmp_path):
     assert st[1] == pytest.approx(np.hypot(1.0, 1.0) * s2[13 * 60 + 25], rel=1e-12)
     g = np.fromfile(tmp_path / "g2.bin", dtype=np.float64).reshape(37, 61, 2)
     assert g[10, 30, 0] == pytest.approx((t2[10, 31] - t2[10, 29]) / 20.0, rel=1e-12)
+    # Solver2D::writeVTK: the field and its gradient, big-endian float32
+    from test_vtk_cpp import Reader, _grid, _scalars
+    r = Reader(tmp_path / "t2.vtk")
+    assert r.title == "travel_time" and r.binary
+    _grid(r, (61, 1, 37), 10.0 * np.arange(61), [0.0], -10.0 * np.arange(37))
+    _scalars(r, "travel_time", t2.ravel().astype(np.float32), f"POINT_DATA {61 * 37}")
+    assert r.line() == "VECTORS travel_time_gradient float"
+    gv = r.floats(3 * 61 * 37).reshape(-1, 3)
+    np.testing.assert_array_equal(gv[:, 0], g[..., 0].ravel().astype(np.float32))
+    np.testing.assert_array_equal(gv[:, 2], g[..., 1].ravel().astype(np.float32))
+    assert r.done()

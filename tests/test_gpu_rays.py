@@ -1,6 +1,8 @@
 """2D gradient ray tracing on the GPU (eikx_trace_rays2d) against the oracle's restatement of
 Ray::GradientTracer2D::trace (src/ray/gradientTracer2d.cpp:339-600), bit for bit: segment
 counts, end points and slownesses, for analytic and solved gradient fields, FP32 and FP64."""
+import os
+
 import numpy as np
 import pytest
 
@@ -96,5 +98,6 @@ def test_cpp_gradient_tracer(ctx, tmp_path):
     analytic gradient, and rays through a solved field whose travel times match the field."""
     import subprocess
     from test_ray_api import build_ray_api
-    r = subprocess.run([build_ray_api(tmp_path), "gpu"], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([build_ray_api(tmp_path), "gpu"], capture_output=True, text=True, timeout=300,
+                       env=dict(os.environ, RAY_VTK_DIR=str(tmp_path)))
     assert r.returncode == 0 and "ray_api ok" in r.stdout, r.stdout + r.stderr

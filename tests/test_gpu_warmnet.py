@@ -99,6 +99,31 @@ def test_prediction_matches_the_oracle(grid):
     assert abs(loss - oloss) <= 1e-2 * oloss
 
 
+@pytest.mark.parametrize("late", [1, 2])
+def test_tensor_core_wait_timeout_drains_and_recovers(late):
+    """Failure detection of the tcgen05 convolutions without a GPU fault: the test hook
+    makes the first input chunk's wait run out while its copies (late = 1) or MMAs
+    (late = 2) still complete; the kernel drains them before it frees TMEM, the call
+    returns EIKX_ERR_TIMEOUT, and the next call on the same network is correct: the
+    forward pass exactly, the gradients to the order of their FP32 atomic sums."""
+    host = _host_samples(14, 2, GRID128)
+    p = _params(10)
+    with ws.WarmNet(GRID128, batch=2, seed=0) as net:
+        net.set_params(p)
+        t_ref, _ = net.predict(_device(host), inflate=1.0)
+        g_ref, _ = net.gradients(_device(host))
+        net.set_test_hooks(spin_limit_log2=10, late=late)
+        with pytest.raises(ex.TimeoutError_):
+            net.predict(_device(host), inflate=1.0)
+        with pytest.raises(ex.TimeoutError_):
+            net.gradients(_device(host))
+        net.set_test_hooks(0, 0)
+        t, _ = net.predict(_device(host), inflate=1.0)
+        g, _ = net.gradients(_device(host))
+    np.testing.assert_array_equal(t, t_ref)
+    assert _rel(g, g_ref) < 1e-5          # weight gradients sum with FP32 atomics, in any order
+
+
 @pytest.mark.parametrize("grid", [GRID, GRID128])
 def test_a_step_moves_against_the_gradient(grid):
     host = _device(_host_samples(13, 2, grid))
