@@ -360,7 +360,9 @@ def run_models(args):
     dev = torch.cuda.current_device()
     n = args.fields
     everything = synthetic.uneven_models(n * world, MODEL_SEED + 1)
-    mine = everything[sharding.shard(n * world, world, rank)]
+    # models of uneven size: split by estimated cost (nodes x sweeps), not by count
+    costs = [sharding.field_cost(*m["grid"][:3], sweeps=8 * (1 + N_SWEEPS_MAX)) for m in everything]
+    mine = [everything[i] for i in sharding.shard_by_cost(costs, world, rank)]
     nodes = sum(m["grid"][0] * m["grid"][1] * m["grid"][2] for m in mine)
     ctx = ex.Context(dev)
     dev_models = [{"grid": m["grid"], "model": torch.from_numpy(m["v"]).to(f"cuda:{dev}"), "nodal": True,
@@ -435,7 +437,7 @@ def run_models(args):
                    "precision": ("fp32 sweeps; fp64 source init and factored (near-source) branch" if NEAR64[0]
                                  else "fp32 sweeps, fp64 source init"), "factored_radius": RADIUS, "tolerance_s": TOL,
                    "max_iterations": N_SWEEPS_MAX, "l2": "flushed (write of 2x L2) between timed steps",
-                   "parallelism": f"replicas x{world} (models sharded, no collective)"},
+                   "parallelism": f"replicas x{world} (models split by estimated cost, no collective)"},
         "roofline": {"bound": "hbm", "kernel": "sweep3ChunkKernel<float,uniform,batch>", "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": rl["algorithmic_bytes"], "node_updates": rl["node_updates"],

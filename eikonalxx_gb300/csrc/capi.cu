@@ -111,7 +111,7 @@ struct EpochMirror {
 
 struct Workspace {
     DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, pairs, init,
-        resetCount, srcs64;
+        resetCount, srcs64, factor;
     EpochMirror epochMirror;
     PinnedBuf stage;
     std::vector<int> orderKey;   // (tilesY, tilesZ, nFields, dim) of the uploaded order table
@@ -121,7 +121,7 @@ struct Workspace {
 // slowness and mailbox packed into one allocation each, plus the cached schedule graph.
 struct BatchWorkspace {
     DevBuf tt, sp, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, units,
-        slow64, input, badFlag, srcs64;
+        slow64, input, badFlag, srcs64, factor;
     EpochMirror epochMirror;
     PinnedBuf stage, srcCells, iterFlags;
     std::vector<double> key;                 // what the cached graph was captured for
@@ -332,11 +332,35 @@ template <class T> int precOf();
 template <> int precOf<float>() { return EIKX_F32; }
 template <> int precOf<double>() { return EIKX_F64; }
 
-// FP64 factored branch of an FP32 sweep (eikx_options.near_fp64): the source offsets,
-// the source-cell slowness as the sweep holds it, and the grid spacing, in FP64.
-template <class T>
-eikx::SourceFp64 sourceFp64(const std::array<double, 3> &off, double s, double dx, double dy, double dz) {
-    return eikx::SourceFp64{off[0], off[1], off[2], static_cast<double>(static_cast<T>(s)), dx, dy, dz};
+// FP64 analytic factor of an FP32 sweep (eikx_options.near_fp64): the source offsets and
+// the grid spacing in FP64, and the field's factor-table box (its entries are assigned
+// by assignFactorBoxes).
+eikx::SourceFp64 sourceFp64(const std::array<double, 3> &off, int isx, int isy, int isz, int radius, int nx, int ny,
+                            int nz, double dx, double dy, double dz) {
+    eikx::SourceFp64 f{};
+    f.xs = off[0]; f.ys = off[1]; f.zs = off[2];
+    f.dx = dx; f.dy = dy; f.dz = dz;
+    int o[3], e[3];
+    if (eikx::factorBox(isx, isy, isz, radius, nx, ny, nz, o, e)) {
+        f.bx0 = o[0]; f.by0 = o[1]; f.bz0 = o[2];
+        f.bnx = e[0]; f.bny = e[1]; f.bnz = e[2];
+    }
+    return f;
+}
+// Lays the fields' factor tables out in `buf` (grown as needed; false on failure) and
+// points each record at its table.  Records whose box is too large keep a null table.
+cudaError_t assignFactorBoxes(std::vector<eikx::SourceFp64> &recs, DevBuf &buf) {
+    size_t total = 0;
+    for (const auto &f : recs) total += static_cast<size_t>(f.bnx) * f.bny * f.bnz;
+    if (total == 0) return cudaSuccess;
+    if (cudaError_t e = buf.ensure(total * sizeof(eikx::FactorEntry)); e != cudaSuccess) return e;
+    size_t off = 0;
+    for (auto &f : recs) {
+        const size_t n = static_cast<size_t>(f.bnx) * f.bny * f.bnz;
+        f.box = n ? buf.as<eikx::FactorEntry>() + off : nullptr;
+        off += n;
+    }
+    return cudaSuccess;
 }
 
 // Shared solve driver for 2D and 3D.
@@ -392,7 +416,9 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     for (int i = 0; i < nSrc; ++i) {
         const double s = srcSlow[i];
         srcT[i].sSrc = static_cast<T>(s);
-        if (DIM == 3 && P == EIKX_F32 && o.near_fp64) srcT64.push_back(sourceFp64<T>(srcOffs[i], s, dx, dy, dz));
+        if (DIM == 3 && P == EIKX_F32 && o.near_fp64)
+            srcT64.push_back(sourceFp64(srcOffs[i], srcT[i].isx, srcT[i].isy, srcT[i].isz, std::max(0, o.factored_radius),
+                                        nx, ny, nz, dx, dy, dz));
         // corner init: slowness as the field type holds it, offsets in FP64
         corners[i] = eikx::Corner3{srcT[i].isx, srcT[i].isy, srcT[i].isz, srcOffs[i][0], srcOffs[i][1], srcOffs[i][2],
                                    static_cast<double>(static_cast<T>(s))};
@@ -461,7 +487,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     const int mailWords = paired ? 2 : static_cast<int>(sizeof(T) / 4);   // tagged 64-bit words per unit
     const size_t mboxBytes = static_cast<size_t>(nProgress) * (DIM == 3 ? ly + lz : 1) * Px * mailWords * 8;
     const void *before[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
-                            w.iterations.p, w.order.p, w.srcs.p, w.corners.p, w.srcs64.p};
+                            w.iterations.p, w.order.p, w.srcs.p, w.corners.p, w.srcs64.p, w.factor.p};
     EIKX_CUDA(w.tt.ensure(ttBytes));
     if (w.mbox.bytes < mboxBytes || !w.mbox.p) {
         // fresh words carry tag 0, which no sweep uses
@@ -481,9 +507,12 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     EIKX_CUDA(w.srcs.ensure(static_cast<size_t>(nSrc) * sizeof(eikx::SourceT<T>)));
     EIKX_CUDA(w.corners.ensure(static_cast<size_t>(nSrc) * sizeof(eikx::Corner3)));
     EIKX_CUDA(w.pairs.ensure(static_cast<size_t>(nUnits) * sizeof(int2)));
-    if (!srcT64.empty()) EIKX_CUDA(w.srcs64.ensure(srcT64.size() * sizeof(eikx::SourceFp64)));
+    if (!srcT64.empty()) {
+        EIKX_CUDA(w.srcs64.ensure(srcT64.size() * sizeof(eikx::SourceFp64)));
+        EIKX_CUDA(assignFactorBoxes(srcT64, w.factor));
+    }
     const void *after[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
-                           w.iterations.p, w.order.p, w.srcs.p, w.corners.p, w.srcs64.p};
+                           w.iterations.p, w.order.p, w.srcs.p, w.corners.p, w.srcs64.p, w.factor.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) dropGraph(c);
 
     // small uploads through pinned staging
@@ -615,6 +644,10 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         int buf = 0;
         EIKX_CUDA(eikx::launchResetState(st, nSrc, buf, c->stream));
         ++launches;
+        if (srcs64) {
+            EIKX_CUDA(eikx::launchFactorBoxes(srcs64, nSrc, c->stream));
+            ++launches;
+        }
         if (warm) {
             EIKX_CUDA(cudaMemsetAsync(w.resetCount.p, 0, sizeof(unsigned long long), c->stream));
             EIKX_CUDA(eikx::launchWarmInit3<T>(w.tt.as<T>(), w.init.as<T>(), nSrc, fieldStride, Px, nx, ny, nz, dx, dy,
@@ -947,7 +980,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
 
     const bool near64 = sizeof(T) == 4 && o.near_fp64;
     const void *before[] = {w.tt.p, w.sp.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p, w.iterations.p,
-                            w.order.p, w.srcs.p, w.corners.p, w.units.p, w.srcs64.p};
+                            w.order.p, w.srcs.p, w.corners.p, w.units.p, w.srcs64.p, w.factor.p};
     EIKX_CUDA(w.tt.ensure(ttElems * sizeof(T)));
     EIKX_CUDA(w.sp.ensure(spElems * sizeof(T)));
     if (w.mbox.bytes < mboxWords * 8 || !w.mbox.p) {
@@ -973,8 +1006,10 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     EIKX_CUDA(w.badFlag.ensure(sizeof(int)));
     EIKX_CUDA(w.srcCells.ensure(static_cast<size_t>(nUnits) * sizeof(double) + sizeof(int)));
     if (near64) EIKX_CUDA(w.srcs64.ensure(static_cast<size_t>(nUnits) * sizeof(eikx::SourceFp64)));
+    // the factor tables are laid out below, once the sources are located; a grown buffer
+    // drops the cached graph there
     const void *after[] = {w.tt.p, w.sp.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p, w.iterations.p,
-                           w.order.p, w.srcs.p, w.corners.p, w.units.p, w.srcs64.p};
+                           w.order.p, w.srcs.p, w.corners.p, w.units.p, w.srcs64.p, w.factor.p};
     if (std::memcmp(before, after, sizeof(before)) != 0) w.dropGraph();
 
     // models -> cell slowness (FP64, natural) -> two padded copies in the sweep precision;
@@ -985,6 +1020,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     std::vector<eikx::Corner3> corners(nUnits);
     std::vector<eikx::Grid3Unit<T>> units(nUnits);
     std::vector<std::array<double, 3>> offs(nUnits), unitSpacing(nUnits);
+    std::vector<std::array<int, 3>> unitGrid(nUnits);
     T *ttBase = w.tt.as<T>();
     T *spBase = w.sp.as<T>();
     unsigned long long *mbBase = w.mbox.as<unsigned long long>();
@@ -1006,6 +1042,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
             srcT[u].isx = cx; srcT[u].isy = cy; srcT[u].isz = cz;
             offs[u] = {ox, oy, oz};
             unitSpacing[u] = {m.dx, m.dy, m.dz};
+            unitGrid[u] = {m.nx, m.ny, m.nz};
         }
         const bool nodal = m.model_kind == EIKX_NODAL_VELOCITY;
         const size_t nCell = static_cast<size_t>(m.nx - 1) * (m.ny - 1) * (m.nz - 1);
@@ -1063,9 +1100,17 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
         srcT[u].zs = static_cast<T>(offs[u][2]);
         srcT[u].sSrc = static_cast<T>(sc);
         if (near64)
-            srcT64.push_back(sourceFp64<T>(offs[u], sc, unitSpacing[u][0], unitSpacing[u][1], unitSpacing[u][2]));
+            srcT64.push_back(sourceFp64(offs[u], srcT[u].isx, srcT[u].isy, srcT[u].isz,
+                                        std::max(0, o.factored_radius), unitGrid[u][0], unitGrid[u][1],
+                                        unitGrid[u][2], unitSpacing[u][0], unitSpacing[u][1], unitSpacing[u][2]));
         corners[u] = eikx::Corner3{srcT[u].isx, srcT[u].isy, srcT[u].isz, offs[u][0], offs[u][1], offs[u][2],
                                    static_cast<double>(static_cast<T>(sc))};
+    }
+
+    if (near64) {
+        const void *fb = w.factor.p;
+        EIKX_CUDA(assignFactorBoxes(srcT64, w.factor));
+        if (w.factor.p != fb) w.dropGraph();
     }
 
     // work order: every unit's warp blocks, sorted by the step at which they can start
@@ -1157,6 +1202,10 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
         int buf = 0;
         EIKX_CUDA(eikx::launchResetState(st, nUnits, buf, c->stream));
         ++launches;
+        if (near64) {
+            EIKX_CUDA(eikx::launchFactorBoxes(w.srcs64.as<eikx::SourceFp64>(), nUnits, c->stream));
+            ++launches;
+        }
         for (int i = 0; i < nM; ++i) {
             const eikx_model3d &m = models[sel[i]];
             EIKX_CUDA(eikx::launchInit3<T>(ttBase + L[i].ttOff, L[i].nSrc, L[i].fieldStride, L[i].Px, m.nx, m.ny, m.nz,

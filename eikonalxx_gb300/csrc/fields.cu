@@ -125,17 +125,11 @@ __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fie
                 st.s7 = cell(cxu, cyo, czo);
                 st.t1 = tv(xs, iy, iz); st.t2 = tv(xs, ys, iz); st.t3 = tv(ix, ys, iz); st.t4 = tv(ix, iy, zs);
                 st.t5 = tv(xs, iy, zs); st.t6 = tv(xs, ys, zs); st.t7 = tv(ix, ys, zs);
-                // a near_fp64 solve gates with the FP64 factored branch its sweeps use
+                // a near_fp64 solve gates with the FP64 analytic factor its sweeps use
                 T u;
-                if constexpr (sizeof(T) == 4) {
-                    if (srcs64 && nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) {
-                        u = UNIFORM ? fd3UniformNearFp64<0>(src.isx, src.isy, src.isz, srcs64 + f, sg, ix, iy, iz, st)
-                                    : fd3NonUniformNearFp64<0>(src.isx, src.isy, src.isz, srcs64 + f, sg, ix, iy,
-                                                                iz, st);
-                    } else {
-                        u = UNIFORM ? fd3Uniform<T>(radius, h, src, sg, ix, iy, iz, st)
-                                    : fd3NonUniform<T>(radius, g, src, sg, ix, iy, iz, st);
-                    }
+                if (srcs64 && nearSource(radius, src.isx, src.isy, src.isz, ix, iy, iz)) {
+                    u = UNIFORM ? fd3UniformNear<T, true>(h, src, sg, ix, iy, iz, st, srcs64 + f)
+                                : fd3NonUniformNear<T, true>(g, src, sg, ix, iy, iz, st, srcs64 + f);
                 } else {
                     u = UNIFORM ? fd3Uniform<T>(radius, h, src, sg, ix, iy, iz, st)
                                 : fd3NonUniform<T>(radius, g, src, sg, ix, iy, iz, st);
@@ -160,6 +154,19 @@ __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fie
         tt[static_cast<long long>(f) * fieldStride + (static_cast<long long>(iz) * ny + iy) * pitch + ix] = v;
     }
     if (resets) atomicAdd(nReset, resets);
+}
+
+// FP64 analytic-factor tables (eikx_options.near_fp64): one block per field fills its box
+// of D and U values around the source with the FP64 terms of factorTerms.
+__global__ void factorBoxKernel(const SourceFp64 *srcs) {
+    const SourceFp64 f = srcs[blockIdx.x];
+    if (!f.box) return;
+    FactorEntry *box = const_cast<FactorEntry *>(f.box);
+    const int n = f.bnx * f.bny * f.bnz;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int bx = i % f.bnx, by = (i / f.bnx) % f.bny, bz = i / (f.bnx * f.bny);
+        box[i] = factorTerms(f, f.bx0 + bx, f.by0 + by, f.bz0 + bz);
+    }
 }
 
 // Pads of the pitched rows (x >= nx) stay HUGE in a warm start.
@@ -488,6 +495,11 @@ template cudaError_t launchWarmInit3<double>(double *, const double *, int, long
                                              double, double, const Corner3 *, const SourceT<double> *, const double *,
                                              int, bool, double, const Spacing3<double> &, double, int, int,
                                              const SourceFp64 *, unsigned long long *, cudaStream_t);
+
+cudaError_t launchFactorBoxes(const SourceFp64 *srcs, int nFields, cudaStream_t s) {
+    factorBoxKernel<<<nFields, 256, 0, s>>>(srcs);
+    return cudaGetLastError();
+}
 
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st) {
     positiveKernel<double><<<gridFor(n), kThreads, 0, st>>>(s, n, flag);

@@ -41,15 +41,6 @@ template <class T> struct SourceT {
     T sSrc;
 };
 
-// The FP64 factored branch of an FP32 sweep (eikx_options.near_fp64): a node within the
-// factored radius is updated by the double-precision operator -- the reference's
-// Solver3D<double> arithmetic -- on its FP32 neighbours widened to double, with the
-// analytic factor T0 and its gradient from these FP64 source offsets, source-cell
-// slowness (as the sweep holds it) and grid spacing; the result is rounded to FP32.
-// Kept apart from SourceT, so the kernels without this branch carry none of it.
-struct SourceFp64 {
-    double xs, ys, zs, s, dx, dy, dz;
-};
 
 // Analytic homogeneous time and gradient (computeAnalyticalTravelTime,
 // solverUtilities3d.hpp:138-208).
@@ -86,6 +77,70 @@ template <class T> struct Stencil3 {
     T s0, s1, s2, s3, s4, s5, s7;
     T t1, t2, t3, t4, t5, t6, t7;
 };
+
+// The FP64 analytic factor of an FP32 sweep (eikx_options.near_fp64).  Within the
+// factored radius the reference forms T0 = s0 |x - xs| (s0 the node's home-cell
+// slowness), its gradient s0 (x - xs) / |x - xs|, the differences tau_k = t_k - T0_k at
+// the 7 upwind neighbours and the candidate T0 + correction in the sweep type
+// (solverUtilities3d.hpp:372-553).  In this mode they are formed in FP64 -- the distance
+// D and the direction U = (x - xs) / D from FP64 offsets and spacing, T0 = s0 D, the
+// differences, the gradient s0 U and the final sum -- and rounded to FP32, while the
+// quadratic solves stay in FP32.  D and U of the nodes around each field's source are
+// tabulated once per solve (`box`); a node outside the box forms them inline with the
+// same FP64 expressions.  Kept apart from SourceT, so the kernels without this mode
+// carry none of it.
+struct alignas(16) FactorEntry {
+    double d, ux, uy, uz;
+};
+struct SourceFp64 {
+    double xs, ys, zs;          // source offsets from the origin (FP64)
+    double dx, dy, dz;          // grid spacing (FP64)
+    const FactorEntry *box;     // D and U of nodes [bx0, bx0 + bnx) x ... (null: inline)
+    int bx0, by0, bz0, bnx, bny, bnz;
+};
+// Largest factor table of one field (nodes); a larger factored region forms D and U inline.
+constexpr int kMaxFactorBox = 32768;
+// D and U of node (ix, iy, iz) in FP64 (the distance as analyticT3<double> forms it).
+__host__ __device__ inline FactorEntry factorTerms(const SourceFp64 &f, int ix, int iy, int iz) {
+    const double ddx = ix * f.dx - f.xs, ddy = iy * f.dy - f.ys, ddz = iz * f.dz - f.zs;
+    const double d = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+    FactorEntry e;
+    e.d = d;
+    e.ux = d > 0 ? ddx / d : 0.0;
+    e.uy = d > 0 ? ddy / d : 0.0;
+    e.uz = d > 0 ? ddz / d : 0.0;
+    return e;
+}
+// D and U of node (ix, iy, iz): the table's entry or, outside it, the same FP64 terms.
+__device__ __forceinline__ FactorEntry factorEntry(const SourceFp64 &f, int ix, int iy, int iz) {
+    const int bx = ix - f.bx0, by = iy - f.by0, bz = iz - f.bz0;
+    if (f.box && bx >= 0 && bx < f.bnx && by >= 0 && by < f.bny && bz >= 0 && bz < f.bnz)
+        return f.box[(static_cast<long long>(bz) * f.bny + by) * f.bnx + bx];
+    return factorTerms(f, ix, iy, iz);
+}
+// The factor terms of the factored branch at node (ix, iy, iz) with home-cell slowness s0:
+// T0 (FP64, returned), the signed gradient and tau_1..tau_7 rounded to FP32.
+__device__ __forceinline__ double factorFp64(const SourceFp64 &f, const SweepSigns &sg, int ix, int iy, int iz,
+                                             float s0, const Stencil3<float> &n, float &gx, float &gy, float &gz,
+                                             float (&tau)[7]) {
+    const double s = s0;
+    const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
+    const FactorEntry e0 = factorEntry(f, ix, iy, iz);
+    gx = static_cast<float>(s * e0.ux);
+    gy = static_cast<float>(s * e0.uy);
+    gz = static_cast<float>(s * e0.uz);
+    auto tauOf = [&](float t, int x, int y, int z) {
+        return static_cast<float>(static_cast<double>(t) - s * factorEntry(f, x, y, z).d);
+    };
+    tau[0] = tauOf(n.t1, xu, iy, iz);
+    tau[1] = tauOf(n.t2, xu, yu, iz);
+    tau[2] = tauOf(n.t3, ix, yu, iz);
+    tau[3] = tauOf(n.t4, ix, iy, zu);
+    tau[4] = tauOf(n.t5, xu, iy, zu);
+    tau[5] = tauOf(n.t6, xu, yu, zu);
+    tau[6] = tauOf(n.t7, ix, yu, zu);
+    return s * e0.d;
+}
 
 // 3D uniform-grid update (solverUtilities3d.hpp:258-558), split at the reference's
 // branch on the factored radius (:286-300): fd3UniformFar is the Cartesian branch, taken
@@ -196,22 +251,38 @@ __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t
     return dmin(t1d, dmin(t2d, third * (S + dsqrt(det))));
 }
 
-template <class T>
+// F64: the analytic factor in FP64 (SourceFp64, eikx_options.near_fp64; FP32 sweeps only).
+template <class T, bool F64 = false>
 __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const SweepSigns &sg,
-                                            int ix, int iy, int iz, const Stencil3<T> &n) {
+                                            int ix, int iy, int iz, const Stencil3<T> &n,
+                                            const SourceFp64 *f64 = nullptr) {
     EIKX_FD3_UNIFORM_PREFIX
     {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
         T t0, dt0dx, dt0dy, dt0dz;
-        analyticTG3(ix, iy, iz, h, h, h, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
-        const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
-        T tau1 = t1 - analyticT3(xu, iy, iz, h, h, h, xs, ys, zs, s0);
-        T tau2 = t2 - analyticT3(xu, yu, iz, h, h, h, xs, ys, zs, s0);
-        T tau3 = t3 - analyticT3(ix, yu, iz, h, h, h, xs, ys, zs, s0);
-        T tau4 = t4 - analyticT3(ix, iy, zu, h, h, h, xs, ys, zs, s0);
-        T tau5 = t5 - analyticT3(xu, iy, zu, h, h, h, xs, ys, zs, s0);
-        T tau6 = t6 - analyticT3(xu, yu, zu, h, h, h, xs, ys, zs, s0);
-        T tau7 = t7 - analyticT3(ix, yu, zu, h, h, h, xs, ys, zs, s0);
+        T tau1, tau2, tau3, tau4, tau5, tau6, tau7;
+        double t0d = 0;
+        if constexpr (F64 && sizeof(T) == 4) {
+            T tau[7];
+            t0d = factorFp64(*f64, sg, ix, iy, iz, s0, n, dt0dx, dt0dy, dt0dz, tau);
+            t0 = static_cast<T>(t0d);
+            tau1 = tau[0]; tau2 = tau[1]; tau3 = tau[2]; tau4 = tau[3]; tau5 = tau[4]; tau6 = tau[5]; tau7 = tau[6];
+        } else {
+            analyticTG3(ix, iy, iz, h, h, h, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
+            const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
+            tau1 = t1 - analyticT3(xu, iy, iz, h, h, h, xs, ys, zs, s0);
+            tau2 = t2 - analyticT3(xu, yu, iz, h, h, h, xs, ys, zs, s0);
+            tau3 = t3 - analyticT3(ix, yu, iz, h, h, h, xs, ys, zs, s0);
+            tau4 = t4 - analyticT3(ix, iy, zu, h, h, h, xs, ys, zs, s0);
+            tau5 = t5 - analyticT3(xu, iy, zu, h, h, h, xs, ys, zs, s0);
+            tau6 = t6 - analyticT3(xu, yu, zu, h, h, h, xs, ys, zs, s0);
+            tau7 = t7 - analyticT3(ix, yu, zu, h, h, h, xs, ys, zs, s0);
+        }
+        // T0 + correction: in FP64 when the factor is
+        auto plusT0 = [&](T d) -> T {
+            if constexpr (F64 && sizeof(T) == 4) return static_cast<T>(t0d + static_cast<double>(d));
+            else return t0 + d;
+        };
         dt0dx = sg.signX * dt0dx;
         dt0dy = sg.signY * dt0dy;
         dt0dz = sg.signZ * dt0dz;
@@ -227,7 +298,7 @@ __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const Sw
         T det = b * b - 4 * a * c;
         T t2d = huge;
         if (det > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03) {
-            t2d = t0 + (-b + dsqrt(det)) / (2 * a);
+            t2d = plusT0((-b + dsqrt(det)) / (2 * a));
             if (t2d < t1 || t2d < t4) t2d = huge;
         }
         T pYZ = tau3 - tau4 + tau7;
@@ -238,7 +309,7 @@ __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const Sw
         det = b * b - 4 * a * c;
         T t2d2 = huge;
         if (det >= 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01) {
-            t2d2 = t0 + (-b + dsqrt(det)) / (2 * a);
+            t2d2 = plusT0((-b + dsqrt(det)) / (2 * a));
             if (t2d2 < t3 || t2d2 < t4) t2d2 = huge;
         }
         t2d = dmin(t2d, t2d2);
@@ -250,7 +321,7 @@ __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const Sw
         det = b * b - 4 * a * c;
         T t2d3 = huge;
         if (det >= 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04) {
-            t2d3 = t0 + (-b + dsqrt(det)) / (2 * a);
+            t2d3 = plusT0((-b + dsqrt(det)) / (2 * a));
             if (t2d3 < t1 || t2d3 < t3) t2d3 = huge;
         }
         t2d = dmin(t2d, t2d3);
@@ -264,7 +335,7 @@ __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const Sw
             c = h2inv * (taux * taux + tauy * tauy + tauz * tauz) -
                 (6 * hi) * (dt0dx * taux + dt0dy * tauy + dt0dz * tauz) + 9 * (sSrc * sSrc - s0 * s0);
             det = b * b - 4 * a * c;
-            if (det >= 0) t3d = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (det >= 0) t3d = plusT0((-b + dsqrt(det)) / (2 * a));
             if (t3d < t1 || t3d < t3 || t3d < t4) t3d = huge;
         }
         tUpd = dmin(t1d, dmin(t2d, t3d));
@@ -361,23 +432,36 @@ __device__ __forceinline__ T fd3NonUniformFar(const Spacing3<T> &g, const Stenci
     return tUpd;
 }
 
-template <class T>
+template <class T, bool F64 = false>
 __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const SourceT<T> &src,
                                                const SweepSigns &sg, int ix, int iy, int iz,
-                                               const Stencil3<T> &n) {
+                                               const Stencil3<T> &n, const SourceFp64 *f64 = nullptr) {
     EIKX_FD3_NONUNIFORM_PREFIX
     {
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
         T t0, dt0dx, dt0dy, dt0dz;
-        analyticTG3(ix, iy, iz, dx, dy, dz, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
-        const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
-        T tau1 = t1 - analyticT3(xu, iy, iz, dx, dy, dz, xs, ys, zs, s0);
-        T tau2 = t2 - analyticT3(xu, yu, iz, dx, dy, dz, xs, ys, zs, s0);
-        T tau3 = t3 - analyticT3(ix, yu, iz, dx, dy, dz, xs, ys, zs, s0);
-        T tau4 = t4 - analyticT3(ix, iy, zu, dx, dy, dz, xs, ys, zs, s0);
-        T tau5 = t5 - analyticT3(xu, iy, zu, dx, dy, dz, xs, ys, zs, s0);
-        T tau6 = t6 - analyticT3(xu, yu, zu, dx, dy, dz, xs, ys, zs, s0);
-        T tau7 = t7 - analyticT3(ix, yu, zu, dx, dy, dz, xs, ys, zs, s0);
+        T tau1, tau2, tau3, tau4, tau5, tau6, tau7;
+        double t0d = 0;
+        if constexpr (F64 && sizeof(T) == 4) {
+            T tau[7];
+            t0d = factorFp64(*f64, sg, ix, iy, iz, s0, n, dt0dx, dt0dy, dt0dz, tau);
+            t0 = static_cast<T>(t0d);
+            tau1 = tau[0]; tau2 = tau[1]; tau3 = tau[2]; tau4 = tau[3]; tau5 = tau[4]; tau6 = tau[5]; tau7 = tau[6];
+        } else {
+            analyticTG3(ix, iy, iz, dx, dy, dz, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
+            const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
+            tau1 = t1 - analyticT3(xu, iy, iz, dx, dy, dz, xs, ys, zs, s0);
+            tau2 = t2 - analyticT3(xu, yu, iz, dx, dy, dz, xs, ys, zs, s0);
+            tau3 = t3 - analyticT3(ix, yu, iz, dx, dy, dz, xs, ys, zs, s0);
+            tau4 = t4 - analyticT3(ix, iy, zu, dx, dy, dz, xs, ys, zs, s0);
+            tau5 = t5 - analyticT3(xu, iy, zu, dx, dy, dz, xs, ys, zs, s0);
+            tau6 = t6 - analyticT3(xu, yu, zu, dx, dy, dz, xs, ys, zs, s0);
+            tau7 = t7 - analyticT3(ix, yu, zu, dx, dy, dz, xs, ys, zs, s0);
+        }
+        auto plusT0 = [&](T d) -> T {
+            if constexpr (F64 && sizeof(T) == 4) return static_cast<T>(t0d + static_cast<double>(d));
+            else return t0 + d;
+        };
         dt0dx = sg.signX * dt0dx;
         dt0dy = sg.signY * dt0dy;
         dt0dz = sg.signZ * dt0dz;
@@ -392,7 +476,7 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
         T det = b * b - 4 * a * c;
         T t2d = huge;
         if (det > 0 && t1 < t4 + dz * minS0S3 && t4 < t1 + dx * minS0S3) {
-            t2d = t0 + (-b + dsqrt(det)) / (2 * a);
+            t2d = plusT0((-b + dsqrt(det)) / (2 * a));
             if (t2d < t1 || t2d < t4) t2d = huge;
         }
         p = tau3 - tau4 + tau7;
@@ -404,7 +488,7 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
         det = b * b - 4 * a * c;
         T t2d2 = huge;
         if (det > 0 && t3 < t4 + dz * minS0S1 && t4 < t3 + dy * minS0S1) {
-            t2d2 = t0 + (-b + dsqrt(det)) / (2 * a);
+            t2d2 = plusT0((-b + dsqrt(det)) / (2 * a));
             if (t2d2 < t3 || t2d2 < t4) t2d2 = huge;
         }
         t2d = dmin(t2d, t2d2);
@@ -417,7 +501,7 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
         det = b * b - 4 * a * c;
         T t2d3 = huge;
         if (det > 0 && t3 < t1 + dx * minS0S4 && t1 < t3 + dy * minS0S4) {
-            t2d3 = t0 + (-b + dsqrt(det)) / (2 * a);
+            t2d3 = plusT0((-b + dsqrt(det)) / (2 * a));
             if (t2d3 < t1 || t2d3 < t3) t2d3 = huge;
         }
         t2d = dmin(t2d, t2d3);
@@ -434,7 +518,7 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
                 6 * (dt0dx * taux * dxInv + dt0dy * tauy * dyInv + dt0dz * tauz * dzInv) +
                 9 * (sSrc * sSrc - s0 * s0);
             det = b * b - 4 * a * c;
-            if (det >= 0) t3d = t0 + (-b + dsqrt(det)) / (2 * a);
+            if (det >= 0) t3d = plusT0((-b + dsqrt(det)) / (2 * a));
             if (t3d < t1 || t3d < t3 || t3d < t4) t3d = huge;
         }
         tUpd = dmin(t1d, dmin(t2d, t3d));
@@ -442,47 +526,6 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
     return tUpd;
 }
 #undef EIKX_FD3_NONUNIFORM_PREFIX
-
-// The FP64 factored branch of an FP32 sweep (SourceFp64): the operands widened to
-// double, the double-precision operator of the reference (Solver3D is instantiated for
-// double only, src/solver3d.cpp:626-627), the result rounded to FP32.  Out of line: only
-// the few hundred nodes per field within the factored radius take it.
-__device__ __forceinline__ Stencil3<double> widen(const Stencil3<float> &n) {
-    Stencil3<double> m;
-    m.s0 = n.s0; m.s1 = n.s1; m.s2 = n.s2; m.s3 = n.s3; m.s4 = n.s4; m.s5 = n.s5; m.s7 = n.s7;
-    m.t1 = n.t1; m.t2 = n.t2; m.t3 = n.t3; m.t4 = n.t4; m.t5 = n.t5; m.t6 = n.t6; m.t7 = n.t7;
-    return m;
-}
-__device__ __forceinline__ SourceT<double> sourceFp64(int isx, int isy, int isz, const SourceFp64 &d) {
-    SourceT<double> r;
-    r.isx = isx; r.isy = isy; r.isz = isz;
-    r.xs = d.xs; r.ys = d.ys; r.zs = d.zs; r.sSrc = d.s;
-    return r;
-}
-template <int D>
-__device__ __noinline__ float fd3UniformNearFp64(int isx, int isy, int isz, const SourceFp64 *dp, const SweepSigns sg,
-                                                 int ix, int iy, int iz, const Stencil3<float> n) {
-    const SourceFp64 d = *dp;
-    return static_cast<float>(fd3UniformNear<double>(d.dx, sourceFp64(isx, isy, isz, d), sg, ix, iy, iz, widen(n)));
-}
-template <int D>
-__device__ __noinline__ float fd3NonUniformNearFp64(int isx, int isy, int isz, const SourceFp64 *dp,
-                                                    const SweepSigns sg, int ix, int iy, int iz,
-                                                    const Stencil3<float> n) {
-    const SourceFp64 d = *dp;
-    // the non-uniform constants in double, as the host forms them for an FP64 solve
-    // (include/private/solver3d.hpp:247-261)
-    Spacing3<double> g;
-    g.dx = d.dx; g.dy = d.dy; g.dz = d.dz;
-    g.dxInv = 1 / d.dx; g.dyInv = 1 / d.dy; g.dzInv = 1 / d.dz;
-    g.dx2Inv = 1 / (d.dx * d.dx); g.dy2Inv = 1 / (d.dy * d.dy); g.dz2Inv = 1 / (d.dz * d.dz);
-    g.dx_dz = d.dx / d.dz; g.dz_dx = d.dz / d.dx; g.dy_dz = d.dy / d.dz; g.dz_dy = d.dz / d.dy;
-    g.dx_dy = d.dx / d.dy; g.dy_dx = d.dy / d.dx;
-    g.dx2_p_dz2_inv = 1 / (d.dx * d.dx + d.dz * d.dz);
-    g.dy2_p_dz2_inv = 1 / (d.dy * d.dy + d.dz * d.dz);
-    g.dx2_p_dy2_inv = 1 / (d.dx * d.dx + d.dy * d.dy);
-    return static_cast<float>(fd3NonUniformNear<double>(g, sourceFp64(isx, isy, isz, d), sg, ix, iy, iz, widen(n)));
-}
 
 template <class T>
 __device__ __forceinline__ T fd3NonUniform(int radius, const Spacing3<T> &g, const SourceT<T> &src,

@@ -110,16 +110,16 @@ __global__ void orderKernel(int4 *order, int tilesY, int tilesZ, int ly, int lz)
 }
 
 // Source table of the field: the source-cell slowness is read from the caller's model;
-// src64 (FP64 factored branch, eikx_options.near_fp64) is filled when not null.
+// src64 (the FP64 analytic factor, eikx_options.near_fp64) is copied when not null.
 __global__ void sourceKernel(eikx::SourceT<float> *src, eikx::Corner3 *corner, eikx::SourceFp64 *src64,
-                             const float *slowness, int ncx, int ncy, int cx, int cy, int cz, double ox, double oy,
-                             double oz, double dx, double dy, double dz) {
+                             eikx::SourceFp64 f64, const float *slowness, int ncx, int ncy, int cx, int cy, int cz,
+                             double ox, double oy, double oz) {
     if (blockIdx.x != 0 || threadIdx.x != 0) return;
     const float s = slowness[(static_cast<long long>(cz) * ncy + cy) * ncx + cx];
     src->isx = cx; src->isy = cy; src->isz = cz;
     src->xs = static_cast<float>(ox); src->ys = static_cast<float>(oy); src->zs = static_cast<float>(oz);
     src->sSrc = s;
-    if (src64) *src64 = eikx::SourceFp64{ox, oy, oz, static_cast<double>(s), dx, dy, dz};
+    if (src64) *src64 = f64;
     corner->isx = cx; corner->isy = cy; corner->isz = cz;
     corner->xo = ox; corner->yo = oy; corner->zo = oz;
     corner->s = static_cast<double>(s);
@@ -182,6 +182,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     plan.take<eikx::SourceT<float>>(1);
     plan.take<eikx::Corner3>(1);
     plan.take<eikx::SourceFp64>(1);
+    if (o.near_fp64) plan.take<eikx::FactorEntry>(eikx::kMaxFactorBox);         // FP64 factor table
     if (plan.used > kScratchBytes)
         return err(EIKX_ERR_INVALID, "grid " + std::to_string(nx) + "x" + std::to_string(ny) + "x" +
                                          std::to_string(nz) + " needs " + std::to_string(plan.used) +
@@ -207,6 +208,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     eikx::SourceT<float> *srcDev = cv.take<eikx::SourceT<float>>(1);
     eikx::Corner3 *cornerDev = cv.take<eikx::Corner3>(1);
     eikx::SourceFp64 *src64Dev = cv.take<eikx::SourceFp64>(1);
+    eikx::FactorEntry *factorDev = o.near_fp64 ? cv.take<eikx::FactorEntry>(eikx::kMaxFactorBox) : nullptr;
 
     int numSMs = 0;
     NOALLOC_CUDA(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device));
@@ -248,9 +250,21 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     if (bad) return err(EIKX_ERR_INVALID, "Non-positive velocities detected");
     orderKernel<<<(nTiles + 127) / 128, 128, 0, stream>>>(order, tilesY, tilesZ, ly, lz);
     NOALLOC_CUDA(cudaGetLastError());
-    sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, o.near_fp64 ? src64Dev : nullptr, slowness, nx - 1, ny - 1,
-                                       cx, cy, cz, ox, oy, oz, dx, dy, dz);
+    // FP64 analytic factor: offsets, spacing and the factor table carved from the scratch
+    eikx::SourceFp64 f64{};
+    f64.xs = ox; f64.ys = oy; f64.zs = oz; f64.dx = dx; f64.dy = dy; f64.dz = dz;
+    if (o.near_fp64) {
+        int bo[3], be[3];
+        if (eikx::factorBox(cx, cy, cz, o.factored_radius, nx, ny, nz, bo, be)) {
+            f64.box = factorDev;
+            f64.bx0 = bo[0]; f64.by0 = bo[1]; f64.bz0 = bo[2];
+            f64.bnx = be[0]; f64.bny = be[1]; f64.bnz = be[2];
+        }
+    }
+    sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, o.near_fp64 ? src64Dev : nullptr, f64, slowness, nx - 1,
+                                       ny - 1, cx, cy, cz, ox, oy, oz);
     NOALLOC_CUDA(cudaGetLastError());
+    if (o.near_fp64 && f64.box) NOALLOC_CUDA(eikx::launchFactorBoxes(src64Dev, 1, stream));
     NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spPos, spPitch, 3, slowness, nx, ny, nz, stream)));
     NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spNeg, spPitch, 0, slowness, nx, ny, nz, stream)));
     NOALLOC_CUDA(eikx::launchResetState(st, 1, 0, stream));

@@ -171,16 +171,18 @@ __device__ __noinline__ T nearNonUniform(const Spacing3<T> g, const SourceT<T> s
                                          int iy, int iz, const Stencil3<T> n) {
     return fd3NonUniformNear(g, src, sg, ix, iy, iz, n);
 }
-// The FP64 factored branch of FP32 sweeps (eikx_options.near_fp64).
+// The factored branch with the analytic factor in FP64 (eikx_options.near_fp64, FP32).
 template <class T>
-__device__ __forceinline__ T nearFp64(bool uniform, const SourceT<T> &src, const SourceFp64 *d, const SweepSigns &sg,
-                                      int ix, int iy, int iz, const Stencil3<T> &n) {
-    if constexpr (sizeof(T) == 4) {
-        return uniform ? fd3UniformNearFp64<0>(src.isx, src.isy, src.isz, d, sg, ix, iy, iz, n)
-                       : fd3NonUniformNearFp64<0>(src.isx, src.isy, src.isz, d, sg, ix, iy, iz, n);
-    } else {
-        return T(0);   // never instantiated for FP64 sweeps
-    }
+__device__ __noinline__ T nearUniform64(T h, const SourceT<T> src, const SourceFp64 *f, const SweepSigns sg, int ix,
+                                        int iy, int iz, const Stencil3<T> n) {
+    const SourceFp64 d = *f;
+    return fd3UniformNear<T, true>(h, src, sg, ix, iy, iz, n, &d);
+}
+template <class T>
+__device__ __noinline__ T nearNonUniform64(const Spacing3<T> g, const SourceT<T> src, const SourceFp64 *f,
+                                           const SweepSigns sg, int ix, int iy, int iz, const Stencil3<T> n) {
+    const SourceFp64 d = *f;
+    return fd3NonUniformNear<T, true>(g, src, sg, ix, iy, iz, n, &d);
 }
 
 __device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
@@ -188,9 +190,9 @@ __device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
 }
 
 // INIT: the source-limited initialisation pass (a.init = 1), compiled apart so that the
-// refinement sweeps carry none of its block skipping.  NEAR64: the FP64 factored branch
-// of FP32 sweeps (eikx_options.near_fp64), compiled into its own kernels
-// (sweep3ChunkNear64Kernel) so that the others do not reserve its registers.
+// refinement sweeps carry none of its block skipping.  NEAR64: the factored branch with
+// its analytic factor in FP64 (eikx_options.near_fp64, FP32 sweeps), compiled into its own
+// kernels (sweep3ChunkNear64Kernel) so that the others carry none of it.
 template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT, bool NEAR64>
 __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
     static_assert(LY * LZ == 32 && LZ + 1 + LY <= 32, "a warp holds 32 pencils and its halo helpers");
@@ -419,7 +421,8 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
                     const T t0 = out.v[e];
                     T tu;
                     if (NEAR64 && near) {
-                        tu = nearFp64<T>(UNIFORM, src, a.srcs64 + f, sg, xa, ya, za, n);
+                        if constexpr (UNIFORM) tu = nearUniform64<T>(h, src, a.srcs64 + f, sg, xa, ya, za, n);
+                        else tu = nearNonUniform64<T>(BATCH ? unit->sp3 : a.sp3, src, a.srcs64 + f, sg, xa, ya, za, n);
                     } else if (UNIFORM) {
                         // the Cartesian operators with lower-bound exits: min(t0, tu) is the
                         // same bit for bit as with fd3UniformFar

@@ -87,12 +87,15 @@ typedef struct {
                               start the 32-bit sweep-tag base this many tags below 2^32, so
                               that the next few solves cross the wrap-around (the host then
                               clears the mailbox and restarts the base at 1) */
-    int near_fp64;         /* 3D FP32 solves: 1 = nodes within the factored radius are updated
-                              in FP64 -- the analytic factor T0 = distance x source slowness,
-                              its gradient, the factored differences tau and the quadratic
-                              solves, i.e. the reference's double-precision operator
-                              (Solver3D<double>) on the FP32 neighbours -- and rounded to
-                              FP32; 0 (default) = in FP32 like the rest of the sweep.
+    int near_fp64;         /* 3D FP32 solves: 1 = the factored (near-source) branch forms its
+                              analytic factor in FP64: the distance D = |x - xs| and direction
+                              (x - xs) / D from FP64 offsets and spacing (tabulated once per
+                              solve around each source), T0 = s0 D with s0 the node's cell
+                              slowness, its gradient, the differences tau = t - T0 at the 7
+                              upwind neighbours and the candidate T0 + correction, each
+                              rounded to FP32; the quadratic solves stay in FP32.  0 (default)
+                              = all in FP32, as the reference's sweep type.  Runs on the
+                              chunk-step kernel (sweep_kernel and pair_fields give way).
                               Ignored by FP64 solves and 2D. */
     int warm_gate;         /* eikx_solve3d_warm's residual gate: 0 (default) = reset nodes
                               whose initial time lies more than gate_tol below the smallest

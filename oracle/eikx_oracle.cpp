@@ -82,13 +82,53 @@ struct Src3 {
     int isx, isy, isz;
     double xo, yo, zo;   // source offsets from the origin (m)
 };
+struct Grid3 {
+    int nx, ny, nz;
+    double dx, dy, dz;
+};
+
+// near_fp64 (FP32 sweeps; the GPU's eikx_options.near_fp64): the analytic factor of the
+// factored branch in FP64.  D = |x - xs| and U = (x - xs) / D from FP64 offsets and
+// spacing; T0 = s0 D, the gradient s0 U, the differences tau_k = t_k - s0 D_k and the sum
+// T0 + correction are formed in FP64 and rounded to the sweep type, the quadratic solves
+// stay in it.
+struct FactorTerms {
+    double d, ux, uy, uz;
+};
+inline FactorTerms factorTerms(const Grid3 &g, const Src3 &src, int ix, int iy, int iz) {
+    const double ddx = ix * g.dx - src.xo, ddy = iy * g.dy - src.yo, ddz = iz * g.dz - src.zo;
+    const double d = std::sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+    return {d, d > 0 ? ddx / d : 0.0, d > 0 ? ddy / d : 0.0, d > 0 ? ddz / d : 0.0};
+}
+// T0 (FP64, returned), the gradient and tau_1..tau_7 in T at node (ix, iy, iz).
+template <class T>
+double factorFp64(const Grid3 &g, const Src3 &src, const Sweep3 &sw, int ix, int iy, int iz, T s0,
+                  T t1, T t2, T t3, T t4, T t5, T t6, T t7, T &gx, T &gy, T &gz, T (&tau)[7]) {
+    const double s = s0;
+    const FactorTerms e0 = factorTerms(g, src, ix, iy, iz);
+    gx = static_cast<T>(s * e0.ux);
+    gy = static_cast<T>(s * e0.uy);
+    gz = static_cast<T>(s * e0.uz);
+    auto tauOf = [&](T t, int x, int y, int z) {
+        return static_cast<T>(static_cast<double>(t) - s * factorTerms(g, src, x, y, z).d);
+    };
+    const int xu = ix + sw.ixShift, yu = iy + sw.iyShift, zu = iz + sw.izShift;
+    tau[0] = tauOf(t1, xu, iy, iz);
+    tau[1] = tauOf(t2, xu, yu, iz);
+    tau[2] = tauOf(t3, ix, yu, iz);
+    tau[3] = tauOf(t4, ix, iy, zu);
+    tau[4] = tauOf(t5, xu, iy, zu);
+    tau[5] = tauOf(t6, xu, yu, zu);
+    tau[6] = tauOf(t7, ix, yu, zu);
+    return s * e0.d;
+}
 
 // Uniform-grid local solver, solverUtilities3d.hpp:258-558 (debug prints removed).
 template <class T>
 T fd3Uniform(int radius, T huge, T h, T sSrc, int ix, int iy, int iz, const Sweep3 &sw,
              const Src3 &src, T xs, T ys, T zs,
              T s0, T s1, T s2, T s3, T s4, T s5, T s7,
-             T t1, T t2, T t3, T t4, T t5, T t6, T t7) {
+             T t1, T t2, T t3, T t4, T t5, T t6, T t7, const Grid3 *g64 = nullptr) {
     T tUpd = huge;
     T minS0S3 = tmin(s0, s3);
     T minS0S1 = tmin(s0, s1);
@@ -133,14 +173,24 @@ T fd3Uniform(int radius, T huge, T h, T sSrc, int ix, int iy, int iz, const Swee
         // Factored ("spherical") branch exactly as the reference ships it: T0 uses the
         // home-cell slowness s0 (solverUtilities3d.hpp:373-378).
         T t0, dt0dx, dt0dy, dt0dz;
-        analyticTG(ix, iy, iz, h, h, h, xs, ys, zs, s0, &t0, &dt0dx, &dt0dy, &dt0dz);
-        T tau1 = t1 - analyticT(ix + sw.ixShift, iy, iz, h, h, h, xs, ys, zs, s0);
-        T tau2 = t2 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz, h, h, h, xs, ys, zs, s0);
-        T tau3 = t3 - analyticT(ix, iy + sw.iyShift, iz, h, h, h, xs, ys, zs, s0);
-        T tau4 = t4 - analyticT(ix, iy, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
-        T tau5 = t5 - analyticT(ix + sw.ixShift, iy, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
-        T tau6 = t6 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
-        T tau7 = t7 - analyticT(ix, iy + sw.iyShift, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
+        T tau1, tau2, tau3, tau4, tau5, tau6, tau7;
+        double t0d = 0;
+        if (g64) {
+            T tau[7];
+            t0d = factorFp64<T>(*g64, src, sw, ix, iy, iz, s0, t1, t2, t3, t4, t5, t6, t7, dt0dx, dt0dy, dt0dz, tau);
+            t0 = static_cast<T>(t0d);
+            tau1 = tau[0]; tau2 = tau[1]; tau3 = tau[2]; tau4 = tau[3]; tau5 = tau[4]; tau6 = tau[5]; tau7 = tau[6];
+        } else {
+            analyticTG(ix, iy, iz, h, h, h, xs, ys, zs, s0, &t0, &dt0dx, &dt0dy, &dt0dz);
+            tau1 = t1 - analyticT(ix + sw.ixShift, iy, iz, h, h, h, xs, ys, zs, s0);
+            tau2 = t2 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz, h, h, h, xs, ys, zs, s0);
+            tau3 = t3 - analyticT(ix, iy + sw.iyShift, iz, h, h, h, xs, ys, zs, s0);
+            tau4 = t4 - analyticT(ix, iy, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
+            tau5 = t5 - analyticT(ix + sw.ixShift, iy, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
+            tau6 = t6 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
+            tau7 = t7 - analyticT(ix, iy + sw.iyShift, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
+        }
+        auto plusT0 = [&](T d) -> T { return g64 ? static_cast<T>(t0d + static_cast<double>(d)) : t0 + d; };
         dt0dx = sw.signX * dt0dx;
         dt0dy = sw.signY * dt0dy;
         dt0dz = sw.signZ * dt0dz;
@@ -159,7 +209,7 @@ T fd3Uniform(int radius, T huge, T h, T sSrc, int ix, int iy, int iz, const Swee
         T t2d1 = huge;
         if (detXZ > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03) {
             tau = (-b + std::sqrt(detXZ)) / (2 * a);
-            t2d1 = t0 + tau;
+            t2d1 = plusT0(tau);
             if (t2d1 < t1 || t2d1 < t4) t2d1 = huge;
         }
         T t2d = t2d1;
@@ -173,7 +223,7 @@ T fd3Uniform(int radius, T huge, T h, T sSrc, int ix, int iy, int iz, const Swee
         T t2d2 = huge;
         if (detYZ >= 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01) {
             tau = (-b + std::sqrt(detYZ)) / (2 * a);
-            t2d2 = t0 + tau;
+            t2d2 = plusT0(tau);
             if (t2d2 < t3 || t2d2 < t4) t2d2 = huge;
         }
         t2d = tmin(t2d, t2d2);
@@ -187,7 +237,7 @@ T fd3Uniform(int radius, T huge, T h, T sSrc, int ix, int iy, int iz, const Swee
         T t2d3 = huge;
         if (detXY >= 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04) {
             tau = (-b + std::sqrt(detXY)) / (2 * a);
-            t2d3 = t0 + tau;
+            t2d3 = plusT0(tau);
             if (t2d3 < t1 || t2d3 < t3) t2d3 = huge;
         }
         t2d = tmin(t2d, t2d3);
@@ -202,7 +252,7 @@ T fd3Uniform(int radius, T huge, T h, T sSrc, int ix, int iy, int iz, const Swee
                 (6 * hi) * (dt0dx * taux + dt0dy * tauy + dt0dz * tauz) +
                 9 * (sSrc * sSrc - s0 * s0);
             T det = b * b - 4 * a * c;
-            if (det >= 0) t3d = t0 + (-b + std::sqrt(det)) / (2 * a);
+            if (det >= 0) t3d = plusT0((-b + std::sqrt(det)) / (2 * a));
             if (t3d < t1 || t3d < t3 || t3d < t4) t3d = huge;
         }
         tUpd = tmin(t1d, tmin(t2d, t3d));
@@ -233,7 +283,7 @@ template <class T>
 T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int iy, int iz,
                 const Sweep3 &sw, const Src3 &src, T xs, T ys, T zs,
                 T s0, T s1, T s2, T s3, T s4, T s5, T s7,
-                T t1, T t2, T t3, T t4, T t5, T t6, T t7) {
+                T t1, T t2, T t3, T t4, T t5, T t6, T t7, const Grid3 *g64 = nullptr) {
     const T dx = g.dx, dy = g.dy, dz = g.dz;
     T tUpd = huge;
     T minS0S3 = tmin(s0, s3);
@@ -292,14 +342,24 @@ T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int
         tUpd = tmin(t1d, tmin(t2d, t3d));
     } else {
         T t0, dt0dx, dt0dy, dt0dz;
-        analyticTG(ix, iy, iz, dx, dy, dz, xs, ys, zs, s0, &t0, &dt0dx, &dt0dy, &dt0dz);
-        T tau1 = t1 - analyticT(ix + sw.ixShift, iy, iz, dx, dy, dz, xs, ys, zs, s0);
-        T tau2 = t2 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz, dx, dy, dz, xs, ys, zs, s0);
-        T tau3 = t3 - analyticT(ix, iy + sw.iyShift, iz, dx, dy, dz, xs, ys, zs, s0);
-        T tau4 = t4 - analyticT(ix, iy, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
-        T tau5 = t5 - analyticT(ix + sw.ixShift, iy, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
-        T tau6 = t6 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
-        T tau7 = t7 - analyticT(ix, iy + sw.iyShift, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
+        T tau1, tau2, tau3, tau4, tau5, tau6, tau7;
+        double t0d = 0;
+        if (g64) {
+            T tau[7];
+            t0d = factorFp64<T>(*g64, src, sw, ix, iy, iz, s0, t1, t2, t3, t4, t5, t6, t7, dt0dx, dt0dy, dt0dz, tau);
+            t0 = static_cast<T>(t0d);
+            tau1 = tau[0]; tau2 = tau[1]; tau3 = tau[2]; tau4 = tau[3]; tau5 = tau[4]; tau6 = tau[5]; tau7 = tau[6];
+        } else {
+            analyticTG(ix, iy, iz, dx, dy, dz, xs, ys, zs, s0, &t0, &dt0dx, &dt0dy, &dt0dz);
+            tau1 = t1 - analyticT(ix + sw.ixShift, iy, iz, dx, dy, dz, xs, ys, zs, s0);
+            tau2 = t2 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz, dx, dy, dz, xs, ys, zs, s0);
+            tau3 = t3 - analyticT(ix, iy + sw.iyShift, iz, dx, dy, dz, xs, ys, zs, s0);
+            tau4 = t4 - analyticT(ix, iy, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
+            tau5 = t5 - analyticT(ix + sw.ixShift, iy, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
+            tau6 = t6 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
+            tau7 = t7 - analyticT(ix, iy + sw.iyShift, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
+        }
+        auto plusT0 = [&](T d) -> T { return g64 ? static_cast<T>(t0d + static_cast<double>(d)) : t0 + d; };
         dt0dx = sw.signX * dt0dx;
         dt0dy = sw.signY * dt0dy;
         dt0dz = sw.signZ * dt0dz;
@@ -315,7 +375,7 @@ T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int
         T detXZ = b * b - 4 * a * c;
         T t2d1 = huge;
         if (detXZ > 0 && t1 < t4 + dz * minS0S3 && t4 < t1 + dx * minS0S3) {
-            t2d1 = t0 + (-b + std::sqrt(detXZ)) / (2 * a);
+            t2d1 = plusT0((-b + std::sqrt(detXZ)) / (2 * a));
             if (t2d1 < t1 || t2d1 < t4) t2d1 = huge;
         }
         T t2d = t2d1;
@@ -329,7 +389,7 @@ T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int
         T detYZ = b * b - 4 * a * c;
         T t2d2 = huge;
         if (detYZ > 0 && t3 < t4 + dz * minS0S1 && t4 < t3 + dy * minS0S1) {
-            t2d2 = t0 + (-b + std::sqrt(detYZ)) / (2 * a);
+            t2d2 = plusT0((-b + std::sqrt(detYZ)) / (2 * a));
             if (t2d2 < t3 || t2d2 < t4) t2d2 = huge;
         }
         t2d = tmin(t2d, t2d2);
@@ -343,7 +403,7 @@ T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int
         T detXY = b * b - 4 * a * c;
         T t2d3 = huge;
         if (detXY > 0 && t3 < t1 + dx * minS0S4 && t1 < t3 + dy * minS0S4) {
-            t2d3 = t0 + (-b + std::sqrt(detXY)) / (2 * a);
+            t2d3 = plusT0((-b + std::sqrt(detXY)) / (2 * a));
             if (t2d3 < t1 || t2d3 < t3) t2d3 = huge;
         }
         t2d = tmin(t2d, t2d3);
@@ -360,7 +420,7 @@ T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int
                 6 * (dt0dx * taux * dxInv + dt0dy * tauy * dyInv + dt0dz * tauz * dzInv) +
                 9 * (sSrc * sSrc - s0 * s0);
             T det = b * b - 4 * a * c;
-            if (det >= 0) t3d = t0 + (-b + std::sqrt(det)) / (2 * a);
+            if (det >= 0) t3d = plusT0((-b + std::sqrt(det)) / (2 * a));
             if (t3d < t1 || t3d < t3 || t3d < t4) t3d = huge;
         }
         tUpd = tmin(t1d, tmin(t2d, t3d));
@@ -368,10 +428,6 @@ T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int
     return tUpd;
 }
 
-struct Grid3 {
-    int nx, ny, nz;
-    double dx, dy, dz;
-};
 
 // getLoopLimits (full, solverUtilities3d.hpp:944-1052) and the source-limited
 // variant used by the initialisation sweeps (:1075-1184), both expressed as
@@ -398,8 +454,8 @@ void loopLimits3(const Grid3 &g, const Sweep3 &sw, bool init, const Src3 &src,
 // Solver3DSweep<T,E>::updateFSM, include/private/solver3d.hpp:150-326, with the
 // stencil addressing of gridToSurroundingSlownessIndices (:1300-1442) and
 // gridToSurroundingTravelTimeIndices (:1460-1586).  Returns the largest decrease.
-// near_fp64 (FP32 solves): nodes within the factored radius take the double-precision
-// operator on their FP32 neighbours, rounded to FP32 -- the GPU's eikx_options.near_fp64.
+// near_fp64 (FP32 solves): the analytic factor of the factored branch in FP64 -- the
+// GPU's eikx_options.near_fp64 (factorFp64 below).
 int gNearFp64 = 0;
 
 template <class T>
@@ -416,7 +472,6 @@ double sweep3(int e, bool init, const Grid3 &g, int radius, const Src3 &src, T s
     const bool uniform = std::abs(g.dx - g.dy) < eps && std::abs(g.dx - g.dz) < eps;
     const T h = static_cast<T>(g.dx);
     NonUniform3<T> nu(static_cast<T>(g.dx), static_cast<T>(g.dy), static_cast<T>(g.dz));
-    const NonUniform3<double> nu64(g.dx, g.dy, g.dz);
     double diffMax = 0;
     auto cidx = [&](int cx, int cy, int cz) {
         return static_cast<size_t>(cz) * ncx * ncy + static_cast<size_t>(cy) * ncx + cx;
@@ -454,24 +509,13 @@ double sweep3(int e, bool init, const Grid3 &g, int radius, const Src3 &src, T s
                 T t5 = tt[gidx(xsft, iy, zsft)];
                 T t6 = tt[gidx(xsft, ysft, zsft)];
                 T t7 = tt[gidx(ix, ysft, zsft)];
-                const bool near = std::abs(src.isx - ix) <= radius && std::abs(src.isy - iy) <= radius &&
-                                  std::abs(src.isz - iz) <= radius;
-                T tUpd;
-                if (gNearFp64 && sizeof(T) == 4 && near) {
-                    // near_fp64: the double-precision operator (the reference's Solver3D<double>)
-                    // on the FP32 neighbours, with FP64 source offsets and spacing, rounded to T
-                    tUpd = static_cast<T>(uniform
-                        ? fd3Uniform<double>(radius, kHuge, g.dx, sSrc, ix, iy, iz, sw, src, src.xo, src.yo, src.zo,
-                                             s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7)
-                        : fd3NonUniform<double>(radius, kHuge, nu64, sSrc, ix, iy, iz, sw, src, src.xo, src.yo,
-                                                src.zo, s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7));
-                } else {
-                    tUpd = uniform
-                        ? fd3Uniform<T>(radius, huge, h, sSrc, ix, iy, iz, sw, src, xs, ys, zs,
-                                        s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7)
-                        : fd3NonUniform<T>(radius, huge, nu, sSrc, ix, iy, iz, sw, src, xs, ys, zs,
-                                           s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7);
-                }
+                // near_fp64 (FP32 sweeps): the analytic factor in FP64
+                const Grid3 *g64 = gNearFp64 && sizeof(T) == 4 ? &g : nullptr;
+                T tUpd = uniform
+                    ? fd3Uniform<T>(radius, huge, h, sSrc, ix, iy, iz, sw, src, xs, ys, zs,
+                                    s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7, g64)
+                    : fd3NonUniform<T>(radius, huge, nu, sSrc, ix, iy, iz, sw, src, xs, ys, zs,
+                                       s0, s1, s2, s3, s4, s5, s7, t1, t2, t3, t4, t5, t6, t7, g64);
                 if (tUpd < t0) {
                     tt[i0] = tUpd;
                     // decrease formed in T (exact by Sterbenz whenever it is below t0/2),
