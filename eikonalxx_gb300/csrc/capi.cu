@@ -333,13 +333,17 @@ template <> int precOf<float>() { return EIKX_F32; }
 template <> int precOf<double>() { return EIKX_F64; }
 
 // FP64 analytic factor of an FP32 sweep (eikx_options.near_fp64): the source offsets and
-// the grid spacing in FP64, and the field's factor-table box (its entries are assigned
-// by assignFactorBoxes).
+// the grid spacing in FP64, the model's unshifted padded FP32 slowness the table is filled
+// from, and the field's factor-table box (its entries are laid out by assignFactorTables).
 eikx::SourceFp64 sourceFp64(const std::array<double, 3> &off, int isx, int isy, int isz, int radius, int nx, int ny,
-                            int nz, double dx, double dy, double dz) {
+                            int nz, double dx, double dy, double dz, const float *spNeg, int spPitch) {
     eikx::SourceFp64 f{};
     f.xs = off[0]; f.ys = off[1]; f.zs = off[2];
     f.dx = dx; f.dy = dy; f.dz = dz;
+    f.sp = spNeg;
+    f.spPitch = spPitch;
+    f.spPlane = static_cast<long long>(spPitch) * (ny + 1);
+    f.ncx = nx - 1; f.ncy = ny - 1; f.ncz = nz - 1;
     int o[3], e[3];
     if (eikx::factorBox(isx, isy, isz, radius, nx, ny, nz, o, e)) {
         f.bx0 = o[0]; f.by0 = o[1]; f.bz0 = o[2];
@@ -347,17 +351,17 @@ eikx::SourceFp64 sourceFp64(const std::array<double, 3> &off, int isx, int isy, 
     }
     return f;
 }
-// Lays the fields' factor tables out in `buf` (grown as needed; false on failure) and
-// points each record at its table.  Records whose box is too large keep a null table.
-cudaError_t assignFactorBoxes(std::vector<eikx::SourceFp64> &recs, DevBuf &buf) {
+// Lays the fields' factor tables (8 sweep orderings x box) out in `buf`, grown as needed,
+// and points each record at its table.  Records whose box is too large keep a null table.
+cudaError_t assignFactorTables(std::vector<eikx::SourceFp64> &recs, DevBuf &buf) {
     size_t total = 0;
-    for (const auto &f : recs) total += static_cast<size_t>(f.bnx) * f.bny * f.bnz;
+    for (const auto &f : recs) total += 8 * static_cast<size_t>(f.bnx) * f.bny * f.bnz;
     if (total == 0) return cudaSuccess;
-    if (cudaError_t e = buf.ensure(total * sizeof(eikx::FactorEntry)); e != cudaSuccess) return e;
+    if (cudaError_t e = buf.ensure(total * sizeof(eikx::NearFactor)); e != cudaSuccess) return e;
     size_t off = 0;
     for (auto &f : recs) {
-        const size_t n = static_cast<size_t>(f.bnx) * f.bny * f.bnz;
-        f.box = n ? buf.as<eikx::FactorEntry>() + off : nullptr;
+        const size_t n = 8 * static_cast<size_t>(f.bnx) * f.bny * f.bnz;
+        f.table = n ? buf.as<eikx::NearFactor>() + off : nullptr;
         off += n;
     }
     return cudaSuccess;
@@ -418,7 +422,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         srcT[i].sSrc = static_cast<T>(s);
         if (DIM == 3 && P == EIKX_F32 && o.near_fp64)
             srcT64.push_back(sourceFp64(srcOffs[i], srcT[i].isx, srcT[i].isy, srcT[i].isz, std::max(0, o.factored_radius),
-                                        nx, ny, nz, dx, dy, dz));
+                                        nx, ny, nz, dx, dy, dz, nullptr, spPitch));
         // corner init: slowness as the field type holds it, offsets in FP64
         corners[i] = eikx::Corner3{srcT[i].isx, srcT[i].isy, srcT[i].isz, srcOffs[i][0], srcOffs[i][1], srcOffs[i][2],
                                    static_cast<double>(static_cast<T>(s))};
@@ -442,6 +446,15 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
                                                                nx, nz, c->stream)));
         }
         spadValid = true;
+    }
+
+    // the factor tables are filled from the unshifted padded copy (FP32 sweeps)
+    for (auto &f : srcT64) {
+        if (f.bnx == 0)
+            return fail(EIKX_ERR_UNSUPPORTED, "near_fp64: the factored region of radius " +
+                                                  std::to_string(o.factored_radius) + " needs more than " +
+                                                  std::to_string(eikx::kMaxFactorTable) + " table entries");
+        f.sp = static_cast<const float *>(spad[1].p);
     }
 
     // geometry in the sweep type (include/private/solver3d.hpp:31-44, solver2d.hpp:29-46)
@@ -509,7 +522,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     EIKX_CUDA(w.pairs.ensure(static_cast<size_t>(nUnits) * sizeof(int2)));
     if (!srcT64.empty()) {
         EIKX_CUDA(w.srcs64.ensure(srcT64.size() * sizeof(eikx::SourceFp64)));
-        EIKX_CUDA(assignFactorBoxes(srcT64, w.factor));
+        EIKX_CUDA(assignFactorTables(srcT64, w.factor));
     }
     const void *after[] = {w.tt.p, w.mbox.p, w.epoch.p, w.residual.p, w.converged.p,
                            w.iterations.p, w.order.p, w.srcs.p, w.corners.p, w.srcs64.p, w.factor.p};
@@ -645,7 +658,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         EIKX_CUDA(eikx::launchResetState(st, nSrc, buf, c->stream));
         ++launches;
         if (srcs64) {
-            EIKX_CUDA(eikx::launchFactorBoxes(srcs64, nSrc, c->stream));
+            EIKX_CUDA(eikx::launchFactorTables(srcs64, nSrc, c->stream));
             ++launches;
         }
         if (warm) {
@@ -1102,14 +1115,20 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
         if (near64)
             srcT64.push_back(sourceFp64(offs[u], srcT[u].isx, srcT[u].isy, srcT[u].isz,
                                         std::max(0, o.factored_radius), unitGrid[u][0], unitGrid[u][1],
-                                        unitGrid[u][2], unitSpacing[u][0], unitSpacing[u][1], unitSpacing[u][2]));
+                                        unitGrid[u][2], unitSpacing[u][0], unitSpacing[u][1], unitSpacing[u][2],
+                                        reinterpret_cast<const float *>(units[u].spNeg), units[u].spPitch));
         corners[u] = eikx::Corner3{srcT[u].isx, srcT[u].isy, srcT[u].isz, offs[u][0], offs[u][1], offs[u][2],
                                    static_cast<double>(static_cast<T>(sc))};
     }
 
     if (near64) {
+        for (const auto &f : srcT64)
+            if (f.bnx == 0)
+                return fail(EIKX_ERR_UNSUPPORTED, "near_fp64: the factored region of radius " +
+                                                      std::to_string(o.factored_radius) + " needs more than " +
+                                                      std::to_string(eikx::kMaxFactorTable) + " table entries");
         const void *fb = w.factor.p;
-        EIKX_CUDA(assignFactorBoxes(srcT64, w.factor));
+        EIKX_CUDA(assignFactorTables(srcT64, w.factor));
         if (w.factor.p != fb) w.dropGraph();
     }
 
@@ -1203,7 +1222,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
         EIKX_CUDA(eikx::launchResetState(st, nUnits, buf, c->stream));
         ++launches;
         if (near64) {
-            EIKX_CUDA(eikx::launchFactorBoxes(w.srcs64.as<eikx::SourceFp64>(), nUnits, c->stream));
+            EIKX_CUDA(eikx::launchFactorTables(w.srcs64.as<eikx::SourceFp64>(), nUnits, c->stream));
             ++launches;
         }
         for (int i = 0; i < nM; ++i) {

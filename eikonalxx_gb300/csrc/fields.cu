@@ -156,16 +156,27 @@ __global__ void warmInit3Kernel(T *tt, const T *init, int nFields, long long fie
     if (resets) atomicAdd(nReset, resets);
 }
 
-// FP64 analytic-factor tables (eikx_options.near_fp64): one block per field fills its box
-// of D and U values around the source with the FP64 terms of factorTerms.
-__global__ void factorBoxKernel(const SourceFp64 *srcs) {
+// FP64 analytic-factor tables (eikx_options.near_fp64): one block per field fills the
+// entries of its box of near-source nodes for all 8 sweep orderings (nearFactor, FP64).
+__global__ void factorTableKernel(const SourceFp64 *srcs) {
     const SourceFp64 f = srcs[blockIdx.x];
-    if (!f.box) return;
-    FactorEntry *box = const_cast<FactorEntry *>(f.box);
-    const int n = f.bnx * f.bny * f.bnz;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int bx = i % f.bnx, by = (i / f.bnx) % f.bny, bz = i / (f.bnx * f.bny);
-        box[i] = factorTerms(f, f.bx0 + bx, f.by0 + by, f.bz0 + bz);
+    if (!f.table) return;
+    NearFactor *table = const_cast<NearFactor *>(f.table);
+    const int box = f.bnx * f.bny * f.bnz;
+    auto clampi = [](int a, int lo, int hi) { return a < lo ? lo : (a > hi ? hi : a); };
+    for (int i = threadIdx.x; i < 8 * box; i += blockDim.x) {
+        const int e = i / box, r = i - e * box;
+        const int ix = f.bx0 + r % f.bnx, iy = f.by0 + (r / f.bnx) % f.bny, iz = f.bz0 + r / (f.bnx * f.bny);
+        const int fx = e & 1, fy = (e >> 1) & 1, fz = (e >> 2) & 1;
+        SweepSigns sg;
+        sg.ixShift = fx ? 1 : -1; sg.iyShift = fy ? 1 : -1; sg.izShift = fz ? 1 : -1;
+        sg.signX = fx ? -1 : 1; sg.signY = fy ? -1 : 1; sg.signZ = fz ? -1 : 1;
+        // the node's home cell in this ordering (the sweep's s0)
+        const int cx = fx ? clampi(ix, 0, f.ncx - 1) : clampi(ix - 1, 0, f.ncx - 1);
+        const int cy = fy ? clampi(iy, 0, f.ncy - 1) : clampi(iy - 1, 0, f.ncy - 1);
+        const int cz = fz ? clampi(iz, 0, f.ncz - 1) : clampi(iz - 1, 0, f.ncz - 1);
+        const float s0 = f.sp[(cz + 1) * f.spPlane + static_cast<long long>(cy + 1) * f.spPitch + cx + 1];
+        table[i] = nearFactor(f, s0, sg, ix, iy, iz);
     }
 }
 
@@ -496,8 +507,8 @@ template cudaError_t launchWarmInit3<double>(double *, const double *, int, long
                                              int, bool, double, const Spacing3<double> &, double, int, int,
                                              const SourceFp64 *, unsigned long long *, cudaStream_t);
 
-cudaError_t launchFactorBoxes(const SourceFp64 *srcs, int nFields, cudaStream_t s) {
-    factorBoxKernel<<<nFields, 256, 0, s>>>(srcs);
+cudaError_t launchFactorTables(const SourceFp64 *srcs, int nFields, cudaStream_t s) {
+    factorTableKernel<<<nFields, 256, 0, s>>>(srcs);
     return cudaGetLastError();
 }
 

@@ -82,64 +82,82 @@ template <class T> struct Stencil3 {
 // factored radius the reference forms T0 = s0 |x - xs| (s0 the node's home-cell
 // slowness), its gradient s0 (x - xs) / |x - xs|, the differences tau_k = t_k - T0_k at
 // the 7 upwind neighbours and the candidate T0 + correction in the sweep type
-// (solverUtilities3d.hpp:372-553).  In this mode they are formed in FP64 -- the distance
-// D and the direction U = (x - xs) / D from FP64 offsets and spacing, T0 = s0 D, the
-// differences, the gradient s0 U and the final sum -- and rounded to FP32, while the
-// quadratic solves stay in FP32.  D and U of the nodes around each field's source are
-// tabulated once per solve (`box`); a node outside the box forms them inline with the
-// same FP64 expressions.  Kept apart from SourceT, so the kernels without this mode
+// (solverUtilities3d.hpp:372-553); in FP32 the differences lose most of their digits to
+// cancellation.  In this mode:
+//   * D = |x - xs| and U = (x - xs) / D are formed in FP64 from FP64 offsets and spacing,
+//     at the unclamped stencil positions, as the reference's analytic times are;
+//   * T0_k = s0 D_k in FP64, carried as the float pair hi = fl(T0_k), lo = fl(T0_k - hi);
+//   * tau_k = fl(fl(t_k - hi_k) - lo_k), the gradient fl(s0 U) (then the sweep's signs),
+//     and the candidate fl(hi_0 + fl(correction + lo_0)), all FP32 operations;
+//   * the quadratic solves stay in FP32.
+// The pairs and gradient of every node within the radius depend on the node, the sweep
+// ordering (its home cell and upwind neighbours) and the model only, so they are
+// tabulated once per solve (FP64, `table`) and the sweep kernels read them: the kernels
+// run no FP64 instruction.  Kept apart from SourceT, so the kernels without this mode
 // carry none of it.
-struct alignas(16) FactorEntry {
-    double d, ux, uy, uz;
+struct alignas(16) NearFactor {
+    float hi[8], lo[8];   // T0 at the node (0) and at its upwind neighbours t1..t7 (1..7)
+    float gx, gy, gz;     // the gradient of T0 (the sweep applies its signs)
+    float pad;
 };
 struct SourceFp64 {
     double xs, ys, zs;          // source offsets from the origin (FP64)
     double dx, dy, dz;          // grid spacing (FP64)
-    const FactorEntry *box;     // D and U of nodes [bx0, bx0 + bnx) x ... (null: inline)
-    int bx0, by0, bz0, bnx, bny, bnz;
+    const NearFactor *table;    // [sweep][bz][by][bx] entries of the nodes within the radius
+    int bx0, by0, bz0, bnx, bny, bnz;   // the table's node box
+    // for filling the table: the model's unshifted edge-replicated FP32 slowness copy
+    // (cell (cx, cy, cz) at (cz + 1) spPlane + (cy + 1) spPitch + cx + 1) and its cells
+    const float *sp;
+    long long spPlane;
+    int spPitch, ncx, ncy, ncz;
 };
-// Largest factor table of one field (nodes); a larger factored region forms D and U inline.
-constexpr int kMaxFactorBox = 32768;
-// D and U of node (ix, iy, iz) in FP64 (the distance as analyticT3<double> forms it).
-__host__ __device__ inline FactorEntry factorTerms(const SourceFp64 &f, int ix, int iy, int iz) {
+// Largest factor table of one field (entries, 8 sweeps x nodes; 80 bytes each): factored
+// radius 15, or a grid of 32,768 nodes, whatever the radius.  near_fp64 solves whose
+// factored region needs more are rejected.
+constexpr int kMaxFactorTable = 1 << 18;
+
+// D of position (ix, iy, iz) in FP64, as analyticT3<double> forms the distance.
+__host__ __device__ inline double factorDistance(const SourceFp64 &f, int ix, int iy, int iz, double *u = nullptr) {
     const double ddx = ix * f.dx - f.xs, ddy = iy * f.dy - f.ys, ddz = iz * f.dz - f.zs;
     const double d = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
-    FactorEntry e;
-    e.d = d;
-    e.ux = d > 0 ? ddx / d : 0.0;
-    e.uy = d > 0 ? ddy / d : 0.0;
-    e.uz = d > 0 ? ddz / d : 0.0;
+    if (u) {
+        u[0] = d > 0 ? ddx / d : 0.0;
+        u[1] = d > 0 ? ddy / d : 0.0;
+        u[2] = d > 0 ? ddz / d : 0.0;
+    }
+    return d;
+}
+// The entry of node (ix, iy, iz) with home-cell slowness s0 (as the sweep holds it) in the
+// sweep with signs sg.
+__host__ __device__ inline NearFactor nearFactor(const SourceFp64 &f, float s0, const SweepSigns &sg, int ix, int iy,
+                                                 int iz) {
+    const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
+    const int px[8] = {ix, xu, xu, ix, ix, xu, xu, ix};
+    const int py[8] = {iy, iy, yu, yu, iy, iy, yu, yu};
+    const int pz[8] = {iz, iz, iz, iz, zu, zu, zu, zu};
+    const double s = s0;
+    NearFactor e;
+    double u[3];
+    for (int k = 0; k < 8; ++k) {
+        const double t0 = s * factorDistance(f, px[k], py[k], pz[k], k == 0 ? u : nullptr);
+        e.hi[k] = static_cast<float>(t0);
+        e.lo[k] = static_cast<float>(t0 - static_cast<double>(e.hi[k]));
+    }
+    e.gx = static_cast<float>(s * u[0]);
+    e.gy = static_cast<float>(s * u[1]);
+    e.gz = static_cast<float>(s * u[2]);
+    e.pad = 0;
     return e;
 }
-// D and U of node (ix, iy, iz): the table's entry or, outside it, the same FP64 terms.
-__device__ __forceinline__ FactorEntry factorEntry(const SourceFp64 &f, int ix, int iy, int iz) {
-    const int bx = ix - f.bx0, by = iy - f.by0, bz = iz - f.bz0;
-    if (f.box && bx >= 0 && bx < f.bnx && by >= 0 && by < f.bny && bz >= 0 && bz < f.bnz)
-        return f.box[(static_cast<long long>(bz) * f.bny + by) * f.bnx + bx];
-    return factorTerms(f, ix, iy, iz);
+// Sweep ordering 0..7 of a set of signs (bit 0: x decreasing, 1: y, 2: z).
+__host__ __device__ inline int sweepOf(const SweepSigns &sg) {
+    return (sg.ixShift > 0 ? 1 : 0) | (sg.iyShift > 0 ? 2 : 0) | (sg.izShift > 0 ? 4 : 0);
 }
-// The factor terms of the factored branch at node (ix, iy, iz) with home-cell slowness s0:
-// T0 (FP64, returned), the signed gradient and tau_1..tau_7 rounded to FP32.
-__device__ __forceinline__ double factorFp64(const SourceFp64 &f, const SweepSigns &sg, int ix, int iy, int iz,
-                                             float s0, const Stencil3<float> &n, float &gx, float &gy, float &gz,
-                                             float (&tau)[7]) {
-    const double s = s0;
-    const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
-    const FactorEntry e0 = factorEntry(f, ix, iy, iz);
-    gx = static_cast<float>(s * e0.ux);
-    gy = static_cast<float>(s * e0.uy);
-    gz = static_cast<float>(s * e0.uz);
-    auto tauOf = [&](float t, int x, int y, int z) {
-        return static_cast<float>(static_cast<double>(t) - s * factorEntry(f, x, y, z).d);
-    };
-    tau[0] = tauOf(n.t1, xu, iy, iz);
-    tau[1] = tauOf(n.t2, xu, yu, iz);
-    tau[2] = tauOf(n.t3, ix, yu, iz);
-    tau[3] = tauOf(n.t4, ix, iy, zu);
-    tau[4] = tauOf(n.t5, xu, iy, zu);
-    tau[5] = tauOf(n.t6, xu, yu, zu);
-    tau[6] = tauOf(n.t7, ix, yu, zu);
-    return s * e0.d;
+// The table entry of node (ix, iy, iz), a node within the factored radius (inside the box).
+__device__ __forceinline__ const NearFactor &nearFactorAt(const SourceFp64 &f, const SweepSigns &sg, int ix, int iy,
+                                                          int iz) {
+    const int bx = ix - f.bx0, by = iy - f.by0, bz = iz - f.bz0;
+    return f.table[((static_cast<long long>(sweepOf(sg)) * f.bnz + bz) * f.bny + by) * f.bnx + bx];
 }
 
 // 3D uniform-grid update (solverUtilities3d.hpp:258-558), split at the reference's
@@ -261,12 +279,15 @@ __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const Sw
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
         T t0, dt0dx, dt0dy, dt0dz;
         T tau1, tau2, tau3, tau4, tau5, tau6, tau7;
-        double t0d = 0;
+        NearFactor nf;
         if constexpr (F64 && sizeof(T) == 4) {
-            T tau[7];
-            t0d = factorFp64(*f64, sg, ix, iy, iz, s0, n, dt0dx, dt0dy, dt0dz, tau);
-            t0 = static_cast<T>(t0d);
-            tau1 = tau[0]; tau2 = tau[1]; tau3 = tau[2]; tau4 = tau[3]; tau5 = tau[4]; tau6 = tau[5]; tau7 = tau[6];
+            nf = nearFactorAt(*f64, sg, ix, iy, iz);
+            t0 = nf.hi[0];
+            tau1 = (t1 - nf.hi[1]) - nf.lo[1]; tau2 = (t2 - nf.hi[2]) - nf.lo[2];
+            tau3 = (t3 - nf.hi[3]) - nf.lo[3]; tau4 = (t4 - nf.hi[4]) - nf.lo[4];
+            tau5 = (t5 - nf.hi[5]) - nf.lo[5]; tau6 = (t6 - nf.hi[6]) - nf.lo[6];
+            tau7 = (t7 - nf.hi[7]) - nf.lo[7];
+            dt0dx = nf.gx; dt0dy = nf.gy; dt0dz = nf.gz;
         } else {
             analyticTG3(ix, iy, iz, h, h, h, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
             const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
@@ -280,7 +301,7 @@ __device__ __forceinline__ T fd3UniformNear(T h, const SourceT<T> &src, const Sw
         }
         // T0 + correction: in FP64 when the factor is
         auto plusT0 = [&](T d) -> T {
-            if constexpr (F64 && sizeof(T) == 4) return static_cast<T>(t0d + static_cast<double>(d));
+            if constexpr (F64 && sizeof(T) == 4) return nf.hi[0] + (d + nf.lo[0]);
             else return t0 + d;
         };
         dt0dx = sg.signX * dt0dx;
@@ -441,12 +462,15 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
         const T xs = src.xs, ys = src.ys, zs = src.zs, sSrc = src.sSrc;
         T t0, dt0dx, dt0dy, dt0dz;
         T tau1, tau2, tau3, tau4, tau5, tau6, tau7;
-        double t0d = 0;
+        NearFactor nf;
         if constexpr (F64 && sizeof(T) == 4) {
-            T tau[7];
-            t0d = factorFp64(*f64, sg, ix, iy, iz, s0, n, dt0dx, dt0dy, dt0dz, tau);
-            t0 = static_cast<T>(t0d);
-            tau1 = tau[0]; tau2 = tau[1]; tau3 = tau[2]; tau4 = tau[3]; tau5 = tau[4]; tau6 = tau[5]; tau7 = tau[6];
+            nf = nearFactorAt(*f64, sg, ix, iy, iz);
+            t0 = nf.hi[0];
+            tau1 = (t1 - nf.hi[1]) - nf.lo[1]; tau2 = (t2 - nf.hi[2]) - nf.lo[2];
+            tau3 = (t3 - nf.hi[3]) - nf.lo[3]; tau4 = (t4 - nf.hi[4]) - nf.lo[4];
+            tau5 = (t5 - nf.hi[5]) - nf.lo[5]; tau6 = (t6 - nf.hi[6]) - nf.lo[6];
+            tau7 = (t7 - nf.hi[7]) - nf.lo[7];
+            dt0dx = nf.gx; dt0dy = nf.gy; dt0dz = nf.gz;
         } else {
             analyticTG3(ix, iy, iz, dx, dy, dz, xs, ys, zs, s0, t0, dt0dx, dt0dy, dt0dz);
             const int xu = ix + sg.ixShift, yu = iy + sg.iyShift, zu = iz + sg.izShift;
@@ -459,7 +483,7 @@ __device__ __forceinline__ T fd3NonUniformNear(const Spacing3<T> &g, const Sourc
             tau7 = t7 - analyticT3(ix, yu, zu, dx, dy, dz, xs, ys, zs, s0);
         }
         auto plusT0 = [&](T d) -> T {
-            if constexpr (F64 && sizeof(T) == 4) return static_cast<T>(t0d + static_cast<double>(d));
+            if constexpr (F64 && sizeof(T) == 4) return nf.hi[0] + (d + nf.lo[0]);
             else return t0 + d;
         };
         dt0dx = sg.signX * dt0dx;

@@ -49,6 +49,8 @@ eikx_status eikxSetLastError(eikx_status code, const char *msg);
 namespace {
 
 constexpr size_t kScratchBytes = 64ull << 20;
+// FP64 analytic-factor table of a near_fp64 solve: 2.6 MB of the array, factored radius 7
+constexpr int kFactorEntries = 32768;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char gScratch[kScratchBytes];
@@ -158,6 +160,14 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
         !locate(src->z, z0, dz, nz, &cz, &oz))
         return err(EIKX_ERR_INVALID, "source position outside the grid");
 
+    // the FP64 analytic factor's table box (near_fp64): the nodes within the radius
+    int bo[3] = {0, 0, 0}, be[3] = {0, 0, 0};
+    if (o.near_fp64 && (!eikx::factorBox(cx, cy, cz, o.factored_radius, nx, ny, nz, bo, be) ||
+                        8ll * be[0] * be[1] * be[2] > kFactorEntries))
+        return err(EIKX_ERR_UNSUPPORTED, "near_fp64: the factored region of radius " +
+                                             std::to_string(o.factored_radius) + " needs more than " +
+                                             std::to_string(kFactorEntries) + " table entries");
+
     // layout and scratch need (same shapes as eikx_solve3d): the chunk-step kernel takes
     // the requested warp-block shape, the node-step kernel is 8x4
     const bool chunk = o.sweep_kernel != eikx::kNodeStep;
@@ -182,7 +192,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     plan.take<eikx::SourceT<float>>(1);
     plan.take<eikx::Corner3>(1);
     plan.take<eikx::SourceFp64>(1);
-    if (o.near_fp64) plan.take<eikx::FactorEntry>(eikx::kMaxFactorBox);         // FP64 factor table
+    if (o.near_fp64) plan.take<eikx::NearFactor>(kFactorEntries);               // FP64 factor table
     if (plan.used > kScratchBytes)
         return err(EIKX_ERR_INVALID, "grid " + std::to_string(nx) + "x" + std::to_string(ny) + "x" +
                                          std::to_string(nz) + " needs " + std::to_string(plan.used) +
@@ -208,7 +218,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     eikx::SourceT<float> *srcDev = cv.take<eikx::SourceT<float>>(1);
     eikx::Corner3 *cornerDev = cv.take<eikx::Corner3>(1);
     eikx::SourceFp64 *src64Dev = cv.take<eikx::SourceFp64>(1);
-    eikx::FactorEntry *factorDev = o.near_fp64 ? cv.take<eikx::FactorEntry>(eikx::kMaxFactorBox) : nullptr;
+    eikx::NearFactor *factorDev = o.near_fp64 ? cv.take<eikx::NearFactor>(kFactorEntries) : nullptr;
 
     int numSMs = 0;
     NOALLOC_CUDA(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, device));
@@ -253,20 +263,20 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
     // FP64 analytic factor: offsets, spacing and the factor table carved from the scratch
     eikx::SourceFp64 f64{};
     f64.xs = ox; f64.ys = oy; f64.zs = oz; f64.dx = dx; f64.dy = dy; f64.dz = dz;
+    f64.sp = spNeg; f64.spPitch = spPitch; f64.spPlane = static_cast<long long>(spPitch) * (ny + 1);
+    f64.ncx = nx - 1; f64.ncy = ny - 1; f64.ncz = nz - 1;
     if (o.near_fp64) {
-        int bo[3], be[3];
-        if (eikx::factorBox(cx, cy, cz, o.factored_radius, nx, ny, nz, bo, be)) {
-            f64.box = factorDev;
-            f64.bx0 = bo[0]; f64.by0 = bo[1]; f64.bz0 = bo[2];
-            f64.bnx = be[0]; f64.bny = be[1]; f64.bnz = be[2];
-        }
+        f64.table = factorDev;
+        f64.bx0 = bo[0]; f64.by0 = bo[1]; f64.bz0 = bo[2];
+        f64.bnx = be[0]; f64.bny = be[1]; f64.bnz = be[2];
     }
     sourceKernel<<<1, 32, 0, stream>>>(srcDev, cornerDev, o.near_fp64 ? src64Dev : nullptr, f64, slowness, nx - 1,
                                        ny - 1, cx, cy, cz, ox, oy, oz);
     NOALLOC_CUDA(cudaGetLastError());
-    if (o.near_fp64 && f64.box) NOALLOC_CUDA(eikx::launchFactorBoxes(src64Dev, 1, stream));
+    // the table is filled after the padded slowness copies (below)
     NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spPos, spPitch, 3, slowness, nx, ny, nz, stream)));
     NOALLOC_CUDA((eikx::launchPadSlowness3<float, float>(spNeg, spPitch, 0, slowness, nx, ny, nz, stream)));
+    if (o.near_fp64 && f64.table) NOALLOC_CUDA(eikx::launchFactorTables(src64Dev, 1, stream));
     NOALLOC_CUDA(eikx::launchResetState(st, 1, 0, stream));
     NOALLOC_CUDA(eikx::launchInit3<float>(tt, 1, static_cast<long long>(Px) * ny * nz, Px, nx, ny, nz, dx, dy, dz,
                                           cornerDev, o.init_fp64 ? 1 : 0, stream));

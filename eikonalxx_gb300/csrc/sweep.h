@@ -176,21 +176,22 @@ cudaError_t launchWarmInit3(T *tt, const T *init, int nFields, long long fieldSt
                             int twoSided, int fp64, const SourceFp64 *srcs64, unsigned long long *nReset,
                             cudaStream_t s);
 // Fills the FP64 analytic-factor table of each field whose SourceFp64 has one.
-cudaError_t launchFactorBoxes(const SourceFp64 *srcs, int nFields, cudaStream_t s);
-// Box of the factor table of a field (nodes within radius + 1 of the source cell, clamped
-// to the grid): origin and extents; false when it exceeds kMaxFactorBox nodes.
+cudaError_t launchFactorTables(const SourceFp64 *srcs, int nFields, cudaStream_t s);
+// Box of a field's factor table: the nodes within `radius` of the source cell along every
+// axis (the factored branch's nodes), clamped to the grid; false when 8 sweeps x the box
+// exceed kMaxFactorTable entries.
 inline bool factorBox(int isx, int isy, int isz, int radius, int nx, int ny, int nz, int (&o)[3], int (&e)[3]) {
     const int c[3] = {isx, isy, isz}, n[3] = {nx, ny, nz};
     const long long r = radius;
-    long long vol = 1;
+    long long vol = 8;
     for (int k = 0; k < 3; ++k) {
-        const long long lo = c[k] - r - 1 < 0 ? 0 : c[k] - r - 1;
-        const long long hi = c[k] + r + 1 > n[k] - 1 ? n[k] - 1 : c[k] + r + 1;
+        const long long lo = c[k] - r < 0 ? 0 : c[k] - r;
+        const long long hi = c[k] + r > n[k] - 1 ? n[k] - 1 : c[k] + r;
         o[k] = static_cast<int>(lo);
         e[k] = static_cast<int>(hi - lo + 1);
         vol *= e[k];
     }
-    return vol <= kMaxFactorBox;
+    return vol <= kMaxFactorTable;
 }
 // Sets *flag (ORs 1) if any of the n slownesses is not positive and finite.
 cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStream_t st);

@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<
 // Held to 128 registers (the default kernels' 4 blocks per SM); the out-of-line FP64
 // branch spills what it needs beyond them.
 template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT>
-__global__ void __launch_bounds__(kThreadsC, 4) sweep3ChunkNear64Kernel(const Sweep3Args<T> a) {
+__global__ void __launch_bounds__(kThreadsC) sweep3ChunkNear64Kernel(const Sweep3Args<T> a) {
     sweep3ChunkBody<T, UNIFORM, REV, BATCH, LY, LZ, INIT, true>(a);
 }
 

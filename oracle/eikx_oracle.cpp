@@ -89,9 +89,10 @@ struct Grid3 {
 
 // near_fp64 (FP32 sweeps; the GPU's eikx_options.near_fp64): the analytic factor of the
 // factored branch in FP64.  D = |x - xs| and U = (x - xs) / D from FP64 offsets and
-// spacing; T0 = s0 D, the gradient s0 U, the differences tau_k = t_k - s0 D_k and the sum
-// T0 + correction are formed in FP64 and rounded to the sweep type, the quadratic solves
-// stay in it.
+// spacing at the unclamped stencil positions; T0_k = s0 D_k in FP64, carried as the float
+// pair hi = fl(T0_k), lo = fl(T0_k - hi); tau_k = fl(fl(t_k - hi_k) - lo_k), the gradient
+// fl(s0 U) and the candidate fl(hi_0 + fl(correction + lo_0)); the quadratic solves stay
+// in the sweep type.
 struct FactorTerms {
     double d, ux, uy, uz;
 };
@@ -100,17 +101,22 @@ inline FactorTerms factorTerms(const Grid3 &g, const Src3 &src, int ix, int iy, 
     const double d = std::sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
     return {d, d > 0 ? ddx / d : 0.0, d > 0 ? ddy / d : 0.0, d > 0 ? ddz / d : 0.0};
 }
-// T0 (FP64, returned), the gradient and tau_1..tau_7 in T at node (ix, iy, iz).
+// The node's float pair (hi0, lo0, returned through t0 / lo0), the gradient and tau_1..tau_7.
 template <class T>
-double factorFp64(const Grid3 &g, const Src3 &src, const Sweep3 &sw, int ix, int iy, int iz, T s0,
-                  T t1, T t2, T t3, T t4, T t5, T t6, T t7, T &gx, T &gy, T &gz, T (&tau)[7]) {
+void factorFp64(const Grid3 &g, const Src3 &src, const Sweep3 &sw, int ix, int iy, int iz, T s0,
+                T t1, T t2, T t3, T t4, T t5, T t6, T t7, T &t0, T &lo0, T &gx, T &gy, T &gz, T (&tau)[7]) {
     const double s = s0;
     const FactorTerms e0 = factorTerms(g, src, ix, iy, iz);
+    const double T00 = s * e0.d;
+    t0 = static_cast<T>(T00);
+    lo0 = static_cast<T>(T00 - static_cast<double>(t0));
     gx = static_cast<T>(s * e0.ux);
     gy = static_cast<T>(s * e0.uy);
     gz = static_cast<T>(s * e0.uz);
     auto tauOf = [&](T t, int x, int y, int z) {
-        return static_cast<T>(static_cast<double>(t) - s * factorTerms(g, src, x, y, z).d);
+        const double T0k = s * factorTerms(g, src, x, y, z).d;
+        const T hi = static_cast<T>(T0k), lo = static_cast<T>(T0k - static_cast<double>(hi));
+        return static_cast<T>(static_cast<T>(t - hi) - lo);
     };
     const int xu = ix + sw.ixShift, yu = iy + sw.iyShift, zu = iz + sw.izShift;
     tau[0] = tauOf(t1, xu, iy, iz);
@@ -120,7 +126,6 @@ double factorFp64(const Grid3 &g, const Src3 &src, const Sweep3 &sw, int ix, int
     tau[4] = tauOf(t5, xu, iy, zu);
     tau[5] = tauOf(t6, xu, yu, zu);
     tau[6] = tauOf(t7, ix, yu, zu);
-    return s * e0.d;
 }
 
 // Uniform-grid local solver, solverUtilities3d.hpp:258-558 (debug prints removed).
@@ -174,11 +179,10 @@ T fd3Uniform(int radius, T huge, T h, T sSrc, int ix, int iy, int iz, const Swee
         // home-cell slowness s0 (solverUtilities3d.hpp:373-378).
         T t0, dt0dx, dt0dy, dt0dz;
         T tau1, tau2, tau3, tau4, tau5, tau6, tau7;
-        double t0d = 0;
+        T lo0 = 0;
         if (g64) {
             T tau[7];
-            t0d = factorFp64<T>(*g64, src, sw, ix, iy, iz, s0, t1, t2, t3, t4, t5, t6, t7, dt0dx, dt0dy, dt0dz, tau);
-            t0 = static_cast<T>(t0d);
+            factorFp64<T>(*g64, src, sw, ix, iy, iz, s0, t1, t2, t3, t4, t5, t6, t7, t0, lo0, dt0dx, dt0dy, dt0dz, tau);
             tau1 = tau[0]; tau2 = tau[1]; tau3 = tau[2]; tau4 = tau[3]; tau5 = tau[4]; tau6 = tau[5]; tau7 = tau[6];
         } else {
             analyticTG(ix, iy, iz, h, h, h, xs, ys, zs, s0, &t0, &dt0dx, &dt0dy, &dt0dz);
@@ -190,7 +194,7 @@ T fd3Uniform(int radius, T huge, T h, T sSrc, int ix, int iy, int iz, const Swee
             tau6 = t6 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
             tau7 = t7 - analyticT(ix, iy + sw.iyShift, iz + sw.izShift, h, h, h, xs, ys, zs, s0);
         }
-        auto plusT0 = [&](T d) -> T { return g64 ? static_cast<T>(t0d + static_cast<double>(d)) : t0 + d; };
+        auto plusT0 = [&](T d) -> T { return g64 ? static_cast<T>(t0 + static_cast<T>(d + lo0)) : t0 + d; };
         dt0dx = sw.signX * dt0dx;
         dt0dy = sw.signY * dt0dy;
         dt0dz = sw.signZ * dt0dz;
@@ -343,11 +347,10 @@ T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int
     } else {
         T t0, dt0dx, dt0dy, dt0dz;
         T tau1, tau2, tau3, tau4, tau5, tau6, tau7;
-        double t0d = 0;
+        T lo0 = 0;
         if (g64) {
             T tau[7];
-            t0d = factorFp64<T>(*g64, src, sw, ix, iy, iz, s0, t1, t2, t3, t4, t5, t6, t7, dt0dx, dt0dy, dt0dz, tau);
-            t0 = static_cast<T>(t0d);
+            factorFp64<T>(*g64, src, sw, ix, iy, iz, s0, t1, t2, t3, t4, t5, t6, t7, t0, lo0, dt0dx, dt0dy, dt0dz, tau);
             tau1 = tau[0]; tau2 = tau[1]; tau3 = tau[2]; tau4 = tau[3]; tau5 = tau[4]; tau6 = tau[5]; tau7 = tau[6];
         } else {
             analyticTG(ix, iy, iz, dx, dy, dz, xs, ys, zs, s0, &t0, &dt0dx, &dt0dy, &dt0dz);
@@ -359,7 +362,7 @@ T fd3NonUniform(int radius, T huge, const NonUniform3<T> &g, T sSrc, int ix, int
             tau6 = t6 - analyticT(ix + sw.ixShift, iy + sw.iyShift, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
             tau7 = t7 - analyticT(ix, iy + sw.iyShift, iz + sw.izShift, dx, dy, dz, xs, ys, zs, s0);
         }
-        auto plusT0 = [&](T d) -> T { return g64 ? static_cast<T>(t0d + static_cast<double>(d)) : t0 + d; };
+        auto plusT0 = [&](T d) -> T { return g64 ? static_cast<T>(t0 + static_cast<T>(d + lo0)) : t0 + d; };
         dt0dx = sw.signX * dt0dx;
         dt0dy = sw.signY * dt0dy;
         dt0dz = sw.signZ * dt0dz;

@@ -282,3 +282,18 @@ def test_near_fp64_batch_and_pair_request(ctx, oracle):
         t_or = oracle.solve3d(s, shape, cell, off, n_sweeps=3, radius=3, near_fp64=True)
         assert np.array_equal(_bits(t[i]), _bits(t_or)), i
         assert np.array_equal(_bits(tb[i]), _bits(t_or)), i
+
+
+def test_near_fp64_rejects_a_factored_region_beyond_its_table(ctx):
+    """The FP64 analytic factor is tabulated per solve (8 sweep orderings x the nodes within
+    the radius, at most 2^18 entries per field): a larger factored region is refused."""
+    rng = np.random.default_rng(18)
+    shape = (70, 70, 70, 20., 20., 20.)
+    nx, ny, nz = shape[:3]
+    ctx.set_grid3d(*shape)
+    ctx.set_slowness3d(random_slowness(rng, (nz - 1) * (ny - 1) * (nx - 1), dtype=np.float32))
+    with pytest.raises(ex.EikxError) as e:
+        ctx.solve3d([[690., 690., 690.]], ex.Options(n_sweeps=1, factored_radius=1000, near_fp64=True), ex.F32)
+    assert e.value.code == ex.EIKX_ERR_UNSUPPORTED
+    t = ctx.solve3d([[690., 690., 690.]], ex.Options(n_sweeps=1, factored_radius=3, near_fp64=True), ex.F32)
+    assert np.isfinite(t).all()
