@@ -675,7 +675,8 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
         else
             EIKX_CUDA(eikx::launchInit2<T>(w.tt.as<T>(), nSrc, fieldStride, Px, nx, nz, dx, dz,
                                            w.corners.as<eikx::Corner3>(), o.init_fp64 ? 1 : 0, c->stream));
-        ++launches;
+        // 3D: the fill and the corner kernel; a warm start: its gate and the pitch padding
+        launches += warm ? 1 + (Px > nx ? 1 : 0) : DIM == 3 ? 2 : 1;
         auto sweep = [&](int e, int init, int slot) -> eikx_status {
             if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched], c->stream));
             if (DIM == 3) {
@@ -1230,7 +1231,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
             EIKX_CUDA(eikx::launchInit3<T>(ttBase + L[i].ttOff, L[i].nSrc, L[i].fieldStride, L[i].Px, m.nx, m.ny, m.nz,
                                            m.dx, m.dy, m.dz, w.corners.as<eikx::Corner3>() + L[i].firstUnit,
                                            o.init_fp64 ? 1 : 0, c->stream));
-            ++launches;
+            launches += 2;   // the fill and the corner kernel
         }
         auto sweep = [&](int e, int init, int slot) -> eikx_status {
             if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * sweepsLaunched], c->stream));

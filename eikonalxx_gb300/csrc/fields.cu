@@ -35,34 +35,38 @@ __global__ void positiveKernel(const U *s, long long n, int *flag) {
 
 // Travel-time initialisation (Solver3D::initializeTravelTimes, src/solver3d.cpp:21-84):
 // every node := HUGE, the 8 corners of the source cell := s_src * |x - x_s|, the
-// distance and product evaluated in FP64 (fp64 = 1) or in the field type.
+// distance and product evaluated in FP64 (fp64 = 1) or in the field type.  Two passes:
+// a streaming fill of HUGE over every field (16-byte stores; the pitched rows' padding
+// included), then one thread per source-cell corner.
 template <class T>
-__global__ void init3Kernel(T *tt, int nFields, long long fieldStride, int pitch, int nx, int ny,
-                            int nz, double dx, double dy, double dz, const Corner3 *corners, int fp64) {
-    const long long perField = static_cast<long long>(pitch) * ny * nz;
-    const long long n = perField * nFields;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int f = static_cast<int>(i / perField);
-        long long r = i - f * perField;
-        const int ix = static_cast<int>(r % pitch);
-        r /= pitch;
-        const int iy = static_cast<int>(r % ny);
-        const int iz = static_cast<int>(r / ny);
-        const Corner3 cn = corners[f];
-        T v = static_cast<T>(1.e10);
-        if (ix - cn.isx >= 0 && ix - cn.isx <= 1 && iy - cn.isy >= 0 && iy - cn.isy <= 1 &&
-            iz - cn.isz >= 0 && iz - cn.isz <= 1 && ix < nx) {
-            if (fp64) {
-                v = static_cast<T>(analyticT3<double>(ix, iy, iz, dx, dy, dz, cn.xo, cn.yo, cn.zo, cn.s));
-            } else {
-                v = analyticT3<T>(ix, iy, iz, static_cast<T>(dx), static_cast<T>(dy), static_cast<T>(dz),
-                                  static_cast<T>(cn.xo), static_cast<T>(cn.yo), static_cast<T>(cn.zo),
-                                  static_cast<T>(cn.s));
-            }
-        }
-        tt[static_cast<long long>(f) * fieldStride + r * pitch + ix] = v;
+__global__ void fillHugeKernel(uint4 *tt, long long n16) {
+    const T huge = static_cast<T>(1.e10);
+    uint4 v;
+    T *e = reinterpret_cast<T *>(&v);
+#pragma unroll
+    for (int k = 0; k < static_cast<int>(16 / sizeof(T)); ++k) e[k] = huge;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n16;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        tt[i] = v;
+}
+template <class T>
+__global__ void init3CornerKernel(T *tt, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
+                                  double dx, double dy, double dz, const Corner3 *corners, int fp64) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 8 * nFields) return;
+    const int f = i >> 3, k = i & 7;
+    const Corner3 cn = corners[f];
+    const int ix = cn.isx + (k & 1), iy = cn.isy + ((k >> 1) & 1), iz = cn.isz + ((k >> 2) & 1);
+    if (ix >= nx || iy >= ny || iz >= nz) return;
+    T v;
+    if (fp64) {
+        v = static_cast<T>(analyticT3<double>(ix, iy, iz, dx, dy, dz, cn.xo, cn.yo, cn.zo, cn.s));
+    } else {
+        v = analyticT3<T>(ix, iy, iz, static_cast<T>(dx), static_cast<T>(dy), static_cast<T>(dz),
+                          static_cast<T>(cn.xo), static_cast<T>(cn.yo), static_cast<T>(cn.zo),
+                          static_cast<T>(cn.s));
     }
+    tt[static_cast<long long>(f) * fieldStride + (static_cast<long long>(iz) * ny + iy) * pitch + ix] = v;
 }
 
 // Warm start of a 3D solve from an initial field (natural order): the field is taken as
@@ -425,9 +429,12 @@ __global__ void analytic2Kernel(double *t, int nx, int nz, double dx, double dz,
 template <class T>
 cudaError_t launchInit3(T *tt, int nFields, long long fieldStride, int pitch, int nx, int ny, int nz,
                         double dx, double dy, double dz, const Corner3 *corners, int fp64, cudaStream_t s) {
-    const long long n = static_cast<long long>(pitch) * ny * nz * nFields;
-    init3Kernel<T><<<gridFor(n), kThreads, 0, s>>>(tt, nFields, fieldStride, pitch, nx, ny, nz, dx, dy, dz,
-                                                    corners, fp64);
+    // the fields are contiguous (fieldStride = pitch * ny * nz) and pitch * sizeof(T) is a
+    // multiple of 16 bytes, so the fill covers them in 16-byte stores
+    const long long n16 = fieldStride * nFields * static_cast<long long>(sizeof(T)) / 16;
+    fillHugeKernel<T><<<gridFor(n16), kThreads, 0, s>>>(reinterpret_cast<uint4 *>(tt), n16);
+    init3CornerKernel<T><<<(8 * nFields + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+        tt, nFields, fieldStride, pitch, nx, ny, nz, dx, dy, dz, corners, fp64);
     return cudaGetLastError();
 }
 template <class T>
