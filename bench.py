@@ -801,7 +801,8 @@ def profile_case(fields):
     ctx = ex.Context(torch.cuda.current_device())
     ctx.set_grid3d(NX, NY, NZ, H, H, H)
     ctx.set_nodal_velocity3d(v.ravel())
-    opt = ex.Options(n_sweeps=1, tolerance=-1, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0], sweep_kernel=KERNEL[0])
+    opt = ex.Options(n_sweeps=1, tolerance=-1, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0],
+                     sweep_kernel=KERNEL[0], near_fp64=NEAR64[0])
     out = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device="cuda")
     ctx.solve3d(src, opt, ex.F32, out=out)
     st = ctx.stats()

@@ -225,10 +225,20 @@ __device__ __forceinline__ T fd3UniformFar(T h, const Stencil3<T> &n) {
 // it returns t0 as soon as a lower bound shows that no operator goes below t0, and leaves
 // out the 8-point operator when its lower bound shows that it cannot be the one below t0.
 // The bounds hold for the rounded values, since round-to-nearest is monotone:
-//   * the 2D operators return t5 + r, t7 + r, t2 + r with r >= 0: each >= t5, t7, t2;
+//   * a 2D operator, when its window is open, returns t_d + r (t_d = t5, t7, t2 for XZ, YZ,
+//     XY) with r = sqrt(2 hs^2 - (t_a - t_b)^2) and |t_a - t_b| <= hs by its window (hs the
+//     operator's h * min slowness, t_a, t_b its two axis neighbours).  The window test, the
+//     determinant and the square root round with unit roundoff u (2^-24 in FP32, less in
+//     FP64): the test admits |t_a - t_b| <= hs + u (t_a + t_b + hs), and the computed r is
+//     >= hs - u (t_a + t_b) - 5 u hs up to second-order terms.  So r >= m with
+//     m = hs (1 - 2^-20) - 2^-20 (t1 + t3 + t4), formed in T (t >= 0; a margin of at least
+//     10 u hs and 15 u (t_a + t_b) covers the second-order terms and m's own rounding, and
+//     m < 0 whenever the times are so large that the margin would not), and each operator is
+//     >= t_d + m; a closed window returns huge;
 //   * the 8-point operator returns third * (S + r3) with S = (Tx + Ty) + Tz, r3 >= 0:
 //     it is >= third * S (or huge when its window is closed);
-//   * if t0 <= min(t1d, t2, t5, t7, third * S), fd3UniformFar's result is >= t0;
+//   * if t0 <= min(t1d, t2 + m04, t5 + m03, t7 + m01, third * S), fd3UniformFar's result
+//     is >= t0;
 //   * if third * S >= min(t0, t1d, t2d), fd3UniformFar's result is below t0 only when
 //     min(t1d, t2d) is, and then it equals min(t1d, t2d).
 // So min(t0, result) is min(t0, fd3UniformFar(h, n)) bit for bit.
@@ -244,7 +254,10 @@ __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t
     const T Tz = t4 + half * (-t1 + t5 - t3 + t7) - t2 + t6;
     const T S = (Tx + Ty) + Tz;
     const T lo3 = third * S;
-    if (t0 <= dmin(dmin(t1d, dmin(t2, t5)), dmin(t7, lo3))) return t0;
+    const T c20 = static_cast<T>(1.0 - 1.0 / 1048576.0), e20 = static_cast<T>(1.0 / 1048576.0);
+    const T E = ((t1 + t3) + t4) * e20;
+    const T L2 = t2 + (hs04 * c20 - E), L5 = t5 + (hs03 * c20 - E), L7 = t7 + (hs01 * c20 - E);
+    if (t0 <= dmin(dmin(t1d, dmin(L2, L5)), dmin(L7, lo3))) return t0;
     T dXZ = t1 - t4;
     T detXZ = 2 * (hs03 * hs03) - dXZ * dXZ;
     const bool cXZ = detXZ > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03;
