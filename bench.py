@@ -274,7 +274,11 @@ def run_gpu(args):
     peak, peak_kind = _peaks()
     tr = _traffic()
     shapes = {1: "8x4", 2: "4x8", 3: "16x2"}
-    if tuning:
+    if NEAR64[0]:
+        # the FP64 factor runs the chunk-step kernel's table instances, never the pair or
+        # node-step kernels
+        kernel_name = f"sweep3ChunkNear64Kernel<float,uniform,{shapes.get(tuning['block_shape'] if tuning else 1, '8x4')}>"
+    elif tuning:
         kernel_name = ("sweep3PairKernel" if tuning["pair_fields"] else "sweep3Kernel<float,uniform>"
                        if tuning["sweep_kernel"] == 1 else
                        f"sweep3ChunkKernel<float,uniform,{shapes[tuning['block_shape']]}>")
