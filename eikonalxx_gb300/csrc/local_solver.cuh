@@ -222,64 +222,75 @@ __device__ __forceinline__ T fd3UniformFar(T h, const Stencil3<T> &n) {
 }
 
 // fd3UniformFar for a node whose current time is t0, for callers that keep min(t0, result):
-// it returns t0 as soon as a lower bound shows that no operator goes below t0, and leaves
-// out the 8-point operator when its lower bound shows that it cannot be the one below t0.
-// The bounds hold for the rounded values, since round-to-nearest is monotone:
+// it returns t0 as soon as lower bounds show that no operator goes below t0, and evaluates
+// an operator only where its bound leaves it a chance to.  The bounds hold for the rounded
+// values, since round-to-nearest is monotone (u = unit roundoff: 2^-24 in FP32, less in
+// FP64; all times are >= 0, M = max(t1..t7, 2^-100)):
 //   * a 2D operator, when its window is open, returns t_d + r (t_d = t5, t7, t2 for XZ, YZ,
 //     XY) with r = sqrt(2 hs^2 - (t_a - t_b)^2) and |t_a - t_b| <= hs by its window (hs the
 //     operator's h * min slowness, t_a, t_b its two axis neighbours).  The window test, the
-//     determinant and the square root round with unit roundoff u (2^-24 in FP32, less in
-//     FP64): the test admits |t_a - t_b| <= hs + u (t_a + t_b + hs), and the computed r is
-//     >= hs - u (t_a + t_b) - 5 u hs up to second-order terms.  So r >= m with
-//     m = hs (1 - 2^-20) - 2^-20 (t1 + t3 + t4), formed in T (t >= 0; a margin of at least
-//     10 u hs and 15 u (t_a + t_b) covers the second-order terms and m's own rounding, and
-//     m < 0 whenever the times are so large that the margin would not), and each operator is
-//     >= t_d + m; a closed window returns huge;
-//   * the 8-point operator returns third * (S + r3) with S = (Tx + Ty) + Tz, r3 >= 0:
-//     it is >= third * S (or huge when its window is closed);
-//   * if t0 <= min(t1d, t2 + m04, t5 + m03, t7 + m01, third * S), fd3UniformFar's result
-//     is >= t0;
-//   * if third * S >= min(t0, t1d, t2d), fd3UniformFar's result is below t0 only when
-//     min(t1d, t2d) is, and then it equals min(t1d, t2d).
-// So min(t0, result) is min(t0, fd3UniformFar(h, n)) bit for bit.
+//     determinant and the square root round with unit roundoff u: the test admits
+//     |t_a - t_b| <= hs + u (t_a + t_b + hs), and the computed r is >= hs - u (t_a + t_b)
+//     - 5 u hs up to second-order terms.  So r >= m with m = hs (1 - 2^-20) - 2^-20 (t1 +
+//     t3 + t4), formed in T (a margin of at least 10 u hs and 15 u (t_a + t_b) covers the
+//     second-order terms and m's own rounding, and m < 0 whenever the times are so large
+//     that the margin would not), and the operator is >= L_d = t_d + m; a closed window
+//     returns huge;
+//   * the 8-point operator returns third * (S + r3) with S = (Tx + Ty) + Tz, r3 >= 0, so it
+//     is >= third * S (or huge when its window is closed).  In exact arithmetic Tx + Ty + Tz
+//     = 3 t6.  Each of Tx, Ty, Tz is seven roundings of values within [-3M, 3M]: an error of
+//     at most 9.5 u M; the two sums add 9 u M, and third = 1/3 (1 + d), |d| <= u, so
+//     third * S >= t6 - 15 u M up to second-order terms.  lo3 = t6 - M 2^-18 (64 u M in FP32;
+//     M >= 2^-100 keeps the underflow of the halvings, 2^-150, far below the margin) is a
+//     lower bound of it;
+//   * if t0 <= min(t1d, L2, L5, L7, lo3), fd3UniformFar's result is >= t0;
+//   * a 2D operator with L_d >= t0 and L_d > max(t1, t4, t3) is left out (taken as huge): it
+//     is >= t0, so min(t0, .) does not see it, and it is above the 8-point window's
+//     max(t1, t4, t3), so min(t1d, t2d) > max(t1, t4, t3) holds with it exactly when without;
+//   * if lo3 >= min(t0, t1d, t2d), the 8-point operator is >= that minimum and is left out.
+// So min(t0, result) is min(t0, fd3UniformFar(h, n)) bit for bit.  Over the refinement
+// sweeps of the benchmark model the operators left out are 1.76 of the three 2D operators
+// and 70 % of the 8-point operators per warp that reaches them.
 template <class T>
 __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t0) {
     EIKX_FD3_UNIFORM_PREFIX
     (void)tUpd;
-    const T one = 1;
+    const T c20 = static_cast<T>(1.0 - 1.0 / 1048576.0), e20 = static_cast<T>(1.0 / 1048576.0);
+    const T E = ((t1 + t3) + t4) * e20;
+    const T L2 = t2 + (hs04 * c20 - E), L5 = t5 + (hs03 * c20 - E), L7 = t7 + (hs01 * c20 - E);
+    const T M = dmax(dmax(dmax(t1, t2), dmax(t3, t4)),
+                     dmax(dmax(t5, t6), dmax(t7, static_cast<T>(7.8886090522101181e-31))));   // 2^-100
+    const T lo3 = t6 - M * static_cast<T>(1.0 / 262144.0);
+    if (t0 <= dmin(dmin(t1d, dmin(L2, L5)), dmin(L7, lo3))) return t0;
+    const T m = dmax(dmax(t1, t4), t3);
+    T t2d = huge;
+    if (L5 < t0 || !(L5 > m)) {
+        const T dXZ = t1 - t4;
+        const T detXZ = 2 * (hs03 * hs03) - dXZ * dXZ;
+        if (detXZ > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03) t2d = t5 + dsqrt(detXZ);
+    }
+    if (L7 < t0 || !(L7 > m)) {
+        const T dYZ = t3 - t4;
+        const T detYZ = 2 * (hs01 * hs01) - dYZ * dYZ;
+        if (detYZ > 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01) t2d = dmin(t2d, t7 + dsqrt(detYZ));
+    }
+    if (L2 < t0 || !(L2 > m)) {
+        const T dXY = t1 - t3;
+        const T detXY = 2 * (hs04 * hs04) - dXY * dXY;
+        if (detXY > 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04) t2d = dmin(t2d, t2 + dsqrt(detXY));
+    }
+    // the 8-point operator under fd3UniformFar's condition: min(t1d, t2d, huge) is
+    // min(t1d, t2d)
+    const T t12 = dmin(t1d, t2d);
+    if (lo3 >= dmin(t0, t12) || !(t12 > m)) return t12;
     const T third = static_cast<T>(0.33333333333333333333333);
     const T half = static_cast<T>(0.5);
     const T Tx = t1 + half * (-t4 + t5 - t3 + t2) - t7 + t6;
     const T Ty = t3 + half * (-t4 + t7 - t1 + t2) - t5 + t6;
     const T Tz = t4 + half * (-t1 + t5 - t3 + t7) - t2 + t6;
-    const T S = (Tx + Ty) + Tz;
-    const T lo3 = third * S;
-    const T c20 = static_cast<T>(1.0 - 1.0 / 1048576.0), e20 = static_cast<T>(1.0 / 1048576.0);
-    const T E = ((t1 + t3) + t4) * e20;
-    const T L2 = t2 + (hs04 * c20 - E), L5 = t5 + (hs03 * c20 - E), L7 = t7 + (hs01 * c20 - E);
-    if (t0 <= dmin(dmin(t1d, dmin(L2, L5)), dmin(L7, lo3))) return t0;
-    T dXZ = t1 - t4;
-    T detXZ = 2 * (hs03 * hs03) - dXZ * dXZ;
-    const bool cXZ = detXZ > 0 && t4 <= t1 + hs03 && t1 <= t4 + hs03;
-    const T rXZ = dsqrt(cXZ ? detXZ : one);
-    T t2d = cXZ ? t5 + rXZ : huge;
-    T dYZ = t3 - t4;
-    T detYZ = 2 * (hs01 * hs01) - dYZ * dYZ;
-    const bool cYZ = detYZ > 0 && t3 <= t4 + hs01 && t4 <= t3 + hs01;
-    const T rYZ = dsqrt(cYZ ? detYZ : one);
-    t2d = dmin(t2d, cYZ ? t7 + rYZ : huge);
-    T dXY = t1 - t3;
-    T detXY = 2 * (hs04 * hs04) - dXY * dXY;
-    const bool cXY = detXY > 0 && t3 <= t1 + hs04 && t1 <= t3 + hs04;
-    const T rXY = dsqrt(cXY ? detXY : one);
-    t2d = dmin(t2d, cXY ? t2 + rXY : huge);
-    // the 8-point operator under fd3UniformFar's condition, as a branch (its window is
-    // closed for a whole warp at most nodes): min(t1d, t2d, huge) is min(t1d, t2d)
-    const T t12 = dmin(t1d, t2d);
-    if (lo3 >= dmin(t0, t12) || !(t12 > dmax(dmax(t1, t4), t3))) return t12;
     T det = 27 * (h * s0) * (h * s0) - (Tx - Ty) * (Tx - Ty) - (Tx - Tz) * (Tx - Tz) - (Ty - Tz) * (Ty - Tz);
     if (!(det >= 0)) return t12;
-    return dmin(t1d, dmin(t2d, third * (S + dsqrt(det))));
+    return dmin(t1d, dmin(t2d, third * (((Tx + Ty) + Tz) + dsqrt(det))));
 }
 
 // F64: the analytic factor in FP64 (SourceFp64, eikx_options.near_fp64; FP32 sweeps only).
