@@ -225,24 +225,26 @@ __device__ __forceinline__ T fd3UniformFar(T h, const Stencil3<T> &n) {
 // it returns t0 as soon as lower bounds show that no operator goes below t0, and evaluates
 // an operator only where its bound leaves it a chance to.  The bounds hold for the rounded
 // values, since round-to-nearest is monotone (u = unit roundoff: 2^-24 in FP32, less in
-// FP64; all times are >= 0, M = max(t1..t7, 2^-100)):
+// FP64; all times are >= 0, M = max(t1..t7, 2^-100)).  The bounds are formed with fused
+// multiply-adds: they only need to stay below the operators, which are evaluated unfused,
+// as the reference does.
 //   * a 2D operator, when its window is open, returns t_d + r (t_d = t5, t7, t2 for XZ, YZ,
 //     XY) with r = sqrt(2 hs^2 - (t_a - t_b)^2) and |t_a - t_b| <= hs by its window (hs the
 //     operator's h * min slowness, t_a, t_b its two axis neighbours).  The window test, the
 //     determinant and the square root round with unit roundoff u: the test admits
 //     |t_a - t_b| <= hs + u (t_a + t_b + hs), and the computed r is >= hs - u (t_a + t_b)
-//     - 5 u hs up to second-order terms.  So r >= m with m = hs (1 - 2^-20) - 2^-20 (t1 +
-//     t3 + t4), formed in T (a margin of at least 10 u hs and 15 u (t_a + t_b) covers the
-//     second-order terms and m's own rounding, and m < 0 whenever the times are so large
-//     that the margin would not), and the operator is >= L_d = t_d + m; a closed window
-//     returns huge;
+//     - 5 u hs up to second-order terms.  So r >= m with m = hs (1 - 2^-20) - 3 * 2^-20 M,
+//     formed in T (3 M >= t1 + t3 + t4 >= t_a + t_b, so the margin is at least 10 u hs and
+//     15 u (t_a + t_b), which covers the second-order terms and m's own rounding; m < 0
+//     whenever the times are so large that the margin would not), and the operator is
+//     >= L_d = t_d + m; a closed window returns huge;
 //   * the 8-point operator returns third * (S + r3) with S = (Tx + Ty) + Tz, r3 >= 0, so it
 //     is >= third * S (or huge when its window is closed).  In exact arithmetic Tx + Ty + Tz
 //     = 3 t6.  Each of Tx, Ty, Tz is seven roundings of values within [-3M, 3M]: an error of
 //     at most 9.5 u M; the two sums add 9 u M, and third = 1/3 (1 + d), |d| <= u, so
-//     third * S >= t6 - 15 u M up to second-order terms.  lo3 = t6 - M 2^-18 (64 u M in FP32;
-//     M >= 2^-100 keeps the underflow of the halvings, 2^-150, far below the margin) is a
-//     lower bound of it;
+//     third * S >= t6 - 15 u M up to second-order terms.  lo3 = t6 - M 2^-18 (64 u M in FP32,
+//     one rounding; M >= 2^-100 keeps the underflow of the halvings, 2^-150, far below the
+//     margin) is a lower bound of it;
 //   * if t0 <= min(t1d, L2, L5, L7, lo3), fd3UniformFar's result is >= t0;
 //   * a 2D operator with L_d >= t0 and L_d > max(t1, t4, t3) is left out (taken as huge): it
 //     is >= t0, so min(t0, .) does not see it, and it is above the 8-point window's
@@ -251,16 +253,18 @@ __device__ __forceinline__ T fd3UniformFar(T h, const Stencil3<T> &n) {
 // So min(t0, result) is min(t0, fd3UniformFar(h, n)) bit for bit.  Over the refinement
 // sweeps of the benchmark model the operators left out are 1.76 of the three 2D operators
 // and 70 % of the 8-point operators per warp that reaches them.
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return __fma_rn(a, b, c); }
 template <class T>
 __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t0) {
     EIKX_FD3_UNIFORM_PREFIX
     (void)tUpd;
-    const T c20 = static_cast<T>(1.0 - 1.0 / 1048576.0), e20 = static_cast<T>(1.0 / 1048576.0);
-    const T E = ((t1 + t3) + t4) * e20;
-    const T L2 = t2 + (hs04 * c20 - E), L5 = t5 + (hs03 * c20 - E), L7 = t7 + (hs01 * c20 - E);
+    const T c20 = static_cast<T>(1.0 - 1.0 / 1048576.0);
     const T M = dmax(dmax(dmax(t1, t2), dmax(t3, t4)),
                      dmax(dmax(t5, t6), dmax(t7, static_cast<T>(7.8886090522101181e-31))));   // 2^-100
-    const T lo3 = t6 - M * static_cast<T>(1.0 / 262144.0);
+    const T E = M * static_cast<T>(3.0 / 1048576.0);
+    const T L2 = t2 + fmaT(hs04, c20, -E), L5 = t5 + fmaT(hs03, c20, -E), L7 = t7 + fmaT(hs01, c20, -E);
+    const T lo3 = fmaT(M, static_cast<T>(-1.0 / 262144.0), t6);
     if (t0 <= dmin(dmin(t1d, dmin(L2, L5)), dmin(L7, lo3))) return t0;
     const T m = dmax(dmax(t1, t4), t3);
     T t2d = huge;

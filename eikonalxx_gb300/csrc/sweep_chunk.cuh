@@ -250,8 +250,6 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
             BATCH ? unit->mbox : st.mbox + static_cast<long long>(f) * a.tilesZ * a.tilesY * faceWords;
         const T h = BATCH ? unit->h : a.h;
         const int nChunks = Px / V;
-        const int nSteps = nChunks + LY + LZ - 2;
-
         const int y0 = b * LY, z0 = c * LZ;
         const int yp = y0 + ly, zp = z0 + lz;
         const bool laneValid = yp < ny && zp < nz;
@@ -261,6 +259,14 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         axisBounds(nx, REV, INIT, src.isx, xlo, xhi);
         axisBounds(ny, fy, INIT, src.isy, ylo, yhi);
         axisBounds(nz, fz, INIT, src.isz, zlo, zhi);
+        // Initialisation pass: the update range along x' starts at the source's column, so
+        // the field's lanes all walk from the chunk before the one holding it (whose last
+        // values are the first updated node's x'-1 neighbours; it updates nothing) instead
+        // of from chunk 0.  kBase is the same for every block of a field, so the mailbox
+        // chunks a block waits for are the ones its upstream blocks publish.
+        int kBase = 0;
+        if constexpr (INIT) kBase = max(0, (REV ? Px - 1 - xhi : xlo) / V - 1);
+        const int nSteps = nChunks - kBase + LY + LZ - 2;
         // Initialisation pass: the update range starts at y' = yp0, z' = zp0 and runs to the
         // end of each axis.  Warp blocks wholly before it update nothing: they are left out,
         // and the blocks after them read those rows from the field, which the sweep does not
@@ -274,6 +280,12 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         const bool yzUpd = laneValid && ya >= ylo && ya <= yhi && za >= zlo && za <= zhi;
         // the factored branch applies within `radius` cells of the source cell on every axis
         const bool yzNear = abs(src.isy - ya) <= a.radius && abs(src.isz - za) <= a.radius;
+        // walk positions of the factored x-range (empty when the lane's y', z' are not near;
+        // the radius clamped to the pitch, which no |isx - x| reaches)
+        const int rx = min(a.radius, Px);
+        const int nxa = src.isx - rx, nxb = src.isx + rx;
+        const int nearLo = !yzNear ? 1 << 30 : REV ? Px - 1 - nxb : nxa;
+        const int nearHi = !yzNear ? -1 : REV ? Px - 1 - nxa : nxb;
         T *row = field + (static_cast<long long>(za) * ny + ya) * Px;
         const T *srow = sp + static_cast<long long>(za + (fz ? 0 : 1)) * spPlane +
                         static_cast<long long>(ya + (fy ? 0 : 1)) * spPitch;
@@ -283,8 +295,8 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         auto walk = [&](const Vec<T> &m) { return REV ? reversed(m) : m; };   // memory <-> walk order
         // the own pencil's chunk of step sv into slot sv % kPre; one commit group per step
         auto prefetch = [&](int sv) {
-            const int kv = sv - ly - lz;
-            if (laneValid && kv >= 0 && kv < nChunks) {
+            const int kv = sv - ly - lz + kBase;
+            if (laneValid && kv >= kBase && kv < nChunks) {
                 Vec<T> *slot = pre + (sv & (kPre - 1)) * 64;
                 cpAsync16(slot, tChunk(row, kv));
                 cpAsync16(slot + 32, sChunk(srow, kv));
@@ -323,8 +335,8 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
 
         // Halo pipeline: the chunk a virtual lane produces at step sv goes into ring slot
         // sv; its mailbox words are loaded one step ahead and checked at step sv.
-        auto haloChunk = [&](int sv) { return sv - vly - vlz; };
-        auto haloValid = [&](int kv) { return vValid && kv >= 0 && kv < nChunks; };
+        auto haloChunk = [&](int sv) { return sv - vly - vlz + kBase; };
+        auto haloValid = [&](int kv) { return vValid && kv >= kBase && kv < nChunks; };
         auto haloStore = [&](int sv, const Vec<T> &tv, const Vec<T> &sv_) {
             const int slot = (sv & (kRingC - 1)) * kPlane + vslot;
             tring[slot] = tv;
@@ -374,8 +386,8 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
             ok = consume(s);
             if (!ok) break;
             issue(s + 1);
-            const int k = s - ly - lz;
-            const bool active = laneValid && k >= 0 && k < nChunks;
+            const int k = s - ly - lz + kBase;
+            const bool active = laneValid && k >= kBase && k < nChunks;
             prefetch(s + kAhead);
             cpAsyncWait<kAhead>();   // this step's group has landed
             Vec<T> tOwn = splat(huge), sOwn = splat(huge);
@@ -417,7 +429,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
                     n.s4 = e ? sY.v[e - 1] : cS5;
                     n.s5 = sY.v[e];
                     n.s7 = e ? sOwn.v[e - 1] : cS7;
-                    const bool near = yzNear && abs(src.isx - xa) <= a.radius;
+                    const bool near = xp >= nearLo && xp <= nearHi;
                     const T t0 = out.v[e];
                     T tu;
                     if (NEAR64 && near) {
