@@ -984,9 +984,9 @@ def main():
         SLAB[0] = True
         N_SWEEPS_MAX = 20      # the slab model converges more slowly than 10 iterations
     if args.fields is None:
-        # plain: 64 sources per step, where the sweep kernel's throughput saturates on GB300
-        # (32: 252, 64: 292, 128: 292, 256: 313 grids/s); with fewer, a sweep is bound by one
-        # field's wavefront critical path rather than by work
+        # plain: 64 sources per step, the largest seeded batch whose fields all converge
+        # within 10 iterations; with fewer, a sweep is bound by one field's wavefront
+        # critical path rather than by work
         # learned: 2,500 training models x 8 sources = the configuration's 20,000 fields
         args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8, "models": 32,
                        "learned": 2500}.get(args.workload, 64)
