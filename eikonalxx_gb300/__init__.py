@@ -39,7 +39,7 @@ EXPORTED = [
     "eikx_ray_options_default", "eikx_trace_rays2d",
     "eikx_warmnet_create", "eikx_warmnet_destroy", "eikx_warmnet_num_params", "eikx_warmnet_get_params",
     "eikx_warmnet_set_params", "eikx_warmnet_train_step", "eikx_warmnet_gradients", "eikx_warmnet_predict",
-    "eikx_warmnet_profile_step", "eikx_warmnet_set_test_hooks",
+    "eikx_warmnet_profile_step", "eikx_warmnet_set_test_hooks", "eikx_selftest_operator3d",
 ]
 CELL_SLOWNESS, NODAL_VELOCITY = 0, 1
 
@@ -182,6 +182,8 @@ def load(path=None):
     lib.eikx_warmnet_predict.argtypes = [vp, sp, c_int, c_double, vp, c_int, dp]
     lib.eikx_warmnet_profile_step.argtypes = [vp, sp, c_int, ctypes.c_float, dp, dp]
     lib.eikx_warmnet_set_test_hooks.argtypes = [vp, c_int, c_int]
+    lib.eikx_selftest_operator3d.argtypes = [c_int, c_int, ctypes.c_longlong, ctypes.c_ulonglong,
+                                             ctypes.POINTER(ctypes.c_longlong)]
     lib.eikx_tuning_save.argtypes = [vp, ctypes.c_char_p]
     lib.eikx_tuning_load.argtypes = [vp, ctypes.c_char_p]
     for name in EXPORTED:
@@ -519,6 +521,16 @@ class Context:
         s = _Stats()
         _check(self._lib.eikx_get_stats(self._h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+
+def selftest_operator3d(n, seed=1, precision=F32, device=0):
+    """Run the device self-test of the 3D sweep's operator shortcuts on n seeded stencils at
+    their edges; returns counts: evaluated, mismatches (0 = exact), results equal to t0,
+    stencils whose t0 is the operator's own value."""
+    lib = load()
+    out = (ctypes.c_longlong * 4)()
+    _check(lib.eikx_selftest_operator3d(device, precision, n, seed, out))
+    return dict(zip(("evaluated", "mismatches", "shortcut_t0", "t0_is_operator"), list(out)))
 
 
 def graph3d_tables(sweep, nx, ny, nz):

@@ -1854,6 +1854,23 @@ eikx_status eikx_station_times2d(eikx_ctx *c, int field, const eikx_source2d *st
     return stationsImpl(c, 2, field, st ? xyz.data() : nullptr, n, times);
 }
 
+eikx_status eikx_selftest_operator3d(int device, int precision, long long n, unsigned long long seed,
+                                     long long counts[4]) {
+    if (!counts || n < 0) return fail(EIKX_ERR_INVALID, "counts must not be NULL and n must be >= 0");
+    if (precision != EIKX_F32 && precision != EIKX_F64) return fail(EIKX_ERR_INVALID, "precision must be F32 or F64");
+    EIKX_CUDA(cudaSetDevice(device));
+    unsigned long long *d = nullptr;
+    EIKX_CUDA(cudaMalloc(&d, 4 * sizeof(unsigned long long)));
+    unsigned long long h[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemset(d, 0, sizeof(h));
+    if (e == cudaSuccess) e = eikx::launchOperatorSelftest(precision == EIKX_F32 ? 0 : 1, n, seed, d, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    EIKX_CUDA(e);
+    for (int k = 0; k < 4; ++k) counts[k] = static_cast<long long>(h[k]);
+    return EIKX_OK;
+}
+
 void eikx_ray_options_default(eikx_ray_options *opt) {
     if (!opt) return;
     std::memset(opt, 0, sizeof(*opt));

@@ -12,6 +12,81 @@
 
 namespace eikx {
 
+
+// ---------------------------------------------------------------------------------------
+// Self-test of the Cartesian operator's shortcuts (eikx_selftest_operator3d): on stencils
+// built to sit at the edges of the shortcuts -- node times within a few units in the last
+// place of the operator's own value, neighbour differences at the 2D windows' limits
+// |t_a - t_b| = hs, homogeneous slowness, unreached (huge) neighbours -- min(t0, bounded)
+// must equal min(t0, fd3UniformFar) bit for bit.
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long &x) {
+    unsigned long long z = (x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uni(unsigned long long &x) {
+    return static_cast<double>(splitmix(x) >> 11) * (1.0 / 9007199254740992.0);
+}
+template <class T> __device__ __forceinline__ T ulpStep(T v, int k) {
+    T r = v;
+    const T dir = k > 0 ? static_cast<T>(1.e30) : static_cast<T>(-1.e30);
+    for (int i = 0; i < (k > 0 ? k : -k); ++i) r = nextafter(r, dir);
+    return r;
+}
+template <class T> __device__ __forceinline__ bool sameBits(T a, T b) {
+    if constexpr (sizeof(T) == 4) return __float_as_uint(a) == __float_as_uint(b);
+    else return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+template <class T>
+__global__ void operatorSelftestKernel(long long n, unsigned long long seed, unsigned long long *counts) {
+    unsigned long long local[4] = {0, 0, 0, 0};   // evaluated, mismatches, shortcut exits, t0 = operator
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        unsigned long long x = seed ^ (static_cast<unsigned long long>(i) * 0xD1B54A32D192ED03ull);
+        const double hs[4] = {10.0, 25.0, 50.0, 100.0};
+        const T h = static_cast<T>(hs[splitmix(x) & 3]);
+        Stencil3<T> st;
+        T *s = &st.s0;
+        const bool homogeneous = (splitmix(x) & 3) == 0;
+        const double v0 = 1500.0 + 6500.0 * uni(x);
+        for (int k = 0; k < 7; ++k) s[k] = static_cast<T>(1.0 / (homogeneous ? v0 : 1500.0 + 6500.0 * uni(x)));
+        const double base = (splitmix(x) & 7) == 0 ? 1e-3 * uni(x) : 40.0 * uni(x);
+        const double hsMin = static_cast<double>(h) / 8000.0, hsMax = static_cast<double>(h) / 1500.0;
+        T *t = &st.t1;
+        for (int k = 0; k < 7; ++k) {
+            const unsigned r = static_cast<unsigned>(splitmix(x) & 15);
+            double off;
+            if (r < 4) off = (uni(x) * 3.0 - 1.0) * hsMax;                            // anywhere near
+            else if (r < 8) off = (r & 1 ? 1.0 : -1.0) * static_cast<double>(h) * s[k]; // at a window's edge
+            else if (r < 10) off = static_cast<double>(h) * s[0] * (r & 1 ? 1.4142135623730951 : 1.7320508075688772);
+            else if (r < 11) off = 0.0;
+            else off = (uni(x) * 2.0 - 0.5) * hsMin;
+            t[k] = static_cast<T>(base + off > 0 ? base + off : 0.0);
+            if ((splitmix(x) & 31) == 0) t[k] = static_cast<T>(1.e10);               // unreached
+            if (splitmix(x) & 1) t[k] = ulpStep(t[k], static_cast<int>(splitmix(x) % 5) - 2);
+        }
+        const T r = fd3UniformFar<T>(h, st);
+        T t0;
+        const unsigned mode = static_cast<unsigned>(splitmix(x) % 6);
+        if (mode == 0) t0 = r;
+        else if (mode == 1) t0 = ulpStep(r, static_cast<int>(splitmix(x) % 9) - 4);
+        else if (mode == 2) t0 = static_cast<T>(base + (uni(x) * 3.0 - 1.0) * hsMax);
+        else if (mode == 3) t0 = static_cast<T>(1.e10);
+        else if (mode == 4) t0 = static_cast<T>(static_cast<double>(r) * (1.0 + (uni(x) * 2.0 - 1.0) * 1e-6));
+        else t0 = ulpStep(t[splitmix(x) % 7], static_cast<int>(splitmix(x) % 9) - 4);
+        if (!(t0 >= 0)) t0 = 0;
+        const T b = fd3UniformFarBounded<T>(h, st, t0);
+        const T m1 = b < t0 ? b : t0, m2 = r < t0 ? r : t0;
+        local[0] += 1;
+        local[1] += sameBits(m1, m2) ? 0 : 1;
+        local[2] += sameBits(b, t0) ? 1 : 0;
+        local[3] += sameBits(r, t0) ? 1 : 0;
+    }
+    for (int k = 0; k < 4; ++k) atomicAdd(counts + k, local[k]);
+}
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -173,4 +248,14 @@ template cudaError_t launchStations<float>(const float *, int, int, int, double,
 template cudaError_t launchStations<double>(const double *, int, int, int, double, double, double, const Corner3 &,
                                             int, const int *, const double *, double *, cudaStream_t);
 
+// The operator self-test (see operatorSelftestKernel): counts[4] on the device.
+cudaError_t launchOperatorSelftest(int precision, long long n, unsigned long long seed, unsigned long long *counts,
+                                   cudaStream_t s) {
+    const int blocks = 152 * 8;
+    if (precision == 0) operatorSelftestKernel<float><<<blocks, 256, 0, s>>>(n, seed, counts);
+    else operatorSelftestKernel<double><<<blocks, 256, 0, s>>>(n, seed, counts);
+    return cudaGetLastError();
+}
+
 }  // namespace eikx
+

@@ -231,4 +231,10 @@ cudaError_t launchAnalytic3(double *t, int nx, int ny, int nz, double dx, double
 cudaError_t launchAnalytic2(double *t, int nx, int nz, double dx, double dz, double xs, double zs,
                             double vTop, double vBottom, cudaStream_t s);
 
+// Self-test of the Cartesian operator's lower-bound shortcuts (post.cu): n random stencils
+// at the shortcuts' edges; counts[0..3] += evaluated, mismatches of min(t0, .) against
+// fd3UniformFar, shortcut results equal to t0, stencils whose t0 is the operator's value.
+cudaError_t launchOperatorSelftest(int precision, long long n, unsigned long long seed, unsigned long long *counts,
+                                   cudaStream_t s);
+
 }  // namespace eikx

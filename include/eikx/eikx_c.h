@@ -474,6 +474,18 @@ eikx_status eikx_warmnet_profile_step(eikx_warmnet *net, const eikx_warmnet_samp
  * detection without a GPU fault. */
 eikx_status eikx_warmnet_set_test_hooks(eikx_warmnet *net, int spin_limit_log2, int late);
 
+/* Self-test of the 3D sweep's operator shortcuts on device `device`: n seeded random
+ * stencils, built to sit at the shortcuts' edges (node times a few units in the last place
+ * from the operator's value, neighbour differences at the 2D windows' limits, homogeneous
+ * slowness, unreached neighbours), are evaluated by the uniform-grid Cartesian operator with
+ * and without its lower-bound exits and gated operators, in precision EIKX_F32 or EIKX_F64.
+ * counts[0] = stencils evaluated, counts[1] = stencils where min(t0, result) differs in any
+ * bit (0 when the shortcuts are exact), counts[2] = results equal to t0, counts[3] = stencils
+ * whose t0 is the operator's own value.  A test of the sweep kernels' arithmetic; it
+ * allocates 32 bytes of device memory for the call. */
+eikx_status eikx_selftest_operator3d(int device, int precision, long long n, unsigned long long seed,
+                                     long long counts[4]);
+
 #ifdef __cplusplus
 }
 #endif
