@@ -40,6 +40,9 @@ PAIR = [False]  # pair_fields option of the GPU arm (set from the command line)
 # T0 = distance x source slowness, its gradient and tau in double (eikx_options.near_fp64)
 NEAR64 = [True]
 KERNEL = [0]    # sweep_kernel option of the GPU arm: 0 default, 1 node-step, 2 chunk-step
+# the plain workload as a stream: this many fields in flight (eikx_options.max_in_flight),
+# a converged field's slot taking the next source; 0 = all the step's sources as one batch
+IN_FLIGHT = [0]
 L2_BYTES = 129 * 2 ** 20
 BYTES_PER_NODE_SWEEP = 12          # FP32: read T, read slowness, write T
 
@@ -149,12 +152,15 @@ def workload_config(fields, world):
                          f"degrees, {fields} sources on the top surface per step per GPU" if SLAB[0] else
                          f"station tables, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, {fields} sources on the "
                          f"top surface per step per GPU, one persistent launch per sweep" if SURFACE[0] else
-                         f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, "
-                         f"{fields} independent sources per step per GPU"),
+                         (f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, a stream of {fields} "
+                          f"independent sources per step per GPU, {IN_FLIGHT[0]} in flight" if 0 < IN_FLIGHT[0] < fields
+                          else f"plain 3D solve, {NX}x{NY}x{NZ} h={H:g} m layered+GRF, "
+                               f"{fields} independent sources per step per GPU")),
             "grid": [NX, NY, NZ], "h_m": H, "fields_per_step": fields,
             "precision": ("fp32 sweeps; fp64 source init and factored (near-source) branch" if NEAR64[0] else
                           "fp32 sweeps, fp64 source init"),
             "factored_radius": RADIUS, "tolerance_s": TOL, "max_iterations": N_SWEEPS_MAX,
+            "in_flight": IN_FLIGHT[0] if 0 < IN_FLIGHT[0] < fields else fields,
             "l2": "flushed (write of 2x L2) between timed steps; per-step fields exceed L2",
             "parallelism": f"replicas x{world} (sources sharded, no collective)"}
 
@@ -162,10 +168,32 @@ def workload_config(fields, world):
 FP64_TOL, FP64_MAX_ITERATIONS, ACCURACY_FIELDS = 1e-9, 40, 8
 
 
-def fp64_accuracy(ctx, src, opt, ex, n_fields=ACCURACY_FIELDS, seed=3):
+def fp64_sweeps_arm(ctx, src, opt, ex, pick, judge, max_fields, dev):
+    """The precision that meets the bound where FP32 may not: FP64 sweeps at the workload's
+    own tolerance and iteration cap.  grids/s over up to `max_fields` of the workload's
+    sources (device-timed, device output), and the error of its fields `pick` against the
+    converged FP64 solves `judge`."""
+    import torch
+    n = min(len(src), max_fields)
+    o = ex.Options(n_sweeps=opt.n_sweeps, tolerance=opt.tolerance, factored_radius=opt.factored_radius)
+    out = torch.empty((n, NZ, NY, NX), dtype=torch.float64, device=f"cuda:{dev}")
+    ms = []
+    for i in range(3):
+        ctx.solve3d(src[:n], o, ex.F64, out=out)
+        if i:
+            ms.append(ctx.stats()["device_ms"])
+    del out
+    t = ctx.solve3d(src[pick], o, ex.F64)
+    err = max(float(np.abs(a - b).max()) for a, b in zip(t, judge))
+    return {"grids_s": n / (float(np.mean(ms)) / 1e3), "fields_timed": n, "max_err_vs_fp64_converged_s": err,
+            "meets_1e-4": bool(err <= 1e-4), "tolerance_s": opt.tolerance}
+
+
+def fp64_accuracy(ctx, src, opt, ex, n_fields=ACCURACY_FIELDS, seed=3, fp64_arm_fields=0, dev=0):
     """Max and RMS error of the FP32 fields of `n_fields` seeded sources of `src` (solved
     with the timed options `opt`) against FP64 solves of the same sources run to
-    convergence (tolerance 1e-9 s, at most 40 iterations), over all their nodes."""
+    convergence (tolerance 1e-9 s, at most 40 iterations), over all their nodes.  With
+    fp64_arm_fields > 0 it adds the FP64-sweeps arm (fp64_sweeps_arm) over that many fields."""
     pick = np.sort(np.random.default_rng(seed).choice(len(src), min(n_fields, len(src)), replace=False))
     t32 = ctx.solve3d(src[pick], opt, ex.F32)
     o64 = ex.Options(n_sweeps=FP64_MAX_ITERATIONS, tolerance=FP64_TOL, factored_radius=opt.factored_radius)
@@ -179,10 +207,13 @@ def fp64_accuracy(ctx, src, opt, ex, n_fields=ACCURACY_FIELDS, seed=3):
         mx = max(mx, per[-1])
         sq += float(np.sum(d * d))
         n += d.size
-    return {"max_err_vs_fp64_s": mx, "rms_err_vs_fp64_s": float(np.sqrt(sq / n)), "meets_1e-4": bool(mx <= 1e-4),
-            "fields_checked": [int(i) for i in pick], "max_err_per_field_s": per,
-            "fp64_tolerance_s": FP64_TOL, "fp64_iterations_max": st["iterations_max"],
-            "fp64_converged": bool(st["iterations_max"] < FP64_MAX_ITERATIONS)}
+    acc = {"max_err_vs_fp64_s": mx, "rms_err_vs_fp64_s": float(np.sqrt(sq / n)), "meets_1e-4": bool(mx <= 1e-4),
+           "fields_checked": [int(i) for i in pick], "max_err_per_field_s": per,
+           "fp64_tolerance_s": FP64_TOL, "fp64_iterations_max": st["iterations_max"],
+           "fp64_converged": bool(st["iterations_max"] < FP64_MAX_ITERATIONS)}
+    if fp64_arm_fields > 0:
+        acc["fp64_sweeps"] = fp64_sweeps_arm(ctx, src, opt, ex, pick, t64, fp64_arm_fields, dev)
+    return acc
 
 
 def run_gpu(args):
@@ -205,8 +236,10 @@ def run_gpu(args):
     ctx.set_grid3d(NX, NY, NZ, H, H, H)
     v_host = torch.from_numpy(v.ravel()).pin_memory()
     ctx.set_nodal_velocity3d(v_host)
+    stream = 0 < IN_FLIGHT[0] < fields
+    slots = IN_FLIGHT[0] if stream else fields          # fields per sweep launch
     opt = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS, pair_fields=PAIR[0],
-                     sweep_kernel=KERNEL[0], near_fp64=NEAR64[0])
+                     sweep_kernel=KERNEL[0], near_fp64=NEAR64[0], max_in_flight=slots if stream else 0)
     out_dev = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device=f"cuda:{dev}")
     out_host = torch.empty((fields, NZ, NY, NX), dtype=torch.float32).pin_memory()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
@@ -214,7 +247,8 @@ def run_gpu(args):
     # autotuning (outside the timed region): kernel variant, warp-block shape, grid size
     tuning = None
     if not args.no_autotune and KERNEL[0] == 0 and not PAIR[0]:
-        tuning = ctx.autotune3d(src, ex.F32)
+        # a stream launches its slots' fields: tuned on that many sources
+        tuning = ctx.autotune3d(src[:slots], ex.F32)
 
     def step_device():
         ctx.solve3d(src, opt, ex.F32, out=out_dev)
@@ -225,7 +259,10 @@ def run_gpu(args):
     # bit-identical to the FP64 oracle in the tests)
     acc = {}
     if rank == 0 and not args.skip_accuracy:
-        acc = fp64_accuracy(ctx, src, opt, ex)
+        # the FP64-sweeps arm where the FP32 fields may miss the bound: the station tables and
+        # the full-scale slab model (at most 32 fields of the latter: FP64 fields of 67 M nodes)
+        acc = fp64_accuracy(ctx, src, opt, ex, fp64_arm_fields=(32 if SLAB[0] else fields) if SURFACE[0] else 0,
+                            dev=dev)
         if not SLAB[0]:
             # against closed forms on the same grid: constant velocity, and a linear gradient
             # from the top to the bottom of the grid (nodal model, one source)
@@ -267,9 +304,20 @@ def run_gpu(args):
         ctx.solve3d(src, o, ex.F32, out=out_dev)
         return ctx.stats()
     popts = dict(tolerance=TOL, factored_radius=RADIUS, profile_sweeps=True, pair_fields=PAIR[0], near_fp64=NEAR64[0],
-                 sweep_kernel=KERNEL[0])
-    rl = refinement_roofline(prof_solve, ex.Options(n_sweeps=N_SWEEPS_MAX, **popts),
-                             ex.Options(n_sweeps=0, **popts), BYTES_PER_NODE_SWEEP)
+                 sweep_kernel=KERNEL[0], max_in_flight=slots if stream else 0)
+    if stream:
+        # a stream runs the new fields' initialisation sweeps inside the same launches as the
+        # others' refinement sweeps, so the time of all sweep launches is credited with both:
+        # the refinement updates performed plus one grid of updates per field for its
+        # initialisation pass (its 8 octants cover the grid once)
+        pst = prof_solve(ex.Options(n_sweeps=N_SWEEPS_MAX, **popts))
+        upd = pst["refine_node_updates"] + fields * n_nodes
+        rl = {"achieved": BYTES_PER_NODE_SWEEP * upd / (pst["sweep_ms"] / 1e3) / 1e9,
+              "algorithmic_bytes": BYTES_PER_NODE_SWEEP * upd, "node_updates": upd, "refine_ms": pst["sweep_ms"],
+              "refine_launches": pst["sweeps_launched"], "launch_ms": pst["sweep_ms"] / max(1, pst["sweeps_launched"])}
+    else:
+        rl = refinement_roofline(prof_solve, ex.Options(n_sweeps=N_SWEEPS_MAX, **popts),
+                                 ex.Options(n_sweeps=0, **popts), BYTES_PER_NODE_SWEEP)
     achieved = rl["achieved"]
     peak, peak_kind = _peaks()
     tr = _traffic()
@@ -289,8 +337,8 @@ def run_gpu(args):
     if tr and tr.get("kernel") == kernel_name.replace(",8x4", ""):
         # DRAM bytes of one full sweep from the committed ncu capture, scaled by the
         # fields per launch (traffic grows in proportion to the fields swept)
-        traffic = tr["dram_bytes_per_launch"] * fields / tr["fields"]
-        traffic_src = f"profiles/sweep3d_traffic.json ({tr['fields']} fields, scaled to {fields})"
+        traffic = tr["dram_bytes_per_launch"] * slots / tr["fields"]
+        traffic_src = f"profiles/sweep3d_traffic.json ({tr['fields']} fields, scaled to {slots} per launch)"
 
     # the configuration's own form, one source per solve: bound by one field's wavefront
     # latency rather than by throughput (device-resident, CUDA events, not the headline)
@@ -334,8 +382,14 @@ def run_gpu(args):
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": rl["algorithmic_bytes"], "node_updates": rl["node_updates"],
                      "refine_ms": rl["refine_ms"], "launch_ms": rl["launch_ms"],
-                     "note": "refinement sweeps only; 12 B per node update (read T, read slowness, write T)",
-                     "traffic": traffic, "traffic_source": traffic_src},
+                     "note": ("all sweep launches of the stream, credited with the refinement updates plus one grid "
+                              "per field for its initialisation pass; 12 B per node update (read T, read slowness, "
+                              "write T)" if stream else
+                              "refinement sweeps only; 12 B per node update (read T, read slowness, write T)"),
+                     "traffic": traffic, "traffic_source": traffic_src,
+                     # the bytes a field's update cannot avoid: read T and write T (the slowness
+                     # is one copy shared by all fields through L2)
+                     "compulsory_bytes_per_update": 8, "frac_compulsory": achieved * 8 / 12 / peak},
         "e2e": {"value": e2e, "unit": "grids/s", "h2d_bytes_per_step": int(v.nbytes + 24 * fields),
                 "d2h_bytes_per_step": int(4 * n_nodes * fields), "ms_per_step": float(np.mean(e2e_ms))},
         "gpu_launches": int(launches), "clocks": clk.summary(),
@@ -390,6 +444,20 @@ def run_models(args):
         acc = {"max_err_vs_fp64_s": float(d.max()), "rms_err_vs_fp64_s": float(np.sqrt(np.mean(d ** 2))),
                "meets_1e-4": bool(d.max() <= 1e-4), "models_over_1e-4": int(sum(e > 1e-4 for e in per)),
                "fp64_iterations_max": it64, "fp64_converged": bool(it64 < FP64_MAX_ITERATIONS)}
+        # the precision that meets the bound: FP64 sweeps at the workload's tolerance and cap
+        o_arm = ex.Options(n_sweeps=N_SWEEPS_MAX, tolerance=TOL, factored_radius=RADIUS)
+        m64 = [dict(m, out=torch.empty((1,) + tuple(m["out"].shape[1:]), dtype=torch.float64, device=f"cuda:{dev}"))
+               for m in dev_models]
+        ms64 = []
+        for i in range(3):
+            ctx.solve3d_batch(m64, o_arm, ex.F64)
+            if i:
+                ms64.append(ctx.stats()["device_ms"])
+        e64 = max(float(np.abs(m["out"][0].cpu().numpy() - b).max()) for m, b in zip(m64, t64))
+        del m64
+        acc["fp64_sweeps"] = {"grids_s": n / (float(np.mean(ms64)) / 1e3), "fields_timed": n,
+                              "max_err_vs_fp64_converged_s": e64, "meets_1e-4": bool(e64 <= 1e-4),
+                              "tolerance_s": TOL}
 
     for _ in range(args.warmup):
         ctx.solve3d_batch(dev_models, opt, ex.F32)
@@ -442,11 +510,13 @@ def run_models(args):
                                  else "fp32 sweeps, fp64 source init"), "factored_radius": RADIUS, "tolerance_s": TOL,
                    "max_iterations": N_SWEEPS_MAX, "l2": "flushed (write of 2x L2) between timed steps",
                    "parallelism": f"replicas x{world} (models split by estimated cost, no collective)"},
-        "roofline": {"bound": "hbm", "kernel": "sweep3ChunkKernel<float,uniform,batch>", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": ("sweep3ChunkNear64Kernel<float,uniform,batch>" if NEAR64[0] else
+                                                "sweep3ChunkKernel<float,uniform,batch>"), "achieved": achieved,
                      "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "algorithmic_bytes": rl["algorithmic_bytes"], "node_updates": rl["node_updates"],
                      "refine_ms": rl["refine_ms"], "launch_ms": rl["launch_ms"], "traffic": None,
-                     "note": "refinement sweeps only; 12 B per node update"},
+                     "note": "refinement sweeps only; 12 B per node update",
+                     "compulsory_bytes_per_update": 8, "frac_compulsory": achieved * 8 / 12 / peak},
         "e2e": {"value": e2e, "unit": "grids/s", "h2d_bytes_per_step": int(sum(m["v"].nbytes for m in mine)),
                 "d2h_bytes_per_step": int(4 * nodes), "ms_per_step": float(np.mean(e2e_ms))},
         "gpu_launches": int(launches), "clocks": clk.summary(),
@@ -957,6 +1027,8 @@ def main():
     ap.add_argument("--learn-steps-default", type=int, default=1500,
                     help="plain: training steps of the learned sub-record")
     ap.add_argument("--skip-learned", action="store_true", help="plain: leave out the learned sub-record")
+    ap.add_argument("--in-flight", type=int, default=None,
+                    help="plain: fields in flight of the step's stream of sources (0 = one batch of all of them)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -983,13 +1055,21 @@ def main():
         SURFACE[0] = True
         SLAB[0] = True
         N_SWEEPS_MAX = 20      # the slab model converges more slowly than 10 iterations
+    if args.in_flight is None:
+        # plain: a stream of sources with 256 fields in flight.  A sweep launch costs a fixed
+        # wavefront fill and drain (about 0.33 ms) plus about 0.047 ms per field, so more
+        # fields per launch amortise it; and a stream refills the slots of fields that
+        # converged, so no launch runs with a few slow fields only (64, 128, 256 slots:
+        # 429, 457, 482 grids/s on the bench model)
+        args.in_flight = 256 if args.workload == "plain" and not args.profile_case else 0
     if args.fields is None:
-        # plain: 64 sources per step, the largest seeded batch whose fields all converge
-        # within 10 iterations; with fewer, a sweep is bound by one field's wavefront
-        # critical path rather than by work
+        # plain: 4 sources per slot of the stream; 64 as one batch without one
         # learned: 2,500 training models x 8 sources = the configuration's 20,000 fields
         args.fields = {"stations": 64, "full": 256, "2d": 1, "warmstart": 8, "models": 32,
                        "learned": 2500}.get(args.workload, 64)
+        if args.workload == "plain" and args.in_flight > 0:
+            args.fields = 4 * args.in_flight
+    IN_FLIGHT[0] = args.in_flight
     PAIR[0] = args.pair_fields
     NEAR64[0] = not args.fp32_near
     KERNEL[0] = args.sweep_kernel

@@ -72,7 +72,7 @@ class _Options(ctypes.Structure):
                 ("pair_fields", ctypes.c_int), ("sweep_kernel", ctypes.c_int),
                 ("block_shape", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("test_tag_margin", ctypes.c_int), ("near_fp64", ctypes.c_int), ("warm_gate", ctypes.c_int),
-                ("reserved", ctypes.c_int * 2)]
+                ("max_in_flight", ctypes.c_int), ("reserved", ctypes.c_int)]
 
 
 class _Stats(ctypes.Structure):
@@ -227,6 +227,7 @@ class Options:
     test_tag_margin: int = 0      # test hook only (see eikx_options.test_tag_margin)
     near_fp64: bool = False       # 3D FP32: factored (near-source) updates in FP64
     warm_gate: int = 0            # solve3d_warm residual gate: 0 one-sided, 1 two-sided
+    max_in_flight: int = 0        # solve3d: > 0 = a stream of the sources through this many slots
 
     def _c(self):
         o = _Options()
@@ -245,6 +246,7 @@ class Options:
         o.test_tag_margin = int(self.test_tag_margin)
         o.near_fp64 = int(bool(self.near_fp64))
         o.warm_gate = int(self.warm_gate)
+        o.max_in_flight = int(self.max_in_flight)
         return o
 
 

@@ -117,6 +117,19 @@ struct Workspace {
     std::vector<int> orderKey;   // (tilesY, tilesZ, nFields, dim) of the uploaded order table
 };
 
+// Buffers of a stream of sources through slots (eikx_options.max_in_flight): field buffers
+// for the slots plus those whose copy-out is in flight, per-slot mailbox and control words,
+// the slot table, and the FP64 factor tables of every source of the stream.
+struct StreamWorkspace {
+    DevBuf tt, mbox, epoch, queue, residual, converged, iterations, abortFlag, order, srcs, corners, slots, list,
+        srcs64, srcs64All, factor;
+    EpochMirror epochMirror;
+    PinnedBuf stage, flags;
+    std::vector<int> orderKey;
+    std::vector<cudaEvent_t> bufEv;   // per field buffer: its copy-out has finished
+    cudaEvent_t boundary = nullptr;   // the end of an iteration on the solve stream
+};
+
 // Buffers of multi-model batches (eikx_solve3d_batch): every model's fields, padded
 // slowness and mailbox packed into one allocation each, plus the cached schedule graph.
 struct BatchWorkspace {
@@ -173,6 +186,7 @@ struct eikx_ctx {
     std::vector<cudaEvent_t> iterEv;
     PinnedBuf iterFlags;
     std::vector<cudaEvent_t> sweepEv;   // per-sweep timing (profile_sweeps)
+    StreamWorkspace sw;                 // stream mode (eikx_options.max_in_flight)
     // 3D model
     int nx = 0, ny = 0, nz = 0;
     double dx = 0, dy = 0, dz = 0, x0 = 0, y0 = 0, z0 = 0;
@@ -367,6 +381,305 @@ cudaError_t assignFactorTables(std::vector<eikx::SourceFp64> &recs, DevBuf &buf)
     return cudaSuccess;
 }
 
+// A stream of sources through S = o.max_in_flight slots (3D, chunk-step).  Each slot solves
+// one source at a time in one of S + S/2 field buffers; the sweeps run iteration by
+// iteration (8 launches, each followed by the per-slot convergence test), and at each
+// iteration boundary the host reads the slots' flags: a field that converged (or ran
+// n_sweeps iterations) is copied out on the copy stream, and its slot takes the next source
+// in a free buffer.  A slot's sweep k of its own schedule runs ordering k mod 8 (sources
+// start at iteration boundaries), so every field runs exactly the sweeps of a solve of its
+// source alone.
+template <class T>
+eikx_status solveStream3(eikx_ctx *c, const eikx_options &o, int nSrc, const std::vector<eikx::SourceT<T>> &srcT,
+                         const std::vector<eikx::SourceFp64> &srcT64In, const std::vector<eikx::Corner3> &corners,
+                         bool uniform, int shape, void *tOut, int where, DevBuf *spad) {
+    StreamWorkspace &w = c->sw;
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    const double dx = c->dx, dy = c->dy, dz = c->dz;
+    const int Px = roundUp(nx, 4), spPitch = Px + 8;
+    const long long fieldStride = static_cast<long long>(Px) * ny * nz;
+    const int S = o.max_in_flight;
+    const int nBufs = S + (S + 1) / 2;
+    const int ly = eikx::shapeLY(shape), lz = eikx::shapeLZ(shape);
+    const int tilesY = (ny + ly - 1) / ly, tilesZ = (nz + lz - 1) / lz;
+    const long long nProgressL = static_cast<long long>(S) * tilesY * tilesZ;
+    if (nProgressL > std::numeric_limits<int>::max()) return fail(EIKX_ERR_INVALID, "too many slots for this grid");
+    const int nProgress = static_cast<int>(nProgressL);
+    const int nSweeps = std::max(0, o.n_sweeps);
+    const int initSweeps = o.init_sweeps ? 1 : 0;
+    const int resStride = 8 * (1 + nSweeps);
+    const int W = static_cast<int>(sizeof(T) / 4);
+    // the stream's sweeps: every slot is busy until the sources run out, and a source takes
+    // at most (init + n_sweeps) iterations
+    const long long perSource = initSweeps + nSweeps;
+    const long long maxIters = (static_cast<long long>(nSrc) * perSource + S - 1) / S + perSource + 1;
+    if (8 * maxIters + 1 >= (1ll << 31)) return fail(EIKX_ERR_INVALID, "stream too long for one call");
+    const int epochStride = static_cast<int>(8 * maxIters + 1);
+
+    // buffers
+    const size_t mboxBytes = static_cast<size_t>(nProgress) * (ly + lz) * Px * W * 8;
+    EIKX_CUDA(w.tt.ensure(static_cast<size_t>(fieldStride) * nBufs * sizeof(T)));
+    if (w.mbox.bytes < mboxBytes || !w.mbox.p) {
+        EIKX_CUDA(w.mbox.ensure(mboxBytes));
+        EIKX_CUDA(cudaMemsetAsync(w.mbox.p, 0, w.mbox.bytes, c->stream));
+    }
+    if (!w.epoch.p) {
+        EIKX_CUDA(w.epoch.ensure(2 * sizeof(unsigned)));
+        EIKX_CUDA(cudaMemsetAsync(w.epoch.p, 0, 2 * sizeof(unsigned), c->stream));
+    }
+    EIKX_CUDA(w.queue.ensure(2 * sizeof(unsigned)));
+    EIKX_CUDA(w.residual.ensure(static_cast<size_t>(S) * resStride * 8));
+    EIKX_CUDA(w.converged.ensure(static_cast<size_t>(S) * 4));
+    EIKX_CUDA(w.iterations.ensure(static_cast<size_t>(S) * 4));
+    EIKX_CUDA(w.abortFlag.ensure(sizeof(int)));
+    EIKX_CUDA(w.order.ensure(static_cast<size_t>(nProgress) * 16));
+    EIKX_CUDA(w.srcs.ensure(static_cast<size_t>(S) * sizeof(eikx::SourceT<T>)));
+    EIKX_CUDA(w.corners.ensure(static_cast<size_t>(S) * sizeof(eikx::Corner3)));
+    EIKX_CUDA(w.slots.ensure(static_cast<size_t>(S) * sizeof(int2)));
+    EIKX_CUDA(w.list.ensure(static_cast<size_t>(S) * sizeof(int)));
+    while (static_cast<int>(w.bufEv.size()) < nBufs) {
+        cudaEvent_t e;
+        EIKX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        w.bufEv.push_back(e);
+    }
+    if (!w.boundary) EIKX_CUDA(cudaEventCreateWithFlags(&w.boundary, cudaEventDisableTiming));
+    // FP64 factor tables of every source, filled once
+    std::vector<eikx::SourceFp64> srcT64 = srcT64In;
+    const bool near64 = !srcT64.empty();
+    if (near64) {
+        EIKX_CUDA(assignFactorTables(srcT64, w.factor));
+        EIKX_CUDA(w.srcs64All.ensure(srcT64.size() * sizeof(eikx::SourceFp64)));
+        EIKX_CUDA(w.srcs64.ensure(static_cast<size_t>(S) * sizeof(eikx::SourceFp64)));
+    }
+    // staging: the slot table, sources, corners, FP64 records and the refill list per
+    // boundary; the flags read back per boundary
+    const size_t srcB = sizeof(eikx::SourceT<T>), cornB = sizeof(eikx::Corner3), s64B = sizeof(eikx::SourceFp64);
+    const size_t offSrc = static_cast<size_t>(S) * sizeof(int2), offCorn = offSrc + S * srcB,
+                 offS64 = offCorn + S * cornB, offList = offS64 + S * s64B, offEnd = offList + S * sizeof(int);
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));
+    EIKX_CUDA(w.stage.ensure(std::max(offEnd, near64 ? srcT64.size() * s64B : 0) + 64));
+    EIKX_CUDA(w.flags.ensure(static_cast<size_t>(2 * S + 1) * sizeof(int)));
+    char *stage = static_cast<char *>(w.stage.p);
+    int *flags = static_cast<int *>(w.flags.p);
+    if (near64) {
+        std::memcpy(stage, srcT64.data(), srcT64.size() * s64B);
+        EIKX_CUDA(cudaMemcpyAsync(w.srcs64All.p, stage, srcT64.size() * s64B, cudaMemcpyHostToDevice, c->stream));
+        EIKX_CUDA(eikx::launchFactorTables(w.srcs64All.as<eikx::SourceFp64>(), nSrc, c->stream));
+        EIKX_CUDA(cudaStreamSynchronize(c->stream));   // the staging buffer is reused below
+    }
+    std::vector<int> key = {tilesY, tilesZ, S, 3, ly};
+    if (key != w.orderKey) {
+        const std::vector<int> order = buildOrder(tilesY, tilesZ, S, ly, lz);
+        EIKX_CUDA(cudaMemcpy(w.order.p, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice));
+        w.orderKey = key;
+    }
+
+    eikx::SolveState st{};
+    st.queue[0] = w.queue.as<unsigned>();
+    st.queue[1] = w.queue.as<unsigned>() + 1;
+    st.mbox = w.mbox.as<unsigned long long>();
+    st.epoch = w.epoch.as<unsigned>();
+    st.epochStride = epochStride;
+    st.residual = w.residual.as<unsigned long long>();
+    st.residualStride = resStride;
+    st.converged = w.converged.as<int>();
+    st.sweepsRun = w.iterations.as<int>();
+    st.abortFlag = w.abortFlag.as<int>();
+    const int drop = std::min(std::max(o.test_drop_blocks, 0), nProgress);
+    st.order = w.order.as<int4>() + drop;
+    st.totalItems = nProgress - drop;
+    const int spinLog2 = o.spin_limit_log2 > 0 ? std::min(o.spin_limit_log2, 40) : 22;
+    st.spinLimit = 1ull << spinLog2;
+    int perSM = eikx::sweep3ChunkBlocksPerSM<T>(uniform, false, shape);
+    if (o.blocks_per_sm > 0) perSM = std::min(perSM, o.blocks_per_sm);
+    const int blocks = std::max(1, std::min(c->numSMs * perSM, (nProgress + eikx::kWarpsPerBlock - 1) / eikx::kWarpsPerBlock));
+
+    // slots
+    std::vector<int> slotSrc(S, -1), slotStart(S, -1), slotBuf(S, -1), bufBusy(nBufs, 0), freeBufs;
+    std::vector<int> runOf(nSrc, 0);
+    for (int b = nBufs - 1; b >= 0; --b) freeBufs.push_back(b);
+    auto takeBuffer = [&](int *out) -> eikx_status {
+        for (int b = 0; b < nBufs; ++b)
+            if (bufBusy[b] && cudaEventQuery(w.bufEv[b]) == cudaSuccess) {
+                bufBusy[b] = 0;
+                freeBufs.push_back(b);
+            }
+        if (freeBufs.empty()) {
+            // every spare buffer is still being copied out: wait for one
+            for (int b = 0; b < nBufs; ++b)
+                if (bufBusy[b]) {
+                    EIKX_CUDA(cudaEventSynchronize(w.bufEv[b]));
+                    bufBusy[b] = 0;
+                    freeBufs.push_back(b);
+                    break;
+                }
+        }
+        *out = freeBufs.back();
+        freeBufs.pop_back();
+        return EIKX_OK;
+    };
+    int next = 0, active = 0, launches = 0, sweepsRun = 0, profiled = 0;
+    std::vector<int> list;
+    for (int f = 0; f < S && next < nSrc; ++f) {
+        slotSrc[f] = next++;
+        slotStart[f] = 0;
+        if (eikx_status r = takeBuffer(&slotBuf[f]); r != EIKX_OK) return r;
+        list.push_back(f);
+        ++active;
+    }
+    // the slot table and the new slots' sources, then their fields
+    auto upload = [&]() -> eikx_status {
+        int2 *tab = reinterpret_cast<int2 *>(stage);
+        for (int f = 0; f < S; ++f) tab[f] = make_int2(slotStart[f], slotBuf[f]);
+        for (int f : list) {
+            std::memcpy(stage + offSrc + f * srcB, &srcT[slotSrc[f]], srcB);
+            std::memcpy(stage + offCorn + f * cornB, &corners[slotSrc[f]], cornB);
+            if (near64) std::memcpy(stage + offS64 + f * s64B, &srcT64[slotSrc[f]], s64B);
+        }
+        std::memcpy(stage + offList, list.data(), list.size() * sizeof(int));
+        EIKX_CUDA(cudaMemcpyAsync(w.slots.p, stage, S * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+        for (int f : list) {
+            EIKX_CUDA(cudaMemcpyAsync(w.srcs.as<char>() + f * srcB, stage + offSrc + f * srcB, srcB,
+                                      cudaMemcpyHostToDevice, c->stream));
+            EIKX_CUDA(cudaMemcpyAsync(w.corners.as<char>() + f * cornB, stage + offCorn + f * cornB, cornB,
+                                      cudaMemcpyHostToDevice, c->stream));
+            if (near64)
+                EIKX_CUDA(cudaMemcpyAsync(w.srcs64.as<char>() + f * s64B, stage + offS64 + f * s64B, s64B,
+                                          cudaMemcpyHostToDevice, c->stream));
+        }
+        if (!list.empty()) {
+            EIKX_CUDA(cudaMemcpyAsync(w.list.p, stage + offList, list.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                      c->stream));
+            EIKX_CUDA(eikx::launchRefillSlots<T>(w.tt.as<T>(), fieldStride, Px, nx, ny, nz, dx, dy, dz, st,
+                                                 w.slots.as<int2>(), w.list.as<int>(), static_cast<int>(list.size()),
+                                                 w.corners.as<eikx::Corner3>(), o.init_fp64 ? 1 : 0, c->stream));
+            launches += 2;
+        }
+        return EIKX_OK;
+    };
+
+    const bool profile = o.profile_sweeps != 0;
+    if (eikx_status r = advanceEpoch(w.epochMirror, w.mbox, w.epoch, epochStride, c->stream); r != EIKX_OK) return r;
+    EIKX_CUDA(cudaEventRecord(c->ev0, c->stream));
+    EIKX_CUDA(eikx::launchResetState(st, S, 0, c->stream));
+    ++launches;
+    if (eikx_status r = upload(); r != EIKX_OK) return r;
+    const eikx::Spacing3<T> g = spacing3<T>(dx, dy, dz);
+    const cudaMemcpyKind kind = where == EIKX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const long long nodes = static_cast<long long>(nx) * ny * nz;
+    int buf = 0, aborted = 0;
+    long long refineUpdates = 0;
+    std::vector<int> iterOf(nSrc, 0);
+    while (active > 0) {
+        for (int e = 0; e < 8; ++e) {
+            if (sweepsRun + 1 >= epochStride) return fail(EIKX_ERR_STATE, "stream ran past its sweep bound");
+            if (profile) {
+                while (static_cast<int>(c->sweepEv.size()) < 2 * (profiled + 1)) {
+                    cudaEvent_t ev;
+                    EIKX_CUDA(cudaEventCreate(&ev));
+                    c->sweepEv.push_back(ev);
+                }
+                EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * profiled], c->stream));
+            }
+            eikx::Sweep3Args<T> a{};
+            a.tt = w.tt.as<T>(); a.fieldStride = fieldStride; a.pitch = Px;
+            a.spPos = spad[0].as<T>(); a.spNeg = spad[1].as<T>(); a.spPitch = spPitch;
+            a.spPlane = static_cast<long long>(spPitch) * (ny + 1);
+            a.nx = nx; a.ny = ny; a.nz = nz; a.tilesY = tilesY; a.tilesZ = tilesZ;
+            a.srcs = w.srcs.as<eikx::SourceT<T>>(); a.st = st; a.buf = buf; a.residualSlot = 0;
+            a.sweepIndex = sweepsRun; a.sweep = e; a.init = 0; a.radius = o.factored_radius;
+            a.h = static_cast<T>(dx); a.sp3 = g;
+            a.srcs64 = near64 ? w.srcs64.as<eikx::SourceFp64>() : nullptr;
+            a.slots = w.slots.as<int2>();
+            a.initSweeps = initSweeps;
+            EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, shape, blocks, c->stream));
+            EIKX_CUDA(eikx::launchCheckStream(st, w.slots.as<int2>(), S, sweepsRun, initSweeps, o.tolerance, c->stream));
+            if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * profiled + 1], c->stream));
+            ++profiled;
+            launches += 2;
+            buf ^= 1;
+            ++sweepsRun;
+        }
+        // iteration boundary: the slots' flags and sweep counts
+        EIKX_CUDA(cudaMemcpyAsync(flags, w.converged.p, S * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        EIKX_CUDA(cudaMemcpyAsync(flags + S, w.iterations.p, S * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        EIKX_CUDA(cudaMemcpyAsync(flags + 2 * S, w.abortFlag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        EIKX_CUDA(cudaEventRecord(w.boundary, c->stream));
+        EIKX_CUDA(cudaStreamSynchronize(c->stream));
+        if (flags[2 * S]) {
+            aborted = 1;
+            break;
+        }
+        list.clear();
+        bool changed = false;
+        for (int f = 0; f < S; ++f) {
+            if (slotSrc[f] < 0) continue;
+            const int refined = sweepsRun - slotStart[f] - 8 * initSweeps;
+            if (!flags[f] && refined < 8 * nSweeps) continue;
+            // finished: copy the field out, after this iteration's sweeps
+            const int src = slotSrc[f], b = slotBuf[f];
+            iterOf[src] = flags[S + f];
+            refineUpdates += nodes * flags[S + f];
+            EIKX_CUDA(cudaStreamWaitEvent(c->copyStream, w.boundary, 0));
+            EIKX_CUDA(eikx::copyRows(static_cast<char *>(tOut) + static_cast<size_t>(src) * nodes * sizeof(T),
+                                        static_cast<size_t>(nx) * sizeof(T),
+                                        w.tt.as<T>() + static_cast<size_t>(b) * fieldStride,
+                                        static_cast<size_t>(Px) * sizeof(T), static_cast<size_t>(nx) * sizeof(T),
+                                        static_cast<size_t>(ny) * nz, kind, c->copyStream));
+            EIKX_CUDA(cudaEventRecord(w.bufEv[b], c->copyStream));
+            bufBusy[b] = 1;
+            changed = true;
+            if (next < nSrc) {
+                slotSrc[f] = next++;
+                slotStart[f] = sweepsRun;
+                if (eikx_status r = takeBuffer(&slotBuf[f]); r != EIKX_OK) return r;
+                list.push_back(f);
+            } else {
+                slotSrc[f] = slotStart[f] = slotBuf[f] = -1;
+                --active;
+            }
+        }
+        if (changed && active > 0)
+            if (eikx_status r = upload(); r != EIKX_OK) return r;
+    }
+    // the copies, then the end of the solve
+    EIKX_CUDA(cudaEventRecord(c->copyDone, c->copyStream));
+    EIKX_CUDA(cudaStreamWaitEvent(c->stream, c->copyDone, 0));
+    EIKX_CUDA(cudaEventRecord(c->ev1, c->stream));
+    EIKX_CUDA(cudaStreamSynchronize(c->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    eikx_stats s{};
+    s.n_fields = nSrc;
+    s.iterations_max = 0;
+    s.iterations_min = 1 << 30;
+    for (int i = 0; i < nSrc; ++i) {
+        const int it = (iterOf[i] + 7) / 8;
+        s.iterations_max = std::max(s.iterations_max, it);
+        s.iterations_min = std::min(s.iterations_min, it);
+    }
+    s.refine_node_updates = refineUpdates;
+    s.residual_last = 0;
+    s.sweeps_launched = sweepsRun;
+    s.sweep_ms = -1;
+    if (profile) {
+        double tot = 0;
+        for (int i = 0; i < profiled; ++i) {
+            float m = 0;
+            cudaEventElapsedTime(&m, c->sweepEv[2 * i], c->sweepEv[2 * i + 1]);
+            tot += m;
+        }
+        s.sweep_ms = tot;
+    }
+    s.kernel_launches = launches;
+    s.device_ms = ms;
+    s.reset_nodes = 0;
+    c->stats = s;
+    c->last.valid = false;   // the fields of a stream do not stay on the device
+    if (aborted) return fail(EIKX_ERR_TIMEOUT, "a bounded inter-tile wait ran out; the fields are not valid");
+    return EIKX_OK;
+}
+
 // Shared solve driver for 2D and 3D.
 
 template <class T, int DIM>
@@ -462,7 +775,9 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     const bool uniform = DIM == 3 ? (std::abs(dx - dy) < eps && std::abs(dx - dz) < eps) : (std::abs(dx - dz) < eps);
     // options left at "auto" take the tuned configuration of this grid class
     if (DIM == 3 && o.sweep_kernel == 0 && o.block_shape == 0 && o.blocks_per_sm == 0 && !o.pair_fields) {
-        auto it = c->tuning.find(tuneKey(P, uniform, nx, ny, nz, nSrc));
+        // a stream launches its slots' fields, not all of its sources
+        const int perLaunch = o.max_in_flight > 0 && o.max_in_flight < nSrc ? o.max_in_flight : nSrc;
+        auto it = c->tuning.find(tuneKey(P, uniform, nx, ny, nz, perLaunch));
         if (it != c->tuning.end()) {
             o.sweep_kernel = it->second.sweep_kernel;
             o.pair_fields = it->second.pair_fields;
@@ -474,6 +789,12 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     if (DIM == 3 && P == EIKX_F32 && o.near_fp64) {
         o.sweep_kernel = eikx::kChunkStep;
         o.pair_fields = 0;
+    }
+    // a stream of the sources through max_in_flight slots (chunk-step)
+    if constexpr (DIM == 3) {
+        if (!warm && o.max_in_flight > 0 && o.max_in_flight < nSrc && (o.init_sweeps || o.n_sweeps > 0))
+            return solveStream3<T>(c, o, nSrc, srcT, srcT64, corners, uniform,
+                                   o.block_shape > 0 ? o.block_shape - 1 : eikx::kShape8x4, tOut, where, spad);
     }
     // FP32 uniform 3D batches run two fields per lane (the paired kernel)
     const bool paired = DIM == 3 && P == EIKX_F32 && uniform && nSrc >= 2 && o.pair_fields;
@@ -793,7 +1114,7 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     const cudaMemcpyKind kind = where == EIKX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     const long long nodesPerField = static_cast<long long>(nx) * ny * nz;
     auto copyFields = [&](int f0, int f1, cudaStream_t s) -> cudaError_t {
-        return cudaMemcpy2DAsync(static_cast<char *>(tOut) + static_cast<size_t>(f0) * nodesPerField * sizeof(T),
+        return eikx::copyRows(static_cast<char *>(tOut) + static_cast<size_t>(f0) * nodesPerField * sizeof(T),
                                  static_cast<size_t>(nx) * sizeof(T),
                                  static_cast<char *>(w.tt.p) + static_cast<size_t>(f0) * fieldStride * sizeof(T),
                                  static_cast<size_t>(Px) * sizeof(T), static_cast<size_t>(nx) * sizeof(T),
@@ -1312,7 +1633,7 @@ eikx_status solveBatch3(eikx_ctx *c, const eikx_model3d *models, const std::vect
     auto copyModel = [&](int i, cudaStream_t s) -> cudaError_t {
         const eikx_model3d &m = models[sel[i]];
         const cudaMemcpyKind kind = m.t_where == EIKX_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-        return cudaMemcpy2DAsync(m.t_out, static_cast<size_t>(m.nx) * sizeof(T), ttBase + L[i].ttOff,
+        return eikx::copyRows(m.t_out, static_cast<size_t>(m.nx) * sizeof(T), ttBase + L[i].ttOff,
                                  static_cast<size_t>(L[i].Px) * sizeof(T), static_cast<size_t>(m.nx) * sizeof(T),
                                  static_cast<size_t>(m.ny) * m.nz * m.n_src, kind, s);
     };
@@ -1455,6 +1776,7 @@ eikx_status fillOptions(const eikx_options *in, eikx_options *out) {
     if (out->test_tag_margin < 0) return fail(EIKX_ERR_INVALID, "test_tag_margin must be >= 0");
     if (out->near_fp64 < 0 || out->near_fp64 > 1) return fail(EIKX_ERR_INVALID, "near_fp64 must be 0 or 1");
     if (out->warm_gate < 0 || out->warm_gate > 1) return fail(EIKX_ERR_INVALID, "warm_gate must be 0 or 1");
+    if (out->max_in_flight < 0) return fail(EIKX_ERR_INVALID, "max_in_flight must be >= 0");
     return EIKX_OK;
 }
 
@@ -1510,6 +1832,8 @@ eikx_status eikx_destroy(eikx_ctx *c) {
     if (c->copyDone) cudaEventDestroy(c->copyDone);
     for (cudaEvent_t e : c->iterEv) cudaEventDestroy(e);
     for (cudaEvent_t e : c->sweepEv) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->sw.bufEv) cudaEventDestroy(e);
+    if (c->sw.boundary) cudaEventDestroy(c->sw.boundary);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return EIKX_OK;

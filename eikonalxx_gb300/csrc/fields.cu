@@ -370,6 +370,68 @@ __global__ void checkKernel(SolveState st, int nFields, int firstSlot, int nSlot
     }
 }
 
+// The same test in a stream of sources through slots (eikx_options.max_in_flight): after
+// sweep `sweepIndex` of the stream, slot f's field has run sweepIndex - slots[f].x + 1 sweeps
+// of its own, the first 8 its initialisation pass when initSweeps is set.
+__global__ void checkStreamKernel(SolveState st, const int2 *slots, int nSlots, int sweepIndex, int initSweeps,
+                                  double tol) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nSlots; f += gridDim.x * blockDim.x) {
+        const int start = slots[f].x;
+        if (start < 0 || st.converged[f]) continue;
+        const int r = sweepIndex - start - (initSweeps ? 8 : 0);   // refinement sweep just run
+        if (r < 0) continue;
+        const int lo = r > 7 ? r - 7 : 0;
+        double m = 0;
+        for (int k = lo; k <= r; ++k)
+            m = fmax(m, __longlong_as_double(static_cast<long long>(
+                            st.residual[static_cast<long long>(f) * st.residualStride + 8 + k])));
+        st.sweepsRun[f] = r + 1;
+        if (r >= 7 && m < tol) st.converged[f] = 1;
+    }
+}
+
+// A slot takes a new source (stream mode): its field buffer slots[f].y := HUGE (16-byte
+// stores), then the source-cell corners, its residual row, flag and sweep count cleared.
+template <class T>
+__global__ void refillFillKernel(uint4 *tt, long long fieldStride16, const int2 *slots, const int *list, int n) {
+    const long long total = fieldStride16 * n;
+    const T huge = static_cast<T>(1.e10);
+    uint4 v;
+    T *e = reinterpret_cast<T *>(&v);
+#pragma unroll
+    for (int k = 0; k < static_cast<int>(16 / sizeof(T)); ++k) e[k] = huge;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int f = list[i / fieldStride16];
+        tt[static_cast<long long>(slots[f].y) * fieldStride16 + i % fieldStride16] = v;
+    }
+}
+template <class T>
+__global__ void refillSlotKernel(T *tt, SolveState st, long long fieldStride, int pitch, int nx, int ny, int nz,
+                                 double dx, double dy, double dz, const Corner3 *corners, int fp64, const int2 *slots,
+                                 const int *list, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 8 * n) return;
+    const int f = list[i >> 3], k = i & 7;
+    if (k == 0) {
+        for (int r = 0; r < st.residualStride; ++r) st.residual[static_cast<long long>(f) * st.residualStride + r] = 0ull;
+        st.converged[f] = 0;
+        st.sweepsRun[f] = 0;
+    }
+    const Corner3 cn = corners[f];
+    const int ix = cn.isx + (k & 1), iy = cn.isy + ((k >> 1) & 1), iz = cn.isz + ((k >> 2) & 1);
+    if (ix >= nx || iy >= ny || iz >= nz) return;
+    T v;
+    if (fp64) {
+        v = static_cast<T>(analyticT3<double>(ix, iy, iz, dx, dy, dz, cn.xo, cn.yo, cn.zo, cn.s));
+    } else {
+        v = analyticT3<T>(ix, iy, iz, static_cast<T>(dx), static_cast<T>(dy), static_cast<T>(dz),
+                          static_cast<T>(cn.xo), static_cast<T>(cn.yo), static_cast<T>(cn.zo),
+                          static_cast<T>(cn.s));
+    }
+    tt[static_cast<long long>(slots[f].y) * fieldStride + (static_cast<long long>(iz) * ny + iy) * pitch + ix] = v;
+}
+
 // Analytic linear-gradient / homogeneous travel times in FP64
 // (src/analytic/linearGradient3d.cpp:12-116, linearGradient2d.cpp:12-124).
 __global__ void analytic3Kernel(double *t, int nx, int ny, int nz, double dx, double dy, double dz,
@@ -533,6 +595,29 @@ cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstS
     checkKernel<<<gridFor(nFields, 128), 128, 0, s>>>(st, nFields, firstSlot, nSlots, sweepsDone, tol);
     return cudaGetLastError();
 }
+cudaError_t launchCheckStream(const SolveState &st, const int2 *slots, int nSlots, int sweepIndex, int initSweeps,
+                              double tol, cudaStream_t s) {
+    checkStreamKernel<<<gridFor(nSlots, 128), 128, 0, s>>>(st, slots, nSlots, sweepIndex, initSweeps, tol);
+    return cudaGetLastError();
+}
+template <class T>
+cudaError_t launchRefillSlots(T *tt, long long fieldStride, int pitch, int nx, int ny, int nz, double dx, double dy,
+                              double dz, const SolveState &st, const int2 *slots, const int *list, int n,
+                              const Corner3 *corners, int fp64, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    // fieldStride * sizeof(T) is a multiple of 16 bytes (pitch * sizeof(T) is)
+    const long long f16 = fieldStride * static_cast<long long>(sizeof(T)) / 16;
+    refillFillKernel<T><<<gridFor(f16 * n), kThreads, 0, s>>>(reinterpret_cast<uint4 *>(tt), f16, slots, list, n);
+    refillSlotKernel<T><<<(8 * n + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+        tt, st, fieldStride, pitch, nx, ny, nz, dx, dy, dz, corners, fp64, slots, list, n);
+    return cudaGetLastError();
+}
+template cudaError_t launchRefillSlots<float>(float *, long long, int, int, int, int, double, double, double,
+                                              const SolveState &, const int2 *, const int *, int, const Corner3 *,
+                                              int, cudaStream_t);
+template cudaError_t launchRefillSlots<double>(double *, long long, int, int, int, int, double, double, double,
+                                               const SolveState &, const int2 *, const int *, int, const Corner3 *,
+                                               int, cudaStream_t);
 cudaError_t launchAnalytic3(double *t, int nx, int ny, int nz, double dx, double dy, double dz, double xs,
                             double ys, double zs, double vTop, double vBottom, cudaStream_t s) {
     const long long n = static_cast<long long>(nx) * ny * nz;

@@ -317,7 +317,7 @@ extern "C" eikx_status eikx_solve3d_noalloc(int nx, int ny, int nz, double dx, d
                                                       stream));
         }
     }
-    NOALLOC_CUDA(cudaMemcpy2DAsync(tOut, static_cast<size_t>(nx) * sizeof(float), tt, static_cast<size_t>(Px) * sizeof(float),
+    NOALLOC_CUDA(eikx::copyRows(tOut, static_cast<size_t>(nx) * sizeof(float), tt, static_cast<size_t>(Px) * sizeof(float),
                                    static_cast<size_t>(nx) * sizeof(float), static_cast<size_t>(ny) * nz,
                                    cudaMemcpyDeviceToDevice, stream));
     int aborted = 0;

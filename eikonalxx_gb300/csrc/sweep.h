@@ -66,6 +66,12 @@ template <class T> struct Sweep3Args {
     const Grid3Unit<T> *units;  // multi-model batch: per-unit geometry (chunk-step kernel only)
     const SourceFp64 *srcs64; // per field, FP32 chunk-step only: set = the FP64 factored branch
                               // (eikx_options.near_fp64), its own kernel instances
+    // A stream of sources through slots (chunk-step, one model; eikx_options.max_in_flight):
+    // set = field f is a slot whose current source started at sweep slots[f].x of the stream
+    // (-1 = idle) in field buffer slots[f].y; sweepIndex is this sweep's position in the
+    // stream and `sweep` its ordering (sweepIndex mod 8).
+    const int2 *slots;
+    int initSweeps;           // 1 = a slot's first 8 sweeps are its initialisation pass
 };
 
 template <class T> struct Sweep2Args {
@@ -198,6 +204,15 @@ cudaError_t launchCheckPositive(const double *s, long long n, int *flag, cudaStr
 cudaError_t launchCheckPositive(const float *s, long long n, int *flag, cudaStream_t st);
 // After refinement sweep `sweepsDone - 1`: a field whose residual slots
 // [firstSlot, firstSlot + nSlots) all fell below tol is frozen (later sweeps skip it).
+// Stream mode (eikx_options.max_in_flight): the convergence test after sweep `sweepIndex`
+// of the stream, per slot; and the refill of the listed slots with their new sources
+// (field buffer := HUGE, source-cell corners, residual row, flag and sweep count cleared).
+cudaError_t launchCheckStream(const SolveState &st, const int2 *slots, int nSlots, int sweepIndex, int initSweeps,
+                              double tol, cudaStream_t s);
+template <class T>
+cudaError_t launchRefillSlots(T *tt, long long fieldStride, int pitch, int nx, int ny, int nz, double dx, double dy,
+                              double dz, const SolveState &st, const int2 *slots, const int *list, int n,
+                              const Corner3 *corners, int fp64, cudaStream_t s);
 cudaError_t launchCheckConvergence(const SolveState &st, int nFields, int firstSlot, int nSlots,
                                    int sweepsDone, double tol, cudaStream_t s);
 // 2D gradient ray tracing (rays.cu): grid, source, step rules and output capacity.
@@ -236,5 +251,14 @@ cudaError_t launchAnalytic2(double *t, int nx, int nz, double dx, double dz, dou
 // fd3UniformFar, shortcut results equal to t0, stencils whose t0 is the operator's value.
 cudaError_t launchOperatorSelftest(int precision, long long n, unsigned long long seed, unsigned long long *counts,
                                    cudaStream_t s);
+
+// Rows of `width` bytes from a pitched source to a pitched destination: one contiguous copy
+// when neither has padding (a 2D copy of many short rows moves them row by row), else a 2D
+// copy.
+inline cudaError_t copyRows(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
+                            cudaMemcpyKind kind, cudaStream_t s) {
+    if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * height, kind, s);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, s);
+}
 
 }  // namespace eikx

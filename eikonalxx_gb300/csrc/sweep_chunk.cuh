@@ -189,11 +189,14 @@ __device__ __forceinline__ void clearNextQueue(const SolveState &st, int buf) {
     if (blockIdx.x == 0 && threadIdx.x == 0) *st.queue[buf ^ 1] = 0u;
 }
 
-// INIT: the source-limited initialisation pass (a.init = 1), compiled apart so that the
-// refinement sweeps carry none of its block skipping.  NEAR64: the factored branch with
-// its analytic factor in FP64 (eikx_options.near_fp64, FP32 sweeps), compiled into its own
-// kernels (sweep3ChunkNear64Kernel) so that the others carry none of it.
-template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT, bool NEAR64>
+// INITMODE 1: the source-limited initialisation pass (a.init = 1), compiled apart so that
+// the refinement sweeps (INITMODE 0) carry none of its block skipping.  INITMODE 2: a stream
+// of sources through slots (a.slots, eikx_options.max_in_flight): each slot's field is in
+// its initialisation pass or in refinement according to the sweep at which it started, so
+// the mode, the residual slot and the field buffer are read per work item.  NEAR64: the
+// factored branch with its analytic factor in FP64 (eikx_options.near_fp64, FP32 sweeps),
+// compiled into its own kernels (sweep3ChunkNear64Kernel) so that the others carry none of it.
+template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, int INITMODE, bool NEAR64>
 __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
     static_assert(LY * LZ == 32 && LZ + 1 + LY <= 32, "a warp holds 32 pencils and its halo helpers");
     constexpr int HY = LY + 1, HZ = LZ + 1;          // ring plane incl. halo row/column
@@ -234,6 +237,18 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         const int4 item = st.order[q];
         const int f = item.x, b = item.y, c = item.z;
         if (st.converged[f]) continue;
+        bool init = INITMODE == 1;
+        int residualSlot = a.residualSlot;
+        long long fieldOffset = static_cast<long long>(f) * a.fieldStride;
+        if constexpr (INITMODE == 2) {
+            // the slot's field: started at sweep si.x of the stream, in buffer si.y
+            const int2 si = a.slots[f];
+            const int phase = a.sweepIndex - si.x;
+            if (si.x < 0 || phase < 0) continue;   // an idle slot
+            init = a.initSweeps && phase < 8;
+            residualSlot = phase + (a.initSweeps ? 0 : 8);
+            fieldOffset = static_cast<long long>(si.y) * a.fieldStride;
+        }
         const SourceT<T> src = a.srcs[f];
 
         // grid of this work item: the launch's (one model) or the unit's (batch)
@@ -244,7 +259,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         const int spPitch = BATCH ? unit->spPitch : a.spPitch;
         const long long spPlane = BATCH ? unit->spPlane : a.spPlane;
         const T *sp = BATCH ? (REV ? unit->spNeg : unit->spPos) : (REV ? a.spNeg : a.spPos);
-        T *field = BATCH ? unit->tt : a.tt + static_cast<long long>(f) * a.fieldStride;
+        T *field = BATCH ? unit->tt : a.tt + fieldOffset;
         const long long faceWords = static_cast<long long>(LY + LZ) * Px * W;
         unsigned long long *fieldBox =
             BATCH ? unit->mbox : st.mbox + static_cast<long long>(f) * a.tilesZ * a.tilesY * faceWords;
@@ -256,23 +271,23 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         const int ya = laneValid ? reflect(yp, ny, fy) : 0;
         const int za = laneValid ? reflect(zp, nz, fz) : 0;
         int xlo, xhi, ylo, yhi, zlo, zhi;
-        axisBounds(nx, REV, INIT, src.isx, xlo, xhi);
-        axisBounds(ny, fy, INIT, src.isy, ylo, yhi);
-        axisBounds(nz, fz, INIT, src.isz, zlo, zhi);
+        axisBounds(nx, REV, init, src.isx, xlo, xhi);
+        axisBounds(ny, fy, init, src.isy, ylo, yhi);
+        axisBounds(nz, fz, init, src.isz, zlo, zhi);
         // Initialisation pass: the update range along x' starts at the source's column, so
         // the field's lanes all walk from the chunk before the one holding it (whose last
         // values are the first updated node's x'-1 neighbours; it updates nothing) instead
         // of from chunk 0.  kBase is the same for every block of a field, so the mailbox
         // chunks a block waits for are the ones its upstream blocks publish.
         int kBase = 0;
-        if constexpr (INIT) kBase = max(0, (REV ? Px - 1 - xhi : xlo) / V - 1);
+        if (init) kBase = max(0, (REV ? Px - 1 - xhi : xlo) / V - 1);
         const int nSteps = nChunks - kBase + LY + LZ - 2;
         // Initialisation pass: the update range starts at y' = yp0, z' = zp0 and runs to the
         // end of each axis.  Warp blocks wholly before it update nothing: they are left out,
         // and the blocks after them read those rows from the field, which the sweep does not
         // change, instead of from the mailbox.
         int bStart = 0, cStart = 0;
-        if constexpr (INIT) {
+        if (init) {
             bStart = (fy ? ny - 1 - yhi : ylo) / LY;
             cStart = (fz ? nz - 1 - zhi : zlo) / LZ;
             if (b < bStart || c < cStart) continue;
@@ -314,7 +329,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         const bool vValid = helper && vyp >= 0 && vzp >= 0 && vyp < ny && vzp < nz;
         // the virtual lane's block was left out: its row is read from the field (vbox then
         // holds the row's address)
-        const bool vField = INIT && vValid && ((vly < 0 && b - 1 < bStart) || (vlz < 0 && c - 1 < cStart));
+        const bool vField = init && vValid && ((vly < 0 && b - 1 < bStart) || (vlz < 0 && c - 1 < cStart));
         const unsigned long long *vbox = box;
         const T *vsrow = sp;
         if (vValid) {
@@ -347,7 +362,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         auto issue = [&](int sv) {
             const int kv = haloChunk(sv);
             if (helper && haloValid(kv)) {
-                if (INIT && vField) {
+                if (init && vField) {
                     T *vrow = const_cast<T *>(reinterpret_cast<const T *>(vbox));
                     tagWords(tag, walk(ldVec(tChunk(vrow, kv))), mslot.w);
                 } else {
@@ -463,20 +478,20 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         if (!ok) break;
         const double r = warpMax(static_cast<double>(res));
         if (lane == 0 && r > 0)
-            atomicMax(st.residual + static_cast<long long>(f) * st.residualStride + a.residualSlot,
+            atomicMax(st.residual + static_cast<long long>(f) * st.residualStride + residualSlot,
                       static_cast<unsigned long long>(__double_as_longlong(r)));
     }
 }
 
-template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT>
+template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, int INITMODE>
 __global__ void __launch_bounds__(kThreadsC) sweep3ChunkKernel(const Sweep3Args<T> a) {
-    sweep3ChunkBody<T, UNIFORM, REV, BATCH, LY, LZ, INIT, false>(a);
+    sweep3ChunkBody<T, UNIFORM, REV, BATCH, LY, LZ, INITMODE, false>(a);
 }
 // Held to 128 registers (the default kernels' 4 blocks per SM); the out-of-line FP64
 // branch spills what it needs beyond them.
-template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, bool INIT>
+template <class T, bool UNIFORM, bool REV, bool BATCH, int LY, int LZ, int INITMODE>
 __global__ void __launch_bounds__(kThreadsC) sweep3ChunkNear64Kernel(const Sweep3Args<T> a) {
-    sweep3ChunkBody<T, UNIFORM, REV, BATCH, LY, LZ, INIT, true>(a);
+    sweep3ChunkBody<T, UNIFORM, REV, BATCH, LY, LZ, INITMODE, true>(a);
 }
 
 template <int LY, int LZ> constexpr size_t smemBytes() {
@@ -486,15 +501,19 @@ template <int LY, int LZ> constexpr size_t smemBytes() {
 template <class T, bool U, bool R, bool B, int LY, int LZ>
 void launchOne(const Sweep3Args<T> &a, int blocks, cudaStream_t s) {
     const size_t smem = smemBytes<LY, LZ>();
+    // the stream mode's instances exist for one-model launches only
+    const int mode = !B && a.slots ? 2 : a.init ? 1 : 0;
     if constexpr (sizeof(T) == 4) {
         if (a.srcs64) {
-            if (a.init) sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, true><<<blocks, kThreadsC, smem, s>>>(a);
-            else sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, false><<<blocks, kThreadsC, smem, s>>>(a);
+            if (mode == 1) sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, 1><<<blocks, kThreadsC, smem, s>>>(a);
+            else if (mode == 0) sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, 0><<<blocks, kThreadsC, smem, s>>>(a);
+            else if constexpr (!B) sweep3ChunkNear64Kernel<T, U, R, B, LY, LZ, 2><<<blocks, kThreadsC, smem, s>>>(a);
             return;
         }
     }
-    if (a.init) sweep3ChunkKernel<T, U, R, B, LY, LZ, true><<<blocks, kThreadsC, smem, s>>>(a);
-    else sweep3ChunkKernel<T, U, R, B, LY, LZ, false><<<blocks, kThreadsC, smem, s>>>(a);
+    if (mode == 1) sweep3ChunkKernel<T, U, R, B, LY, LZ, 1><<<blocks, kThreadsC, smem, s>>>(a);
+    else if (mode == 0) sweep3ChunkKernel<T, U, R, B, LY, LZ, 0><<<blocks, kThreadsC, smem, s>>>(a);
+    else if constexpr (!B) sweep3ChunkKernel<T, U, R, B, LY, LZ, 2><<<blocks, kThreadsC, smem, s>>>(a);
 }
 
 template <class T, bool B, int LY, int LZ>
@@ -516,11 +535,11 @@ template <class T, bool B, int LY, int LZ> int blocksPerSM(bool uniform) {
     // and waits only on work dequeued before it, so no wait depends on a block not running.
     const void *k[2];
     if (uniform) {
-        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, false, B, LY, LZ, false>);
-        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, true, B, LY, LZ, false>);
+        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, false, B, LY, LZ, 0>);
+        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, true, true, B, LY, LZ, 0>);
     } else {
-        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, false, B, LY, LZ, false>);
-        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, true, B, LY, LZ, false>);
+        k[0] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, false, B, LY, LZ, 0>);
+        k[1] = reinterpret_cast<const void *>(sweep3ChunkKernel<T, false, true, B, LY, LZ, 0>);
     }
     int best = 1 << 30;
     for (const void *f : k) {

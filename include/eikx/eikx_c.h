@@ -101,7 +101,17 @@ typedef struct {
                               whose initial time lies more than gate_tol below the smallest
                               upwind update of their initial neighbourhood (one-sided);
                               1 = also reset nodes more than gate_tol above it (two-sided) */
-    int reserved[2];
+    int max_in_flight;     /* eikx_solve3d: 0 (default) = all sources in one batch; 0 < n <
+                              n_src = a stream: n slots, each solving one source at a time;
+                              a slot whose field has converged (or reached n_sweeps) is
+                              copied out and takes the next source at the next iteration
+                              boundary, its initialisation sweeps running inside the same
+                              launches as the other slots' refinement sweeps.  The fields
+                              are bit-identical to solving each source alone.  Chunk-step
+                              kernel (sweep_kernel and pair_fields give way); no CUDA graph
+                              (the schedule follows convergence); the fields do not stay on
+                              the device for eikx_gradient3d / eikx_station_times3d. */
+    int reserved;
 } eikx_options;
 
 /* Fills *opt with the defaults above. */
