@@ -21,6 +21,22 @@ template <> __device__ __forceinline__ double dmin(double a, double b) { return 
 template <class T> __device__ __forceinline__ T dmax(T a, T b);
 template <> __device__ __forceinline__ float dmax(float a, float b) { return fmaxf(a, b); }
 template <> __device__ __forceinline__ double dmax(double a, double b) { return fmax(a, b); }
+// Minimum and maximum for operands known not to be negative (slowness values, which the model
+// checks keep positive and finite; a maximum that includes a positive floor): for such doubles
+// the IEEE order is the order of their bit patterns as signed 64-bit integers (a negative value
+// only ever loses a maximum against a positive floor). So the selection runs on the integer
+// pipe instead of GB300's narrow FP64 pipe, with the result fmin / fmax would give. FP32 keeps
+// fminf / fmaxf.
+template <class T> __device__ __forceinline__ T pmin(T a, T b) { return dmin(a, b); }
+template <> __device__ __forceinline__ double pmin(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return __longlong_as_double(x < y ? x : y);
+}
+template <class T> __device__ __forceinline__ T pmax(T a, T b) { return dmax(a, b); }
+template <> __device__ __forceinline__ double pmax(double a, double b) {
+    const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+    return __longlong_as_double(x > y ? x : y);
+}
 __device__ __forceinline__ float dsqrt(float a) { return sqrtf(a); }
 __device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
 
@@ -171,12 +187,12 @@ __device__ __forceinline__ const NearFactor &nearFactorAt(const SourceFp64 &f, c
     const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7; \
     const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7; \
     T tUpd;                                                                            \
-    T minS0S3 = dmin(s0, s3);                                                          \
-    T minS0S1 = dmin(s0, s1);                                                          \
-    T minS0S4 = dmin(s0, s4);                                                          \
-    T t1d1 = t1 + h * dmin(minS0S3, dmin(s4, s7));                                     \
-    T t1d2 = t3 + h * dmin(minS0S4, dmin(s1, s5));                                     \
-    T t1d3 = t4 + h * dmin(minS0S1, dmin(s2, s3));                                     \
+    T minS0S3 = pmin(s0, s3);                                                          \
+    T minS0S1 = pmin(s0, s1);                                                          \
+    T minS0S4 = pmin(s0, s4);                                                          \
+    T t1d1 = t1 + h * pmin(minS0S3, pmin(s4, s7));                                     \
+    T t1d2 = t3 + h * pmin(minS0S4, pmin(s1, s5));                                     \
+    T t1d3 = t4 + h * pmin(minS0S1, pmin(s2, s3));                                     \
     T t1d = dmin(dmin(t1d1, t1d2), t1d3);                                              \
     T hs03 = h * minS0S3;                                                              \
     T hs01 = h * minS0S1;                                                              \
@@ -260,8 +276,8 @@ __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t
     EIKX_FD3_UNIFORM_PREFIX
     (void)tUpd;
     const T c20 = static_cast<T>(1.0 - 1.0 / 1048576.0);
-    const T M = dmax(dmax(dmax(t1, t2), dmax(t3, t4)),
-                     dmax(dmax(t5, t6), dmax(t7, static_cast<T>(7.8886090522101181e-31))));   // 2^-100
+    const T M = pmax(pmax(pmax(t1, t2), pmax(t3, t4)),
+                     pmax(pmax(t5, t6), pmax(t7, static_cast<T>(7.8886090522101181e-31))));   // 2^-100
     const T E = M * static_cast<T>(3.0 / 1048576.0);
     const T L2 = t2 + fmaT(hs04, c20, -E), L5 = t5 + fmaT(hs03, c20, -E), L7 = t7 + fmaT(hs01, c20, -E);
     const T lo3 = fmaT(M, static_cast<T>(-1.0 / 262144.0), t6);
@@ -421,12 +437,12 @@ template <class T> struct Spacing3 {
     const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7; \
     const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7; \
     T tUpd;                                                                            \
-    T minS0S3 = dmin(s0, s3);                                                          \
-    T minS0S1 = dmin(s0, s1);                                                          \
-    T minS0S4 = dmin(s0, s4);                                                          \
-    T t1d1 = t1 + dx * dmin(minS0S3, dmin(s4, s7));                                    \
-    T t1d2 = t3 + dy * dmin(minS0S4, dmin(s1, s5));                                    \
-    T t1d3 = t4 + dz * dmin(minS0S1, dmin(s2, s3));                                    \
+    T minS0S3 = pmin(s0, s3);                                                          \
+    T minS0S1 = pmin(s0, s1);                                                          \
+    T minS0S4 = pmin(s0, s4);                                                          \
+    T t1d1 = t1 + dx * pmin(minS0S3, pmin(s4, s7));                                    \
+    T t1d2 = t3 + dy * pmin(minS0S4, pmin(s1, s5));                                    \
+    T t1d3 = t4 + dz * pmin(minS0S1, pmin(s2, s3));                                    \
     T t1d = dmin(dmin(t1d1, t1d2), t1d3);
 
 template <class T>
