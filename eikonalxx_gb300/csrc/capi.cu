@@ -196,6 +196,8 @@ struct eikx_ctx {
     mutable bool hostSlow3Valid = false;
     DevBuf spad3[2][2];            // [precision][0: shifted for +x sweeps, 1: unshifted]
     bool spadValid3[2] = {false, false};
+    DevBuf shad3[2][2];            // the same multiplied by h (uniform grids, FP64 chunk-step kernel)
+    bool shadValid3[2] = {false, false};
     // 2D model
     int nx2 = 0, nz2 = 0;
     double dx2 = 0, dz2 = 0, x02 = 0, z02 = 0;
@@ -313,6 +315,7 @@ eikx_status finishModel(eikx_ctx *c, int dim) {
         c->haveSlow3 = false;
         c->hostSlow3Valid = false;
         c->spadValid3[0] = c->spadValid3[1] = false;
+        c->shadValid3[0] = c->shadValid3[1] = false;
     } else {
         c->haveSlow2 = false;
         c->hostSlow2Valid = false;
@@ -394,6 +397,7 @@ eikx_status solveStream3(eikx_ctx *c, const eikx_options &o, int nSrc, const std
                          const std::vector<eikx::SourceFp64> &srcT64In, const std::vector<eikx::Corner3> &corners,
                          bool uniform, int shape, void *tOut, int where, DevBuf *spad) {
     StreamWorkspace &w = c->sw;
+    DevBuf *shad = c->shad3[sizeof(T) == 4 ? EIKX_F32 : EIKX_F64];   // uniform FP64 grids: the scaled copies
     const int nx = c->nx, ny = c->ny, nz = c->nz;
     const double dx = c->dx, dy = c->dy, dz = c->dz;
     const int Px = roundUp(nx, 4), spPitch = Px + 8;
@@ -592,6 +596,10 @@ eikx_status solveStream3(eikx_ctx *c, const eikx_options &o, int nSrc, const std
             a.srcs64 = near64 ? w.srcs64.as<eikx::SourceFp64>() : nullptr;
             a.slots = w.slots.as<int2>();
             a.initSweeps = initSweeps;
+            if (uniform && sizeof(T) == 8) {
+                a.hsPos = shad[0].as<T>(); a.hsNeg = shad[1].as<T>();
+                a.cells = c->slow3.p; a.cells64 = 1;
+            }
             EIKX_CUDA(eikx::launchSweep3Chunk<T>(a, uniform, shape, blocks, c->stream));
             EIKX_CUDA(eikx::launchCheckStream(st, w.slots.as<int2>(), S, sweepsRun, initSweeps, o.tolerance, c->stream));
             if (profile) EIKX_CUDA(cudaEventRecord(c->sweepEv[2 * profiled + 1], c->stream));
@@ -773,6 +781,18 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
     // geometry in the sweep type (include/private/solver3d.hpp:31-44, solver2d.hpp:29-46)
     const double eps = std::numeric_limits<T>::epsilon() * 100;
     const bool uniform = DIM == 3 ? (std::abs(dx - dy) < eps && std::abs(dx - dz) < eps) : (std::abs(dx - dz) < eps);
+    // uniform 3D grids in FP64: the padded copies multiplied by h, which the chunk-step kernel reads
+    DevBuf *shad = c->shad3[P];
+    if (DIM == 3 && sizeof(T) == 8 && uniform && (!c->shadValid3[P] || shad[0].bytes < spElems * sizeof(T))) {
+        if (shad[0].bytes < spElems * sizeof(T)) dropGraph(c);
+        for (int k = 0; k < 2; ++k) {
+            EIKX_CUDA(shad[k].ensure(spElems * sizeof(T)));
+            const int shift = k == 0 ? static_cast<int>(16 / sizeof(T)) - 1 : 0;
+            EIKX_CUDA((eikx::launchPadSlowness3<T, double>(shad[k].as<T>(), spPitch, shift, c->slow3.as<double>(),
+                                                           nx, ny, nz, c->stream, static_cast<T>(dx))));
+        }
+        c->shadValid3[P] = true;
+    }
     // options left at "auto" take the tuned configuration of this grid class
     if (DIM == 3 && o.sweep_kernel == 0 && o.block_shape == 0 && o.blocks_per_sm == 0 && !o.pair_fields) {
         // a stream launches its slots' fields, not all of its sources
@@ -1010,6 +1030,10 @@ eikx_status solveImpl(eikx_ctx *c, const double *srcXYZ, int nSrc, eikx_options 
                 a.sweepIndex = sweepsLaunched;
                 a.sweep = e; a.init = init; a.radius = o.factored_radius; a.h = static_cast<T>(dx);
                 a.srcs64 = srcs64;
+                if (uniform && sizeof(T) == 8) {
+                    a.hsPos = shad[0].as<T>(); a.hsNeg = shad[1].as<T>();
+                    a.cells = c->slow3.p; a.cells64 = 1;
+                }
                 const T tdx = static_cast<T>(dx), tdy = static_cast<T>(dy), tdz = static_cast<T>(dz);
                 eikx::Spacing3<T> g;
                 g.dx = tdx; g.dy = tdy; g.dz = tdz;
@@ -1865,6 +1889,7 @@ eikx_status eikx_set_grid3d(eikx_ctx *c, int nx, int ny, int nz, double dx, doub
     c->haveGrid3 = true;
     c->haveSlow3 = false;
     c->spadValid3[0] = c->spadValid3[1] = false;
+    c->shadValid3[0] = c->shadValid3[1] = false;
     dropGraph(c);
     return EIKX_OK;
 }

@@ -231,7 +231,7 @@ __global__ void init2Kernel(T *tt, int nFields, long long fieldStride, int pitch
 // copy is stored `shift` columns to the right, which aligns the cells a forward sweep
 // streams with the 16-byte chunks of its travel-time rows.
 template <class T, class U>
-__global__ void pad3Kernel(T *sp, int spPitch, int shift, const U *s, int nx, int ny, int nz) {
+__global__ void pad3Kernel(T *sp, int spPitch, int shift, const U *s, int nx, int ny, int nz, T h) {
     const int ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
     const long long n = static_cast<long long>(spPitch) * (ny + 1) * (nz + 1);
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
@@ -242,9 +242,11 @@ __global__ void pad3Kernel(T *sp, int spPitch, int shift, const U *s, int nx, in
         const int pz = static_cast<int>(r / (ny + 1));
         const int cx = clampi(px - 1 - shift, 0, ncx - 1), cy = clampi(py - 1, 0, ncy - 1),
                   cz = clampi(pz - 1, 0, ncz - 1);
-        sp[i] = static_cast<T>(s[(static_cast<long long>(cz) * ncy + cy) * ncx + cx]);
+        const T v = static_cast<T>(s[(static_cast<long long>(cz) * ncy + cy) * ncx + cx]);
+        sp[i] = h > 0 ? v * h : v;
     }
 }
+
 
 template <class T, class U>
 __global__ void pad2Kernel(T *sp, int spPitch, int shift, const U *s, int nx, int nz) {
@@ -507,9 +509,10 @@ cudaError_t launchInit2(T *tt, int nFields, long long fieldStride, int pitch, in
     return cudaGetLastError();
 }
 template <class T, class U>
-cudaError_t launchPadSlowness3(T *sp, int spPitch, int shift, const U *s, int nx, int ny, int nz, cudaStream_t st) {
+cudaError_t launchPadSlowness3(T *sp, int spPitch, int shift, const U *s, int nx, int ny, int nz, cudaStream_t st,
+                               T h) {
     const long long n = static_cast<long long>(spPitch) * (ny + 1) * (nz + 1);
-    pad3Kernel<T, U><<<gridFor(n), kThreads, 0, st>>>(sp, spPitch, shift, s, nx, ny, nz);
+    pad3Kernel<T, U><<<gridFor(n), kThreads, 0, st>>>(sp, spPitch, shift, s, nx, ny, nz, h);
     return cudaGetLastError();
 }
 template <class T, class U>
@@ -639,10 +642,12 @@ template cudaError_t launchInit2<float>(float *, int, long long, int, int, int, 
                                         int, cudaStream_t);
 template cudaError_t launchInit2<double>(double *, int, long long, int, int, int, double, double,
                                          const Corner3 *, int, cudaStream_t);
-template cudaError_t launchPadSlowness3<float, double>(float *, int, int, const double *, int, int, int, cudaStream_t);
+template cudaError_t launchPadSlowness3<float, double>(float *, int, int, const double *, int, int, int, cudaStream_t,
+                                                       float);
 template cudaError_t launchPadSlowness3<double, double>(double *, int, int, const double *, int, int, int,
-                                                        cudaStream_t);
-template cudaError_t launchPadSlowness3<float, float>(float *, int, int, const float *, int, int, int, cudaStream_t);
+                                                        cudaStream_t, double);
+template cudaError_t launchPadSlowness3<float, float>(float *, int, int, const float *, int, int, int, cudaStream_t,
+                                                      float);
 template cudaError_t launchPadSlowness2<float, double>(float *, int, int, const double *, int, int, cudaStream_t);
 template cudaError_t launchPadSlowness2<double, double>(double *, int, int, const double *, int, int, cudaStream_t);
 template cudaError_t launchNodalToCell3<float>(double *, const float *, int, int, int, int, cudaStream_t);

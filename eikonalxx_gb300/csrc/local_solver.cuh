@@ -37,6 +37,20 @@ template <> __device__ __forceinline__ double pmax(double a, double b) {
     const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
     return __longlong_as_double(x > y ? x : y);
 }
+// t0 <= min(a, b, c, d, e), for values that are not NaN.  FP64 compares order keys on the
+// integer pipe: the bit pattern for x >= +0, minus its magnitude bits for x <= -0, which is
+// monotone in x and equal for -0 and +0.
+template <class T> __device__ __forceinline__ bool atMostAll(T t0, T a, T b, T c, T d, T e) {
+    return t0 <= dmin(dmin(a, dmin(b, c)), dmin(d, e));
+}
+__device__ __forceinline__ long long orderKey(double x) {
+    const long long v = __double_as_longlong(x);
+    return v >= 0 ? v : -(v & 0x7fffffffffffffffLL);
+}
+template <> __device__ __forceinline__ bool atMostAll(double t0, double a, double b, double c, double d, double e) {
+    const long long k = orderKey(t0);
+    return (k <= orderKey(a)) & (k <= orderKey(b)) & (k <= orderKey(c)) & (k <= orderKey(d)) & (k <= orderKey(e));
+}
 __device__ __forceinline__ float dsqrt(float a) { return sqrtf(a); }
 __device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
 
@@ -271,17 +285,32 @@ __device__ __forceinline__ T fd3UniformFar(T h, const Stencil3<T> &n) {
 // and 70 % of the 8-point operators per warp that reaches them.
 __device__ __forceinline__ float fmaT(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fmaT(double a, double b, double c) { return __fma_rn(a, b, c); }
-template <class T>
+// HS: the stencil's slowness values are the cells' slowness already multiplied by h (the FP64
+// sweeps' scaled copies).  With h > 0, round-to-nearest multiplication is monotone, so h times
+// a minimum is the minimum of the products, bit for bit: every term below is the one the
+// unscaled form computes.
+template <class T, bool HS = false>
 __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t0) {
-    EIKX_FD3_UNIFORM_PREFIX
-    (void)tUpd;
+    const T huge = static_cast<T>(1.e10);
+    const T s0 = n.s0, s1 = n.s1, s2 = n.s2, s3 = n.s3, s4 = n.s4, s5 = n.s5, s7 = n.s7;
+    const T t1 = n.t1, t2 = n.t2, t3 = n.t3, t4 = n.t4, t5 = n.t5, t6 = n.t6, t7 = n.t7;
+    auto byH = [h](T x) -> T {
+        if constexpr (HS) return x;
+        else return h * x;
+    };
+    const T minS0S3 = pmin(s0, s3), minS0S1 = pmin(s0, s1), minS0S4 = pmin(s0, s4);
+    const T t1d1 = t1 + byH(pmin(minS0S3, pmin(s4, s7)));
+    const T t1d2 = t3 + byH(pmin(minS0S4, pmin(s1, s5)));
+    const T t1d3 = t4 + byH(pmin(minS0S1, pmin(s2, s3)));
+    const T t1d = dmin(dmin(t1d1, t1d2), t1d3);
+    const T hs03 = byH(minS0S3), hs01 = byH(minS0S1), hs04 = byH(minS0S4);
     const T c20 = static_cast<T>(1.0 - 1.0 / 1048576.0);
     const T M = pmax(pmax(pmax(t1, t2), pmax(t3, t4)),
                      pmax(pmax(t5, t6), pmax(t7, static_cast<T>(7.8886090522101181e-31))));   // 2^-100
     const T E = M * static_cast<T>(3.0 / 1048576.0);
     const T L2 = t2 + fmaT(hs04, c20, -E), L5 = t5 + fmaT(hs03, c20, -E), L7 = t7 + fmaT(hs01, c20, -E);
     const T lo3 = fmaT(M, static_cast<T>(-1.0 / 262144.0), t6);
-    if (t0 <= dmin(dmin(t1d, dmin(L2, L5)), dmin(L7, lo3))) return t0;
+    if (atMostAll(t0, t1d, L2, L5, L7, lo3)) return t0;
     const T m = dmax(dmax(t1, t4), t3);
     T t2d = huge;
     if (L5 < t0 || !(L5 > m)) {
@@ -308,7 +337,7 @@ __device__ __forceinline__ T fd3UniformFarBounded(T h, const Stencil3<T> &n, T t
     const T Tx = t1 + half * (-t4 + t5 - t3 + t2) - t7 + t6;
     const T Ty = t3 + half * (-t4 + t7 - t1 + t2) - t5 + t6;
     const T Tz = t4 + half * (-t1 + t5 - t3 + t7) - t2 + t6;
-    T det = 27 * (h * s0) * (h * s0) - (Tx - Ty) * (Tx - Ty) - (Tx - Tz) * (Tx - Tz) - (Ty - Tz) * (Ty - Tz);
+    T det = 27 * byH(s0) * byH(s0) - (Tx - Ty) * (Tx - Ty) - (Tx - Tz) * (Tx - Tz) - (Ty - Tz) * (Ty - Tz);
     if (!(det >= 0)) return t12;
     return dmin(t1d, dmin(t2d, third * (((Tx + Ty) + Tz) + dsqrt(det))));
 }

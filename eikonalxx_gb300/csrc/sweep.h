@@ -72,6 +72,13 @@ template <class T> struct Sweep3Args {
     // stream and `sweep` its ordering (sweepIndex mod 8).
     const int2 *slots;
     int initSweeps;           // 1 = a slot's first 8 sweeps are its initialisation pass
+    // FP64 chunk-step kernel on a uniform grid, one model (required there): the padded
+    // slowness copies multiplied by h (launchPadSlowness3 with h), laid out as spPos / spNeg,
+    // and the model's natural-order cell slowness for the factored branch (FP64 cells, or FP32
+    // cells with cells64 = 0)
+    const T *hsPos, *hsNeg;
+    const void *cells;
+    int cells64;
 };
 
 template <class T> struct Sweep2Args {
@@ -155,10 +162,11 @@ cudaError_t launchInit3(T *tt, int nFields, long long fieldStride, int pitch, in
 template <class T>
 cudaError_t launchInit2(T *tt, int nFields, long long fieldStride, int pitch, int nx, int nz,
                         double dx, double dz, const Corner3 *corners, int fp64, cudaStream_t s);
-// Edge-replicated slowness: element (pz, py, i) = S[clamp(pz-1), clamp(py-1), clamp(i-1-shift)].
+// Edge-replicated slowness: element (pz, py, i) = S[clamp(pz-1), clamp(py-1), clamp(i-1-shift)],
+// in T; with h > 0 each element is then multiplied by h (in T).
 template <class T, class U>
 cudaError_t launchPadSlowness3(T *sp, int spPitch, int shift, const U *s, int nx, int ny, int nz,
-                               cudaStream_t st);
+                               cudaStream_t st, T h = 0);
 template <class T, class U>
 cudaError_t launchPadSlowness2(T *sp, int spPitch, int shift, const U *s, int nx, int nz, cudaStream_t st);
 template <class U>

@@ -159,11 +159,38 @@ __device__ __forceinline__ void putChunk(unsigned long long *p, unsigned tag, co
     stRelaxed2(p + 2, w[2], w[3]);
 }
 
+// The raw slowness of a node's stencil cells (the reference's cell indices, clamped to the
+// grid: Solver3DSweep::updateFSM in include/private/solver3d.hpp), from the model's
+// natural-order cells, for launches whose stencils carry the scaled slowness.
+template <class T>
+__device__ __forceinline__ void rawStencilCells(Stencil3<T> &n, const void *cells, int cells64, int nx, int ny, int nz,
+                                                const SweepSigns &sg, int ix, int iy, int iz) {
+    const int ncx = nx - 1, ncy = ny - 1, ncz = nz - 1;
+    auto cl = [](int v, int hi) { return v < 0 ? 0 : (v > hi ? hi : v); };
+    const bool fx = sg.ixShift > 0, fy = sg.iyShift > 0, fz = sg.izShift > 0;
+    const int cxu = cl(fx ? ix : ix - 1, ncx - 1), cxo = cl(fx ? cxu - 1 : cxu + 1, ncx - 1);
+    const int cyu = cl(fy ? iy : iy - 1, ncy - 1), cyo = cl(fy ? cyu - 1 : cyu + 1, ncy - 1);
+    const int czu = cl(fz ? iz : iz - 1, ncz - 1), czo = cl(fz ? czu - 1 : czu + 1, ncz - 1);
+    auto S = [&](int cx, int cy, int cz) -> T {
+        const long long i = (static_cast<long long>(cz) * ncy + cy) * ncx + cx;
+        return cells64 ? static_cast<T>(static_cast<const double *>(cells)[i])
+                       : static_cast<T>(static_cast<const float *>(cells)[i]);
+    };
+    n.s0 = S(cxu, cyu, czu); n.s1 = S(cxo, cyu, czu); n.s2 = S(cxo, cyo, czu); n.s3 = S(cxu, cyo, czu);
+    n.s4 = S(cxu, cyu, czo); n.s5 = S(cxo, cyu, czo); n.s7 = S(cxu, cyo, czo);
+}
+
 // Factored (near-source) updates, out of line: taken by a few hundred nodes per field,
 // so the V inlined copies of the update hold only the Cartesian operators.
 template <class T>
 __device__ __noinline__ T nearUniform(T h, const SourceT<T> src, const SweepSigns sg, int ix, int iy, int iz,
                                       const Stencil3<T> n) {
+    return fd3UniformNear(h, src, sg, ix, iy, iz, n);
+}
+template <class T>
+__device__ __noinline__ T nearUniformRaw(T h, const SourceT<T> src, const SweepSigns sg, int ix, int iy, int iz,
+                                         Stencil3<T> n, const void *cells, int cells64, int nx, int ny, int nz) {
+    rawStencilCells(n, cells, cells64, nx, ny, nz, sg, ix, iy, iz);
     return fd3UniformNear(h, src, sg, ix, iy, iz, n);
 }
 template <class T>
@@ -175,6 +202,14 @@ __device__ __noinline__ T nearNonUniform(const Spacing3<T> g, const SourceT<T> s
 template <class T>
 __device__ __noinline__ T nearUniform64(T h, const SourceT<T> src, const SourceFp64 *f, const SweepSigns sg, int ix,
                                         int iy, int iz, const Stencil3<T> n) {
+    const SourceFp64 d = *f;
+    return fd3UniformNear<T, true>(h, src, sg, ix, iy, iz, n, &d);
+}
+template <class T>
+__device__ __noinline__ T nearUniform64Raw(T h, const SourceT<T> src, const SourceFp64 *f, const SweepSigns sg, int ix,
+                                           int iy, int iz, Stencil3<T> n, const void *cells, int cells64, int nx,
+                                           int ny, int nz) {
+    rawStencilCells(n, cells, cells64, nx, ny, nz, sg, ix, iy, iz);
     const SourceFp64 d = *f;
     return fd3UniformNear<T, true>(h, src, sg, ix, iy, iz, n, &d);
 }
@@ -221,6 +256,13 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
     sg.ixShift = REV ? 1 : -1; sg.iyShift = fy ? 1 : -1; sg.izShift = fz ? 1 : -1;
     sg.signX = REV ? -1 : 1; sg.signY = fy ? -1 : 1; sg.signZ = fz ? -1 : 1;
     const T huge = static_cast<T>(1.e10);
+    // FP64 sweeps of one model on a uniform grid read the slowness copies multiplied by h
+    // (a.hsPos, a.hsNeg): with h > 0 round-to-nearest multiplication is monotone, so
+    // h * min(s, ...) equals min(h * s, ...) bit for bit, and the Cartesian operators take their
+    // slowness terms without GB300's narrow FP64 multiplies.  Their factored branch reads the
+    // raw cells.  (In FP32 the same change measured no faster.)
+    constexpr bool SCALED = UNIFORM && !BATCH && sizeof(T) == 8;
+    const T sHuge = SCALED ? a.h * huge : huge;   // the slowness of a cell beyond the walk
 
     // helper lanes stand in for the virtual upwind lanes of the halo row/column
     const bool helper = lane < HZ + LY;
@@ -258,7 +300,8 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         const int tilesY = BATCH ? unit->tilesY : a.tilesY;
         const int spPitch = BATCH ? unit->spPitch : a.spPitch;
         const long long spPlane = BATCH ? unit->spPlane : a.spPlane;
-        const T *sp = BATCH ? (REV ? unit->spNeg : unit->spPos) : (REV ? a.spNeg : a.spPos);
+        const T *sp = BATCH ? (REV ? unit->spNeg : unit->spPos)
+                            : SCALED ? (REV ? a.hsNeg : a.hsPos) : (REV ? a.spNeg : a.spPos);
         T *field = BATCH ? unit->tt : a.tt + fieldOffset;
         const long long faceWords = static_cast<long long>(LY + LZ) * Px * W;
         unsigned long long *fieldBox =
@@ -358,7 +401,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
             sring[slot] = sv_;
         };
         MailChunk<T> mslot;
-        Vec<T> sslot = splat(huge);
+        Vec<T> sslot = splat(sHuge);
         auto issue = [&](int sv) {
             const int kv = haloChunk(sv);
             if (helper && haloValid(kv)) {
@@ -375,7 +418,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
             bool good = true;
             if (helper) {
                 const int kv = haloChunk(sv);
-                Vec<T> tv = splat(huge), svv = splat(huge);
+                Vec<T> tv = splat(huge), svv = splat(sHuge);
                 if (haloValid(kv)) {
                     good = mslot.take(vbox + static_cast<long long>(kv) * V * W, tag, st.abortFlag, st.spinLimit);
                     tv = mslot.value();
@@ -395,7 +438,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
         if (ok) issue(0);
         // x'-1 values of the chunks read the step before (walk position k*V - 1)
         T cT1 = huge, cT3 = huge, cT4 = huge, cT7 = huge;
-        T cS1 = huge, cS2 = huge, cS5 = huge, cS7 = huge;
+        T cS1 = sHuge, cS2 = sHuge, cS5 = sHuge, cS7 = sHuge;
         T res = 0;
         for (int s = 0; s < nSteps && ok; ++s) {
             ok = consume(s);
@@ -405,7 +448,7 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
             const bool active = laneValid && k >= kBase && k < nChunks;
             prefetch(s + kAhead);
             cpAsyncWait<kAhead>();   // this step's group has landed
-            Vec<T> tOwn = splat(huge), sOwn = splat(huge);
+            Vec<T> tOwn = splat(huge), sOwn = splat(sHuge);
             if (active) {
                 const Vec<T> *slot = pre + (s & (kPre - 1)) * 64;
                 tOwn = walk(slot[0]);
@@ -448,11 +491,17 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
                     const T t0 = out.v[e];
                     T tu;
                     if (NEAR64 && near) {
-                        if constexpr (UNIFORM) tu = nearUniform64<T>(h, src, a.srcs64 + f, sg, xa, ya, za, n);
+                        if constexpr (SCALED)
+                            tu = nearUniform64Raw<T>(h, src, a.srcs64 + f, sg, xa, ya, za, n, a.cells, a.cells64, nx,
+                                                     ny, nz);
+                        else if constexpr (UNIFORM) tu = nearUniform64<T>(h, src, a.srcs64 + f, sg, xa, ya, za, n);
                         else tu = nearNonUniform64<T>(BATCH ? unit->sp3 : a.sp3, src, a.srcs64 + f, sg, xa, ya, za, n);
-                    } else if (UNIFORM) {
+                    } else if (SCALED) {
                         // the Cartesian operators with lower-bound exits: min(t0, tu) is the
                         // same bit for bit as with fd3UniformFar
+                        tu = near ? nearUniformRaw<T>(h, src, sg, xa, ya, za, n, a.cells, a.cells64, nx, ny, nz)
+                                  : fd3UniformFarBounded<T, true>(h, n, t0);
+                    } else if (UNIFORM) {
                         tu = near ? nearUniform<T>(h, src, sg, xa, ya, za, n) : fd3UniformFarBounded<T>(h, n, t0);
                     } else {
                         const Spacing3<T> &g = BATCH ? unit->sp3 : a.sp3;
@@ -557,8 +606,13 @@ template <class T, bool B, int LY, int LZ> int blocksPerSM(bool uniform) {
     template <class T>                                                                                \
     cudaError_t launchSweep3Chunk_##LY_##x##LZ_(const Sweep3Args<T> &a, bool uniform, int blocks,     \
                                                 cudaStream_t s) {                                     \
-        if (a.units) chunk::launchShape<T, true, LY_, LZ_>(a, uniform, blocks, s);                    \
-        else chunk::launchShape<T, false, LY_, LZ_>(a, uniform, blocks, s);                           \
+        if (a.units) {                                                                                \
+            chunk::launchShape<T, true, LY_, LZ_>(a, uniform, blocks, s);                             \
+        } else {                                                                                      \
+            if (sizeof(T) == 8 && uniform && (!a.hsPos || !a.hsNeg || !a.cells))                     \
+                return cudaErrorInvalidValue;                                                         \
+            chunk::launchShape<T, false, LY_, LZ_>(a, uniform, blocks, s);                            \
+        }                                                                                             \
         return cudaGetLastError();                                                                    \
     }                                                                                                 \
     template <class T> int sweep3ChunkBlocksPerSM_##LY_##x##LZ_(bool uniform, bool batch) {           \
