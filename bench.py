@@ -895,10 +895,11 @@ def profile_learned_case(batch=4):
     torch.cuda.synchronize()
 
 
-def profile_case(fields):
+def profile_case(fields, fp64=False):
     """The workload's grid and model, `fields` sources, one refinement iteration, without
     the CUDA graph: 8 source-limited sweeps then 8 full sweeps (launches 9-16).  With
-    --in-flight below `fields`: the stream of those sources to the bench's tolerance."""
+    --in-flight below `fields`: the stream of those sources to the bench's tolerance.  fp64:
+    FP64 sweeps (the reference's own precision) instead of FP32 with the FP64 factor."""
     import torch
     import eikonalxx_gb300 as ex
     v, src = make_workload(fields)
@@ -908,10 +909,10 @@ def profile_case(fields):
     stream = 0 < IN_FLIGHT[0] < fields
     # a stream: the bench's tolerance, so that slots refill; else one refinement iteration
     opt = ex.Options(n_sweeps=N_SWEEPS_MAX if stream else 1, tolerance=TOL if stream else -1, factored_radius=RADIUS,
-                     profile_sweeps=True, pair_fields=PAIR[0], sweep_kernel=KERNEL[0], near_fp64=NEAR64[0],
-                     max_in_flight=IN_FLIGHT[0] if stream else 0)
-    out = torch.empty((fields, NZ, NY, NX), dtype=torch.float32, device="cuda")
-    ctx.solve3d(src, opt, ex.F32, out=out)
+                     profile_sweeps=True, pair_fields=PAIR[0], sweep_kernel=KERNEL[0],
+                     near_fp64=NEAR64[0] and not fp64, max_in_flight=IN_FLIGHT[0] if stream else 0)
+    out = torch.empty((fields, NZ, NY, NX), dtype=torch.float64 if fp64 else torch.float32, device="cuda")
+    ctx.solve3d(src, opt, ex.F64 if fp64 else ex.F32, out=out)
     st = ctx.stats()
     print(json.dumps({"profile_case": True, "fields": fields, "sweep_ms_mean": st["sweep_ms"] / st["sweeps_launched"],
                       "device_ms": st["device_ms"]}))
@@ -1077,6 +1078,8 @@ def main():
                     help="sweep two fields per lane (the paired FP32 kernel) instead of one")
     ap.add_argument("--profile-case", action="store_true",
                     help="one solve of the workload (1 refinement iteration) for ncu captures")
+    ap.add_argument("--profile-fp64", action="store_true",
+                    help="with --profile-case: FP64 sweeps instead of FP32")
     args = ap.parse_args()
     global NX, NY, NZ, H
     if args.workload == "stations":
@@ -1110,7 +1113,7 @@ def main():
         if args.workload == "learned":
             profile_learned_case()
         else:
-            profile_case(args.fields)
+            profile_case(args.fields, fp64=args.profile_fp64)
         return
     if args.warmup < 3:
         args.warmup = 3
