@@ -206,14 +206,6 @@ __device__ __noinline__ T nearUniform64(T h, const SourceT<T> src, const SourceF
     return fd3UniformNear<T, true>(h, src, sg, ix, iy, iz, n, &d);
 }
 template <class T>
-__device__ __noinline__ T nearUniform64Raw(T h, const SourceT<T> src, const SourceFp64 *f, const SweepSigns sg, int ix,
-                                           int iy, int iz, Stencil3<T> n, const void *cells, int cells64, int nx,
-                                           int ny, int nz) {
-    rawStencilCells(n, cells, cells64, nx, ny, nz, sg, ix, iy, iz);
-    const SourceFp64 d = *f;
-    return fd3UniformNear<T, true>(h, src, sg, ix, iy, iz, n, &d);
-}
-template <class T>
 __device__ __noinline__ T nearNonUniform64(const Spacing3<T> g, const SourceT<T> src, const SourceFp64 *f,
                                            const SweepSigns sg, int ix, int iy, int iz, const Stencil3<T> n) {
     const SourceFp64 d = *f;
@@ -491,10 +483,8 @@ __device__ __forceinline__ void sweep3ChunkBody(const Sweep3Args<T> &a) {
                     const T t0 = out.v[e];
                     T tu;
                     if (NEAR64 && near) {
-                        if constexpr (SCALED)
-                            tu = nearUniform64Raw<T>(h, src, a.srcs64 + f, sg, xa, ya, za, n, a.cells, a.cells64, nx,
-                                                     ny, nz);
-                        else if constexpr (UNIFORM) tu = nearUniform64<T>(h, src, a.srcs64 + f, sg, xa, ya, za, n);
+                        // FP32 only, so the stencil holds raw slowness values
+                        if constexpr (UNIFORM) tu = nearUniform64<T>(h, src, a.srcs64 + f, sg, xa, ya, za, n);
                         else tu = nearNonUniform64<T>(BATCH ? unit->sp3 : a.sp3, src, a.srcs64 + f, sg, xa, ya, za, n);
                     } else if (SCALED) {
                         // the Cartesian operators with lower-bound exits: min(t0, tu) is the
